@@ -1,0 +1,259 @@
+/*
+ * gxy_gpu.h -- C ABI of the GB300 ray-processing path (libgxy_gpu.so).
+ *
+ * Plain C: pointers, sizes and integer status codes; no C++ or torch types.
+ * Every entry point returns GXY_OK (0) or a negative GXY_ERR_* code and never
+ * throws across the boundary.  Buffers are owned by the caller unless a
+ * function name says otherwise.  Entry points are safe to call from several
+ * host threads as long as each thread passes its own stream.
+ *
+ * What each group replaces in Galaxy (paths are inside the Galaxy source tree):
+ *
+ *   gxy_gpu_trace_raylist       TraceRays::Trace (src/renderer/TraceRays.cpp:68-146), i.e.
+ *                               the ISPC exports TraceRays_TraceRays (TraceRays.ispc:326),
+ *                               TraceRays_ambientLighting (:735), TraceRays_generateAORays (:625),
+ *                               TraceRays_diffuseLighting (:859), TraceRays_generateShadowRays (:763)
+ *                               run in the GXY_REVERSE_LIGHTING order (TraceRays.cpp:124-131).
+ *   gxy_gpu_classify            Renderer::Classify            (src/renderer/Renderer.cpp:304-421)
+ *   gxy_gpu_assign_destinations Renderer::AssignDestinations  (src/renderer/Renderer.cpp:423-454)
+ *   gxy_gpu_accumulate_terminated Renderer::HandleTerminatedRays + Rendering::AddLocalPixels
+ *                               (src/renderer/Renderer.cpp:456-502, Rendering.cpp:125-153)
+ *   gxy_gpu_generate_initial_rays Camera::generate_initial_rays / SpawnRays
+ *                               (src/renderer/Camera.cpp:379-493, 528-829) for one partition.
+ *   gxy_gpu_scene_commit        Visualization::SetOsprayObjects + Visualization_commit +
+ *                               ospCommit(model) (Visualization.cpp:207-285,
+ *                               Visualization.ispc:48-93): uploads volumes, transfer
+ *                               functions and geometry and builds the BVH on the GPU.
+ *   gxy_gpu_render              one frame of Renderer::Start for a RenderingSet
+ *                               (Renderer.cpp:179-269, 504-656): ray generation, trace,
+ *                               shade, classify, partition hand-off and framebuffer
+ *                               accumulation, all on the device.
+ */
+#ifndef GXY_GPU_H
+#define GXY_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------- */
+#define GXY_OK              0
+#define GXY_ERR_INVALID    -1   /* bad argument (null pointer, size, count)  */
+#define GXY_ERR_CUDA       -2   /* a CUDA runtime call failed                */
+#define GXY_ERR_OOM        -3   /* device allocation failed / budget exceeded */
+#define GXY_ERR_OVERFLOW   -4   /* a device ray queue overflowed (rays lost)  */
+#define GXY_ERR_TIMEOUT    -5   /* a bounded device or host wait ran out      */
+#define GXY_ERR_ADMISSION  -6   /* request refused by the HBM budget          */
+#define GXY_ERR_NOT_INIT   -7   /* gxy_gpu_init has not been called           */
+
+/* ---- ray flags: src/renderer/RayFlags.h:28-36 -------------------------- */
+#define GXY_RAY_PRIMARY    0x001
+#define GXY_RAY_SHADOW     0x002
+#define GXY_RAY_AO         0x004
+#define GXY_RAY_EMPTY      0x008
+#define GXY_RAY_SURFACE    0x001
+#define GXY_RAY_OPAQUE     0x002
+#define GXY_RAY_BOUNDARY   0x004
+#define GXY_RAY_TIMEOUT    0x008
+
+/* classifications: src/renderer/Renderer.cpp:78-82 (values >= 0 are partitions) */
+#define GXY_TERMINATED     (-1)
+#define GXY_DROP_ON_FLOOR  (-2)
+#define GXY_KEEP_HERE      (-3)
+#define GXY_UNDETERMINED   (-4)
+
+/* light types: src/renderer/Lighting.cpp:58-115, Rendering.cpp:186-200 */
+#define GXY_LIGHT_DIRECTIONAL 0
+#define GXY_LIGHT_CAMERA      1   /* resolved to GXY_LIGHT_POINT per camera */
+#define GXY_LIGHT_POINT       2
+
+#define GXY_TF_SIZE        256
+#define GXY_MAX_LIGHTS     8
+#define GXY_MAX_SLICES     8
+#define GXY_MAX_ISOVALUES  8
+#define GXY_MAX_VOLUMES    4
+#define GXY_MAX_PARTITIONS 64
+
+/* Transfer function after MappedVis::local_commit (MappedVis.cpp:277-338):
+ * 256 resampled RGB entries, 256 resampled opacities and the valueRange. */
+typedef struct gxy_tf {
+    float colors[GXY_TF_SIZE * 3];
+    float opacities[GXY_TF_SIZE];
+    float range[2];
+} gxy_tf;
+
+/* One VolumeVis over a structured fp32 grid (x fastest).  The grid is the
+ * whole dataset; Galaxy's 1-voxel outer ghost shell and brick partition
+ * (Volume.cpp:133-172, 379-390) are applied by the scene commit. */
+typedef struct gxy_volume_vis {
+    const float *samples;
+    int32_t counts[3];
+    float   origin[3];
+    float   deltas[3];
+    gxy_tf  tf;
+    int32_t n_slices;
+    float   slices[GXY_MAX_SLICES][4];        /* plane (nx,ny,nz,d): n.p = d */
+    int32_t n_isovalues;
+    float   isovalues[GXY_MAX_ISOVALUES];
+    int32_t volume_render;
+} gxy_volume_vis;
+
+/* TrianglesVis over a triangle mesh (DataDrivenTriangleMesh). */
+typedef struct gxy_triangles_vis {
+    const float   *vertices;    /* 3 * n_vertices */
+    int64_t        n_vertices;
+    const int32_t *indices;     /* 3 * n_triangles */
+    int64_t        n_triangles;
+    const float   *normals;     /* 3 * n_vertices, or NULL (geometric normal) */
+    const float   *data;        /* n_vertices, or NULL (white surface)        */
+    gxy_tf         tf;
+} gxy_triangles_vis;
+
+/* ParticlesVis over spheres (DataDrivenSpheres; radius rules at
+ * DataDrivenSpheres.ispc:104-116, ParticlesVis.cpp:104-118). */
+typedef struct gxy_particles_vis {
+    const float *centers;       /* 3 * n */
+    const float *data;          /* n, or NULL */
+    int64_t      n;
+    float        radius0, radius1, value0, value1;
+    gxy_tf       tf;
+} gxy_particles_vis;
+
+/* Lighting_ispc (Lighting.ih:23-32).  Directional vectors are normalised on
+ * load (Lighting.cpp:76-90); camera lights must be resolved first with
+ * gxy_resolve_lights. */
+typedef struct gxy_lighting {
+    int32_t n_lights;
+    float   lights[GXY_MAX_LIGHTS][3];
+    int32_t types[GXY_MAX_LIGHTS];
+    float   Ka, Kd;
+    int32_t n_ao;
+    float   ao_radius;
+    int32_t shadows;
+} gxy_lighting;
+
+/* Camera (Camera.h): eye, view direction (not necessarily normalised), up,
+ * angle of view in degrees (0 = orthographic) and image size. */
+typedef struct gxy_camera {
+    float   eye[3];
+    float   dir[3];
+    float   up[3];
+    float   aov;
+    int32_t width, height;
+} gxy_camera;
+
+/* A Visualization: the scene the tracer consumes. */
+typedef struct gxy_scene_desc {
+    int32_t                  n_volumes;
+    const gxy_volume_vis    *volumes;
+    int32_t                  n_triangle_sets;
+    const gxy_triangles_vis *triangles;
+    int32_t                  n_particle_sets;
+    const gxy_particles_vis *particles;
+    int32_t partitions[3];   /* brick grid (Galaxy's global_partitions); {1,1,1} = one */
+    int32_t has_box;         /* geometry-only scenes: explicit global box below       */
+    float   box[6];          /* xmin ymin zmin xmax ymax zmax                          */
+    float   sampling_rate;   /* volume samples per voxel; 1.0 in Galaxy                */
+    float   opaque_alpha;    /* early-termination alpha; 0.999 in Galaxy               */
+    float   epsilon;         /* Renderer.epsilon; 0.001 in Galaxy                      */
+} gxy_scene_desc;
+
+/* RayList_ispc (Rays.ih:21-48): 25 SoA arrays plus the count.  Host memory. */
+typedef struct gxy_raylist {
+    float   *ox, *oy, *oz, *dx, *dy, *dz, *nx, *ny, *nz, *sample;
+    float   *r, *g, *b, *o, *sr, *sg, *sb, *so, *t, *tMax;
+    int32_t *x, *y, *type, *term, *classification;
+    int32_t  n;
+} gxy_raylist;
+
+/* Partition geometry as committed (Visualization local/global boxes and
+ * neighbours, Visualization.cpp:135-205). */
+typedef struct gxy_partition_info {
+    float   global_box[6];
+    float   local_box[6];
+    int32_t neighbors[6];
+    int32_t n_partitions;
+} gxy_partition_info;
+
+/* Device counters of the last gxy_gpu_render call. */
+typedef struct gxy_counters {
+    int64_t primary_rays;     /* primary rays generated               */
+    int64_t secondary_rays;   /* shadow + AO rays spawned             */
+    int64_t shadow_rays;
+    int64_t ao_rays;
+    int64_t segments;         /* ray x partition traces               */
+    int64_t handoffs;         /* rays passed to a neighbour partition */
+    int64_t terminated;       /* framebuffer contributions            */
+    int64_t dropped;          /* DROP_ON_FLOOR                        */
+    int64_t kept;             /* KEEP_HERE re-traces                  */
+    int64_t bounces;          /* queue generations processed          */
+    int64_t samples;          /* volume samples taken                 */
+    int64_t nodes;            /* BVH8 node lines visited              */
+    int64_t prim_tests;       /* primitive intersection tests         */
+    int32_t overflow;         /* non-zero if a queue overflowed       */
+    int32_t pad;
+} gxy_counters;
+
+typedef struct gxy_scene_s *gxy_scene;
+
+/* ---- device and scene lifetime ---------------------------------------- */
+
+/* Select the device, cap the bytes this library may allocate (0 = no cap). */
+int gxy_gpu_init(int device, size_t hbm_budget_bytes);
+int gxy_gpu_shutdown(void);
+/* Copy the last error message of this thread into buf. */
+int gxy_gpu_last_error(char *buf, int buflen);
+/* Bytes currently allocated by the library on the device. */
+int gxy_gpu_hbm_in_use(size_t *bytes);
+
+int gxy_gpu_scene_commit(const gxy_scene_desc *desc, gxy_scene *out);
+int gxy_gpu_scene_release(gxy_scene scene);
+int gxy_gpu_scene_partition_info(gxy_scene scene, int partition, gxy_partition_info *out);
+/* BVH statistics: wide nodes, leaf primitive references, build time (ms). */
+int gxy_gpu_scene_bvh_info(gxy_scene scene, int64_t *n_nodes, int64_t *n_prim_refs,
+                           double *build_ms);
+
+/* Rendering::resolve_lights (Rendering.cpp:157-216): camera-relative lights
+ * become point lights for the given camera.  Host-only arithmetic. */
+int gxy_resolve_lights(const gxy_lighting *in, const gxy_camera *camera, gxy_lighting *out);
+
+/* ---- whole-frame path (device resident) -------------------------------- */
+
+/* Render one frame of `camera` into the device framebuffer `fb_rgba`
+ * (width*height*4 fp32, pixel (x,y) at (y*width+x)*4, y=0 is the bottom row).
+ * Contributions are ADDED (Rendering::AddLocalPixels); the caller clears.
+ * `stream` is a cudaStream_t (NULL = legacy default stream).  The call is
+ * asynchronous with respect to the host except for the per-bounce queue
+ * count read-back. */
+int gxy_gpu_render(gxy_scene scene, const gxy_camera *camera, const gxy_lighting *lighting,
+                   float *fb_rgba, void *stream);
+/* Same with a host framebuffer: clears a device framebuffer, renders, copies
+ * the image back (the end-to-end call a host application makes). */
+int gxy_gpu_render_host(gxy_scene scene, const gxy_camera *camera,
+                        const gxy_lighting *lighting, float *host_fb_rgba, void *stream);
+int gxy_gpu_query_counters(gxy_scene scene, gxy_counters *out);
+
+/* ---- RayList-level drop-in (host buffers) ------------------------------ */
+
+/* Camera::generate_initial_rays for partition `partition`: fills `out`
+ * (capacity out->n on entry) and sets *n_out to the rays emitted. */
+int gxy_gpu_generate_initial_rays(gxy_scene scene, int partition, const gxy_camera *camera,
+                                  gxy_raylist *out, int32_t *n_out);
+/* TraceRays::Trace for the rays of `in` inside partition `partition`:
+ * updates `in` in place and writes the secondary list (AO block first, then
+ * shadow block, as TraceRays.cpp:89-117 orders it) into `out` (capacity
+ * out->n on entry); *n_out receives its length. */
+int gxy_gpu_trace_raylist(gxy_scene scene, int partition, const gxy_lighting *lighting,
+                          gxy_raylist *in, gxy_raylist *out, int32_t *n_out);
+int gxy_gpu_classify(gxy_raylist *rays);
+int gxy_gpu_assign_destinations(gxy_scene scene, int partition, gxy_raylist *rays);
+/* Adds every TERMINATED ray's (r,g,b,o) to host framebuffer fb (w*h*4). */
+int gxy_gpu_accumulate_terminated(const gxy_raylist *rays, float *fb_rgba, int width, int height);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GXY_GPU_H */
