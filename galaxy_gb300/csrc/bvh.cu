@@ -1,0 +1,452 @@
+// bvh.cu -- GPU construction of the 8-wide BVH over triangles and spheres.
+//
+// Replaces the Embree BVH that ospCommit(model) builds in Galaxy
+// (Visualization::SetOsprayObjects, src/renderer/Visualization.cpp:207-285).
+//
+// Steps, all on the device:
+//  1. primitive bounds and centroid bounds;
+//  2. 63-bit Morton codes (21 bits per axis) and a radix sort of (code, id);
+//  3. Karras' binary radix tree (LBVH) over the sorted codes;
+//  4. bottom-up refit of the binary nodes' boxes;
+//  5. top-down collapse to 8-wide nodes, one kernel per level: each wide node
+//     starts from a binary node's two children and repeatedly opens the child
+//     with the largest surface area (the surface-area-heuristic greedy
+//     choice) until it has 8 children; subtrees of at most kLeafMax
+//     primitives become leaves.  Child boxes are quantised to 16 bits
+//     against a power-of-two grid so a node fills one 128-byte line.
+#include <cub/cub.cuh>
+
+#include <cfloat>
+#include <chrono>
+#include <vector>
+
+#include "gxy_dev.cuh"
+#include "gxy_host.h"
+
+namespace gxy {
+
+constexpr int kLeafMax = 4;
+
+__device__ __forceinline__ void prim_box(const DevScene &S, uint32_t p, float3 &lo, float3 &hi) {
+    if (p < S.n_tri) {
+        int s = 0;
+        while (s + 1 < S.n_tri_sets && p >= S.tri_sets[s + 1].prim_base) s++;
+        const DevTriSet &T = S.tri_sets[s];
+        int64_t lp = p - T.prim_base;
+        const int32_t *ix = T.indices + 3 * lp;
+        float3 a = make_float3(T.vertices[3 * ix[0]], T.vertices[3 * ix[0] + 1], T.vertices[3 * ix[0] + 2]);
+        float3 b = make_float3(T.vertices[3 * ix[1]], T.vertices[3 * ix[1] + 1], T.vertices[3 * ix[1] + 2]);
+        float3 c = make_float3(T.vertices[3 * ix[2]], T.vertices[3 * ix[2] + 1], T.vertices[3 * ix[2] + 2]);
+        lo = make_float3(fminf(a.x, fminf(b.x, c.x)), fminf(a.y, fminf(b.y, c.y)), fminf(a.z, fminf(b.z, c.z)));
+        hi = make_float3(fmaxf(a.x, fmaxf(b.x, c.x)), fmaxf(a.y, fmaxf(b.y, c.y)), fmaxf(a.z, fmaxf(b.z, c.z)));
+    } else {
+        int s = 0;
+        while (s + 1 < S.n_sph_sets && (int64_t)p >= S.sph_sets[s + 1].prim_base) s++;
+        const DevSphSet &P = S.sph_sets[s];
+        int64_t lp = (int64_t)p - P.prim_base;
+        lo = hi = make_float3(P.centers[3 * lp], P.centers[3 * lp + 1], P.centers[3 * lp + 2]);   // radius added by caller
+    }
+}
+
+struct BuildBuffers {
+    float4 *plo = nullptr, *phi = nullptr;           // primitive boxes (by prim id)
+    unsigned long long *keys = nullptr, *keys2 = nullptr;
+    uint32_t *ids = nullptr, *ids2 = nullptr;
+    int *left = nullptr, *right = nullptr, *parent = nullptr, *first = nullptr, *last = nullptr;
+    int *flags = nullptr;
+    float4 *nlo = nullptr, *nhi = nullptr;           // binary internal node boxes
+    int2 *qa = nullptr, *qb = nullptr;               // work queues (binary ref, wide index)
+    unsigned int *ctr = nullptr;                     // [0] nodes [1] slots [2] queue out
+    unsigned int *cbounds = nullptr;                 // centroid bounds as ordered uints
+};
+
+__device__ __forceinline__ unsigned int f2o(float f) {   // order-preserving float -> uint
+    unsigned int u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float o2f(unsigned int u) {
+    return __uint_as_float((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u);
+}
+
+// Primitive boxes.  Spheres use the radius array prepared by the commit
+// (sph_radius, by sphere index).
+__global__ void k_prim_bounds(DevScene S, const float *sph_radius, int64_t n, float4 *plo, float4 *phi,
+                              unsigned int *cb) {
+    int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    float3 lo = make_float3(FLT_MAX, FLT_MAX, FLT_MAX), hi = make_float3(-FLT_MAX, -FLT_MAX, -FLT_MAX);
+    float3 c = make_float3(0, 0, 0);
+    bool valid = p < n;
+    if (valid) {
+        prim_box(S, (uint32_t)p, lo, hi);
+        if (p >= S.n_tri) {
+            float r = sph_radius[p - S.n_tri];
+            lo = make_float3(lo.x - r, lo.y - r, lo.z - r);
+            hi = make_float3(hi.x + r, hi.y + r, hi.z + r);
+        }
+        plo[p] = make_float4(lo.x, lo.y, lo.z, 0.0f);
+        phi[p] = make_float4(hi.x, hi.y, hi.z, 0.0f);
+        c = make_float3(0.5f * (lo.x + hi.x), 0.5f * (lo.y + hi.y), 0.5f * (lo.z + hi.z));
+    }
+    // block reduction of centroid bounds
+    __shared__ float s[6][32];
+    float v[6] = {valid ? c.x : FLT_MAX, valid ? c.y : FLT_MAX, valid ? c.z : FLT_MAX,
+                  valid ? c.x : -FLT_MAX, valid ? c.y : -FLT_MAX, valid ? c.z : -FLT_MAX};
+    for (int k = 0; k < 6; k++) {
+        for (int o = 16; o > 0; o >>= 1) {
+            float w = __shfl_xor_sync(0xffffffffu, v[k], o);
+            v[k] = k < 3 ? fminf(v[k], w) : fmaxf(v[k], w);
+        }
+    }
+    int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0)
+        for (int k = 0; k < 6; k++) s[k][warp] = v[k];
+    __syncthreads();
+    if (warp == 0) {
+        int nw = blockDim.x >> 5;
+        for (int k = 0; k < 6; k++) {
+            float w = lane < nw ? s[k][lane] : (k < 3 ? FLT_MAX : -FLT_MAX);
+            for (int o = 16; o > 0; o >>= 1) {
+                float x = __shfl_xor_sync(0xffffffffu, w, o);
+                w = k < 3 ? fminf(w, x) : fmaxf(w, x);
+            }
+            if (lane == 0) {
+                if (k < 3) atomicMin(&cb[k], f2o(w));
+                else atomicMax(&cb[k], f2o(w));
+            }
+        }
+    }
+}
+
+__device__ __forceinline__ unsigned long long spread21(unsigned long long x) {
+    x &= 0x1fffffull;
+    x = (x | x << 32) & 0x1f00000000ffffull;
+    x = (x | x << 16) & 0x1f0000ff0000ffull;
+    x = (x | x << 8) & 0x100f00f00f00f00full;
+    x = (x | x << 4) & 0x10c30c30c30c30c3ull;
+    x = (x | x << 2) & 0x1249249249249249ull;
+    return x;
+}
+
+__global__ void k_morton(int64_t n, const float4 *plo, const float4 *phi, const unsigned int *cb,
+                         unsigned long long *keys, uint32_t *ids) {
+    int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    float lo[3] = {o2f(cb[0]), o2f(cb[1]), o2f(cb[2])};
+    float hi[3] = {o2f(cb[3]), o2f(cb[4]), o2f(cb[5])};
+    float4 a = plo[p], b = phi[p];
+    float c[3] = {0.5f * (a.x + b.x), 0.5f * (a.y + b.y), 0.5f * (a.z + b.z)};
+    unsigned long long q[3];
+    for (int k = 0; k < 3; k++) {
+        float e = hi[k] - lo[k];
+        float f = e > 0.0f ? (c[k] - lo[k]) / e : 0.5f;
+        f = fminf(fmaxf(f, 0.0f), 1.0f);
+        q[k] = (unsigned long long)fminf(f * 2097152.0f, 2097151.0f);
+    }
+    keys[p] = (spread21(q[0]) << 2) | (spread21(q[1]) << 1) | spread21(q[2]);
+    ids[p] = (uint32_t)p;
+}
+
+__device__ __forceinline__ int delta(const unsigned long long *k, int n, int i, int j) {
+    if (j < 0 || j >= n) return -1;
+    unsigned long long a = k[i], b = k[j];
+    if (a == b) return 64 + __clz((unsigned)(i ^ j));
+    return __clzll(a ^ b);
+}
+
+// Karras 2012: internal node i of the binary radix tree.  Children are
+// encoded as >= 0 internal index or ~leaf for leaves.
+__global__ void k_karras(int n, const unsigned long long *k, int *left, int *right, int *parent, int *first, int *last,
+                         int *leaf_parent) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n - 1) return;
+    int d = (delta(k, n, i, i + 1) - delta(k, n, i, i - 1)) >= 0 ? 1 : -1;
+    int dmin = delta(k, n, i, i - d);
+    int lmax = 2;
+    while (delta(k, n, i, i + lmax * d) > dmin) lmax <<= 1;
+    int l = 0;
+    for (int t = lmax >> 1; t >= 1; t >>= 1)
+        if (delta(k, n, i, i + (l + t) * d) > dmin) l += t;
+    int j = i + l * d;
+    int dnode = delta(k, n, i, j);
+    int s = 0;
+    int t = l;
+    do {
+        t = (t + 1) >> 1;
+        if (delta(k, n, i, i + (s + t) * d) > dnode) s += t;
+    } while (t > 1);
+    int g = i + s * d + (d < 0 ? -1 : 0);
+    int lo = i < j ? i : j, hi = i < j ? j : i;
+    int lc = (lo == g) ? ~g : g;
+    int rc = (hi == g + 1) ? ~(g + 1) : g + 1;
+    left[i] = lc;
+    right[i] = rc;
+    first[i] = lo;
+    last[i] = hi;
+    if (lc >= 0) parent[lc] = i; else leaf_parent[~lc] = i;
+    if (rc >= 0) parent[rc] = i; else leaf_parent[~rc] = i;
+}
+
+__global__ void k_refit(int n, const uint32_t *ids, const float4 *plo, const float4 *phi, const int *left,
+                        const int *right, const int *parent, const int *leaf_parent, int *flags, float4 *nlo,
+                        float4 *nhi) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int node = leaf_parent[i];
+    while (node >= 0) {
+        __threadfence();
+        if (atomicAdd(&flags[node], 1) == 0) return;   // first arrival: sibling not ready
+        __threadfence();
+        int c[2] = {left[node], right[node]};
+        float4 lo = make_float4(FLT_MAX, FLT_MAX, FLT_MAX, 0), hi = make_float4(-FLT_MAX, -FLT_MAX, -FLT_MAX, 0);
+        for (int k = 0; k < 2; k++) {
+            float4 a, b;
+            if (c[k] >= 0) { a = __ldcg(&nlo[c[k]]); b = __ldcg(&nhi[c[k]]); }
+            else { uint32_t p = ids[~c[k]]; a = plo[p]; b = phi[p]; }
+            lo = make_float4(fminf(lo.x, a.x), fminf(lo.y, a.y), fminf(lo.z, a.z), 0);
+            hi = make_float4(fmaxf(hi.x, b.x), fmaxf(hi.y, b.y), fmaxf(hi.z, b.z), 0);
+        }
+        __stcg(&nlo[node], lo);
+        __stcg(&nhi[node], hi);
+        node = node == 0 ? -1 : parent[node];
+    }
+}
+
+__device__ __forceinline__ float half_area(float4 lo, float4 hi) {
+    float x = hi.x - lo.x, y = hi.y - lo.y, z = hi.z - lo.z;
+    return x * y + y * z + z * x;
+}
+
+__device__ __forceinline__ uint8_t quant_exp(float extent) {
+    float s = extent / 65535.0f;
+    if (!(s > 0.0f)) return 1;
+    uint32_t b = __float_as_uint(s);
+    uint32_t e = (b >> 23) & 0xffu;
+    if (b & 0x7fffffu) e++;
+    if (e < 1) e = 1;
+    if (e > 254) e = 254;
+    return (uint8_t)e;
+}
+
+// Leaf primitive slot record (3 float4), see BVH8Node in gxy_dev.cuh.
+__device__ void write_slot(const DevScene &S, const float *sph_radius, uint32_t p, float4 *slots, uint32_t s) {
+    float4 *r = slots + 3 * (size_t)s;
+    if (p < S.n_tri) {
+        int k = 0;
+        while (k + 1 < S.n_tri_sets && (int64_t)p >= S.tri_sets[k + 1].prim_base) k++;
+        const DevTriSet &T = S.tri_sets[k];
+        const int32_t *ix = T.indices + 3 * ((int64_t)p - T.prim_base);
+        const float *V = T.vertices;
+        r[0] = make_float4(V[3 * ix[0]], V[3 * ix[0] + 1], V[3 * ix[0] + 2], __uint_as_float(p));
+        r[1] = make_float4(V[3 * ix[1]], V[3 * ix[1] + 1], V[3 * ix[1] + 2], 0.0f);
+        r[2] = make_float4(V[3 * ix[2]], V[3 * ix[2] + 1], V[3 * ix[2] + 2], 0.0f);
+    } else {
+        int k = 0;
+        while (k + 1 < S.n_sph_sets && (int64_t)p >= S.sph_sets[k + 1].prim_base) k++;
+        const DevSphSet &P = S.sph_sets[k];
+        int64_t lp = (int64_t)p - P.prim_base;
+        r[0] = make_float4(P.centers[3 * lp], P.centers[3 * lp + 1], P.centers[3 * lp + 2],
+                           __uint_as_float(p | kSphereBit));
+        r[1] = make_float4(sph_radius[(int64_t)p - S.n_tri], P.eps, 0.0f, 0.0f);
+        r[2] = make_float4(0, 0, 0, 0);
+    }
+}
+
+// One level of the collapse.  Work item: (binary ref, wide node index).
+__global__ void k_collapse(DevScene S, const float *sph_radius, int n, const int2 *qin, int nq, int2 *qout,
+                           unsigned int *ctr, const int *left, const int *right, const int *first, const int *last,
+                           const uint32_t *ids, const float4 *plo, const float4 *phi, const float4 *nlo,
+                           const float4 *nhi, BVH8Node *nodes, float4 *slots, int max_nodes, int max_slots) {
+    int w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= nq) return;
+    int2 item = qin[w];
+    int ref = item.x;
+    int widx = item.y;
+    int ch[8];
+    int nc = 0;
+    auto size_of = [&](int r) { return r >= 0 ? last[r] - first[r] + 1 : 1; };
+    auto box_of = [&](int r, float4 &lo, float4 &hi) {
+        if (r >= 0) { lo = nlo[r]; hi = nhi[r]; }
+        else { uint32_t p = ids[~r]; lo = plo[p]; hi = phi[p]; }
+    };
+    if (ref >= 0 && size_of(ref) > kLeafMax) {
+        ch[nc++] = left[ref];
+        ch[nc++] = right[ref];
+        while (nc < 8) {
+            int best = -1;
+            float ba = -1.0f;
+            for (int k = 0; k < nc; k++) {
+                if (ch[k] >= 0 && size_of(ch[k]) > kLeafMax) {
+                    float4 lo, hi;
+                    box_of(ch[k], lo, hi);
+                    float a = half_area(lo, hi);
+                    if (a > ba) { ba = a; best = k; }
+                }
+            }
+            if (best < 0) break;
+            int r = ch[best];
+            ch[best] = left[r];
+            ch[nc++] = right[r];
+        }
+    } else {
+        ch[nc++] = ref;   // whole (small) tree as one leaf: only for a small root
+    }
+    int n_int = 0, n_prims = 0;
+    for (int k = 0; k < nc; k++) {
+        if (ch[k] >= 0 && size_of(ch[k]) > kLeafMax) n_int++;
+        else n_prims += size_of(ch[k]);
+    }
+    unsigned int cbase = n_int ? atomicAdd(&ctr[0], (unsigned)n_int) : 0u;
+    unsigned int pbase = n_prims ? atomicAdd(&ctr[1], (unsigned)n_prims) : 0u;
+    if ((int)(cbase + n_int) > max_nodes || (int)(pbase + n_prims) > max_slots) {
+        atomicExch(&ctr[3], 1u);
+        return;
+    }
+    float4 lo = make_float4(FLT_MAX, FLT_MAX, FLT_MAX, 0), hi = make_float4(-FLT_MAX, -FLT_MAX, -FLT_MAX, 0);
+    float4 clo[8], chi[8];
+    for (int k = 0; k < nc; k++) {
+        box_of(ch[k], clo[k], chi[k]);
+        lo = make_float4(fminf(lo.x, clo[k].x), fminf(lo.y, clo[k].y), fminf(lo.z, clo[k].z), 0);
+        hi = make_float4(fmaxf(hi.x, chi[k].x), fmaxf(hi.y, chi[k].y), fmaxf(hi.z, chi[k].z), 0);
+    }
+    BVH8Node nd;
+    nd.ox = lo.x; nd.oy = lo.y; nd.oz = lo.z;
+    nd.child_base = cbase;
+    nd.prim_base = pbase;
+    nd.ex = quant_exp(hi.x - lo.x);
+    nd.ey = quant_exp(hi.y - lo.y);
+    nd.ez = quant_exp(hi.z - lo.z);
+    float sc[3] = {__uint_as_float((uint32_t)nd.ex << 23), __uint_as_float((uint32_t)nd.ey << 23),
+                   __uint_as_float((uint32_t)nd.ez << 23)};
+    float org[3] = {lo.x, lo.y, lo.z};
+    nd.imask = 0;
+    int irank = 0, poff = 0;
+    for (int k = 0; k < 8; k++) {
+        nd.meta[k] = 0xff;
+        for (int a = 0; a < 3; a++) { nd.qlo[a][k] = 0; nd.qhi[a][k] = 0; }
+    }
+    for (int k = 0; k < nc; k++) {
+        float cl[3] = {clo[k].x, clo[k].y, clo[k].z}, chh[3] = {chi[k].x, chi[k].y, chi[k].z};
+        for (int a = 0; a < 3; a++) {
+            float ql = floorf((cl[a] - org[a]) / sc[a]) - 1.0f;
+            float qh = ceilf((chh[a] - org[a]) / sc[a]) + 1.0f;
+            nd.qlo[a][k] = (uint16_t)fminf(fmaxf(ql, 0.0f), 65535.0f);
+            nd.qhi[a][k] = (uint16_t)fminf(fmaxf(qh, 0.0f), 65535.0f);
+        }
+        int r = ch[k];
+        if (r >= 0 && size_of(r) > kLeafMax) {
+            nd.imask |= (uint8_t)(1u << k);
+            nd.meta[k] = (uint8_t)irank;
+            unsigned int qi = atomicAdd(&ctr[2], 1u);
+            qout[qi] = make_int2(r, (int)(cbase + irank));
+            irank++;
+        } else {
+            int f = r >= 0 ? first[r] : ~r;
+            int cnt = size_of(r);
+            nd.meta[k] = (uint8_t)(((cnt - 1) << 5) | poff);
+            for (int j = 0; j < cnt; j++) write_slot(S, sph_radius, ids[f + j], slots, pbase + poff + j);
+            poff += cnt;
+        }
+    }
+    nodes[widx] = nd;
+}
+
+static inline unsigned blocks_for(int64_t n, int b) { return (unsigned)((n + b - 1) / b); }
+
+// Build the BVH8 for the geometry described by S (S.nodes/S.slots are set
+// on success).  sph_radius: per-sphere radius (device).
+int build_bvh8(DevScene &S, const float *sph_radius, DeviceArena &arena, cudaStream_t st, BVHInfo &info) {
+    auto t_start = std::chrono::steady_clock::now();
+    int64_t n64 = S.n_tri + S.n_sph;
+    info = BVHInfo{};
+    if (n64 == 0) {
+        S.nodes = nullptr;
+        S.slots = nullptr;
+        return GXY_OK;
+    }
+    if (n64 >= (int64_t)0x7fffffff) return set_error(GXY_ERR_INVALID, "too many primitives for the BVH");
+    int n = (int)n64;
+    BuildBuffers B;
+    ScratchList scratch(arena);
+    int rc = GXY_OK;
+#define ALLOC(p, cnt)                                                                        \
+    do {                                                                                     \
+        rc = scratch.alloc((void **)&(p), sizeof(*(p)) * (size_t)(cnt));                    \
+        if (rc) return rc;                                                                   \
+    } while (0)
+    ALLOC(B.plo, n); ALLOC(B.phi, n);
+    ALLOC(B.keys, n); ALLOC(B.keys2, n); ALLOC(B.ids, n); ALLOC(B.ids2, n);
+    int ni = n > 1 ? n - 1 : 1;
+    ALLOC(B.left, ni); ALLOC(B.right, ni); ALLOC(B.parent, ni); ALLOC(B.first, ni); ALLOC(B.last, ni);
+    ALLOC(B.flags, ni); ALLOC(B.nlo, ni); ALLOC(B.nhi, ni);
+    int *leaf_parent;
+    ALLOC(leaf_parent, n);
+    ALLOC(B.ctr, 8);
+    ALLOC(B.cbounds, 8);
+    // worst-case wide nodes: every wide node has >= 2 children
+    int max_nodes = n + 1;
+    int max_slots = n;
+    ALLOC(B.qa, max_nodes); ALLOC(B.qb, max_nodes);
+    unsigned int hb[8] = {0xffffffffu, 0xffffffffu, 0xffffffffu, 0, 0, 0, 0, 0};
+    CK(cudaMemcpyAsync(B.cbounds, hb, sizeof hb, cudaMemcpyHostToDevice, st));
+    k_prim_bounds<<<blocks_for(n, 256), 256, 0, st>>>(S, sph_radius, n, B.plo, B.phi, B.cbounds);
+    k_morton<<<blocks_for(n, 256), 256, 0, st>>>(n, B.plo, B.phi, B.cbounds, B.keys, B.ids);
+    CK(cudaGetLastError());
+    size_t tmp_bytes = 0;
+    cub::DeviceRadixSort::SortPairs(nullptr, tmp_bytes, B.keys, B.keys2, B.ids, B.ids2, n, 0, 63, st);
+    unsigned char *tmp;
+    ALLOC(tmp, tmp_bytes);
+    CK(cub::DeviceRadixSort::SortPairs(tmp, tmp_bytes, B.keys, B.keys2, B.ids, B.ids2, n, 0, 63, st));
+    if (n > 1) {
+        CK(cudaMemsetAsync(B.flags, 0, sizeof(int) * ni, st));
+        k_karras<<<blocks_for(n - 1, 256), 256, 0, st>>>(n, B.keys2, B.left, B.right, B.parent, B.first, B.last,
+                                                         leaf_parent);
+        k_refit<<<blocks_for(n, 256), 256, 0, st>>>(n, B.ids2, B.plo, B.phi, B.left, B.right, B.parent, leaf_parent,
+                                                    B.flags, B.nlo, B.nhi);
+        CK(cudaGetLastError());
+    }
+    BVH8Node *nodes;
+    float4 *slots;
+    rc = arena.alloc((void **)&nodes, sizeof(BVH8Node) * (size_t)max_nodes);
+    if (rc) return rc;
+    rc = arena.alloc((void **)&slots, sizeof(float4) * 3 * (size_t)max_slots);
+    if (rc) { arena.free(nodes); return rc; }
+    // root: wide node 0 from binary root 0 (or the single leaf)
+    int2 root = make_int2(n > 1 ? 0 : ~0, 0);
+    unsigned int c0[8] = {1, 0, 0, 0, 0, 0, 0, 0};
+    CK(cudaMemcpyAsync(B.ctr, c0, sizeof c0, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(B.qa, &root, sizeof root, cudaMemcpyHostToDevice, st));
+    int nq = 1;
+    int levels = 0;
+    while (nq > 0) {
+        CK(cudaMemsetAsync(B.ctr + 2, 0, sizeof(unsigned int), st));
+        k_collapse<<<blocks_for(nq, 128), 128, 0, st>>>(S, sph_radius, n, B.qa, nq, B.qb, B.ctr, B.left, B.right,
+                                                        B.first, B.last, B.ids2, B.plo, B.phi, B.nlo, B.nhi, nodes,
+                                                        slots, max_nodes, max_slots);
+        CK(cudaGetLastError());
+        unsigned int hc[4];
+        CK(cudaMemcpyAsync(hc, B.ctr, sizeof hc, cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        if (hc[3]) {
+            arena.free(nodes);
+            arena.free(slots);
+            return set_error(GXY_ERR_OVERFLOW, "BVH8 collapse exceeded its node budget");
+        }
+        nq = (int)hc[2];
+        std::swap(B.qa, B.qb);
+        levels++;
+        info.n_nodes = hc[0];
+        info.n_slots = hc[1];
+        if (levels > 200) return set_error(GXY_ERR_INVALID, "BVH8 collapse did not converge");
+    }
+    S.nodes = nodes;
+    S.slots = slots;
+    info.levels = levels;
+    info.nodes_ptr = nodes;
+    info.slots_ptr = slots;
+    info.build_ms =
+        std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start).count();
+    return GXY_OK;
+#undef ALLOC
+}
+
+}  // namespace gxy

@@ -1,0 +1,422 @@
+// gxy_dev.cuh -- device-side data layout and per-ray algorithms of the
+// GB300 ray path: scene tables, the 128-byte BVH8 node, the 64-byte queue
+// record, primitive tests, BVH8 traversal, the volume march and the
+// shading/spawn arithmetic.
+//
+// Arithmetic contract: translation units that include this header are built
+// with -fmad=false, so every expression below rounds exactly as written
+// (the same IEEE single-precision operations, in the same order, as the
+// semantics stated for Galaxy's TraceRays.ispc).  The only fused operations
+// are the explicit __fmaf_rn calls of the BVH box test, which decides only
+// which primitives are tested, never a result.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/gxy_gpu.h"
+
+namespace gxy {
+
+// ----------------------------------------------------------------- layout
+constexpr int kMaxVol = GXY_MAX_VOLUMES;
+constexpr int kMaxPart = GXY_MAX_PARTITIONS;
+constexpr uint32_t kSphereBit = 0x80000000u;
+
+struct DevTF {                       // one resampled transfer function, 4 KB
+    float colors[GXY_TF_SIZE * 3];
+    float opac[GXY_TF_SIZE];
+    float r0, r1, pad0, pad1;
+};
+
+struct DevVolume {
+    const float *data;
+    int nx, ny, nz;
+    float ox, oy, oz, dx, dy, dz;
+    float ux, uy, uz;                // clamp bounds: float just below n-1
+    int tf;                          // index into DevScene::tfs
+    int n_slices;
+    float4 slices[GXY_MAX_SLICES];
+    int n_iso;
+    float iso[GXY_MAX_ISOVALUES];
+    int volume_render;
+};
+
+struct DevPartition {
+    float lo[3], hi[3];
+    int nb[6];
+};
+
+struct DevTriSet {                   // triangles [prim_base, prim_base+n)
+    int64_t prim_base, n;
+    const int32_t *indices;          // 3 per triangle (set-local vertex ids)
+    const float *vertices;           // 3 per vertex
+    const float *normals;            // 3 per vertex or null
+    const float *data;               // per vertex or null
+    int tf;
+};
+
+struct DevSphSet {                   // spheres [prim_base, prim_base+n)
+    int64_t prim_base, n;
+    const float *centers;
+    const float *data;
+    int tf;
+    float eps;
+};
+
+// 128-byte wide node: one L2 line.  Child i's box is
+// origin + q * 2^(e-127) per axis, with q the 16-bit lower/upper bounds.
+struct __align__(128) BVH8Node {
+    float ox, oy, oz;
+    uint32_t child_base;             // first internal child node
+    uint32_t prim_base;              // first leaf primitive slot
+    uint8_t ex, ey, ez, imask;       // exponents; bit i: child i is internal
+    uint8_t meta[8];                 // internal: rank; leaf: (count-1)<<5 | offset; 0xff: empty
+    uint16_t qlo[3][8];
+    uint16_t qhi[3][8];
+};
+static_assert(sizeof(BVH8Node) == 128, "BVH8 node must fill one 128-byte line");
+
+// Leaf primitive slot: 3 float4.  Triangle: (v0, id) (v1, -) (v2, -).
+// Sphere: (center, id | kSphereBit) (radius, eps, -, -) (-).
+struct DevScene {
+    int n_vol;
+    DevVolume vol[kMaxVol];
+    int np;
+    float glo[3], ghi[3];
+    DevPartition part[kMaxPart];
+    int integrate;
+    float step, march_eps, epsilon, opaque_alpha, rate;
+    // geometry
+    const BVH8Node *nodes;
+    const float4 *slots;
+    int64_t n_tri, n_sph;
+    int n_tri_sets, n_sph_sets;
+    DevTriSet tri_sets[4];
+    DevSphSet sph_sets[4];
+    const DevTF *tfs;
+    const float4 *ao;                // 256 x (cos 2pi u, sin 2pi u, sqrt(1-v), sqrt(v))
+};
+
+// 64-byte queue record.
+struct __align__(16) DRay {
+    float4 o;                        // origin, t
+    float4 d;                        // direction, tMax
+    float4 c;                        // r g b o
+    int4 m;                          // x, y, meta (type | part<<4 | job<<12), spare
+};
+__host__ __device__ inline int ray_type(int meta) { return meta & 0xf; }
+__host__ __device__ inline int ray_part(int meta) { return (meta >> 4) & 0xff; }
+__host__ __device__ inline int ray_job(int meta) { return (meta >> 12) & 0xfffff; }
+__host__ __device__ inline int make_meta(int type, int part, int job) { return type | (part << 4) | (job << 12); }
+
+// Per-frame constants: camera and lighting of one render job.
+struct DevCamera {
+    float3 eye, center, vr, vu, vdir;
+    float off_x, off_y, scaling;
+    int ortho;
+    int width, height;
+};
+struct DevLights {
+    int n;
+    float3 l[GXY_MAX_LIGHTS];
+    int type[GXY_MAX_LIGHTS];
+    float Ka, Kd;
+    int n_ao;
+    float ao_radius;
+    int shadows;
+};
+
+struct DevCounters {
+    unsigned long long primary, shadow, ao, segments, handoffs, terminated, dropped, kept, samples, nodes, tri_tests,
+        sph_tests, enqueued;
+    int overflow;        // a queue or a traversal stack ran out of room
+    int pad;
+};
+
+// ------------------------------------------------------------ vector math
+struct V3 {
+    float x, y, z;
+};
+__device__ __forceinline__ V3 v3(float x, float y, float z) { return V3{x, y, z}; }
+__device__ __forceinline__ V3 operator+(V3 a, V3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+__device__ __forceinline__ V3 operator-(V3 a, V3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+__device__ __forceinline__ V3 operator*(float s, V3 a) { return {s * a.x, s * a.y, s * a.z}; }
+__device__ __forceinline__ float dot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ V3 cross(V3 a, V3 b) {
+    return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+__device__ __forceinline__ V3 neg(V3 a) { return {-a.x, -a.y, -a.z}; }
+__device__ __forceinline__ V3 nrm(V3 a) {   // v * (1/sqrt(v.v)); zero stays zero
+    float l2 = dot(a, a);
+    if (l2 == 0.0f) return a;
+    float inv = 1.0f / sqrtf(l2);
+    return inv * a;
+}
+__device__ __forceinline__ float fmin_(float a, float b) { return (b < a) ? b : a; }   // std::min
+__device__ __forceinline__ float fmax_(float a, float b) { return (a < b) ? b : a; }   // std::max
+
+// ------------------------------------------------------ transfer function
+// Piecewise-linear lookup over 256 entries (NaN -> 0, clamp outside range).
+__device__ __forceinline__ float tf_opacity(const DevTF &tf, float v) {
+    if (isnan(v)) return 0.0f;
+    if (v <= tf.r0) return tf.opac[0];
+    if (v >= tf.r1) return tf.opac[255];
+    float f = (v - tf.r0) / (tf.r1 - tf.r0) * 255.0f;
+    int i = (int)floorf(f);
+    i = i > 254 ? 254 : (i < 0 ? 0 : i);
+    float rem = f - (float)i;
+    return (1.0f - rem) * tf.opac[i] + rem * tf.opac[i + 1];
+}
+__device__ __forceinline__ V3 tf_color(const DevTF &tf, float v) {
+    if (isnan(v)) return v3(0, 0, 0);
+    const float *c = tf.colors;
+    if (v <= tf.r0) return v3(c[0], c[1], c[2]);
+    if (v >= tf.r1) return v3(c[765], c[766], c[767]);
+    float f = (v - tf.r0) / (tf.r1 - tf.r0) * 255.0f;
+    int i = (int)floorf(f);
+    i = i > 254 ? 254 : (i < 0 ? 0 : i);
+    float rem = f - (float)i;
+    float a = 1.0f - rem;
+    return v3(a * c[3 * i] + rem * c[3 * i + 3], a * c[3 * i + 1] + rem * c[3 * i + 4],
+              a * c[3 * i + 2] + rem * c[3 * i + 5]);
+}
+
+// ---------------------------------------------------------------- volume
+// Trilinear sample of the dataset grid at world point p, clamped to the grid.
+__device__ __forceinline__ float vol_sample(const DevVolume &v, V3 p) {
+    float gx = (p.x - v.ox) / v.dx;
+    float gy = (p.y - v.oy) / v.dy;
+    float gz = (p.z - v.oz) / v.dz;
+    if (!(gx >= 0.0f)) gx = 0.0f;
+    if (!(gy >= 0.0f)) gy = 0.0f;
+    if (!(gz >= 0.0f)) gz = 0.0f;
+    if (gx > v.ux) gx = v.ux;
+    if (gy > v.uy) gy = v.uy;
+    if (gz > v.uz) gz = v.uz;
+    int ix = (int)gx, iy = (int)gy, iz = (int)gz;
+    float fx = gx - (float)ix, fy = gy - (float)iy, fz = gz - (float)iz;
+    size_t sy = (size_t)v.nx, sz = (size_t)v.nx * (size_t)v.ny;
+    const float *b = v.data + (size_t)iz * sz + (size_t)iy * sy + (size_t)ix;
+    float v000 = __ldg(b), v100 = __ldg(b + 1), v010 = __ldg(b + sy), v110 = __ldg(b + sy + 1);
+    float v001 = __ldg(b + sz), v101 = __ldg(b + sz + 1), v011 = __ldg(b + sz + sy), v111 = __ldg(b + sz + sy + 1);
+    float ax = 1.0f - fx;
+    float v00 = ax * v000 + fx * v100;
+    float v10 = ax * v010 + fx * v110;
+    float v01 = ax * v001 + fx * v101;
+    float v11 = ax * v011 + fx * v111;
+    float ay = 1.0f - fy;
+    float v0 = ay * v00 + fy * v10;
+    float v1 = ay * v01 + fy * v11;
+    return (1.0f - fz) * v0 + fz * v1;
+}
+
+// Same sample, with the 8 corner values of the last cell kept in registers:
+// consecutive half-voxel steps usually stay in one cell.
+struct CellCache {
+    int ix, iy, iz;
+    float c[8];
+};
+__device__ __forceinline__ float vol_sample_cached(const DevVolume &v, V3 p, CellCache &cc) {
+    float gx = (p.x - v.ox) / v.dx;
+    float gy = (p.y - v.oy) / v.dy;
+    float gz = (p.z - v.oz) / v.dz;
+    if (!(gx >= 0.0f)) gx = 0.0f;
+    if (!(gy >= 0.0f)) gy = 0.0f;
+    if (!(gz >= 0.0f)) gz = 0.0f;
+    if (gx > v.ux) gx = v.ux;
+    if (gy > v.uy) gy = v.uy;
+    if (gz > v.uz) gz = v.uz;
+    int ix = (int)gx, iy = (int)gy, iz = (int)gz;
+    if (ix != cc.ix || iy != cc.iy || iz != cc.iz) {
+        size_t sy = (size_t)v.nx, sz = (size_t)v.nx * (size_t)v.ny;
+        const float *b = v.data + (size_t)iz * sz + (size_t)iy * sy + (size_t)ix;
+        cc.c[0] = __ldg(b); cc.c[1] = __ldg(b + 1); cc.c[2] = __ldg(b + sy); cc.c[3] = __ldg(b + sy + 1);
+        cc.c[4] = __ldg(b + sz); cc.c[5] = __ldg(b + sz + 1); cc.c[6] = __ldg(b + sz + sy);
+        cc.c[7] = __ldg(b + sz + sy + 1);
+        cc.ix = ix; cc.iy = iy; cc.iz = iz;
+    }
+    float fx = gx - (float)ix, fy = gy - (float)iy, fz = gz - (float)iz;
+    float ax = 1.0f - fx;
+    float v00 = ax * cc.c[0] + fx * cc.c[1];
+    float v10 = ax * cc.c[2] + fx * cc.c[3];
+    float v01 = ax * cc.c[4] + fx * cc.c[5];
+    float v11 = ax * cc.c[6] + fx * cc.c[7];
+    float ay = 1.0f - fy;
+    float v0 = ay * v00 + fy * v10;
+    float v1 = ay * v01 + fy * v11;
+    return (1.0f - fz) * v0 + fz * v1;
+}
+
+// Central-difference gradient, one grid spacing either side.
+__device__ __forceinline__ V3 vol_gradient(const DevVolume &v, V3 p) {
+    V3 g;
+    g.x = (vol_sample(v, v3(p.x + v.dx, p.y, p.z)) - vol_sample(v, v3(p.x - v.dx, p.y, p.z))) / (2.0f * v.dx);
+    g.y = (vol_sample(v, v3(p.x, p.y + v.dy, p.z)) - vol_sample(v, v3(p.x, p.y - v.dy, p.z))) / (2.0f * v.dy);
+    g.z = (vol_sample(v, v3(p.x, p.y, p.z + v.dz)) - vol_sample(v, v3(p.x, p.y, p.z - v.dz))) / (2.0f * v.dz);
+    return g;
+}
+
+// -------------------------------------------------------------- primitives
+// Moller-Trumbore; caller checks t against (t0, tfar).
+__device__ __forceinline__ bool tri_test(V3 org, V3 dir, V3 v0, V3 v1, V3 v2, float &t, float &u, float &v) {
+    V3 e1 = v1 - v0, e2 = v2 - v0;
+    V3 pv = cross(dir, e2);
+    float det = dot(e1, pv);
+    if (det == 0.0f) return false;
+    float inv = 1.0f / det;
+    V3 tv = org - v0;
+    u = dot(tv, pv) * inv;
+    if (u < 0.0f || u > 1.0f) return false;
+    V3 qv = cross(tv, e1);
+    v = dot(dir, qv) * inv;
+    if (v < 0.0f || u + v > 1.0f) return false;
+    t = dot(e2, qv) * inv;
+    return true;
+}
+
+// Data-driven sphere: t_in if in (t0, tfar), else t_out if in (t0+eps, tfar).
+__device__ __forceinline__ bool sph_test(V3 org, V3 dir, V3 c, float r, float eps, float t0, float tfar, float &t) {
+    float approx = dot(c - org, dir);
+    V3 close = org + approx * dir;
+    V3 A = c - close;
+    float a = dot(dir, dir);
+    float b = 2.0f * dot(dir, A);
+    float cc = dot(A, A) - r * r;
+    float rad = b * b - 4.0f * a * cc;
+    if (rad < 0.0f) return false;
+    float srad = sqrtf(rad);
+    float r2a = 1.0f / (2.0f * a);
+    float tin = (b - srad) * r2a + approx;
+    float tout = (b + srad) * r2a + approx;
+    if (tin > t0 && tin < tfar) { t = tin; return true; }
+    if (tout > t0 + eps && tout < tfar) { t = tout; return true; }
+    return false;
+}
+
+// --------------------------------------------------------- BVH8 traversal
+struct GeoHit {
+    float t, u, v;
+    uint32_t prim;   // global primitive id (with kSphereBit for spheres)
+};
+
+// Closest hit in (t0, tfar) with ties broken by the smaller primitive id.
+// ANY: return at the first accepted hit.  Returns whether a hit was found;
+// node/prim visit counts are added to *nodes / *prims.
+template <bool ANY>
+__device__ __noinline__ bool bvh_closest(const DevScene &S, V3 org, V3 dir, float t0, float tfar, GeoHit &h,
+                                         unsigned &nodes, unsigned &tris, unsigned &sphs, int &ovf) {
+    if (!S.nodes) return false;
+    const float idx = 1.0f / dir.x, idy = 1.0f / dir.y, idz = 1.0f / dir.z;
+    const bool sx = idx < 0.0f, sy = idy < 0.0f, sz = idz < 0.0f;
+    h.t = tfar;
+    h.prim = 0xffffffffu;
+    bool found = false;
+    // stack of (node index, entry distance)
+    uint2 stack[64];
+    int sp = 0;
+    uint32_t cur = 0;
+    float cur_tn = t0;
+    for (;;) {
+        if (cur_tn <= h.t) {
+            const float4 *np = reinterpret_cast<const float4 *>(S.nodes + cur);
+            float4 n0 = __ldg(np), n1 = __ldg(np + 1);
+            uint32_t child_base = __float_as_uint(n0.w);
+            uint32_t prim_base = __float_as_uint(n1.x);
+            uint32_t e4 = __float_as_uint(n1.y);
+            uint32_t meta_lo = __float_as_uint(n1.z), meta_hi = __float_as_uint(n1.w);
+            float4 q[6];
+#pragma unroll
+            for (int k = 0; k < 6; k++) q[k] = __ldg(np + 2 + k);
+            nodes++;
+            const uint16_t *ql = reinterpret_cast<const uint16_t *>(q);   // qlo[3][8] then qhi[3][8]
+            float scx = __uint_as_float((e4 & 0xffu) << 23);
+            float scy = __uint_as_float(((e4 >> 8) & 0xffu) << 23);
+            float scz = __uint_as_float(((e4 >> 16) & 0xffu) << 23);
+            uint32_t imask = e4 >> 24;
+            // t = (origin + q*s - org) * id = q*(s*id) + (origin-org)*id
+            float ax = scx * idx, bx = (n0.x - org.x) * idx;
+            float ay = scy * idy, by = (n0.y - org.y) * idy;
+            float az = scz * idz, bz = (n0.z - org.z) * idz;
+            float tn_c[8];
+            uint32_t hitmask = 0;
+#pragma unroll
+            for (int i = 0; i < 8; i++) {
+                uint32_t mb = (i < 4 ? meta_lo >> (8 * i) : meta_hi >> (8 * (i - 4))) & 0xffu;
+                float lx = (float)ql[0 * 8 + i], ly = (float)ql[1 * 8 + i], lz = (float)ql[2 * 8 + i];
+                float hx = (float)ql[24 + 0 * 8 + i], hy = (float)ql[24 + 1 * 8 + i], hz = (float)ql[24 + 2 * 8 + i];
+                float txa = __fmaf_rn(sx ? hx : lx, ax, bx), txb = __fmaf_rn(sx ? lx : hx, ax, bx);
+                float tya = __fmaf_rn(sy ? hy : ly, ay, by), tyb = __fmaf_rn(sy ? ly : hy, ay, by);
+                float tza = __fmaf_rn(sz ? hz : lz, az, bz), tzb = __fmaf_rn(sz ? lz : hz, az, bz);
+                float tn = fmaxf(fmaxf(txa, tya), fmaxf(tza, t0));
+                float tf = fminf(fminf(txb, tyb), fminf(tzb, h.t));
+                tn_c[i] = tn;
+                if (mb != 0xffu && tn <= tf * 1.00000048f + 1e-30f) hitmask |= 1u << i;
+            }
+            // leaf children first (they can shrink h.t before internal children are ordered)
+            uint32_t leafhits = hitmask & ~imask;
+            while (leafhits) {
+                int i = __ffs(leafhits) - 1;
+                leafhits &= leafhits - 1;
+                uint32_t mb = (i < 4 ? meta_lo >> (8 * i) : meta_hi >> (8 * (i - 4))) & 0xffu;
+                uint32_t s = prim_base + (mb & 31u);
+                uint32_t cnt = (mb >> 5) + 1;
+                for (uint32_t k = 0; k < cnt; k++, s++) {
+                    const float4 *rp = S.slots + 3 * (size_t)s;
+                    float4 r0 = __ldg(rp), r1 = __ldg(rp + 1);
+                    uint32_t id = __float_as_uint(r0.w);
+                    float t, u = 0.0f, v = 0.0f;
+                    bool ok;
+                    if (id & kSphereBit) {
+                        sphs++;
+                        ok = sph_test(org, dir, v3(r0.x, r0.y, r0.z), r1.x, r1.y, t0, tfar, t);
+                    } else {
+                        tris++;
+                        float4 r2 = __ldg(rp + 2);
+                        ok = tri_test(org, dir, v3(r0.x, r0.y, r0.z), v3(r1.x, r1.y, r1.z), v3(r2.x, r2.y, r2.z), t, u,
+                                      v) &&
+                             t > t0 && t < tfar;
+                    }
+                    if (ok && (t < h.t || (t == h.t && id < h.prim))) {
+                        h.t = t; h.u = u; h.v = v; h.prim = id;
+                        found = true;
+                        if (ANY) return true;
+                    }
+                }
+            }
+            // internal children: nearest first, the rest pushed far to near
+            uint32_t inner = hitmask & imask;
+            if (inner) {
+                uint32_t idxs[8];
+                float tns[8];
+                int k = 0;
+                while (inner) {
+                    int i = __ffs(inner) - 1;
+                    inner &= inner - 1;
+                    uint32_t mb = (i < 4 ? meta_lo >> (8 * i) : meta_hi >> (8 * (i - 4))) & 0xffu;
+                    uint32_t ci = child_base + mb;
+                    float tn = tn_c[i];
+                    // insertion into descending order
+                    int j = k++;
+                    while (j > 0 && tns[j - 1] < tn) { tns[j] = tns[j - 1]; idxs[j] = idxs[j - 1]; j--; }
+                    tns[j] = tn;
+                    idxs[j] = ci;
+                }
+                for (int j = 0; j < k - 1; j++) {
+                    if (sp < 64) stack[sp++] = make_uint2(idxs[j], __float_as_uint(tns[j]));
+                    else ovf = 1;   // reported as GXY_ERR_OVERFLOW by the host
+                }
+                cur = idxs[k - 1];
+                cur_tn = tns[k - 1];
+                continue;
+            }
+        }
+        if (sp == 0) break;
+        uint2 e = stack[--sp];
+        cur = e.x;
+        cur_tn = __uint_as_float(e.y);
+    }
+    return found;
+}
+
+}  // namespace gxy

@@ -1,0 +1,1393 @@
+// render.cu -- scene commit, the fused wavefront kernels and the C ABI of
+// libgxy_gpu.so.
+//
+// Frame path (gxy_gpu_render): one launch per queue generation.
+//   generation 0: k_frame<primary> -- one thread per pixel builds the camera
+//     ray (Camera::generate_initial_rays, Camera.cpp:528-829) for every
+//     partition whose box the ray enters first, then traces it.
+//   generation g>0: k_frame<queue> over the previous generation's queue.
+// In both, each ray is traced (trace_core), shaded if it is a primary
+// surface hit (ambient, AO spawn, diffuse, shadow spawn), classified and
+// routed in the same thread: a TERMINATED contribution is added to the
+// framebuffer with one float4 atomic, a ray handed to a neighbour partition
+// or kept for re-tracing and every spawned secondary is appended to the next
+// generation's queue through one warp-aggregated atomic per warp.  This is
+// the device form of processRays_task::work (Renderer.cpp:511-651), where
+// Galaxy's MPI partitions become partitions of one device-resident scene.
+//
+// RayList path (gxy_gpu_trace_raylist etc.): the same per-ray code over the
+// 25-array RayList layout, one kernel per ISPC export, for ray-level parity.
+#include <cub/cub.cuh>
+
+#include <cfloat>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "gxy_dev.cuh"
+#include "gxy_host.h"
+#include "trace.cuh"
+
+namespace gxy {
+
+// ================================================================ errors
+static thread_local std::string g_err;
+int set_error(int code, const std::string &msg) {
+    g_err = msg;
+    return code;
+}
+const std::string &last_error() { return g_err; }
+
+// ================================================================= arena
+int DeviceArena::alloc(void **p, size_t bytes) {
+    std::lock_guard<std::mutex> lk(mu_);
+    if (budget_ && in_use_ + bytes > budget_)
+        return set_error(GXY_ERR_OOM, "HBM budget exceeded: " + std::to_string(in_use_ + bytes) + " > " +
+                                          std::to_string(budget_));
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return set_error(GXY_ERR_OOM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    }
+    in_use_ += bytes;
+    live_.emplace_back(*p, bytes);
+    return GXY_OK;
+}
+void DeviceArena::free(void *p) {
+    if (!p) return;
+    std::lock_guard<std::mutex> lk(mu_);
+    for (size_t i = 0; i < live_.size(); i++)
+        if (live_[i].first == p) {
+            in_use_ -= live_[i].second;
+            live_[i] = live_.back();
+            live_.pop_back();
+            cudaFree(p);
+            return;
+        }
+}
+size_t DeviceArena::in_use() const {
+    std::lock_guard<std::mutex> lk(mu_);
+    return in_use_;
+}
+size_t DeviceArena::budget() const {
+    std::lock_guard<std::mutex> lk(mu_);
+    return budget_;
+}
+void DeviceArena::set_budget(size_t b) {
+    std::lock_guard<std::mutex> lk(mu_);
+    budget_ = b;
+}
+bool DeviceArena::would_fit(size_t bytes) const {
+    std::lock_guard<std::mutex> lk(mu_);
+    return !budget_ || in_use_ + bytes <= budget_;
+}
+DeviceArena &arena() {
+    static DeviceArena a;
+    return a;
+}
+
+static bool g_init = false;
+static int g_device = 0;
+
+// ========================================================== host helpers
+struct F3h {
+    float x, y, z;
+};
+static inline F3h h3(float x, float y, float z) { return {x, y, z}; }
+static inline F3h hadd(F3h a, F3h b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+static inline F3h hmul(float s, F3h a) { return {s * a.x, s * a.y, s * a.z}; }
+static inline F3h hcross(F3h a, F3h b) { return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
+// Galaxy's vec3f normalize (src/data/dtypes.h:164): len in float, 1.0/len in double.
+static inline F3h gnorm(F3h a) {
+    float l = std::sqrt(a.x * a.x + a.y * a.y + a.z * a.z);
+    if (l != 0.0f) {
+        float d = (float)(1.0 / (double)l);
+        a.x *= d; a.y *= d; a.z *= d;
+    }
+    return a;
+}
+
+// Camera set-up of Camera::generate_initial_rays (Camera.cpp:542-582).
+static DevCamera setup_camera(const gxy_camera &c) {
+    DevCamera C;
+    F3h veye = h3(c.eye[0], c.eye[1], c.eye[2]);
+    F3h vu = h3(c.up[0], c.up[1], c.up[2]);
+    F3h vdir = h3(c.dir[0], c.dir[1], c.dir[2]);
+    F3h center;
+    C.ortho = c.aov == 0.0f;
+    if (C.ortho) {
+        center = hadd(veye, vdir);
+        vdir = gnorm(vdir);
+    } else {
+        float d = (float)(1.0 / tan(2 * 3.1415926 * (c.aov / 2.0) / 360.0));
+        vdir = gnorm(vdir);
+        center = hadd(veye, hmul(d, vdir));
+    }
+    F3h vr = gnorm(hcross(vdir, vu));
+    vu = gnorm(hcross(vr, vdir));
+    int w = c.width, h = c.height;
+    float pixel_scaling = (float)((((w < h) ? w : h) - 1.0) / 2.0);
+    C.off_x = (float)((w - 1) / 2.0);
+    C.off_y = (float)((h - 1) / 2.0);
+    C.scaling = (float)(1.0 / pixel_scaling);
+    C.eye = make_float3(veye.x, veye.y, veye.z);
+    C.center = make_float3(center.x, center.y, center.z);
+    C.vr = make_float3(vr.x, vr.y, vr.z);
+    C.vu = make_float3(vu.x, vu.y, vu.z);
+    C.vdir = make_float3(vdir.x, vdir.y, vdir.z);
+    C.width = w;
+    C.height = h;
+    return C;
+}
+
+static int setup_lights(const gxy_lighting &l, DevLights &L) {
+    if (l.n_lights < 0 || l.n_lights > GXY_MAX_LIGHTS) return set_error(GXY_ERR_INVALID, "bad light count");
+    memset(&L, 0, sizeof L);
+    L.n = l.n_lights;
+    for (int i = 0; i < l.n_lights; i++) {
+        if (l.types[i] == GXY_LIGHT_CAMERA)
+            return set_error(GXY_ERR_INVALID, "camera-relative light not resolved (gxy_resolve_lights)");
+        L.l[i] = make_float3(l.lights[i][0], l.lights[i][1], l.lights[i][2]);
+        L.type[i] = l.types[i];
+    }
+    L.Ka = l.Ka;
+    L.Kd = l.Kd;
+    L.n_ao = l.n_ao < 0 ? 0 : l.n_ao;
+    L.ao_radius = l.ao_radius;
+    L.shadows = l.shadows ? 1 : 0;
+    if (L.n_ao > 64) return set_error(GXY_ERR_INVALID, "at most 64 AO rays per hit");
+    return GXY_OK;
+}
+
+// AO tables: radical inverse base 2 / base 3 in float32 rounded through
+// "%.6g" (the 256-entry randomU / randomV tables of src/renderer/UV.ih),
+// stored with the derived quantities the AO direction needs.
+static void ao_tables(float4 *out) {
+    char buf[64];
+    for (int i = 0; i < 256; i++) {
+        float r[2];
+        for (int b = 0; b < 2; b++) {
+            int base = b ? 3 : 2;
+            float inv = 1.0f / (float)base, f = inv, acc = 0.0f;
+            int k = i;
+            while (k > 0) {
+                acc = acc + f * (float)(k % base);
+                f = f * inv;
+                k /= base;
+            }
+            snprintf(buf, sizeof buf, "%.6g", (double)acc);
+            r[b] = strtof(buf, nullptr);
+        }
+        float a = 6.28318530717958647692f * r[0];
+        out[i] = make_float4(cosf(a), sinf(a), sqrtf(1.0f - r[1]), sqrtf(r[1]));
+    }
+}
+
+// ================================================================ scene
+struct Scene {
+    DevScene S;
+    gxy_partition_info pinfo;
+    std::vector<void *> owned;
+    BVHInfo bvh;
+    DRay *qa = nullptr, *qb = nullptr;
+    size_t qcap = 0;
+    unsigned int *qcount = nullptr;     // [0],[1] counts of the two queues
+    DevCounters *ctr = nullptr;
+    DevCounters last{};
+    int64_t bounces = 0;
+    float *fbtmp = nullptr;
+    size_t fbtmp_elems = 0;
+    std::mutex mu;                      // one render at a time per scene
+    ~Scene() {
+        for (void *p : owned) arena().free(p);
+        arena().free(qa);
+        arena().free(qb);
+        arena().free(qcount);
+        arena().free(ctr);
+        arena().free(fbtmp);
+        if (bvh.nodes_ptr) arena().free(bvh.nodes_ptr);
+        if (bvh.slots_ptr) arena().free(bvh.slots_ptr);
+    }
+    int upload(const void *src, size_t bytes, void **dst) {
+        int rc = arena().alloc(dst, bytes ? bytes : 16);
+        if (rc) return rc;
+        owned.push_back(*dst);
+        if (bytes) CK(cudaMemcpy(*dst, src, bytes, cudaMemcpyHostToDevice));
+        return GXY_OK;
+    }
+};
+
+// Brick partitions and neighbours: Volume::partition (Volume.cpp:133-172,
+// 371-390) on the first volume's grid, or an even split of the geometry box.
+static void make_partitions(const gxy_scene_desc &d, const std::vector<float> &geo_box, DevScene &S) {
+    int PX = d.partitions[0] < 1 ? 1 : d.partitions[0];
+    int PY = d.partitions[1] < 1 ? 1 : d.partitions[1];
+    int PZ = d.partitions[2] < 1 ? 1 : d.partitions[2];
+    S.np = PX * PY * PZ;
+    for (int k = 0; k < PZ; k++)
+        for (int j = 0; j < PY; j++)
+            for (int i = 0; i < PX; i++) {
+                int p = i + j * PX + k * PX * PY;
+                DevPartition &P = S.part[p];
+                if (d.n_volumes > 0) {
+                    const gxy_volume_vis &v = d.volumes[0];
+                    int ni = v.counts[0] - 2, nj = v.counts[1] - 2, nk = v.counts[2] - 2;
+                    int di = ni / PX, dj = nj / PY, dk = nk / PZ;
+                    int off[3] = {1 + i * di, 1 + j * dj, 1 + k * dk};
+                    int cnt[3] = {1 + ((i == PX - 1) ? ni - off[0] : di), 1 + ((j == PY - 1) ? nj - off[1] : dj),
+                                  1 + ((k == PZ - 1) ? nk - off[2] : dk)};
+                    for (int a = 0; a < 3; a++) {
+                        P.lo[a] = v.origin[a] + (off[a] * v.deltas[a]);
+                        P.hi[a] = P.lo[a] + (cnt[a] - 1) * v.deltas[a];
+                    }
+                    if (p == 0) {
+                        int gc[3] = {ni, nj, nk};
+                        for (int a = 0; a < 3; a++) {
+                            S.glo[a] = v.origin[a] + v.deltas[a];
+                            S.ghi[a] = S.glo[a] + (gc[a] - 1) * v.deltas[a];
+                        }
+                    }
+                } else {
+                    const float *g = geo_box.data();
+                    float ex = (g[3] - g[0]) / PX, ey = (g[4] - g[1]) / PY, ez = (g[5] - g[2]) / PZ;
+                    P.lo[0] = g[0] + i * ex; P.lo[1] = g[1] + j * ey; P.lo[2] = g[2] + k * ez;
+                    P.hi[0] = i == PX - 1 ? g[3] : g[0] + (i + 1) * ex;
+                    P.hi[1] = j == PY - 1 ? g[4] : g[1] + (j + 1) * ey;
+                    P.hi[2] = k == PZ - 1 ? g[5] : g[2] + (k + 1) * ez;
+                    for (int a = 0; a < 3; a++) { S.glo[a] = g[a]; S.ghi[a] = g[3 + a]; }
+                }
+                P.nb[0] = (i > 0) ? p - 1 : -1;
+                P.nb[1] = (i < PX - 1) ? p + 1 : -1;
+                P.nb[2] = (j > 0) ? p - PX : -1;
+                P.nb[3] = (j < PY - 1) ? p + PX : -1;
+                P.nb[4] = (k > 0) ? p - PX * PY : -1;
+                P.nb[5] = (k < PZ - 1) ? p + PX * PY : -1;
+            }
+}
+
+static float sphere_radius(const gxy_particles_vis &p, int64_t i) {   // DataDrivenSpheres.ispc:104-116
+    if (p.value0 != p.value1 && p.data) {
+        float d = (p.data[i] - p.value0) / (p.value1 - p.value0);
+        if (d > 1) return p.radius1;
+        else if (d < 0) return p.radius0;
+        else return p.radius0 + d * (p.radius1 - p.radius0);
+    }
+    return p.radius0;
+}
+static float sphere_epsilon(float r0) {   // DataDrivenSpheres.ispc:211-220
+    float e = logf(r0);
+    if (e < 0.f) e = -1.f / e;
+    if (e > r0 / 100.0f) e = r0 / 100.0f;
+    return e;
+}
+
+static void tf_to_dev(const gxy_tf &t, DevTF &d) {
+    memcpy(d.colors, t.colors, sizeof d.colors);
+    memcpy(d.opac, t.opacities, sizeof d.opac);
+    d.r0 = t.range[0];
+    d.r1 = t.range[1];
+    d.pad0 = d.pad1 = 0;
+}
+
+static int commit(const gxy_scene_desc *d, Scene *sc) {
+    DevScene &S = sc->S;
+    memset(&S, 0, sizeof S);
+    if (d->n_volumes < 0 || d->n_volumes > kMaxVol) return set_error(GXY_ERR_INVALID, "bad volume count");
+    if (d->n_triangle_sets < 0 || d->n_triangle_sets > 4 || d->n_particle_sets < 0 || d->n_particle_sets > 4)
+        return set_error(GXY_ERR_INVALID, "at most 4 triangle sets and 4 particle sets");
+    int np = (d->partitions[0] < 1 ? 1 : d->partitions[0]) * (d->partitions[1] < 1 ? 1 : d->partitions[1]) *
+             (d->partitions[2] < 1 ? 1 : d->partitions[2]);
+    if (np > kMaxPart) return set_error(GXY_ERR_INVALID, "too many partitions");
+    float rate = d->sampling_rate > 0 ? d->sampling_rate : 1.0f;
+    S.rate = rate;
+    S.opaque_alpha = d->opaque_alpha > 0 ? d->opaque_alpha : 0.999f;
+    S.epsilon = d->epsilon;
+    std::vector<DevTF> tfs;
+    S.step = -1;
+    int rc;
+    for (int m = 0; m < d->n_volumes; m++) {
+        const gxy_volume_vis &v = d->volumes[m];
+        if (!v.samples || v.counts[0] < 2 || v.counts[1] < 2 || v.counts[2] < 2)
+            return set_error(GXY_ERR_INVALID, "volume needs samples and counts >= 2");
+        if (v.n_slices < 0 || v.n_slices > GXY_MAX_SLICES || v.n_isovalues < 0 || v.n_isovalues > GXY_MAX_ISOVALUES)
+            return set_error(GXY_ERR_INVALID, "too many slices or isovalues");
+        DevVolume &V = S.vol[m];
+        size_t nvox = (size_t)v.counts[0] * v.counts[1] * v.counts[2];
+        void *p;
+        if ((rc = sc->upload(v.samples, nvox * sizeof(float), &p))) return rc;
+        V.data = (const float *)p;
+        V.nx = v.counts[0]; V.ny = v.counts[1]; V.nz = v.counts[2];
+        V.ox = v.origin[0]; V.oy = v.origin[1]; V.oz = v.origin[2];
+        V.dx = v.deltas[0]; V.dy = v.deltas[1]; V.dz = v.deltas[2];
+        V.ux = nextafterf((float)(V.nx - 1), 0.0f);
+        V.uy = nextafterf((float)(V.ny - 1), 0.0f);
+        V.uz = nextafterf((float)(V.nz - 1), 0.0f);
+        V.tf = (int)tfs.size();
+        DevTF t;
+        tf_to_dev(v.tf, t);
+        tfs.push_back(t);
+        V.n_slices = v.n_slices;
+        for (int k = 0; k < v.n_slices; k++)
+            V.slices[k] = make_float4(v.slices[k][0], v.slices[k][1], v.slices[k][2], v.slices[k][3]);
+        V.n_iso = v.n_isovalues;
+        for (int k = 0; k < v.n_isovalues; k++) V.iso[k] = v.isovalues[k];
+        V.volume_render = v.volume_render ? 1 : 0;
+        if (v.volume_render || v.n_isovalues > 0) S.integrate = 1;
+        // samplingStep = smallest spacing; step = samplingStep / rate (TraceRays.ispc:342-361)
+        float ss = fminf(v.deltas[0], fminf(v.deltas[1], v.deltas[2]));
+        float st = ss / rate;
+        if (S.step < 0 || S.step > st) {
+            S.step = st;
+            S.march_eps = d->epsilon * st;
+        }
+    }
+    S.n_vol = d->n_volumes;
+    // geometry
+    std::vector<float> gbox = {FLT_MAX, FLT_MAX, FLT_MAX, -FLT_MAX, -FLT_MAX, -FLT_MAX};
+    int64_t prim = 0;
+    for (int s = 0; s < d->n_triangle_sets; s++) {
+        const gxy_triangles_vis &t = d->triangles[s];
+        DevTriSet &T = S.tri_sets[s];
+        T.prim_base = prim;
+        T.n = t.n_triangles;
+        void *p;
+        if ((rc = sc->upload(t.vertices, sizeof(float) * 3 * t.n_vertices, &p))) return rc;
+        T.vertices = (const float *)p;
+        if ((rc = sc->upload(t.indices, sizeof(int32_t) * 3 * t.n_triangles, &p))) return rc;
+        T.indices = (const int32_t *)p;
+        for (int64_t i = 0; i < 3 * t.n_triangles; i++)
+            if (t.indices[i] < 0 || t.indices[i] >= t.n_vertices)
+                return set_error(GXY_ERR_INVALID, "triangle index out of range");
+        if (t.normals) {
+            if ((rc = sc->upload(t.normals, sizeof(float) * 3 * t.n_vertices, &p))) return rc;
+            T.normals = (const float *)p;
+        }
+        if (t.data) {
+            if ((rc = sc->upload(t.data, sizeof(float) * t.n_vertices, &p))) return rc;
+            T.data = (const float *)p;
+        }
+        T.tf = (int)tfs.size();
+        DevTF tt;
+        tf_to_dev(t.tf, tt);
+        tfs.push_back(tt);
+        for (int64_t i = 0; i < t.n_vertices; i++)
+            for (int a = 0; a < 3; a++) {
+                gbox[a] = fminf(gbox[a], t.vertices[3 * i + a]);
+                gbox[3 + a] = fmaxf(gbox[3 + a], t.vertices[3 * i + a]);
+            }
+        prim += t.n_triangles;
+    }
+    S.n_tri = prim;
+    S.n_tri_sets = d->n_triangle_sets;
+    std::vector<float> radius;
+    for (int s = 0; s < d->n_particle_sets; s++) {
+        const gxy_particles_vis &q = d->particles[s];
+        DevSphSet &P = S.sph_sets[s];
+        P.prim_base = prim;
+        P.n = q.n;
+        void *p;
+        if ((rc = sc->upload(q.centers, sizeof(float) * 3 * q.n, &p))) return rc;
+        P.centers = (const float *)p;
+        if (q.data) {
+            if ((rc = sc->upload(q.data, sizeof(float) * q.n, &p))) return rc;
+            P.data = (const float *)p;
+        }
+        P.tf = (int)tfs.size();
+        DevTF tt;
+        tf_to_dev(q.tf, tt);
+        tfs.push_back(tt);
+        P.eps = sphere_epsilon(q.radius0);
+        for (int64_t i = 0; i < q.n; i++) {
+            float r = sphere_radius(q, i);
+            radius.push_back(r);
+            for (int a = 0; a < 3; a++) {
+                gbox[a] = fminf(gbox[a], q.centers[3 * i + a] - r);
+                gbox[3 + a] = fmaxf(gbox[3 + a], q.centers[3 * i + a] + r);
+            }
+        }
+        prim += q.n;
+    }
+    S.n_sph = prim - S.n_tri;
+    S.n_sph_sets = d->n_particle_sets;
+    if (d->has_box) gbox.assign(d->box, d->box + 6);
+    else if (prim == 0) gbox = {-1, -1, -1, 1, 1, 1};
+    make_partitions(*d, gbox, S);
+    void *p;
+    if (tfs.empty()) tfs.resize(1);
+    if ((rc = sc->upload(tfs.data(), tfs.size() * sizeof(DevTF), &p))) return rc;
+    S.tfs = (const DevTF *)p;
+    float4 ao[256];
+    ao_tables(ao);
+    if ((rc = sc->upload(ao, sizeof ao, &p))) return rc;
+    S.ao = (const float4 *)p;
+    float *drad = nullptr;
+    if (!radius.empty()) {
+        if ((rc = sc->upload(radius.data(), radius.size() * sizeof(float), &p))) return rc;
+        drad = (float *)p;
+    }
+    if ((rc = build_bvh8(S, drad, arena(), 0, sc->bvh))) return rc;
+    CK(cudaDeviceSynchronize());
+    if ((rc = arena().alloc((void **)&sc->qcount, 16 * sizeof(unsigned int)))) return rc;
+    if ((rc = arena().alloc((void **)&sc->ctr, sizeof(DevCounters)))) return rc;
+    return GXY_OK;
+}
+
+// ============================================================== kernels
+constexpr int kThreads = 256;
+
+__device__ __forceinline__ void load_tfs(const DevScene &S, DevTF *sh) {
+    for (int m = 0; m < S.n_vol; m++) {
+        const float4 *src = reinterpret_cast<const float4 *>(S.tfs + S.vol[m].tf);
+        float4 *dst = reinterpret_cast<float4 *>(sh + m);
+        for (int i = threadIdx.x; i < (int)(sizeof(DevTF) / 16); i += blockDim.x) dst[i] = __ldg(src + i);
+    }
+    __syncthreads();
+}
+
+// Box::intersect (src/data/Box.cpp:107-150).
+__device__ __forceinline__ bool box_intersect(const float lo[3], const float hi[3], V3 org, V3 dir, float &tmin,
+                                              float &tmax) {
+    tmin = (lo[0] - org.x) / dir.x;
+    tmax = (hi[0] - org.x) / dir.x;
+    if (tmin > tmax) { float t = tmin; tmin = tmax; tmax = t; }
+    if (tmax < 0) return false;
+    float tymin = (lo[1] - org.y) / dir.y;
+    float tymax = (hi[1] - org.y) / dir.y;
+    if (tymin > tymax) { float t = tymin; tymin = tymax; tymax = t; }
+    if (tymax < 0) return false;
+    if ((tmin > tymax) || (tymin > tmax)) return false;
+    if (tymin > tmin) tmin = tymin;
+    if (tymax < tmax) tmax = tymax;
+    float tzmin = (lo[2] - org.z) / dir.z;
+    float tzmax = (hi[2] - org.z) / dir.z;
+    if (tzmin > tzmax) { float t = tzmin; tzmin = tzmax; tzmax = t; }
+    if (tzmax < 0) return false;
+    if ((tmin > tzmax) || (tzmin > tmax)) return false;
+    if (tzmin > tmin) tmin = tzmin;
+    if (tzmax < tmax) tmax = tzmax;
+    if (tmin < 0) tmin = 0;
+    return true;
+}
+
+// SpawnRays (Camera.cpp:403-441) for pixel (x, y): the ray and the mask of
+// partitions that emit it.
+__device__ __forceinline__ uint64_t camera_ray(const DevScene &S, const DevCamera &C, int x, int y, V3 &org, V3 &dir) {
+    float fx = ((float)x - C.off_x) * C.scaling;
+    float fy = ((float)y - C.off_y) * C.scaling;
+    V3 xy = v3(C.center.x + fx * C.vr.x + fy * C.vu.x, C.center.y + fx * C.vr.y + fy * C.vu.y,
+               C.center.z + fx * C.vr.z + fy * C.vu.z);
+    if (C.ortho) {
+        org = xy - v3(C.vdir.x, C.vdir.y, C.vdir.z);
+        dir = v3(C.vdir.x, C.vdir.y, C.vdir.z);
+    } else {
+        org = v3(C.eye.x, C.eye.y, C.eye.z);
+        V3 d = xy - org;
+        float l = sqrtf(d.x * d.x + d.y * d.y + d.z * d.z);
+        if (l != 0.0f) {
+            float s = (float)(1.0 / (double)l);
+            d.x *= s; d.y *= s; d.z *= s;
+        }
+        dir = d;
+    }
+    float gmin, gmax;
+    if (!box_intersect(S.glo, S.ghi, org, dir, gmin, gmax)) return 0;
+    uint64_t mask = 0;
+    for (int p = 0; p < S.np; p++) {
+        float lmin, lmax;
+        if (!box_intersect(S.part[p].lo, S.part[p].hi, org, dir, lmin, lmax)) continue;
+        float dd = fabsf(lmin) - fabsf(gmin);
+        if ((lmax >= 0) && (dd < 0.000001f) && (dd > -0.000001f)) mask |= 1ull << p;
+    }
+    return mask;
+}
+
+// Inclusive warp scan of v; returns the exclusive prefix, total in *tot.
+__device__ __forceinline__ unsigned warp_excl_scan(unsigned v, unsigned &tot) {
+    int lane = threadIdx.x & 31;
+    unsigned s = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        unsigned t = __shfl_up_sync(0xffffffffu, s, o);
+        if (lane >= o) s += t;
+    }
+    tot = __shfl_sync(0xffffffffu, s, 31);
+    return s - v;
+}
+
+__device__ __forceinline__ void put_ray(DRay *q, unsigned idx, V3 o, float t, V3 d, float tmax, float r, float g,
+                                        float b, float a, int x, int y, int meta) {
+    DRay *p = q + idx;
+    p->o = make_float4(o.x, o.y, o.z, t);
+    p->d = make_float4(d.x, d.y, d.z, tmax);
+    p->c = make_float4(r, g, b, a);
+    p->m = make_int4(x, y, meta, 0);
+}
+
+struct FrameArgs {
+    DevCamera cam;
+    DevLights L;
+    float *fb;
+    const DRay *qin;
+    unsigned nin;
+    DRay *qout;
+    unsigned *qout_count;
+    unsigned qcap;
+    DevCounters *ctr;
+};
+
+// One generation of the wavefront.  PRIMARY: generate camera rays from the
+// pixel index; otherwise read the input queue.
+template <bool PRIMARY, bool ANYSEC>
+__global__ void __launch_bounds__(kThreads) k_frame(DevScene S, FrameArgs A) {
+    __shared__ DevTF tfs[kMaxVol];
+    load_tfs(S, tfs);
+    const DevLights &L = A.L;
+    const int lane = threadIdx.x & 31;
+    const int64_t n_items = PRIMARY ? (int64_t)A.cam.width * A.cam.height : (int64_t)A.nin;
+    RayStats st;
+    unsigned long long c_prim = 0, c_sh = 0, c_ao = 0, c_seg = 0, c_hand = 0, c_term = 0, c_drop = 0, c_keep = 0,
+                       c_enq = 0;
+    int ovf = 0;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n_items; base += stride) {
+        int64_t i = base + threadIdx.x;
+        bool valid = i < n_items;
+        TraceIn in;
+        uint64_t pending = 0;
+        int x = 0, y = 0;
+        if (valid) {
+            if (PRIMARY) {
+                x = (int)(i % A.cam.width);
+                y = (int)(i / A.cam.width);
+                pending = camera_ray(S, A.cam, x, y, in.org, in.dir);
+                in.t = 0.0f;
+                in.tmax = FLT_MAX;
+                in.r = in.g = in.b = in.o = 0.0f;
+                in.type = GXY_RAY_PRIMARY;
+            } else {
+                const float4 *src = reinterpret_cast<const float4 *>(A.qin + i);
+                float4 a = __ldg(src), b = __ldg(src + 1), c = __ldg(src + 2);
+                int4 m = __ldg(reinterpret_cast<const int4 *>(src + 3));
+                in.org = v3(a.x, a.y, a.z);
+                in.t = a.w;
+                in.dir = v3(b.x, b.y, b.z);
+                in.tmax = b.w;
+                in.r = c.x; in.g = c.y; in.b = c.z; in.o = c.w;
+                x = m.x;
+                y = m.y;
+                in.type = ray_type(m.z);
+                in.part = ray_part(m.z);
+                pending = 1;
+            }
+        }
+        while (__any_sync(0xffffffffu, pending != 0)) {
+            bool act = pending != 0;
+            TraceOut T;
+            int dest = GXY_DROP_ON_FLOOR;
+            unsigned nspawn = 0;
+            float ar = 0, ag = 0, ab = 0, o_post = 0;
+            ShadeIn sh;
+            if (act) {
+                if (PRIMARY) {
+                    int p = __ffsll((long long)pending) - 1;
+                    pending &= pending - 1;
+                    in.part = p;
+                    c_prim++;
+                } else {
+                    pending = 0;
+                }
+                c_seg++;
+                T = trace_core<ANYSEC>(S, tfs, in, st);
+                if (in.type == GXY_RAY_PRIMARY && T.surface) {
+                    // ambient (TraceRays.ispc:735-761)
+                    float s = L.Ka * (1.0f - T.o);
+                    float ka_ao = L.n_ao ? -L.Ka / L.n_ao : 0.0f;
+                    float as = ka_ao * (1.0f - T.o);
+                    ar = as * T.sc.x; ag = as * T.sc.y; ab = as * T.sc.z;
+                    T.r += s * T.sc.x;
+                    T.g += s * T.sc.y;
+                    T.b += s * T.sc.z;
+                    // diffuse (TraceRays.ispc:859-923)
+                    float Kd = L.Kd / L.n;
+                    float tr = 0, tg = 0, tb = 0;
+                    for (int k = 0; k < L.n; k++) {
+                        V3 lv;
+                        if (L.type[k]) {
+                            float t = T.t;
+                            V3 sp = v3(in.org.x + t * in.dir.x, in.org.y + t * in.dir.y, in.org.z + t * in.dir.z);
+                            lv = nrm(v3(L.l[k].x, L.l[k].y, L.l[k].z) - sp);
+                        } else {
+                            lv = neg(v3(L.l[k].x, L.l[k].y, L.l[k].z));
+                        }
+                        float dd = dot(T.n, lv);
+                        if (dd > 0) {
+                            float dff = (1.0f - T.o) * dd;
+                            tr += dff * T.sc.x;
+                            tg += dff * T.sc.y;
+                            tb += dff * T.sc.z;
+                        }
+                    }
+                    float f = Kd * (1 - T.o);
+                    T.r = T.r + f * tr;
+                    T.g = T.g + f * tg;
+                    T.b = T.b + f * tb;
+                    o_post = T.o + f * T.o;
+                    nspawn = L.n_ao + (L.shadows ? L.n : 0);
+                    sh.org = in.org; sh.dir = in.dir; sh.t = T.t; sh.n = T.n; sh.sc = T.sc; sh.x = x; sh.y = y;
+                    T.o = o_post;
+                    c_ao += L.n_ao;
+                    c_sh += L.shadows ? L.n : 0;
+                }
+                int cls = classify_ray(in.type, T.term);
+                dest = assign_destination(S, in.part, in.type, cls, in.org, in.dir);
+                if (dest == GXY_TERMINATED) {
+                    c_term++;
+                    if (T.r != 0.0f || T.g != 0.0f || T.b != 0.0f || T.o != 0.0f) {
+                        float4 *px = reinterpret_cast<float4 *>(A.fb) + ((size_t)y * A.cam.width + x);
+                        atomicAdd(px, make_float4(T.r, T.g, T.b, T.o));
+                    }
+                } else if (dest == GXY_DROP_ON_FLOOR) {
+                    c_drop++;
+                } else if (dest == GXY_KEEP_HERE) {
+                    c_keep++;
+                } else {
+                    c_hand++;
+                }
+            }
+            unsigned cont = (act && (dest >= 0 || dest == GXY_KEEP_HERE)) ? 1u : 0u;
+            unsigned cnt = nspawn + cont;
+            unsigned tot;
+            unsigned pre = warp_excl_scan(cnt, tot);
+            unsigned wbase = 0;
+            if (tot) {
+                if (lane == 0) wbase = atomicAdd(A.qout_count, tot);
+                wbase = __shfl_sync(0xffffffffu, wbase, 0);
+            }
+            if (cnt) {
+                unsigned idx = wbase + pre;
+                c_enq += cnt;
+                if (idx + cnt > A.qcap) {
+                    ovf = 1;
+                } else {
+                    if (cont) {
+                        int np_ = dest >= 0 ? dest : in.part;
+                        put_ray(A.qout, idx++, in.org, T.t, in.dir, in.tmax, T.r, T.g, T.b, T.o, x, y,
+                                make_meta(in.type, np_, 0));
+                    }
+                    if (nspawn) {
+                        // AO rays (TraceRays.ispc:661-730); payload uses o before diffuse
+                        if (L.n_ao) {
+                            V3 b0, b1;
+                            ao_basis(sh.n, b0, b1);
+                            V3 o = v3(sh.org.x + sh.t * sh.dir.x, sh.org.y + sh.t * sh.dir.y,
+                                      sh.org.z + sh.t * sh.dir.z);
+                            o = v3(o.x + S.epsilon * sh.n.x, o.y + S.epsilon * sh.n.y, o.z + S.epsilon * sh.n.z);
+                            for (int j = 0; j < L.n_ao; j++) {
+                                Spawned s = ao_ray(S, L, sh, j, ar, ag, ab, b0, b1, o);
+                                put_ray(A.qout, idx++, s.o, 0.0f, s.d, s.tmax, s.r, s.g, s.b, 0.0f, x, y,
+                                        make_meta(GXY_RAY_AO, in.part, 0));
+                            }
+                        }
+                        // shadow rays (TraceRays.ispc:813-854); payload uses o after diffuse
+                        if (L.shadows) {
+                            float Kd = -L.Kd / L.n;
+                            for (int k = 0; k < L.n; k++) {
+                                V3 sp = v3(sh.org.x + sh.t * sh.dir.x + S.epsilon * sh.n.x,
+                                           sh.org.y + sh.t * sh.dir.y + S.epsilon * sh.n.y,
+                                           sh.org.z + sh.t * sh.dir.z + S.epsilon * sh.n.z);
+                                V3 lv;
+                                if (L.type[k]) lv = nrm(v3(L.l[k].x, L.l[k].y, L.l[k].z) - sp);
+                                else lv = neg(v3(L.l[k].x, L.l[k].y, L.l[k].z));
+                                lv = nrm(lv);
+                                float dd = dot(sh.n, lv);
+                                if (dd < 0) dd = 0;
+                                float dff = (1.0f - o_post) * Kd * dd;
+                                put_ray(A.qout, idx++, sp, 0.0f, lv, INFINITY, dff * sh.sc.x, dff * sh.sc.y,
+                                        dff * sh.sc.z, 0.0f, x, y, make_meta(GXY_RAY_SHADOW, in.part, 0));
+                            }
+                        }
+                    }
+                }
+            }
+        }
+    }
+    ovf |= st.ovf;
+    // block-level counter reduction, one atomic per counter per block
+    __shared__ unsigned long long red[16];
+    if (threadIdx.x < 16) red[threadIdx.x] = 0;
+    __syncthreads();
+    unsigned long long vals[14] = {c_prim, c_sh, c_ao, c_seg, c_hand, c_term, c_drop, c_keep, st.samples, st.nodes,
+                                   st.tris, st.sphs, c_enq, (unsigned long long)ovf};
+#pragma unroll
+    for (int k = 0; k < 14; k++) {
+        unsigned long long v = vals[k];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0 && v) atomicAdd(&red[k], v);
+    }
+    __syncthreads();
+    if (threadIdx.x < 13 && red[threadIdx.x]) atomicAdd(&(&A.ctr->primary)[threadIdx.x], red[threadIdx.x]);
+    if (threadIdx.x == 13 && red[13]) atomicExch(&A.ctr->overflow, 1);
+}
+
+// -------------------------------------------------------- RayList kernels
+struct RLDev {
+    float *f[20];
+    int32_t *i[5];
+    int n;
+};
+enum { F_OX, F_OY, F_OZ, F_DX, F_DY, F_DZ, F_NX, F_NY, F_NZ, F_SAMPLE, F_R, F_G, F_B, F_O, F_SR, F_SG, F_SB, F_SO, F_T,
+       F_TMAX };
+enum { I_X, I_Y, I_TYPE, I_TERM, I_CLS };
+
+__global__ void k_rl_trace(DevScene S, int part, RLDev R, DevCounters *ctr) {
+    __shared__ DevTF tfs[kMaxVol];
+    load_tfs(S, tfs);
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    RayStats st;
+    if (i < R.n) {
+        TraceIn in;
+        in.org = v3(R.f[F_OX][i], R.f[F_OY][i], R.f[F_OZ][i]);
+        in.dir = v3(R.f[F_DX][i], R.f[F_DY][i], R.f[F_DZ][i]);
+        in.t = R.f[F_T][i];
+        in.tmax = R.f[F_TMAX][i];
+        in.r = R.f[F_R][i]; in.g = R.f[F_G][i]; in.b = R.f[F_B][i]; in.o = R.f[F_O][i];
+        in.type = R.i[I_TYPE][i];
+        in.part = part;
+        TraceOut T = trace_core<false>(S, tfs, in, st);
+        R.f[F_R][i] = T.r; R.f[F_G][i] = T.g; R.f[F_B][i] = T.b; R.f[F_O][i] = T.o;
+        R.i[I_TERM][i] = T.term;
+        R.f[F_T][i] = T.t;
+        if (T.surface) {
+            R.f[F_SR][i] = T.sc.x; R.f[F_SG][i] = T.sc.y; R.f[F_SB][i] = T.sc.z; R.f[F_SO][i] = 1.0f;
+            R.f[F_NX][i] = T.n.x; R.f[F_NY][i] = T.n.y; R.f[F_NZ][i] = T.n.z;
+        }
+        if (st.ovf) atomicExch(&ctr->overflow, 1);
+    }
+}
+
+// counts of secondaries per ray: [0,n) AO, [n,2n) shadow
+__global__ void k_rl_counts(RLDev R, int n_ao, int n_sh, int *cnt) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= R.n) return;
+    bool hit = R.i[I_TYPE][i] == GXY_RAY_PRIMARY && (R.i[I_TERM][i] & GXY_RAY_SURFACE);
+    cnt[i] = hit ? n_ao : 0;
+    cnt[R.n + i] = hit ? n_sh : 0;
+}
+
+__device__ __forceinline__ void rl_put(RLDev &O, int k, V3 o, V3 d, float r, float g, float b, float tmax, int x, int y,
+                                       int type) {
+    O.f[F_OX][k] = o.x; O.f[F_OY][k] = o.y; O.f[F_OZ][k] = o.z;
+    O.f[F_DX][k] = d.x; O.f[F_DY][k] = d.y; O.f[F_DZ][k] = d.z;
+    O.f[F_R][k] = r; O.f[F_G][k] = g; O.f[F_B][k] = b; O.f[F_O][k] = 0.0f;
+    O.f[F_T][k] = 0.0f; O.f[F_TMAX][k] = tmax;
+    O.i[I_X][k] = x; O.i[I_Y][k] = y; O.i[I_TYPE][k] = type; O.i[I_TERM][k] = 0;
+}
+
+// Ambient, AO spawn, diffuse, shadow spawn in the order of TraceRays::Trace
+// with GXY_REVERSE_LIGHTING (TraceRays.cpp:124-131).  off: exclusive scans
+// of the per-ray counts ([0,n) AO, [n,2n) shadow, shadow block after AO).
+__global__ void k_rl_shade(DevScene S, DevLights L, RLDev R, RLDev O, const int *off, int ao_total) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= R.n) return;
+    if (!(R.i[I_TYPE][i] == GXY_RAY_PRIMARY && (R.i[I_TERM][i] & GXY_RAY_SURFACE))) return;
+    float o = R.f[F_O][i];
+    V3 n = v3(R.f[F_NX][i], R.f[F_NY][i], R.f[F_NZ][i]);
+    V3 sc = v3(R.f[F_SR][i], R.f[F_SG][i], R.f[F_SB][i]);
+    V3 org = v3(R.f[F_OX][i], R.f[F_OY][i], R.f[F_OZ][i]);
+    V3 dir = v3(R.f[F_DX][i], R.f[F_DY][i], R.f[F_DZ][i]);
+    float t = R.f[F_T][i];
+    int x = R.i[I_X][i], y = R.i[I_Y][i];
+    // ambient
+    float s = L.Ka * (1.0f - o);
+    R.f[F_R][i] += s * sc.x;
+    R.f[F_G][i] += s * sc.y;
+    R.f[F_B][i] += s * sc.z;
+    // AO
+    if (L.n_ao) {
+        float Ka = -L.Ka / L.n_ao;
+        float as = Ka * (1.0f - o);
+        float ar = as * sc.x, ag = as * sc.y, ab = as * sc.z;
+        V3 b0, b1;
+        ao_basis(n, b0, b1);
+        V3 p = v3(org.x + t * dir.x, org.y + t * dir.y, org.z + t * dir.z);
+        p = v3(p.x + S.epsilon * n.x, p.y + S.epsilon * n.y, p.z + S.epsilon * n.z);
+        ShadeIn h;
+        h.n = n; h.x = x; h.y = y;
+        int base = off[i];
+        for (int j = 0; j < L.n_ao; j++) {
+            Spawned sp = ao_ray(S, L, h, j, ar, ag, ab, b0, b1, p);
+            rl_put(O, base + j, sp.o, sp.d, sp.r, sp.g, sp.b, sp.tmax, x, y, GXY_RAY_AO);
+        }
+    }
+    // diffuse
+    float Kd = L.Kd / L.n;
+    float tr = 0, tg = 0, tb = 0;
+    for (int k = 0; k < L.n; k++) {
+        V3 lv;
+        if (L.type[k]) {
+            V3 sp = v3(org.x + t * dir.x, org.y + t * dir.y, org.z + t * dir.z);
+            lv = nrm(v3(L.l[k].x, L.l[k].y, L.l[k].z) - sp);
+        } else {
+            lv = neg(v3(L.l[k].x, L.l[k].y, L.l[k].z));
+        }
+        float dd = dot(n, lv);
+        if (dd > 0) {
+            float dff = (1.0f - o) * dd;
+            tr += dff * sc.x; tg += dff * sc.y; tb += dff * sc.z;
+        }
+    }
+    float f = Kd * (1 - o);
+    R.f[F_R][i] = R.f[F_R][i] + f * tr;
+    R.f[F_G][i] = R.f[F_G][i] + f * tg;
+    R.f[F_B][i] = R.f[F_B][i] + f * tb;
+    float o2 = o + f * o;
+    R.f[F_O][i] = o2;
+    // shadows
+    if (L.shadows) {
+        float Kds = -L.Kd / L.n;
+        int base = ao_total + off[R.n + i];
+        for (int k = 0; k < L.n; k++) {
+            V3 sp = v3(org.x + t * dir.x + S.epsilon * n.x, org.y + t * dir.y + S.epsilon * n.y,
+                       org.z + t * dir.z + S.epsilon * n.z);
+            V3 lv;
+            if (L.type[k]) lv = nrm(v3(L.l[k].x, L.l[k].y, L.l[k].z) - sp);
+            else lv = neg(v3(L.l[k].x, L.l[k].y, L.l[k].z));
+            lv = nrm(lv);
+            float dd = dot(n, lv);
+            if (dd < 0) dd = 0;
+            float dff = (1.0f - o2) * Kds * dd;
+            rl_put(O, base + k, sp, lv, dff * sc.x, dff * sc.y, dff * sc.z, INFINITY, x, y, GXY_RAY_SHADOW);
+        }
+    }
+}
+
+__global__ void k_rl_classify(RLDev R) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= R.n) return;
+    R.i[I_CLS][i] = classify_ray(R.i[I_TYPE][i], R.i[I_TERM][i]);
+}
+
+__global__ void k_rl_assign(DevScene S, int part, RLDev R) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= R.n) return;
+    V3 o = v3(R.f[F_OX][i], R.f[F_OY][i], R.f[F_OZ][i]);
+    V3 d = v3(R.f[F_DX][i], R.f[F_DY][i], R.f[F_DZ][i]);
+    R.i[I_CLS][i] = assign_destination(S, part, R.i[I_TYPE][i], R.i[I_CLS][i], o, d);
+}
+
+__global__ void k_rl_accumulate(RLDev R, float *fb, int w, int h) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= R.n) return;
+    if (R.i[I_CLS][i] != GXY_TERMINATED) return;
+    int x = R.i[I_X][i], y = R.i[I_Y][i];
+    if (x < 0 || y < 0 || x >= w || y >= h) return;
+    float4 *p = reinterpret_cast<float4 *>(fb) + ((size_t)y * w + x);
+    atomicAdd(p, make_float4(R.f[F_R][i], R.f[F_G][i], R.f[F_B][i], R.f[F_O][i]));
+}
+
+// camera rays of one partition: flag pass, then ordered scatter
+__global__ void k_rl_camera_flags(DevScene S, DevCamera C, int part, int *flag) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= (int64_t)C.width * C.height) return;
+    V3 o, d;
+    uint64_t m = camera_ray(S, C, (int)(i % C.width), (int)(i / C.width), o, d);
+    flag[i] = (m >> part) & 1ull;
+}
+__global__ void k_rl_camera_write(DevScene S, DevCamera C, int part, const int *flag, const int *pos, RLDev O) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= (int64_t)C.width * C.height || !flag[i]) return;
+    V3 o, d;
+    int x = (int)(i % C.width), y = (int)(i / C.width);
+    camera_ray(S, C, x, y, o, d);
+    int k = pos[i];
+    O.f[F_OX][k] = o.x; O.f[F_OY][k] = o.y; O.f[F_OZ][k] = o.z;
+    O.f[F_DX][k] = d.x; O.f[F_DY][k] = d.y; O.f[F_DZ][k] = d.z;
+    O.f[F_R][k] = 0; O.f[F_G][k] = 0; O.f[F_B][k] = 0; O.f[F_O][k] = 0;
+    O.f[F_T][k] = 0; O.f[F_TMAX][k] = FLT_MAX;
+    O.i[I_X][k] = x; O.i[I_Y][k] = y; O.i[I_TYPE][k] = GXY_RAY_PRIMARY; O.i[I_TERM][k] = 0;
+}
+
+// ============================================================ frame driver
+static unsigned grid_for(int64_t n) {
+    int sms = 152;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, g_device);
+    int64_t want = (n + kThreads - 1) / kThreads;
+    int64_t cap = (int64_t)sms * 8;   // persistent-style grid-stride cap
+    if (want > cap) want = cap;
+    return (unsigned)(want < 1 ? 1 : want);
+}
+
+static int ensure_queues(Scene *sc, size_t need) {
+    if (sc->qcap >= need) return GXY_OK;
+    arena().free(sc->qa);
+    arena().free(sc->qb);
+    sc->qa = sc->qb = nullptr;
+    sc->qcap = 0;
+    int rc;
+    if ((rc = arena().alloc((void **)&sc->qa, need * sizeof(DRay)))) return rc;
+    if ((rc = arena().alloc((void **)&sc->qb, need * sizeof(DRay)))) {
+        arena().free(sc->qa);
+        sc->qa = nullptr;
+        return rc;
+    }
+    sc->qcap = need;
+    return GXY_OK;
+}
+
+static int render(Scene *sc, const gxy_camera &cam, const gxy_lighting &lt, float *fb, cudaStream_t st) {
+    if (cam.width <= 0 || cam.height <= 0) return set_error(GXY_ERR_INVALID, "bad image size");
+    DevScene &S = sc->S;
+    FrameArgs A;
+    A.cam = setup_camera(cam);
+    int rc = setup_lights(lt, A.L);
+    if (rc) return rc;
+    if (A.L.n == 0) return set_error(GXY_ERR_INVALID, "lighting needs at least one light");
+    int64_t npix = (int64_t)cam.width * cam.height;
+    size_t per = 1 + (size_t)A.L.n_ao + (A.L.shadows ? A.L.n : 0);
+    size_t need = (size_t)npix * per + (size_t)npix / 8 + 4096;
+    if ((rc = ensure_queues(sc, need))) return rc;
+    CK(cudaMemsetAsync(sc->ctr, 0, sizeof(DevCounters), st));
+    CK(cudaMemsetAsync(sc->qcount, 0, 16 * sizeof(unsigned), st));
+    A.fb = fb;
+    A.ctr = sc->ctr;
+    A.qcap = (unsigned)sc->qcap;
+    bool anysec = !S.integrate;
+    // generation 0: camera rays
+    A.qin = nullptr;
+    A.nin = 0;
+    A.qout = sc->qa;
+    A.qout_count = sc->qcount + 0;
+    unsigned g = grid_for(npix);
+    if (anysec) k_frame<true, true><<<g, kThreads, 0, st>>>(S, A);
+    else k_frame<true, false><<<g, kThreads, 0, st>>>(S, A);
+    CK(cudaGetLastError());
+    DRay *qin = sc->qa, *qout = sc->qb;
+    unsigned *cin = sc->qcount + 0, *cout = sc->qcount + 1;
+    int64_t gens = 1;
+    for (;;) {
+        unsigned n = 0;
+        CK(cudaMemcpyAsync(&n, cin, sizeof n, cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        if (n > sc->qcap) n = (unsigned)sc->qcap;   // overflow already flagged
+        if (n == 0) break;
+        CK(cudaMemsetAsync(cout, 0, sizeof(unsigned), st));
+        A.qin = qin;
+        A.nin = n;
+        A.qout = qout;
+        A.qout_count = cout;
+        g = grid_for(n);
+        if (anysec) k_frame<false, true><<<g, kThreads, 0, st>>>(S, A);
+        else k_frame<false, false><<<g, kThreads, 0, st>>>(S, A);
+        CK(cudaGetLastError());
+        std::swap(qin, qout);
+        std::swap(cin, cout);
+        gens++;
+        if (gens > 10000) return set_error(GXY_ERR_TIMEOUT, "ray queues did not drain");
+    }
+    CK(cudaMemcpyAsync(&sc->last, sc->ctr, sizeof(DevCounters), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    sc->bounces = gens;
+    if (sc->last.overflow) return set_error(GXY_ERR_OVERFLOW, "a ray queue or traversal stack overflowed");
+    return GXY_OK;
+}
+
+// ------------------------------------------------- RayList host plumbing
+struct DevRayList {
+    RLDev d{};
+    std::vector<void *> bufs;
+    ~DevRayList() {
+        for (void *p : bufs) arena().free(p);
+    }
+    int alloc(int n) {
+        d.n = n;
+        size_t cnt = n > 0 ? (size_t)n : 1;
+        for (int k = 0; k < 20; k++) {
+            int rc = arena().alloc((void **)&d.f[k], cnt * sizeof(float));
+            if (rc) return rc;
+            bufs.push_back(d.f[k]);
+        }
+        for (int k = 0; k < 5; k++) {
+            int rc = arena().alloc((void **)&d.i[k], cnt * sizeof(int32_t));
+            if (rc) return rc;
+            bufs.push_back(d.i[k]);
+        }
+        return GXY_OK;
+    }
+};
+static float *const *host_f(const gxy_raylist &r, float **tmp) {
+    float *f[20] = {r.ox, r.oy, r.oz, r.dx, r.dy, r.dz, r.nx, r.ny, r.nz, r.sample,
+                    r.r, r.g, r.b, r.o, r.sr, r.sg, r.sb, r.so, r.t, r.tMax};
+    for (int k = 0; k < 20; k++) tmp[k] = f[k];
+    return tmp;
+}
+static int32_t *const *host_i(const gxy_raylist &r, int32_t **tmp) {
+    int32_t *v[5] = {r.x, r.y, r.type, r.term, r.classification};
+    for (int k = 0; k < 5; k++) tmp[k] = v[k];
+    return tmp;
+}
+static int rl_upload(const gxy_raylist &h, DevRayList &d, int n) {
+    float *hf[20];
+    int32_t *hi[5];
+    host_f(h, hf);
+    host_i(h, hi);
+    for (int k = 0; k < 20; k++) {
+        if (hf[k]) CK(cudaMemcpy(d.d.f[k], hf[k], n * sizeof(float), cudaMemcpyHostToDevice));
+        else CK(cudaMemset(d.d.f[k], 0, n * sizeof(float)));
+    }
+    for (int k = 0; k < 5; k++) {
+        if (hi[k]) CK(cudaMemcpy(d.d.i[k], hi[k], n * sizeof(int32_t), cudaMemcpyHostToDevice));
+        else CK(cudaMemset(d.d.i[k], 0, n * sizeof(int32_t)));
+    }
+    return GXY_OK;
+}
+static int rl_download(const DevRayList &d, gxy_raylist &h, int n) {
+    float *hf[20];
+    int32_t *hi[5];
+    host_f(h, hf);
+    host_i(h, hi);
+    for (int k = 0; k < 20; k++)
+        if (hf[k] && n) CK(cudaMemcpy(hf[k], d.d.f[k], n * sizeof(float), cudaMemcpyDeviceToHost));
+    for (int k = 0; k < 5; k++)
+        if (hi[k] && n) CK(cudaMemcpy(hi[k], d.d.i[k], n * sizeof(int32_t), cudaMemcpyDeviceToHost));
+    return GXY_OK;
+}
+
+}  // namespace gxy
+
+using namespace gxy;
+
+// ================================================================== C ABI
+#define GUARD_BEGIN try {
+#define GUARD_END                                                       \
+    }                                                                   \
+    catch (const std::exception &e) {                                   \
+        return set_error(GXY_ERR_INVALID, std::string("exception: ") + e.what()); \
+    }                                                                   \
+    catch (...) {                                                       \
+        return set_error(GXY_ERR_INVALID, "unknown exception");         \
+    }
+
+extern "C" {
+
+int gxy_gpu_init(int device, size_t hbm_budget_bytes) {
+    GUARD_BEGIN
+    int n = 0;
+    CK(cudaGetDeviceCount(&n));
+    if (device < 0 || device >= n) return set_error(GXY_ERR_INVALID, "no such device");
+    CK(cudaSetDevice(device));
+    g_device = device;
+    arena().set_budget(hbm_budget_bytes);
+    g_init = true;
+    return GXY_OK;
+    GUARD_END
+}
+
+int gxy_gpu_shutdown(void) {
+    GUARD_BEGIN
+    if (g_init) cudaDeviceSynchronize();
+    g_init = false;
+    return GXY_OK;
+    GUARD_END
+}
+
+int gxy_gpu_last_error(char *buf, int buflen) {
+    if (!buf || buflen <= 0) return GXY_ERR_INVALID;
+    snprintf(buf, (size_t)buflen, "%s", last_error().c_str());
+    return GXY_OK;
+}
+
+int gxy_gpu_hbm_in_use(size_t *bytes) {
+    if (!bytes) return GXY_ERR_INVALID;
+    *bytes = arena().in_use();
+    return GXY_OK;
+}
+
+int gxy_gpu_scene_commit(const gxy_scene_desc *desc, gxy_scene *out) {
+    GUARD_BEGIN
+    if (!g_init) return set_error(GXY_ERR_NOT_INIT, "gxy_gpu_init not called");
+    if (!desc || !out) return set_error(GXY_ERR_INVALID, "null argument");
+    std::unique_ptr<Scene> sc(new Scene());
+    int rc = commit(desc, sc.get());
+    if (rc) return rc;
+    *out = reinterpret_cast<gxy_scene>(sc.release());
+    return GXY_OK;
+    GUARD_END
+}
+
+int gxy_gpu_scene_release(gxy_scene scene) {
+    GUARD_BEGIN
+    if (!scene) return set_error(GXY_ERR_INVALID, "null scene");
+    cudaDeviceSynchronize();
+    delete reinterpret_cast<Scene *>(scene);
+    return GXY_OK;
+    GUARD_END
+}
+
+int gxy_gpu_scene_partition_info(gxy_scene scene, int partition, gxy_partition_info *out) {
+    if (!scene || !out) return set_error(GXY_ERR_INVALID, "null argument");
+    Scene *sc = reinterpret_cast<Scene *>(scene);
+    if (partition < 0 || partition >= sc->S.np) return set_error(GXY_ERR_INVALID, "bad partition");
+    const DevPartition &P = sc->S.part[partition];
+    for (int a = 0; a < 3; a++) {
+        out->global_box[a] = sc->S.glo[a];
+        out->global_box[3 + a] = sc->S.ghi[a];
+        out->local_box[a] = P.lo[a];
+        out->local_box[3 + a] = P.hi[a];
+    }
+    for (int k = 0; k < 6; k++) out->neighbors[k] = P.nb[k];
+    out->n_partitions = sc->S.np;
+    return GXY_OK;
+}
+
+int gxy_gpu_scene_bvh_info(gxy_scene scene, int64_t *n_nodes, int64_t *n_prim_refs, double *build_ms) {
+    if (!scene) return set_error(GXY_ERR_INVALID, "null scene");
+    Scene *sc = reinterpret_cast<Scene *>(scene);
+    if (n_nodes) *n_nodes = sc->bvh.n_nodes;
+    if (n_prim_refs) *n_prim_refs = sc->bvh.n_slots;
+    if (build_ms) *build_ms = sc->bvh.build_ms;
+    return GXY_OK;
+}
+
+int gxy_resolve_lights(const gxy_lighting *in, const gxy_camera *camera, gxy_lighting *out) {
+    if (!in || !camera || !out) return set_error(GXY_ERR_INVALID, "null argument");
+    // Rendering::resolve_lights (Rendering.cpp:157-216)
+    F3h vp = h3(camera->eye[0], camera->eye[1], camera->eye[2]);
+    F3h vu = gnorm(h3(camera->up[0], camera->up[1], camera->up[2]));
+    F3h vd = gnorm(h3(camera->dir[0], camera->dir[1], camera->dir[2]));
+    F3h right = gnorm(hcross(vd, vu));
+    F3h up = hcross(vd, right);
+    gxy_lighting r = *in;
+    for (int i = 0; i < in->n_lights && i < GXY_MAX_LIGHTS; i++) {
+        if (in->types[i] == GXY_LIGHT_CAMERA) {
+            const float *l = in->lights[i];
+            F3h p = hadd(hadd(hadd(vp, hmul(l[0], right)), hmul(l[1], up)), hmul(l[2], vd));
+            r.lights[i][0] = p.x; r.lights[i][1] = p.y; r.lights[i][2] = p.z;
+            r.types[i] = GXY_LIGHT_POINT;
+        }
+    }
+    *out = r;
+    return GXY_OK;
+}
+
+int gxy_gpu_render(gxy_scene scene, const gxy_camera *camera, const gxy_lighting *lighting, float *fb_rgba,
+                   void *stream) {
+    GUARD_BEGIN
+    if (!scene || !camera || !lighting || !fb_rgba) return set_error(GXY_ERR_INVALID, "null argument");
+    Scene *sc = reinterpret_cast<Scene *>(scene);
+    std::lock_guard<std::mutex> lk(sc->mu);
+    return render(sc, *camera, *lighting, fb_rgba, (cudaStream_t)stream);
+    GUARD_END
+}
+
+int gxy_gpu_render_host(gxy_scene scene, const gxy_camera *camera, const gxy_lighting *lighting,
+                        float *host_fb_rgba, void *stream) {
+    GUARD_BEGIN
+    if (!scene || !camera || !lighting || !host_fb_rgba) return set_error(GXY_ERR_INVALID, "null argument");
+    Scene *sc = reinterpret_cast<Scene *>(scene);
+    std::lock_guard<std::mutex> lk(sc->mu);
+    cudaStream_t st = (cudaStream_t)stream;
+    size_t elems = (size_t)camera->width * camera->height * 4;
+    if (sc->fbtmp_elems < elems) {
+        arena().free(sc->fbtmp);
+        sc->fbtmp = nullptr;
+        sc->fbtmp_elems = 0;
+        int rc = arena().alloc((void **)&sc->fbtmp, elems * sizeof(float));
+        if (rc) return rc;
+        sc->fbtmp_elems = elems;
+    }
+    CK(cudaMemsetAsync(sc->fbtmp, 0, elems * sizeof(float), st));
+    int rc = render(sc, *camera, *lighting, sc->fbtmp, st);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(host_fb_rgba, sc->fbtmp, elems * sizeof(float), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    return GXY_OK;
+    GUARD_END
+}
+
+int gxy_gpu_query_counters(gxy_scene scene, gxy_counters *out) {
+    if (!scene || !out) return set_error(GXY_ERR_INVALID, "null argument");
+    Scene *sc = reinterpret_cast<Scene *>(scene);
+    const DevCounters &c = sc->last;
+    memset(out, 0, sizeof *out);
+    out->primary_rays = (int64_t)c.primary;
+    out->shadow_rays = (int64_t)c.shadow;
+    out->ao_rays = (int64_t)c.ao;
+    out->secondary_rays = (int64_t)(c.shadow + c.ao);
+    out->segments = (int64_t)c.segments;
+    out->handoffs = (int64_t)c.handoffs;
+    out->terminated = (int64_t)c.terminated;
+    out->dropped = (int64_t)c.dropped;
+    out->kept = (int64_t)c.kept;
+    out->bounces = sc->bounces;
+    out->samples = (int64_t)c.samples;
+    out->nodes = (int64_t)c.nodes;
+    out->prim_tests = (int64_t)(c.tri_tests + c.sph_tests);
+    out->overflow = c.overflow;
+    return GXY_OK;
+}
+
+// extra counters for the roofline: triangle and sphere tests, queue records written
+int gxy_gpu_query_counters_ex(gxy_scene scene, int64_t *tri_tests, int64_t *sph_tests, int64_t *enqueued) {
+    if (!scene) return set_error(GXY_ERR_INVALID, "null scene");
+    Scene *sc = reinterpret_cast<Scene *>(scene);
+    if (tri_tests) *tri_tests = (int64_t)sc->last.tri_tests;
+    if (sph_tests) *sph_tests = (int64_t)sc->last.sph_tests;
+    if (enqueued) *enqueued = (int64_t)sc->last.enqueued;
+    return GXY_OK;
+}
+
+int gxy_gpu_generate_initial_rays(gxy_scene scene, int partition, const gxy_camera *camera, gxy_raylist *out,
+                                  int32_t *n_out) {
+    GUARD_BEGIN
+    if (!scene || !camera || !out || !n_out) return set_error(GXY_ERR_INVALID, "null argument");
+    Scene *sc = reinterpret_cast<Scene *>(scene);
+    if (partition < 0 || partition >= sc->S.np) return set_error(GXY_ERR_INVALID, "bad partition");
+    DevCamera C = setup_camera(*camera);
+    int64_t n = (int64_t)camera->width * camera->height;
+    if (n <= 0 || n > 0x7fffffff) return set_error(GXY_ERR_INVALID, "bad image size");
+    ScratchList tmp(arena());
+    int *flag, *pos;
+    int rc;
+    if ((rc = tmp.alloc((void **)&flag, n * sizeof(int)))) return rc;
+    if ((rc = tmp.alloc((void **)&pos, n * sizeof(int)))) return rc;
+    unsigned g = (unsigned)((n + 255) / 256);
+    k_rl_camera_flags<<<g, 256>>>(sc->S, C, partition, flag);
+    size_t tb = 0;
+    cub::DeviceScan::ExclusiveSum(nullptr, tb, flag, pos, (int)n);
+    void *tv;
+    if ((rc = tmp.alloc(&tv, tb))) return rc;
+    CK(cub::DeviceScan::ExclusiveSum(tv, tb, flag, pos, (int)n));
+    int last_pos = 0, last_flag = 0;
+    CK(cudaMemcpy(&last_pos, pos + n - 1, sizeof(int), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(&last_flag, flag + n - 1, sizeof(int), cudaMemcpyDeviceToHost));
+    int total = last_pos + last_flag;
+    *n_out = total;
+    if (total > out->n) return set_error(GXY_ERR_OVERFLOW, "output RayList too small");
+    DevRayList O;
+    if ((rc = O.alloc(total))) return rc;
+    for (int k = 0; k < 20; k++) CK(cudaMemset(O.d.f[k], 0, (total ? total : 1) * sizeof(float)));
+    for (int k = 0; k < 5; k++) CK(cudaMemset(O.d.i[k], 0, (total ? total : 1) * sizeof(int32_t)));
+    k_rl_camera_write<<<g, 256>>>(sc->S, C, partition, flag, pos, O.d);
+    CK(cudaGetLastError());
+    return rl_download(O, *out, total);
+    GUARD_END
+}
+
+int gxy_gpu_trace_raylist(gxy_scene scene, int partition, const gxy_lighting *lighting, gxy_raylist *in,
+                          gxy_raylist *out, int32_t *n_out) {
+    GUARD_BEGIN
+    if (!scene || !lighting || !in || !n_out) return set_error(GXY_ERR_INVALID, "null argument");
+    Scene *sc = reinterpret_cast<Scene *>(scene);
+    if (partition < 0 || partition >= sc->S.np) return set_error(GXY_ERR_INVALID, "bad partition");
+    DevLights L;
+    int rc = setup_lights(*lighting, L);
+    if (rc) return rc;
+    int n = in->n;
+    if (n < 0) return set_error(GXY_ERR_INVALID, "negative ray count");
+    *n_out = 0;
+    if (n == 0) return GXY_OK;
+    DevRayList R;
+    if ((rc = R.alloc(n))) return rc;
+    if ((rc = rl_upload(*in, R, n))) return rc;
+    CK(cudaMemset(sc->ctr, 0, sizeof(DevCounters)));
+    unsigned g = (unsigned)((n + 255) / 256);
+    k_rl_trace<<<g, 256>>>(sc->S, partition, R.d, sc->ctr);
+    CK(cudaGetLastError());
+    ScratchList tmp(arena());
+    int *cnt, *off;
+    if ((rc = tmp.alloc((void **)&cnt, 2 * (size_t)n * sizeof(int)))) return rc;
+    if ((rc = tmp.alloc((void **)&off, 2 * (size_t)n * sizeof(int)))) return rc;
+    int n_sh = L.shadows ? L.n : 0;
+    k_rl_counts<<<g, 256>>>(R.d, L.n_ao, n_sh, cnt);
+    size_t tb = 0;
+    cub::DeviceScan::ExclusiveSum(nullptr, tb, cnt, off, n);
+    void *tv;
+    if ((rc = tmp.alloc(&tv, tb))) return rc;
+    CK(cub::DeviceScan::ExclusiveSum(tv, tb, cnt, off, n));
+    CK(cub::DeviceScan::ExclusiveSum(tv, tb, cnt + n, off + n, n));
+    int la[4];
+    CK(cudaMemcpy(&la[0], off + n - 1, sizeof(int), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(&la[1], cnt + n - 1, sizeof(int), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(&la[2], off + 2 * n - 1, sizeof(int), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(&la[3], cnt + 2 * n - 1, sizeof(int), cudaMemcpyDeviceToHost));
+    int ao_total = la[0] + la[1], sh_total = la[2] + la[3];
+    int total = ao_total + sh_total;
+    DevRayList O;
+    if ((rc = O.alloc(total))) return rc;
+    for (int k = 0; k < 20; k++) CK(cudaMemset(O.d.f[k], 0, (total ? total : 1) * sizeof(float)));
+    for (int k = 0; k < 5; k++) CK(cudaMemset(O.d.i[k], 0, (total ? total : 1) * sizeof(int32_t)));
+    k_rl_shade<<<g, 256>>>(sc->S, L, R.d, O.d, off, ao_total);
+    CK(cudaGetLastError());
+    if ((rc = rl_download(R, *in, n))) return rc;
+    DevCounters c;
+    CK(cudaMemcpy(&c, sc->ctr, sizeof c, cudaMemcpyDeviceToHost));
+    if (c.overflow) return set_error(GXY_ERR_OVERFLOW, "BVH traversal stack overflowed");
+    *n_out = total;
+    if (total) {
+        if (!out || total > out->n) return set_error(GXY_ERR_OVERFLOW, "secondary RayList too small");
+        if ((rc = rl_download(O, *out, total))) return rc;
+    }
+    return GXY_OK;
+    GUARD_END
+}
+
+int gxy_gpu_classify(gxy_raylist *rays) {
+    GUARD_BEGIN
+    if (!rays || rays->n < 0) return set_error(GXY_ERR_INVALID, "bad RayList");
+    int n = rays->n;
+    if (!n) return GXY_OK;
+    DevRayList R;
+    int rc;
+    if ((rc = R.alloc(n))) return rc;
+    if ((rc = rl_upload(*rays, R, n))) return rc;
+    k_rl_classify<<<(n + 255) / 256, 256>>>(R.d);
+    CK(cudaGetLastError());
+    CK(cudaMemcpy(rays->classification, R.d.i[I_CLS], n * sizeof(int32_t), cudaMemcpyDeviceToHost));
+    return GXY_OK;
+    GUARD_END
+}
+
+int gxy_gpu_assign_destinations(gxy_scene scene, int partition, gxy_raylist *rays) {
+    GUARD_BEGIN
+    if (!scene || !rays || rays->n < 0) return set_error(GXY_ERR_INVALID, "bad argument");
+    Scene *sc = reinterpret_cast<Scene *>(scene);
+    if (partition < 0 || partition >= sc->S.np) return set_error(GXY_ERR_INVALID, "bad partition");
+    int n = rays->n;
+    if (!n) return GXY_OK;
+    DevRayList R;
+    int rc;
+    if ((rc = R.alloc(n))) return rc;
+    if ((rc = rl_upload(*rays, R, n))) return rc;
+    k_rl_assign<<<(n + 255) / 256, 256>>>(sc->S, partition, R.d);
+    CK(cudaGetLastError());
+    CK(cudaMemcpy(rays->classification, R.d.i[I_CLS], n * sizeof(int32_t), cudaMemcpyDeviceToHost));
+    return GXY_OK;
+    GUARD_END
+}
+
+int gxy_gpu_accumulate_terminated(const gxy_raylist *rays, float *fb_rgba, int width, int height) {
+    GUARD_BEGIN
+    if (!rays || !fb_rgba || width <= 0 || height <= 0 || rays->n < 0)
+        return set_error(GXY_ERR_INVALID, "bad argument");
+    int n = rays->n;
+    if (!n) return GXY_OK;
+    DevRayList R;
+    int rc;
+    if ((rc = R.alloc(n))) return rc;
+    if ((rc = rl_upload(*rays, R, n))) return rc;
+    ScratchList tmp(arena());
+    float *fb;
+    size_t bytes = (size_t)width * height * 4 * sizeof(float);
+    if ((rc = tmp.alloc((void **)&fb, bytes))) return rc;
+    CK(cudaMemcpy(fb, fb_rgba, bytes, cudaMemcpyHostToDevice));
+    k_rl_accumulate<<<(n + 255) / 256, 256>>>(R.d, fb, width, height);
+    CK(cudaGetLastError());
+    CK(cudaMemcpy(fb_rgba, fb, bytes, cudaMemcpyDeviceToHost));
+    return GXY_OK;
+    GUARD_END
+}
+
+}  // extern "C"

@@ -1,0 +1,355 @@
+// trace.cuh -- the per-ray body of Galaxy's tracer on the GPU.
+//
+// trace_core follows TraceRays_TraceRays (src/renderer/TraceRays.ispc:366-620)
+// statement by statement: zero direction components -> 1e-6, slab clip
+// against the partition box (MyIntersectBox, :90-106), slice planes
+// (LookForSliceHit, :143-250), closest geometry hit through the BVH8
+// (LookForGeometryHit, :108-141), the front-to-back march with isosurface
+// search and compositing (:446-570) and the termination flags (:574-617).
+// shade_* follow TraceRays_ambientLighting / generateAORays /
+// diffuseLighting / generateShadowRays (:625-923) in the reverse-lighting
+// order of TraceRays::Trace (TraceRays.cpp:124-131).
+#pragma once
+
+#include "gxy_dev.cuh"
+
+namespace gxy {
+
+struct TraceIn {
+    V3 org, dir;        // as stored in the ray list (dir not yet adjusted)
+    float t, tmax;
+    float r, g, b, o;
+    int type, part;
+};
+
+struct TraceOut {
+    float t;
+    int term;
+    float r, g, b, o;
+    V3 n;               // surface normal (valid when term & SURFACE)
+    V3 sc;              // surface colour
+    bool surface;
+};
+
+struct RayStats {
+    unsigned samples = 0, nodes = 0, tris = 0, sphs = 0;
+    int ovf = 0;
+};
+
+// Surface attributes of a geometry hit: normal (normalised, face-forwarded)
+// and colour, as OSPRay postIntersect with DG_NG|DG_NS|DG_NORMALIZE|
+// DG_FACEFORWARD|DG_COLOR over the DataDrivenTriangleMesh /
+// DataDrivenSpheres post-intersect functions.
+__device__ __noinline__ void geometry_shade(const DevScene &S, const GeoHit &gh, V3 org, V3 dir, V3 &n_out,
+                                            V3 &c_out) {
+    V3 Ng, Ns;
+    V3 col = v3(1.f, 1.f, 1.f);
+    if (!(gh.prim & kSphereBit)) {
+        int64_t p = gh.prim;
+        int k = 0;
+        while (k + 1 < S.n_tri_sets && p >= S.tri_sets[k + 1].prim_base) k++;
+        const DevTriSet &T = S.tri_sets[k];
+        int64_t lp = p - T.prim_base;
+        const int32_t *ix = T.indices + 3 * lp;
+        int i0 = __ldg(ix), i1 = __ldg(ix + 1), i2 = __ldg(ix + 2);
+        const float *V = T.vertices;
+        V3 a = v3(__ldg(V + 3 * i0), __ldg(V + 3 * i0 + 1), __ldg(V + 3 * i0 + 2));
+        V3 b = v3(__ldg(V + 3 * i1), __ldg(V + 3 * i1 + 1), __ldg(V + 3 * i1 + 2));
+        V3 c = v3(__ldg(V + 3 * i2), __ldg(V + 3 * i2 + 1), __ldg(V + 3 * i2 + 2));
+        Ng = cross(b - a, c - a);
+        Ns = Ng;
+        float bx = 1.0f - gh.u - gh.v, by = gh.u, bz = gh.v;
+        if (T.normals) {
+            const float *N = T.normals;
+            V3 na = v3(__ldg(N + 3 * i0), __ldg(N + 3 * i0 + 1), __ldg(N + 3 * i0 + 2));
+            V3 nb = v3(__ldg(N + 3 * i1), __ldg(N + 3 * i1 + 1), __ldg(N + 3 * i1 + 2));
+            V3 nc = v3(__ldg(N + 3 * i2), __ldg(N + 3 * i2 + 1), __ldg(N + 3 * i2 + 2));
+            Ns = (bx * na + by * nb) + bz * nc;
+        }
+        if (T.data) {
+            float dv = bx * __ldg(T.data + i0) + by * __ldg(T.data + i1) + bz * __ldg(T.data + i2);
+            col = tf_color(S.tfs[T.tf], dv);
+        }
+    } else {
+        int64_t p = gh.prim & ~kSphereBit;
+        int k = 0;
+        while (k + 1 < S.n_sph_sets && p >= S.sph_sets[k + 1].prim_base) k++;
+        const DevSphSet &P = S.sph_sets[k];
+        int64_t lp = p - P.prim_base;
+        V3 c = v3(__ldg(P.centers + 3 * lp), __ldg(P.centers + 3 * lp + 1), __ldg(P.centers + 3 * lp + 2));
+        Ng = (org + gh.t * dir) - c;
+        Ns = Ng;
+        if (P.data) col = tf_color(S.tfs[P.tf], __ldg(P.data + lp));
+    }
+    Ng = nrm(Ng);
+    Ns = nrm(Ns);
+    if (dot(dir, Ng) >= 0.f) Ng = neg(Ng);
+    if (dot(Ng, Ns) < 0.f) Ns = neg(Ns);
+    n_out = Ns;
+    c_out = col;
+}
+
+// tfs: the volumes' transfer functions (shared-memory copies), indexed by volume.
+// ANY_SECONDARY: shadow/AO rays of a scene without volume integration may
+// stop at the first geometry hit (their fate does not depend on which).
+template <bool ANY_SECONDARY>
+__device__ __forceinline__ TraceOut trace_core(const DevScene &S, const DevTF *tfs, const TraceIn &R, RayStats &st) {
+    const DevPartition &P = S.part[R.part];
+    const bool shade = R.type == GXY_RAY_PRIMARY;
+    V3 org = R.org, dir = R.dir;
+    if (dir.x == 0.f) dir.x = 1e-6f;
+    if (dir.y == 0.f) dir.y = 1e-6f;
+    if (dir.z == 0.f) dir.z = 1e-6f;
+    float ray_t0 = R.t, ray_t = R.tmax;
+    const float tTimeout = ray_t;
+    float cr = R.r, cg = R.g, cb = R.b, ca = R.o;
+    float tEntry, tExitVolume;
+    {
+        float rx = 1.0f / dir.x, ry = 1.0f / dir.y, rz = 1.0f / dir.z;
+        float mnx = (P.lo[0] - org.x) * rx, mxx = (P.hi[0] - org.x) * rx;
+        float mny = (P.lo[1] - org.y) * ry, mxy = (P.hi[1] - org.y) * ry;
+        float mnz = (P.lo[2] - org.z) * rz, mxz = (P.hi[2] - org.z) * rz;
+        tEntry = fmax_(fmin_(mnx, mxx), fmax_(fmin_(mny, mxy), fmin_(mnz, mxz)));
+        tExitVolume = fmin_(fmax_(mnx, mxx), fmin_(fmax_(mny, mxy), fmax_(mnz, mxz)));
+    }
+    if (tEntry < ray_t0) tEntry = ray_t0;
+    else if (tEntry > ray_t0) ray_t0 = tEntry;
+    ray_t = fmin_(ray_t, tExitVolume);
+
+    bool surface_hit = false;
+    float hit_t = 0.f, hit_opacity = 0.f, hit_sample = 0.f;
+    V3 hit_n = v3(0, 0, 0), hit_c = v3(0, 0, 0);
+    // slice planes
+    {
+        int vid = -1;
+        for (int m = 0; m < S.n_vol; m++) {
+            const DevVolume &vv = S.vol[m];
+            for (int k = 0; k < vv.n_slices; k++) {
+                float4 pl = vv.slices[k];
+                V3 pn = v3(pl.x, pl.y, pl.z);
+                float denom = dot(dir, pn);
+                if (fabsf(denom) > 0.0001f) {
+                    float t = (pl.w - dot(org, pn)) / denom;
+                    if (t >= ray_t0 && t <= ray_t) {
+                        hit_n = denom > 0 ? neg(pn) : pn;
+                        hit_opacity = 1.0f;
+                        hit_t = t;
+                        vid = m;
+                        ray_t = t;
+                        surface_hit = true;
+                    }
+                }
+            }
+        }
+        if (surface_hit && shade) {
+            V3 p = org + hit_t * dir;
+            hit_sample = vol_sample(S.vol[vid], p);
+            hit_c = tf_color(tfs[vid], hit_sample);
+            hit_opacity = 1.0f;
+        }
+    }
+    // geometry
+    if (S.nodes && !(ANY_SECONDARY && !shade && surface_hit)) {
+        GeoHit gh;
+        bool any = ANY_SECONDARY && !shade;
+        bool h = any ? bvh_closest<true>(S, org, dir, ray_t0, ray_t, gh, st.nodes, st.tris, st.sphs, st.ovf)
+                     : bvh_closest<false>(S, org, dir, ray_t0, ray_t, gh, st.nodes, st.tris, st.sphs, st.ovf);
+        if (h) {
+            ray_t = gh.t;
+            surface_hit = true;
+            if (shade) {
+                geometry_shade(S, gh, org, dir, hit_n, hit_c);
+                hit_opacity = 1.0f;
+                hit_t = gh.t;
+            }
+        }
+    }
+    float tTermination = ray_t;
+    if (S.integrate) {
+        const float step = S.step, epsilon = S.march_eps, oa = S.opaque_alpha, rate = S.rate;
+        const int nv = S.n_vol;
+        float sLast[kMaxVol], sThis[kMaxVol];
+        CellCache cc;
+        cc.ix = -1; cc.iy = -1; cc.iz = -1;
+        bool hit_iso = false;
+        float tLast = tEntry + epsilon;
+        bool opaque = (fmin_(fmin_(cr, cg), cb) >= 1.0f || ca > oa);
+        float tThis = tEntry;
+        while (tThis <= tTermination && !opaque && !hit_iso) {
+            V3 coord = org + tThis * dir;
+            if (nv == 1) sThis[0] = vol_sample_cached(S.vol[0], coord, cc);
+            else
+                for (int m = 0; m < nv; m++) sThis[m] = vol_sample(S.vol[m], coord);
+            st.samples++;
+            if (tThis > tEntry && tLast >= epsilon) {
+                bool h = false;
+                int vid = -1;
+                for (int m = 0; m < nv; m++) {
+                    const DevVolume &vv = S.vol[m];
+                    float sl = sLast[m], sti = sThis[m];
+                    for (int k = 0; k < vv.n_iso; k++) {
+                        float iso = vv.iso[k];
+                        if (((iso >= sl) && (iso < sti)) || ((iso <= sl) && (iso > sti))) {
+                            h = true;
+                            vid = m;
+                            hit_t = tLast + ((iso - sl) / (sti - sl)) * (tThis - tLast);
+                            hit_sample = iso;
+                        }
+                    }
+                }
+                if (h) {
+                    if (shade) {
+                        V3 hp = org + hit_t * dir;
+                        V3 n = nrm(vol_gradient(S.vol[vid], hp));
+                        if (dot(dir, n) > 0) n = neg(n);
+                        hit_n = n;
+                        hit_c = tf_color(tfs[vid], hit_sample);
+                        hit_opacity = 1.0f;
+                    }
+                    tTermination = hit_t;
+                    tThis = hit_t;
+                    surface_hit = true;
+                    hit_iso = true;
+                    V3 c2 = org + tThis * dir;
+                    for (int m = 0; m < nv; m++) sThis[m] = vol_sample(S.vol[m], c2);
+                }
+                for (int m = 0; m < nv; m++) {
+                    const DevVolume &vv = S.vol[m];
+                    if (vv.volume_render) {
+                        float sv = (sLast[m] + sThis[m]) / 2.0f;
+                        float so = tf_opacity(tfs[m], sv);
+                        if (so > 0.0f) {
+                            float wo = so / rate;
+                            if (wo > 1.0f) wo = 1.0f;
+                            if (wo < 0.0f) wo = 0.0f;
+                            if (shade) {
+                                V3 sc = tf_color(tfs[m], sv);
+                                float f = 1.0f - ca;
+                                cr = cr + f * (wo * sc.x);
+                                cg = cg + f * (wo * sc.y);
+                                cb = cb + f * (wo * sc.z);
+                                ca = ca + f * wo;
+                            } else {
+                                float w = ((tThis - tLast) / step) * wo;
+                                float f = 1.0f - w;
+                                cr = cr * f;
+                                cg = cg * f;
+                                cb = cb * f;
+                                ca = ca * f;
+                            }
+                        }
+                    }
+                    sLast[m] = sThis[m];
+                }
+            }
+            for (int m = 0; m < nv; m++) sLast[m] = sThis[m];
+            opaque = (fmin_(fmin_(cr, cg), cb) >= 1.0f || ca > oa);
+            if (opaque) tTermination = tThis;
+            tLast = tThis;
+            tThis = (tThis == tEntry) ? (tEntry + epsilon)
+                    : (((tThis + step) > tTermination) && (tThis < tTermination)) ? tTermination
+                                                                                   : tThis + step;
+        }
+        ray_t = tTermination;
+    }
+    TraceOut out;
+    out.r = cr; out.g = cg; out.b = cb; out.o = ca;
+    bool op = fmin_(fmin_(cr, cg), cb) >= 1.0f || ca > S.opaque_alpha;
+    int term = op ? GXY_RAY_OPAQUE : 0;
+    out.t = ray_t;
+    out.surface = surface_hit;
+    if (surface_hit) {
+        term |= GXY_RAY_SURFACE;
+        if (hit_opacity > 0.999f) term |= GXY_RAY_OPAQUE;
+        out.n = hit_n;
+        out.sc = hit_c;
+    } else if (tTermination == tExitVolume) {
+        term |= GXY_RAY_BOUNDARY;
+    } else if (tTermination == tTimeout) {
+        term |= GXY_RAY_TIMEOUT;
+    }
+    out.term = term;
+    return out;
+}
+
+// Box::exit_face (src/data/Box.cpp:84-97).
+__device__ __forceinline__ int exit_face(const DevPartition &b, V3 o, V3 d) {
+    const float FM = 3.402823466e+38f;
+    float tx = (d.x > 0.0001f) ? ((b.hi[0] - o.x) / d.x) : (d.x < -0.0001f) ? ((b.lo[0] - o.x) / d.x) : FM;
+    float ty = (d.y > 0.0001f) ? ((b.hi[1] - o.y) / d.y) : (d.y < -0.0001f) ? ((b.lo[1] - o.y) / d.y) : FM;
+    float tz = (d.z > 0.0001f) ? ((b.hi[2] - o.z) / d.z) : (d.z < -0.0001f) ? ((b.lo[2] - o.z) / d.z) : FM;
+    if (tx < 0) tx = FM;
+    if (ty < 0) ty = FM;
+    if (tz < 0) tz = FM;
+    if (tx < ty && tx < tz) return (d.x < 0) ? 0 : 1;
+    else if (ty < tz) return (d.y < 0) ? 2 : 3;
+    else return (d.z < 0) ? 4 : 5;
+}
+
+// Renderer::Classify (Renderer.cpp:304-421), reverse lighting; RAY_BOUNDARY
+// (4) marks "to the exit face" until destinations are assigned.
+__device__ __forceinline__ int classify_ray(int type, int term) {
+    if (type == GXY_RAY_PRIMARY) {
+        if (term & GXY_RAY_BOUNDARY) return GXY_RAY_BOUNDARY;
+        if ((term & GXY_RAY_OPAQUE) | (term & GXY_RAY_TIMEOUT)) return GXY_TERMINATED;
+        return GXY_KEEP_HERE;
+    }
+    if (type == GXY_RAY_SHADOW || type == GXY_RAY_AO) {
+        if ((term & GXY_RAY_OPAQUE) | (term & GXY_RAY_SURFACE)) return GXY_TERMINATED;
+        if (term & GXY_RAY_BOUNDARY) return GXY_RAY_BOUNDARY;
+        return GXY_DROP_ON_FLOOR;
+    }
+    return GXY_DROP_ON_FLOOR;
+}
+
+// Renderer::AssignDestinations (Renderer.cpp:423-454) for one ray.
+__device__ __forceinline__ int assign_destination(const DevScene &S, int part, int type, int cls, V3 o, V3 d) {
+    if (cls != GXY_RAY_BOUNDARY) return cls;
+    int f = exit_face(S.part[part], o, d);
+    int nb = S.part[part].nb[f];
+    if (nb >= 0) return nb;
+    return (type == GXY_RAY_SHADOW || type == GXY_RAY_AO) ? GXY_DROP_ON_FLOOR : GXY_TERMINATED;
+}
+
+// One secondary ray produced by shading.
+struct Spawned {
+    V3 o, d;
+    float r, g, b, tmax;
+    int type;
+};
+
+// Surface point + normal of a primary surface hit, the inputs of the
+// lighting functions.
+struct ShadeIn {
+    V3 org, dir;      // stored (unadjusted) ray
+    float t;
+    V3 n, sc;
+    int x, y;
+};
+
+// AO ray j (TraceRays.ispc:661-730) with payload ambient_{r,g,b}.
+__device__ __forceinline__ Spawned ao_ray(const DevScene &S, const DevLights &L, const ShadeIn &h, int j, float ar,
+                                          float ag, float ab, V3 b0, V3 b1, V3 o) {
+    int r = ((h.x * 9949 + h.y * 9613 + j * 9151) >> 8) & 0xff;
+    float4 tab = __ldg(S.ao + r);
+    float x = tab.x * tab.z;
+    float y = tab.y * tab.z;
+    float z = tab.w + S.epsilon;
+    V3 rd = (x * b0 + y * b1) + z * h.n;
+    Spawned s;
+    s.o = o;
+    s.d = rd;
+    s.r = ar; s.g = ag; s.b = ab;
+    s.tmax = L.ao_radius;
+    s.type = GXY_RAY_AO;
+    return s;
+}
+
+__device__ __forceinline__ void ao_basis(V3 n, V3 &b0, V3 &b1) {
+    b0 = v3(1.f, 0.f, 0.f);
+    if (fabsf(dot(b0, n)) > 0.95f) b0 = v3(0.f, 1.f, 0.f);
+    b1 = nrm(cross(b0, n));
+    b0 = nrm(cross(b1, n));
+}
+
+}  // namespace gxy

@@ -1,0 +1,193 @@
+"""ctypes binding of libgxy_gpu.so (include/gxy_gpu.h).
+
+The GPU library is the only implementation of the ray path in this package:
+if it is missing or fails to load, every call raises -- there is no CPU
+fallback.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import _abi as A
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_build", "libgxy_gpu.so")
+_lib = None
+_initialised = False
+
+
+class GxyError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("gxy error %d: %s" % (code, msg))
+        self.code = code
+
+
+def lib():
+    """Load libgxy_gpu.so (built by galaxy_gb300.build)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError("libgxy_gpu.so is not built (%s); run galaxy_gb300.build.build()" % LIB_PATH)
+    L = C.CDLL(LIB_PATH)
+    vp, i32, i64 = C.c_void_p, C.c_int32, C.c_int64
+    sig = {
+        "gxy_gpu_init": [C.c_int, C.c_size_t],
+        "gxy_gpu_shutdown": [],
+        "gxy_gpu_last_error": [C.c_char_p, C.c_int],
+        "gxy_gpu_hbm_in_use": [C.POINTER(C.c_size_t)],
+        "gxy_gpu_scene_commit": [C.POINTER(A.gxy_scene_desc), C.POINTER(vp)],
+        "gxy_gpu_scene_release": [vp],
+        "gxy_gpu_scene_partition_info": [vp, C.c_int, C.POINTER(A.gxy_partition_info)],
+        "gxy_gpu_scene_bvh_info": [vp, C.POINTER(i64), C.POINTER(i64), C.POINTER(C.c_double)],
+        "gxy_resolve_lights": [C.POINTER(A.gxy_lighting), C.POINTER(A.gxy_camera), C.POINTER(A.gxy_lighting)],
+        "gxy_gpu_render": [vp, C.POINTER(A.gxy_camera), C.POINTER(A.gxy_lighting), vp, vp],
+        "gxy_gpu_render_host": [vp, C.POINTER(A.gxy_camera), C.POINTER(A.gxy_lighting), A.f32p, vp],
+        "gxy_gpu_query_counters": [vp, C.POINTER(A.gxy_counters)],
+        "gxy_gpu_query_counters_ex": [vp, C.POINTER(i64), C.POINTER(i64), C.POINTER(i64)],
+        "gxy_gpu_generate_initial_rays": [vp, C.c_int, C.POINTER(A.gxy_camera), C.POINTER(A.gxy_raylist),
+                                          C.POINTER(i32)],
+        "gxy_gpu_trace_raylist": [vp, C.c_int, C.POINTER(A.gxy_lighting), C.POINTER(A.gxy_raylist),
+                                  C.POINTER(A.gxy_raylist), C.POINTER(i32)],
+        "gxy_gpu_classify": [C.POINTER(A.gxy_raylist)],
+        "gxy_gpu_assign_destinations": [vp, C.c_int, C.POINTER(A.gxy_raylist)],
+        "gxy_gpu_accumulate_terminated": [C.POINTER(A.gxy_raylist), A.f32p, C.c_int, C.c_int],
+    }
+    for name, args in sig.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = C.c_int
+    _lib = L
+    return L
+
+
+def check(rc):
+    if rc != A.GXY_OK:
+        buf = C.create_string_buffer(1024)
+        lib().gxy_gpu_last_error(buf, 1024)
+        raise GxyError(rc, buf.value.decode(errors="replace"))
+    return rc
+
+
+def init(device=0, hbm_budget=0):
+    global _initialised
+    check(lib().gxy_gpu_init(device, hbm_budget))
+    _initialised = True
+
+
+def ensure_init():
+    if not _initialised:
+        init()
+
+
+def hbm_in_use():
+    v = C.c_size_t(0)
+    check(lib().gxy_gpu_hbm_in_use(C.byref(v)))
+    return v.value
+
+
+def resolve_lights(lighting, camera):
+    """Rendering::resolve_lights through the C ABI; returns a gxy_lighting."""
+    out = A.gxy_lighting()
+    L = lighting.c() if hasattr(lighting, "c") else lighting
+    cam = camera.c() if hasattr(camera, "c") else camera
+    check(lib().gxy_resolve_lights(C.byref(L), C.byref(cam), C.byref(out)))
+    return out
+
+
+class Scene:
+    """A committed Visualization on the device (gxy_gpu_scene_commit)."""
+
+    def __init__(self, vis):
+        ensure_init()
+        self.desc = vis.desc()
+        h = C.c_void_p()
+        check(lib().gxy_gpu_scene_commit(C.byref(self.desc), C.byref(h)))
+        self.h = h
+
+    def release(self):
+        if getattr(self, "h", None) and self.h.value:
+            lib().gxy_gpu_scene_release(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.release()
+        except Exception:
+            pass
+
+    def partition_info(self, p):
+        pi = A.gxy_partition_info()
+        check(lib().gxy_gpu_scene_partition_info(self.h, p, C.byref(pi)))
+        return pi
+
+    def bvh_info(self):
+        n, s, ms = C.c_int64(), C.c_int64(), C.c_double()
+        check(lib().gxy_gpu_scene_bvh_info(self.h, C.byref(n), C.byref(s), C.byref(ms)))
+        return {"nodes": n.value, "prim_refs": s.value, "build_ms": ms.value}
+
+    def render(self, camera, lighting, fb_ptr, stream=None):
+        """Device framebuffer (pointer) path; contributions are added."""
+        cam = camera.c() if hasattr(camera, "c") else camera
+        L = lighting if isinstance(lighting, A.gxy_lighting) else lighting.c()
+        check(lib().gxy_gpu_render(self.h, C.byref(cam), C.byref(L), C.c_void_p(fb_ptr),
+                                   C.c_void_p(stream or 0)))
+
+    def render_host(self, camera, lighting, out=None, stream=None):
+        """Host framebuffer path: returns (height, width, 4) float32."""
+        cam = camera.c() if hasattr(camera, "c") else camera
+        L = lighting if isinstance(lighting, A.gxy_lighting) else lighting.c()
+        if out is None:
+            out = np.zeros((cam.height, cam.width, 4), np.float32)
+        check(lib().gxy_gpu_render_host(self.h, C.byref(cam), C.byref(L), A.fptr(out), C.c_void_p(stream or 0)))
+        return out
+
+    def counters(self):
+        c = A.gxy_counters()
+        check(lib().gxy_gpu_query_counters(self.h, C.byref(c)))
+        d = {f: getattr(c, f) for f, _ in A.gxy_counters._fields_ if f != "pad"}
+        t, s, e = C.c_int64(), C.c_int64(), C.c_int64()
+        check(lib().gxy_gpu_query_counters_ex(self.h, C.byref(t), C.byref(s), C.byref(e)))
+        d.update(tri_tests=t.value, sph_tests=s.value, enqueued=e.value)
+        return d
+
+    # ---- RayList drop-in
+    def generate_initial_rays(self, p, camera, capacity=None):
+        cam = camera.c() if hasattr(camera, "c") else camera
+        out = A.RayListArrays(capacity or cam.width * cam.height)
+        n = C.c_int32(0)
+        rl = out.c()
+        check(lib().gxy_gpu_generate_initial_rays(self.h, p, C.byref(cam), C.byref(rl), C.byref(n)))
+        return out.truncate(n.value)
+
+    def trace(self, p, lighting, rays, capacity=None):
+        """TraceRays::Trace on a copy of `rays`: returns (traced, secondary)."""
+        rin = rays.copy()
+        L = lighting if isinstance(lighting, A.gxy_lighting) else lighting.c()
+        cap = capacity if capacity is not None else max(1, rays.n * 40)
+        out = A.RayListArrays(cap)
+        n = C.c_int32(0)
+        ci, co = rin.c(), out.c()
+        check(lib().gxy_gpu_trace_raylist(self.h, p, C.byref(L), C.byref(ci), C.byref(co), C.byref(n)))
+        return rin, out.truncate(n.value)
+
+    def assign_destinations(self, p, rays):
+        r = rays.copy()
+        c = r.c()
+        check(lib().gxy_gpu_assign_destinations(self.h, p, C.byref(c)))
+        return r
+
+
+def classify(rays):
+    r = rays.copy()
+    c = r.c()
+    check(lib().gxy_gpu_classify(C.byref(c)))
+    return r
+
+
+def accumulate_terminated(rays, fb):
+    c = rays.c()
+    h, w, _ = fb.shape
+    check(lib().gxy_gpu_accumulate_terminated(C.byref(c), A.fptr(fb), w, h))
+    return fb

@@ -235,6 +235,10 @@ int gxy_gpu_render(gxy_scene scene, const gxy_camera *camera, const gxy_lighting
 int gxy_gpu_render_host(gxy_scene scene, const gxy_camera *camera,
                         const gxy_lighting *lighting, float *host_fb_rgba, void *stream);
 int gxy_gpu_query_counters(gxy_scene scene, gxy_counters *out);
+/* Per-type primitive test counts and queue records written by the last
+ * gxy_gpu_render (inputs of the algorithmic-bytes model). */
+int gxy_gpu_query_counters_ex(gxy_scene scene, int64_t *tri_tests, int64_t *sph_tests,
+                              int64_t *enqueued);
 
 /* ---- RayList-level drop-in (host buffers) ------------------------------ */
 

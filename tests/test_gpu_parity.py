@@ -1,0 +1,217 @@
+"""GPU path against the CPU oracle on the same seeded scenes.
+
+Tolerances (floating-point path; the GPU kernels and the oracle evaluate the
+same IEEE single-precision expressions in the same order, so most results are
+bit-identical; differences come from the order of float atomics in the
+framebuffer and from the rare primitive whose hit distance ties):
+  * primary and shadow hit/miss agreement >= 99.99 %,
+  * hit distance t within 1e-5 relative,
+  * images: max 2/255 per channel on 99.9 % of channels and RMSE <= 1e-3,
+  * composited volume samples within 1e-4 of the oracle's FP64 re-evaluation.
+"""
+import numpy as np
+import pytest
+
+import gold_scenes as G
+import oracle_lib as O
+from galaxy_gb300 import _abi as A
+from galaxy_gb300 import scene as S
+from galaxy_gb300 import scenes
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def gpu():
+    from galaxy_gb300 import gpu as g
+    g.init(0)
+    return g
+
+
+def image_close(img, ref, rmse_tol=1e-3, ch_tol=2.0 / 255, frac=0.999):
+    d = np.abs(img[..., :3] - ref[..., :3])
+    rmse = float(np.sqrt(np.mean(d ** 2)))
+    ok = float(np.mean(d <= ch_tol))
+    assert rmse <= rmse_tol, ("rmse", rmse)
+    assert ok >= frac, ("fraction within %g" % ch_tol, ok, float(d.max()))
+    return rmse, float(d.max())
+
+
+def render_both(gpu, cam, vis, threads=8):
+    L = S.resolve_lights(vis.lighting, cam)
+    sc = gpu.Scene(vis)
+    img = sc.render_host(cam, L)
+    ref, cnt = O.OracleScene(vis).render(cam, L, nthreads=threads)
+    return img, ref, sc, cnt
+
+
+@pytest.mark.parametrize("name", ["absolute", "absolute-shadow", "camera-shadow", "infinite", "nineBalls",
+                                  "oneBall", "xyz"])
+def test_gold_scenes_match_oracle(gpu, name):
+    for cam, vis, _ in G.load_gold_state(name, size=192, n=128)[:2]:
+        img, ref, sc, cnt = render_both(gpu, cam, vis)
+        image_close(img, ref)
+        c = sc.counters()
+        assert c["primary_rays"] == cnt["primary"]
+        assert c["shadow_rays"] == cnt["shadow"] and c["ao_rays"] == cnt["ao"]
+
+
+def test_partitioned_gold_scene(gpu):
+    cam, vis, _ = G.load_gold_state("absolute-shadow", size=160, n=96, partitions=(2, 2, 1))[0]
+    img, ref, sc, cnt = render_both(gpu, cam, vis)
+    image_close(img, ref)
+    c = sc.counters()
+    assert c["handoffs"] > 0 and c["primary_rays"] == cnt["primary"]
+
+
+def test_triangle_scene(gpu):
+    cam, vis = scenes.triangle_spheres_scene(width=160, height=160, n_seg=24)
+    img, ref, sc, cnt = render_both(gpu, cam, vis)
+    image_close(img, ref)
+    c = sc.counters()
+    assert c["primary_rays"] == 160 * 160 == cnt["primary"]
+    assert c["shadow_rays"] == cnt["shadow"]
+
+
+def test_mixed_partitioned_scene(gpu):
+    cam, vis = scenes.mixed_scene(n=64, n_spheres=20000, width=128, height=128, partitions=(2, 2, 2), n_ao=4)
+    img, ref, sc, cnt = render_both(gpu, cam, vis)
+    image_close(img, ref)
+    c = sc.counters()
+    assert c["primary_rays"] == cnt["primary"]
+    assert abs(c["ao_rays"] - cnt["ao"]) <= 0.001 * cnt["ao"] + 8
+
+
+def test_volume_scene(gpu):
+    cam, vis = scenes.volume_scene(n=96, width=128, height=128)
+    img, ref, sc, cnt = render_both(gpu, cam, vis)
+    image_close(img, ref)
+    assert sc.counters()["samples"] == cnt["samples"]
+
+
+# ------------------------------------------------------------ RayList level
+def _fields_equal(a, b, names, rtol=0.0):
+    for f in names:
+        x, y = getattr(a, f), getattr(b, f)
+        if rtol == 0.0:
+            assert np.array_equal(x, y), f
+        else:
+            np.testing.assert_allclose(x, y, rtol=rtol, atol=1e-6, err_msg=f)
+
+
+def test_raylist_camera_rays_identical(gpu):
+    cam, vis = scenes.mixed_scene(n=64, n_spheres=5000, width=96, height=80, partitions=(2, 2, 1))
+    g = gpu.Scene(vis)
+    o = O.OracleScene(vis)
+    for p in range(4):
+        a = g.generate_initial_rays(p, cam)
+        b = o.generate_initial_rays(p, cam)
+        assert a.n == b.n
+        _fields_equal(a, b, ("x", "y", "type", "ox", "oy", "oz", "dx", "dy", "dz", "t", "tMax"))
+
+
+def _hit_agreement(a, b):
+    ha = (a.term & A.RAY_SURFACE) != 0
+    hb = (b.term & A.RAY_SURFACE) != 0
+    return float(np.mean(ha == hb)), ha & hb
+
+
+@pytest.mark.parametrize("which", ["triangles", "mixed", "iso"])
+def test_raylist_trace_matches_oracle(gpu, which):
+    if which == "triangles":
+        cam, vis = scenes.triangle_spheres_scene(width=128, height=128, n_seg=32)
+    elif which == "mixed":
+        cam, vis = scenes.mixed_scene(n=64, n_spheres=20000, width=96, height=96, partitions=(1, 1, 1), n_ao=4)
+    else:
+        cam, vis, _ = G.load_gold_state("oneBall", size=96, n=96)[0]
+    L = S.resolve_lights(vis.lighting, cam)
+    g = gpu.Scene(vis)
+    o = O.OracleScene(vis)
+    rays = o.generate_initial_rays(0, cam)
+    ta, sa = g.trace(0, L, rays)
+    tb, sb = o.trace(0, L, rays)
+    agree, both = _hit_agreement(ta, tb)
+    assert agree >= 0.9999, agree
+    np.testing.assert_allclose(ta.t[both], tb.t[both], rtol=1e-5)
+    assert sa.n == sb.n
+    np.testing.assert_allclose(np.stack([ta.r, ta.g, ta.b, ta.o]), np.stack([tb.r, tb.g, tb.b, tb.o]), atol=2e-6)
+    # secondary rays: same order (AO block, then shadow block), same payloads
+    _fields_equal(sa, sb, ("x", "y", "type"))
+    _fields_equal(sa, sb, ("ox", "oy", "oz", "dx", "dy", "dz", "r", "g", "b", "tMax"), rtol=1e-5)
+    # trace the secondaries: shadow/AO hit/miss agreement
+    ua, _ = g.trace(0, L, sb)
+    ub, _ = o.trace(0, L, sb)
+    agree2, _ = _hit_agreement(ua, ub)
+    assert agree2 >= 0.9999, agree2
+    # classify and destinations
+    ca = gpu.classify(ua)
+    cb = o.classify(ub)
+    assert np.mean(ca.classification == cb.classification) >= 0.9999
+
+
+def test_assign_destinations_identical(gpu):
+    cam, vis = scenes.mixed_scene(n=64, n_spheres=2000, width=64, height=64, partitions=(2, 2, 2))
+    L = S.resolve_lights(vis.lighting, cam)
+    g = gpu.Scene(vis)
+    o = O.OracleScene(vis)
+    for p in range(8):
+        rays = o.generate_initial_rays(p, cam)
+        if rays.n == 0:
+            continue
+        tb, _ = o.trace(p, L, rays)
+        cb = o.classify(tb)
+        da = g.assign_destinations(p, cb)
+        db = o.assign_destinations(p, cb)
+        assert np.array_equal(da.classification, db.classification)
+
+
+def test_accumulate_terminated(gpu):
+    rng = np.random.default_rng(5)
+    n = 5000
+    r = A.RayListArrays(n, x=rng.integers(0, 32, n), y=rng.integers(0, 16, n),
+                        r=rng.normal(size=n), g=rng.normal(size=n), b=rng.normal(size=n), o=rng.normal(size=n),
+                        classification=rng.choice([A.TERMINATED, A.DROP_ON_FLOOR, 3], n))
+    fb = np.zeros((16, 32, 4), np.float32)
+    gpu.accumulate_terminated(r, fb)
+    ref = np.zeros((16, 32, 4), np.float64)
+    m = r.classification == A.TERMINATED
+    np.add.at(ref, (r.y[m], r.x[m]), np.stack([r.r, r.g, r.b, r.o], -1)[m])
+    np.testing.assert_allclose(fb, ref, atol=1e-4)
+
+
+def test_volume_composite_fp64(gpu):
+    """Composited primary-ray colour against the oracle's FP64 re-evaluation
+    of the same sample positions."""
+    cam, vis = scenes.volume_scene(n=128, width=96, height=96)
+    L = S.resolve_lights(vis.lighting, cam)
+    g = gpu.Scene(vis)
+    o = O.OracleScene(vis)
+    rays = o.generate_initial_rays(0, cam)
+    ta, _ = g.trace(0, L, rays)
+    ref64 = o.trace_f64(0, rays)
+    got = np.stack([ta.r, ta.g, ta.b, ta.o], -1).astype(np.float64)
+    err = np.abs(got - ref64)
+    assert float(np.quantile(err, 0.9999)) <= 1e-4, float(err.max())
+
+
+def test_bvh_stats(gpu):
+    cam, vis = scenes.triangle_spheres_scene(width=64, height=64, n_seg=40)
+    g = gpu.Scene(vis)
+    info = g.bvh_info()
+    n = len(vis.operators[0].dataset.indices)
+    assert info["prim_refs"] == n
+    assert n / 8 <= info["nodes"] <= n
+
+
+def test_errors_are_reported(gpu):
+    from galaxy_gb300.gpu import GxyError
+    cam, vis = scenes.triangle_spheres_scene(width=32, height=32, n_seg=8)
+    g = gpu.Scene(vis)
+    L = vis.lighting.c()
+    L.n_lights = 99
+    with pytest.raises(GxyError):
+        g.render_host(cam, L)
+    bad = vis.lighting.c()
+    bad.types[0] = 1    # unresolved camera light
+    with pytest.raises(GxyError):
+        g.render_host(cam, bad)
