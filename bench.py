@@ -1,0 +1,336 @@
+"""Benchmark of the GB300 ray path (plain GPU path, one frame per step).
+
+Workload (default "mixed"): the partitioned mixed scene -- a 512^3 fp32
+Gaussian-blob volume (64 blobs) in 2x2x2 brick partitions plus 4M spheres of
+radius 0.002 (half uniform, half in 32 clusters), 2048x2048, one directional
+light, shadows plus 4 AO rays per surface hit, rays handed between partition
+queues on the device.  Other workloads: "volume" (256^3, 1024x1024, 0.5-voxel
+steps, alpha 0.99) and "triangles" (9 displaced spheres, ~197k triangles,
+512x512, shadows).  All inputs are seeded synthetic data.
+
+metric value: rays traced per second (primary + shadow + AO rays of a frame
+divided by the frame's device time), whole job over N GPUs; frames are
+independent replicas on every GPU ("replicas only": the path is a
+single-GPU frame, no collective).  --impl reference times the CPU
+restatement of Galaxy's path (oracle/, the only CPU implementation of the
+path that builds here) on the host cores, on a bounded band of image rows.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "rays/s + p50/p99 frame latency: served vs plain GPU path at RMSE≤1e-3"
+
+
+def make_workload(name):
+    from galaxy_gb300 import scenes
+    if name == "mixed":
+        cam, vis = scenes.mixed_scene()
+        cfg = {"workload": "partitioned mixed scene: 512^3 fp32 blob volume in 2x2x2 bricks + 4M spheres r=0.002, "
+                           "2048x2048, shadows + 4 AO rays per hit",
+               "image": [2048, 2048], "volume": [512, 512, 512], "spheres": 4_000_000, "partitions": [2, 2, 2],
+               "ao_rays": 4, "shadows": True}
+    elif name == "volume":
+        cam, vis = scenes.volume_scene()
+        cfg = {"workload": "volume: 256^3 fp32 blob volume, 1024x1024, 0.5-voxel steps, early termination 0.99",
+               "image": [1024, 1024], "volume": [256, 256, 256]}
+    elif name == "triangles":
+        cam, vis = scenes.triangle_spheres_scene()
+        cfg = {"workload": "triangles: 9 displaced UV spheres (~197k triangles), 512x512, directional light, shadows",
+               "image": [512, 512], "triangles": int(len(vis.operators[0].dataset.indices))}
+    else:
+        raise SystemExit("unknown workload " + name)
+    return cam, vis, cfg
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(5)
+        except Exception:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"], "samples": 0}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def algorithmic_bytes(g):
+    """Algorithmic bytes of one generation's kernel: 64 B per queue record
+    read and written, 128 B per BVH8 node line, 48 B per triangle and 16 B
+    per sphere tested, 4 B per volume sample, 32 B per framebuffer
+    contribution (read + write of fp32 RGBA)."""
+    return (64 * g["rays_in"] + 64 * g["enqueued"] + 128 * g["nodes"] + 48 * g["tri_tests"] +
+            16 * g["sph_tests"] + 4 * g["samples"] + 32 * g["terminated"])
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def cpu_baseline(cam, vis, target_s=15.0, threads=None):
+    """The oracle (CPU restatement of Galaxy's path) on a band of image rows
+    around the middle of the image, sized to about target_s seconds."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_lib as O
+    from galaxy_gb300 import scene as S
+    threads = threads or os.cpu_count() or 1
+    L = S.resolve_lights(vis.lighting, cam)
+    t0 = time.time()
+    osc = O.OracleScene(vis)
+    setup = time.time() - t0
+    mid = cam.height // 2
+    rows = max(4, threads)
+    # probe band, then size the sample to target_s
+    r0 = mid - rows // 2
+    t0 = time.time()
+    _, c = osc.render(cam, L, nthreads=threads, rows=(r0, r0 + rows))
+    dt = max(time.time() - t0, 1e-3)
+    rows2 = int(min(cam.height, max(rows, rows * target_s / dt)))
+    r0 = max(0, mid - rows2 // 2)
+    t0 = time.time()
+    _, c = osc.render(cam, L, nthreads=threads, rows=(r0, r0 + rows2))
+    dt = time.time() - t0
+    rays = c["primary"] + c["shadow"] + c["ao"]
+    return {"value": rays / dt, "unit": "rays/s", "cores": threads, "kind": "port",
+            "sample": "rows %d-%d of %dx%d (%d rays, %.1f s; scene set-up %.1f s excluded)" % (
+                r0, r0 + rows2, cam.width, cam.height, rays, dt, setup), "seconds": dt}, osc, L
+
+
+def dist_setup(n_gpus):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("gloo")
+    return rank, world, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def allreduce_max(x, world):
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def run_reference(args):
+    rank, world, local = dist_setup(args.gpus)
+    if rank != 0:
+        return
+    cam, vis, cfg = make_workload(args.workload)
+    threads = os.cpu_count() or 1
+    per_step = max(2.0, 90.0 / max(1, args.steps + args.warmup))
+    # the first call sizes the row band; every step then renders that band
+    base, osc, L = cpu_baseline(cam, vis, target_s=per_step, threads=threads)
+    band = [int(x) for x in base["sample"].split()[1].split("-")]
+    vals, secs = [], []
+    for i in range(args.warmup + args.steps):
+        t0 = time.time()
+        _, c = osc.render(cam, L, nthreads=threads, rows=(band[0], band[1]))
+        dt = time.time() - t0
+        if i >= args.warmup:
+            vals.append((c["primary"] + c["shadow"] + c["ao"]) / dt)
+            secs.append(dt)
+    v = float(np.median(vals))
+    base["seconds"] = float(np.median(secs))
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "rays/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": base["seconds"] * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "config": cfg,
+            "cpu_baseline": {"value": v, "unit": "rays/s", "cores": threads, "kind": "port",
+                             "sample": base["sample"]},
+            "e2e": {"value": v, "unit": "rays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="mixed", choices=["mixed", "volume", "triangles"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    args.warmup = max(3, args.warmup)
+
+    import torch
+    rank, world, local = dist_setup(args.gpus)
+    torch.cuda.set_device(local)
+    from galaxy_gb300 import _abi as A
+    from galaxy_gb300 import gpu
+    from galaxy_gb300 import scene as S
+
+    cam, vis, cfg = make_workload(args.workload)
+    gpu.init(local)
+    t0 = time.time()
+    sc = gpu.Scene(vis)
+    commit_s = time.time() - t0
+    L = S.resolve_lights(vis.lighting, cam)
+    cam_c = cam.c()
+    stream = torch.cuda.current_stream()
+    fb = torch.zeros((cam.height, cam.width, 4), dtype=torch.float32, device="cuda")
+
+    def frame():
+        fb.zero_()
+        sc.render(cam_c, L, fb.data_ptr(), stream.cuda_stream)
+
+    sc.set_profiling(True)
+    for _ in range(args.warmup):
+        frame()
+    torch.cuda.synchronize()
+    c = sc.counters()
+    rays_per_frame = c["primary_rays"] + c["shadow_rays"] + c["ao_rays"]
+
+    # ---- timed region: K frames, per-frame events, clocks sampled
+    clocks = ClockSampler(local)
+    barrier(world)
+    torch.cuda.synchronize()
+    clocks.start()
+    time.sleep(0.3)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    gen_ms, gen_bytes = {}, {}
+    launches = 0
+    t_start = torch.cuda.Event(enable_timing=True)
+    t_end = torch.cuda.Event(enable_timing=True)
+    t_start.record(stream)
+    for k in range(args.steps):
+        ev[k][0].record(stream)
+        frame()
+        ev[k][1].record(stream)
+        gens = sc.generations()
+        launches += len(gens)
+        for gi, g in enumerate(gens):
+            gen_ms.setdefault(gi, []).append(g["ms"])
+            gen_bytes.setdefault(gi, []).append(algorithmic_bytes(g))
+    t_end.record(stream)
+    torch.cuda.synchronize()
+    barrier(world)
+    clk = clocks.stop()
+    total_ms = t_start.elapsed_time(t_end)
+    frame_ms = [a.elapsed_time(b) for a, b in ev]
+    total_ms = allreduce_max(total_ms, world)
+    value = rays_per_frame * args.steps * world / (total_ms / 1e3)
+
+    # ---- end to end through the host-framebuffer C ABI call
+    host_fb = torch.empty((cam.height, cam.width, 4), dtype=torch.float32, pin_memory=True).numpy()
+    sc.set_profiling(False)
+    sc.render_host(cam_c, L, out=host_fb, stream=stream.cuda_stream)
+    torch.cuda.synchronize()
+    e2e_steps = max(3, min(args.steps, 10))
+    barrier(world)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        sc.render_host(cam_c, L, out=host_fb, stream=stream.cuda_stream)
+    torch.cuda.synchronize()
+    e2e_s = allreduce_max(time.perf_counter() - t0, world)
+    e2e = {"value": rays_per_frame * e2e_steps * world / e2e_s, "unit": "rays/s",
+           "h2d_bytes_per_step": int(ctypes_size(A.gxy_camera) + ctypes_size(A.gxy_lighting)),
+           "d2h_bytes_per_step": int(host_fb.nbytes)}
+
+    # ---- roofline of the dominant kernel (largest share of device time)
+    dom = max(gen_ms, key=lambda g: sum(gen_ms[g]))
+    dom_ms = float(np.mean(gen_ms[dom]))
+    dom_bytes = float(np.mean(gen_bytes[dom]))
+    peak, peak_kind = measured_peaks()
+    achieved = dom_bytes / (dom_ms / 1e3) / 1e9
+    share = sum(gen_ms[dom]) / max(1e-9, sum(sum(v) for v in gen_ms.values()))
+    traffic = None
+    tf = os.path.join(ROOT, "profiles", "traffic_%s.json" % args.workload)
+    if os.path.exists(tf):
+        t = json.load(open(tf))
+        traffic = t.get("bytes_per_launch")
+    roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": traffic, "peak_source": peak_kind,
+            "kernel": "k_frame generation %d (%s)" % (dom, "camera rays" if dom == 0 else "queue"),
+            "kernel_ms": dom_ms, "algorithmic_bytes": dom_bytes, "share_of_frame_kernel_time": share}
+
+    out = {"metric": METRIC, "value": value, "unit": "rays/s", "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+           "config": dict(cfg, l2="inputs larger than L2 (volume 512 MiB + spheres)" if args.workload == "mixed"
+                          else "L2 not flushed; working set may be L2-resident", parallelism="replicas"),
+           "latency_ms": {"p50": float(np.percentile(frame_ms, 50)), "p95": float(np.percentile(frame_ms, 95)),
+                          "p99": float(np.percentile(frame_ms, 99))},
+           "rays_per_frame": rays_per_frame,
+           "rays": {"primary": c["primary_rays"], "shadow": c["shadow_rays"], "ao": c["ao_rays"],
+                    "segments": c["segments"], "handoffs": c["handoffs"], "generations": c["bounces"],
+                    "samples": c["samples"], "bvh_nodes": c["nodes"], "prim_tests": c["prim_tests"]},
+           "scene_commit_s": commit_s, "bvh": sc.bvh_info(),
+           "gpu_launches": launches, "roofline": roof, "e2e": e2e, "clocks": clk}
+    if rank == 0 and not args.no_cpu_baseline:
+        base, _, _ = cpu_baseline(cam, vis, target_s=args.cpu_seconds)
+        base.pop("seconds", None)
+        out["cpu_baseline"] = base
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+
+
+def ctypes_size(t):
+    import ctypes
+    return ctypes.sizeof(t)
+
+
+if __name__ == "__main__":
+    main()

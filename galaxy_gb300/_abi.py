@@ -166,3 +166,8 @@ class RayListArrays:
         for f in RAY_FLOAT_FIELDS + RAY_INT_FIELDS:
             setattr(out, f, np.ascontiguousarray(getattr(self, f)[idx]))
         return out
+
+
+class gxy_generation_stats(C.Structure):
+    _fields_ = [("ms", C.c_double)] + [(n, C.c_int64) for n in (
+        "rays_in", "enqueued", "segments", "samples", "nodes", "tri_tests", "sph_tests", "terminated")]

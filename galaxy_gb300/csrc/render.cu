@@ -200,6 +200,8 @@ struct Scene {
     int64_t bounces = 0;
     float *fbtmp = nullptr;
     size_t fbtmp_elems = 0;
+    int profile = 0;
+    std::vector<gxy_generation_stats> gens;
     std::mutex mu;                      // one render at a time per scene
     ~Scene() {
         for (void *p : owned) arena().free(p);
@@ -955,22 +957,55 @@ static int render(Scene *sc, const gxy_camera &cam, const gxy_lighting &lt, floa
     A.ctr = sc->ctr;
     A.qcap = (unsigned)sc->qcap;
     bool anysec = !S.integrate;
+    // optional per-generation timing and counter snapshots
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    DevCounters prev{};
+    sc->gens.clear();
+    if (sc->profile) {
+        CK(cudaEventCreate(&ev0));
+        CK(cudaEventCreate(&ev1));
+    }
+    auto gen_done = [&](unsigned rays_in) -> int {
+        if (!sc->profile) return GXY_OK;
+        DevCounters now;
+        CK(cudaMemcpyAsync(&now, sc->ctr, sizeof now, cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        float ms = 0;
+        CK(cudaEventElapsedTime(&ms, ev0, ev1));
+        gxy_generation_stats g{};
+        g.ms = ms;
+        g.rays_in = rays_in;
+        g.enqueued = (int64_t)(now.enqueued - prev.enqueued);
+        g.segments = (int64_t)(now.segments - prev.segments);
+        g.samples = (int64_t)(now.samples - prev.samples);
+        g.nodes = (int64_t)(now.nodes - prev.nodes);
+        g.tri_tests = (int64_t)(now.tri_tests - prev.tri_tests);
+        g.sph_tests = (int64_t)(now.sph_tests - prev.sph_tests);
+        g.terminated = (int64_t)(now.terminated - prev.terminated);
+        sc->gens.push_back(g);
+        prev = now;
+        return GXY_OK;
+    };
     // generation 0: camera rays
     A.qin = nullptr;
     A.nin = 0;
     A.qout = sc->qa;
     A.qout_count = sc->qcount + 0;
     unsigned g = grid_for(npix);
+    if (sc->profile) CK(cudaEventRecord(ev0, st));
     if (anysec) k_frame<true, true><<<g, kThreads, 0, st>>>(S, A);
     else k_frame<true, false><<<g, kThreads, 0, st>>>(S, A);
     CK(cudaGetLastError());
+    if (sc->profile) CK(cudaEventRecord(ev1, st));
     DRay *qin = sc->qa, *qout = sc->qb;
     unsigned *cin = sc->qcount + 0, *cout = sc->qcount + 1;
     int64_t gens = 1;
+    unsigned last_in = 0;
     for (;;) {
         unsigned n = 0;
         CK(cudaMemcpyAsync(&n, cin, sizeof n, cudaMemcpyDeviceToHost, st));
         CK(cudaStreamSynchronize(st));
+        if ((rc = gen_done(last_in))) return rc;
         if (n > sc->qcap) n = (unsigned)sc->qcap;   // overflow already flagged
         if (n == 0) break;
         CK(cudaMemsetAsync(cout, 0, sizeof(unsigned), st));
@@ -979,14 +1014,19 @@ static int render(Scene *sc, const gxy_camera &cam, const gxy_lighting &lt, floa
         A.qout = qout;
         A.qout_count = cout;
         g = grid_for(n);
+        if (sc->profile) CK(cudaEventRecord(ev0, st));
         if (anysec) k_frame<false, true><<<g, kThreads, 0, st>>>(S, A);
         else k_frame<false, false><<<g, kThreads, 0, st>>>(S, A);
         CK(cudaGetLastError());
+        if (sc->profile) CK(cudaEventRecord(ev1, st));
+        last_in = n;
         std::swap(qin, qout);
         std::swap(cin, cout);
         gens++;
         if (gens > 10000) return set_error(GXY_ERR_TIMEOUT, "ray queues did not drain");
     }
+    if (ev0) cudaEventDestroy(ev0);
+    if (ev1) cudaEventDestroy(ev1);
     CK(cudaMemcpyAsync(&sc->last, sc->ctr, sizeof(DevCounters), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
     sc->bounces = gens;
@@ -1236,6 +1276,21 @@ int gxy_gpu_query_counters_ex(gxy_scene scene, int64_t *tri_tests, int64_t *sph_
     if (tri_tests) *tri_tests = (int64_t)sc->last.tri_tests;
     if (sph_tests) *sph_tests = (int64_t)sc->last.sph_tests;
     if (enqueued) *enqueued = (int64_t)sc->last.enqueued;
+    return GXY_OK;
+}
+
+int gxy_gpu_set_profiling(gxy_scene scene, int on) {
+    if (!scene) return set_error(GXY_ERR_INVALID, "null scene");
+    reinterpret_cast<Scene *>(scene)->profile = on ? 1 : 0;
+    return GXY_OK;
+}
+
+int gxy_gpu_query_generations(gxy_scene scene, gxy_generation_stats *out, int max, int32_t *n) {
+    if (!scene || !n || (max > 0 && !out)) return set_error(GXY_ERR_INVALID, "null argument");
+    Scene *sc = reinterpret_cast<Scene *>(scene);
+    int k = (int)sc->gens.size();
+    *n = k;
+    for (int i = 0; i < k && i < max; i++) out[i] = sc->gens[i];
     return GXY_OK;
 }
 

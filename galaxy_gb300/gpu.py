@@ -50,6 +50,8 @@ def lib():
                                           C.POINTER(i32)],
         "gxy_gpu_trace_raylist": [vp, C.c_int, C.POINTER(A.gxy_lighting), C.POINTER(A.gxy_raylist),
                                   C.POINTER(A.gxy_raylist), C.POINTER(i32)],
+        "gxy_gpu_set_profiling": [vp, C.c_int],
+        "gxy_gpu_query_generations": [vp, C.POINTER(A.gxy_generation_stats), C.c_int, C.POINTER(i32)],
         "gxy_gpu_classify": [C.POINTER(A.gxy_raylist)],
         "gxy_gpu_assign_destinations": [vp, C.c_int, C.POINTER(A.gxy_raylist)],
         "gxy_gpu_accumulate_terminated": [C.POINTER(A.gxy_raylist), A.f32p, C.c_int, C.c_int],
@@ -151,6 +153,17 @@ class Scene:
         check(lib().gxy_gpu_query_counters_ex(self.h, C.byref(t), C.byref(s), C.byref(e)))
         d.update(tri_tests=t.value, sph_tests=s.value, enqueued=e.value)
         return d
+
+    def set_profiling(self, on=True):
+        check(lib().gxy_gpu_set_profiling(self.h, 1 if on else 0))
+
+    def generations(self):
+        """Per-generation kernel time and counters of the last render
+        (recorded while profiling is on)."""
+        buf = (A.gxy_generation_stats * 256)()
+        n = C.c_int32(0)
+        check(lib().gxy_gpu_query_generations(self.h, buf, 256, C.byref(n)))
+        return [{f: getattr(buf[i], f) for f, _ in A.gxy_generation_stats._fields_} for i in range(min(n.value, 256))]
 
     # ---- RayList drop-in
     def generate_initial_rays(self, p, camera, capacity=None):

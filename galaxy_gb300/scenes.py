@@ -89,9 +89,10 @@ def blob_field(n, n_blobs, seed, noise=0.05, lattice=16):
         W = np.zeros((n, m), f32)
         W[np.arange(n), i0] = 1 - fr
         W[np.arange(n), i0 + 1] += fr
-        t = np.einsum("zi,ijk->zjk", W, lat)
-        t = np.einsum("yj,zjk->zyk", W, t)
-        field += np.einsum("xk,zyk->zyx", W, t).astype(f32)
+        t = (W @ lat.reshape(m, m * m)).reshape(n, m, m)          # z
+        t = np.matmul(W[None], t)                                  # y: (n, n, m)
+        for z0 in range(0, n, 64):
+            field[z0:z0 + 64] += np.matmul(t[z0:z0 + 64], W.T)     # x
     return field
 
 

@@ -240,6 +240,18 @@ int gxy_gpu_query_counters(gxy_scene scene, gxy_counters *out);
 int gxy_gpu_query_counters_ex(gxy_scene scene, int64_t *tri_tests, int64_t *sph_tests,
                               int64_t *enqueued);
 
+/* Per-generation statistics of the last gxy_gpu_render, recorded when
+ * profiling is on: device time of the generation's kernel (CUDA events on
+ * the render stream) and the counters it added. */
+typedef struct gxy_generation_stats {
+    double  ms;
+    int64_t rays_in;       /* queue records read (0 for the camera generation) */
+    int64_t enqueued;      /* queue records written                         */
+    int64_t segments, samples, nodes, tri_tests, sph_tests, terminated;
+} gxy_generation_stats;
+int gxy_gpu_set_profiling(gxy_scene scene, int on);
+int gxy_gpu_query_generations(gxy_scene scene, gxy_generation_stats *out, int max, int32_t *n);
+
 /* ---- RayList-level drop-in (host buffers) ------------------------------ */
 
 /* Camera::generate_initial_rays for partition `partition`: fills `out`

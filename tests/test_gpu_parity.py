@@ -200,7 +200,7 @@ def test_bvh_stats(gpu):
     info = g.bvh_info()
     n = len(vis.operators[0].dataset.indices)
     assert info["prim_refs"] == n
-    assert n / 8 <= info["nodes"] <= n
+    assert n / 32 <= info["nodes"] <= n
 
 
 def test_errors_are_reported(gpu):
