@@ -210,6 +210,7 @@ def main():
     ap.add_argument("--workload", default="mixed", choices=["mixed", "volume", "triangles"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--image", type=int, default=0, help="override the image side (smaller profiling cases)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -223,6 +224,9 @@ def main():
     from galaxy_gb300 import scene as S
 
     cam, vis, cfg = make_workload(args.workload)
+    if args.image:
+        cam.width = cam.height = args.image
+        cfg = dict(cfg, image=[args.image, args.image], workload=cfg["workload"] + " (image %d^2)" % args.image)
     gpu.init(local)
     t0 = time.time()
     sc = gpu.Scene(vis)
@@ -268,6 +272,7 @@ def main():
     torch.cuda.synchronize()
     barrier(world)
     clk = clocks.stop()
+    sc_last_gens = sc.generations()
     total_ms = t_start.elapsed_time(t_end)
     frame_ms = [a.elapsed_time(b) for a, b in ev]
     total_ms = allreduce_max(total_ms, world)
@@ -317,6 +322,8 @@ def main():
            "rays": {"primary": c["primary_rays"], "shadow": c["shadow_rays"], "ao": c["ao_rays"],
                     "segments": c["segments"], "handoffs": c["handoffs"], "generations": c["bounces"],
                     "samples": c["samples"], "bvh_nodes": c["nodes"], "prim_tests": c["prim_tests"]},
+           "generations": [{k: (round(v, 4) if isinstance(v, float) else v) for k, v in g.items()}
+                           for g in sc_last_gens],
            "scene_commit_s": commit_s, "bvh": sc.bvh_info(),
            "gpu_launches": launches, "roofline": roof, "e2e": e2e, "clocks": clk}
     if rank == 0 and not args.no_cpu_baseline:
