@@ -169,5 +169,5 @@ class RayListArrays:
 
 
 class gxy_generation_stats(C.Structure):
-    _fields_ = [("ms", C.c_double)] + [(n, C.c_int64) for n in (
+    _fields_ = [("ms", C.c_double), ("generation", C.c_int32), ("kind", C.c_int32)] + [(n, C.c_int64) for n in (
         "rays_in", "enqueued", "segments", "samples", "nodes", "tri_tests", "sph_tests", "terminated")]

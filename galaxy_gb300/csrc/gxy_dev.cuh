@@ -26,7 +26,7 @@ constexpr uint32_t kSphereBit = 0x80000000u;
 struct DevTF {                       // one resampled transfer function, 4 KB
     float colors[GXY_TF_SIZE * 3];
     float opac[GXY_TF_SIZE];
-    float r0, r1, pad0, pad1;
+    float r0, r1, k, pad;            // k = 255 / (r1 - r0)
 };
 
 struct DevVolume {
@@ -34,6 +34,7 @@ struct DevVolume {
     int nx, ny, nz;
     float ox, oy, oz, dx, dy, dz;
     float ux, uy, uz;                // clamp bounds: float just below n-1
+    float ix, iy, iz;                // 1 / delta
     int tf;                          // index into DevScene::tfs
     int n_slices;
     float4 slices[GXY_MAX_SLICES];
@@ -85,7 +86,8 @@ struct DevScene {
     int np;
     float glo[3], ghi[3];
     DevPartition part[kMaxPart];
-    int integrate;
+    int integrate;                   // some volume is rendered or has isovalues
+    int has_iso;                     // some volume has isovalues
     float step, march_eps, epsilon, opaque_alpha, rate;
     // geometry
     const BVH8Node *nodes;
@@ -157,12 +159,13 @@ __device__ __forceinline__ float fmin_(float a, float b) { return (b < a) ? b : 
 __device__ __forceinline__ float fmax_(float a, float b) { return (a < b) ? b : a; }   // std::max
 
 // ------------------------------------------------------ transfer function
-// Piecewise-linear lookup over 256 entries (NaN -> 0, clamp outside range).
+// Piecewise-linear lookup over 256 entries (NaN -> 0, clamp outside range,
+// index f = (v - r0) * (255 / (r1 - r0))).
 __device__ __forceinline__ float tf_opacity(const DevTF &tf, float v) {
     if (isnan(v)) return 0.0f;
     if (v <= tf.r0) return tf.opac[0];
     if (v >= tf.r1) return tf.opac[255];
-    float f = (v - tf.r0) / (tf.r1 - tf.r0) * 255.0f;
+    float f = (v - tf.r0) * tf.k;
     int i = (int)floorf(f);
     i = i > 254 ? 254 : (i < 0 ? 0 : i);
     float rem = f - (float)i;
@@ -173,7 +176,7 @@ __device__ __forceinline__ V3 tf_color(const DevTF &tf, float v) {
     const float *c = tf.colors;
     if (v <= tf.r0) return v3(c[0], c[1], c[2]);
     if (v >= tf.r1) return v3(c[765], c[766], c[767]);
-    float f = (v - tf.r0) / (tf.r1 - tf.r0) * 255.0f;
+    float f = (v - tf.r0) * tf.k;
     int i = (int)floorf(f);
     i = i > 254 ? 254 : (i < 0 ? 0 : i);
     float rem = f - (float)i;
@@ -183,11 +186,12 @@ __device__ __forceinline__ V3 tf_color(const DevTF &tf, float v) {
 }
 
 // ---------------------------------------------------------------- volume
-// Trilinear sample of the dataset grid at world point p, clamped to the grid.
+// Trilinear sample of the dataset grid at world point p, clamped to the grid;
+// grid coordinate (p - origin) * (1 / delta).
 __device__ __forceinline__ float vol_sample(const DevVolume &v, V3 p) {
-    float gx = (p.x - v.ox) / v.dx;
-    float gy = (p.y - v.oy) / v.dy;
-    float gz = (p.z - v.oz) / v.dz;
+    float gx = (p.x - v.ox) * v.ix;
+    float gy = (p.y - v.oy) * v.iy;
+    float gz = (p.z - v.oz) * v.iz;
     if (!(gx >= 0.0f)) gx = 0.0f;
     if (!(gy >= 0.0f)) gy = 0.0f;
     if (!(gz >= 0.0f)) gz = 0.0f;
@@ -218,9 +222,9 @@ struct CellCache {
     float c[8];
 };
 __device__ __forceinline__ float vol_sample_cached(const DevVolume &v, V3 p, CellCache &cc) {
-    float gx = (p.x - v.ox) / v.dx;
-    float gy = (p.y - v.oy) / v.dy;
-    float gz = (p.z - v.oz) / v.dz;
+    float gx = (p.x - v.ox) * v.ix;
+    float gy = (p.y - v.oy) * v.iy;
+    float gz = (p.z - v.oz) * v.iz;
     if (!(gx >= 0.0f)) gx = 0.0f;
     if (!(gy >= 0.0f)) gy = 0.0f;
     if (!(gz >= 0.0f)) gz = 0.0f;
@@ -300,9 +304,22 @@ struct GeoHit {
     uint32_t prim;   // global primitive id (with kSphereBit for spheres)
 };
 
+// 32-bit compare-exchange for the sorting network below.
+__device__ __forceinline__ void cas(uint32_t &a, uint32_t &b) {
+    uint32_t lo = min(a, b), hi = max(a, b);
+    a = lo;
+    b = hi;
+}
+
 // Closest hit in (t0, tfar) with ties broken by the smaller primitive id.
-// ANY: return at the first accepted hit.  Returns whether a hit was found;
-// node/prim visit counts are added to *nodes / *prims.
+// ANY: return at the first accepted hit.  Per wide node: the 8 child boxes
+// are tested from the quantised planes with one fused multiply-add per slab;
+// leaf children are intersected at once; hit internal children are ordered
+// near to far by a 19-comparator sorting network over 32-bit keys (entry
+// distance with the child slot in the low 3 bits -- non-negative floats
+// order like their bit patterns), the nearest is visited next and the rest
+// go on a stack of (node, entry distance) pairs.  Everything stays in
+// registers except the stack.
 template <bool ANY>
 __device__ __noinline__ bool bvh_closest(const DevScene &S, V3 org, V3 dir, float t0, float tfar, GeoHit &h,
                                          unsigned &nodes, unsigned &tris, unsigned &sphs, int &ovf) {
@@ -312,7 +329,6 @@ __device__ __noinline__ bool bvh_closest(const DevScene &S, V3 org, V3 dir, floa
     h.t = tfar;
     h.prim = 0xffffffffu;
     bool found = false;
-    // stack of (node index, entry distance)
     uint2 stack[64];
     int sp = 0;
     uint32_t cur = 0;
@@ -325,11 +341,10 @@ __device__ __noinline__ bool bvh_closest(const DevScene &S, V3 org, V3 dir, floa
             uint32_t prim_base = __float_as_uint(n1.x);
             uint32_t e4 = __float_as_uint(n1.y);
             uint32_t meta_lo = __float_as_uint(n1.z), meta_hi = __float_as_uint(n1.w);
-            float4 q[6];
+            uint4 q[6];
 #pragma unroll
-            for (int k = 0; k < 6; k++) q[k] = __ldg(np + 2 + k);
+            for (int k = 0; k < 6; k++) q[k] = __ldg(reinterpret_cast<const uint4 *>(np + 2 + k));
             nodes++;
-            const uint16_t *ql = reinterpret_cast<const uint16_t *>(q);   // qlo[3][8] then qhi[3][8]
             float scx = __uint_as_float((e4 & 0xffu) << 23);
             float scy = __uint_as_float(((e4 >> 8) & 0xffu) << 23);
             float scz = __uint_as_float(((e4 >> 16) & 0xffu) << 23);
@@ -338,23 +353,33 @@ __device__ __noinline__ bool bvh_closest(const DevScene &S, V3 org, V3 dir, floa
             float ax = scx * idx, bx = (n0.x - org.x) * idx;
             float ay = scy * idy, by = (n0.y - org.y) * idy;
             float az = scz * idz, bz = (n0.z - org.z) * idz;
-            float tn_c[8];
-            uint32_t hitmask = 0;
+            uint32_t key[8];
+            uint32_t leafhits = 0;
+            int n_inner = 0;
 #pragma unroll
             for (int i = 0; i < 8; i++) {
                 uint32_t mb = (i < 4 ? meta_lo >> (8 * i) : meta_hi >> (8 * (i - 4))) & 0xffu;
-                float lx = (float)ql[0 * 8 + i], ly = (float)ql[1 * 8 + i], lz = (float)ql[2 * 8 + i];
-                float hx = (float)ql[24 + 0 * 8 + i], hy = (float)ql[24 + 1 * 8 + i], hz = (float)ql[24 + 2 * 8 + i];
+                // 16-bit planes: qlo axis a at q[a*... ] -- word (a*8+i)/2 of 48 bytes, then qhi at +24 words
+                uint32_t wl0 = (&q[0].x)[(0 * 8 + i) >> 1], wl1 = (&q[0].x)[(1 * 8 + i) >> 1],
+                         wl2 = (&q[0].x)[(2 * 8 + i) >> 1];
+                uint32_t wh0 = (&q[0].x)[(24 + 0 * 8 + i) >> 1], wh1 = (&q[0].x)[(24 + 1 * 8 + i) >> 1],
+                         wh2 = (&q[0].x)[(24 + 2 * 8 + i) >> 1];
+                const int sh = (i & 1) * 16;
+                float lx = (float)((wl0 >> sh) & 0xffffu), ly = (float)((wl1 >> sh) & 0xffffu),
+                      lz = (float)((wl2 >> sh) & 0xffffu);
+                float hx = (float)((wh0 >> sh) & 0xffffu), hy = (float)((wh1 >> sh) & 0xffffu),
+                      hz = (float)((wh2 >> sh) & 0xffffu);
                 float txa = __fmaf_rn(sx ? hx : lx, ax, bx), txb = __fmaf_rn(sx ? lx : hx, ax, bx);
                 float tya = __fmaf_rn(sy ? hy : ly, ay, by), tyb = __fmaf_rn(sy ? ly : hy, ay, by);
                 float tza = __fmaf_rn(sz ? hz : lz, az, bz), tzb = __fmaf_rn(sz ? lz : hz, az, bz);
                 float tn = fmaxf(fmaxf(txa, tya), fmaxf(tza, t0));
                 float tf = fminf(fminf(txb, tyb), fminf(tzb, h.t));
-                tn_c[i] = tn;
-                if (mb != 0xffu && tn <= tf * 1.00000048f + 1e-30f) hitmask |= 1u << i;
+                bool hit = mb != 0xffu && tn <= tf * 1.00000048f + 1e-30f;
+                bool inner = hit && ((imask >> i) & 1u);
+                key[i] = inner ? ((__float_as_uint(tn) & ~7u) | (uint32_t)i) : 0xffffffffu;
+                n_inner += inner ? 1 : 0;
+                if (hit && !((imask >> i) & 1u)) leafhits |= 1u << i;
             }
-            // leaf children first (they can shrink h.t before internal children are ordered)
-            uint32_t leafhits = hitmask & ~imask;
             while (leafhits) {
                 int i = __ffs(leafhits) - 1;
                 leafhits &= leafhits - 1;
@@ -384,30 +409,28 @@ __device__ __noinline__ bool bvh_closest(const DevScene &S, V3 org, V3 dir, floa
                     }
                 }
             }
-            // internal children: nearest first, the rest pushed far to near
-            uint32_t inner = hitmask & imask;
-            if (inner) {
-                uint32_t idxs[8];
-                float tns[8];
-                int k = 0;
-                while (inner) {
-                    int i = __ffs(inner) - 1;
-                    inner &= inner - 1;
-                    uint32_t mb = (i < 4 ? meta_lo >> (8 * i) : meta_hi >> (8 * (i - 4))) & 0xffu;
-                    uint32_t ci = child_base + mb;
-                    float tn = tn_c[i];
-                    // insertion into descending order
-                    int j = k++;
-                    while (j > 0 && tns[j - 1] < tn) { tns[j] = tns[j - 1]; idxs[j] = idxs[j - 1]; j--; }
-                    tns[j] = tn;
-                    idxs[j] = ci;
+            if (n_inner) {
+                // sorting network for 8 keys (Batcher, 19 comparators)
+                cas(key[0], key[1]); cas(key[2], key[3]); cas(key[4], key[5]); cas(key[6], key[7]);
+                cas(key[0], key[2]); cas(key[1], key[3]); cas(key[4], key[6]); cas(key[5], key[7]);
+                cas(key[1], key[2]); cas(key[5], key[6]); cas(key[0], key[4]); cas(key[3], key[7]);
+                cas(key[1], key[5]); cas(key[2], key[6]);
+                cas(key[1], key[4]); cas(key[3], key[6]);
+                cas(key[2], key[4]); cas(key[3], key[5]);
+                cas(key[3], key[4]);
+#pragma unroll
+                for (int j = 7; j >= 1; j--) {
+                    if (j < n_inner) {
+                        uint32_t slot = key[j] & 7u;
+                        uint32_t mb = (slot < 4 ? meta_lo >> (8 * slot) : meta_hi >> (8 * (slot - 4))) & 0xffu;
+                        if (sp < 64) stack[sp++] = make_uint2(child_base + mb, key[j] & ~7u);
+                        else ovf = 1;   // reported as GXY_ERR_OVERFLOW by the host
+                    }
                 }
-                for (int j = 0; j < k - 1; j++) {
-                    if (sp < 64) stack[sp++] = make_uint2(idxs[j], __float_as_uint(tns[j]));
-                    else ovf = 1;   // reported as GXY_ERR_OVERFLOW by the host
-                }
-                cur = idxs[k - 1];
-                cur_tn = tns[k - 1];
+                uint32_t slot = key[0] & 7u;
+                uint32_t mb = (slot < 4 ? meta_lo >> (8 * slot) : meta_hi >> (8 * (slot - 4))) & 0xffu;
+                cur = child_base + mb;
+                cur_tn = __uint_as_float(key[0] & ~7u);
                 continue;
             }
         }

@@ -192,24 +192,27 @@ struct Scene {
     gxy_partition_info pinfo;
     std::vector<void *> owned;
     BVHInfo bvh;
-    DRay *qa = nullptr, *qb = nullptr;
-    size_t qcap = 0;
-    unsigned int *qcount = nullptr;     // [0],[1] counts of the two queues
-    DevCounters *ctr = nullptr;
+    static constexpr int kMaxLaunch = 256;   // counter slots per frame
+    DRay *q[2][3] = {{nullptr, nullptr, nullptr}, {nullptr, nullptr, nullptr}};   // ping-pong x (primary, shadow, AO)
+    size_t qcap[3] = {0, 0, 0};
+    unsigned int *qcount = nullptr;     // 2 x 3 queue counters
+    DevCounters *ctr = nullptr;         // kMaxLaunch slots, one per launch
     DevCounters last{};
     int64_t bounces = 0;
     float *fbtmp = nullptr;
     size_t fbtmp_elems = 0;
     int profile = 0;
     std::vector<gxy_generation_stats> gens;
+    std::vector<cudaEvent_t> events;
     std::mutex mu;                      // one render at a time per scene
     ~Scene() {
         for (void *p : owned) arena().free(p);
-        arena().free(qa);
-        arena().free(qb);
+        for (int b = 0; b < 2; b++)
+            for (int k = 0; k < 3; k++) arena().free(q[b][k]);
         arena().free(qcount);
         arena().free(ctr);
         arena().free(fbtmp);
+        for (cudaEvent_t e : events) cudaEventDestroy(e);
         if (bvh.nodes_ptr) arena().free(bvh.nodes_ptr);
         if (bvh.slots_ptr) arena().free(bvh.slots_ptr);
     }
@@ -291,7 +294,8 @@ static void tf_to_dev(const gxy_tf &t, DevTF &d) {
     memcpy(d.opac, t.opacities, sizeof d.opac);
     d.r0 = t.range[0];
     d.r1 = t.range[1];
-    d.pad0 = d.pad1 = 0;
+    d.k = 255.0f / (t.range[1] - t.range[0]);
+    d.pad = 0;
 }
 
 static int commit(const gxy_scene_desc *d, Scene *sc) {
@@ -327,6 +331,9 @@ static int commit(const gxy_scene_desc *d, Scene *sc) {
         V.ux = nextafterf((float)(V.nx - 1), 0.0f);
         V.uy = nextafterf((float)(V.ny - 1), 0.0f);
         V.uz = nextafterf((float)(V.nz - 1), 0.0f);
+        V.ix = 1.0f / V.dx;
+        V.iy = 1.0f / V.dy;
+        V.iz = 1.0f / V.dz;
         V.tf = (int)tfs.size();
         DevTF t;
         tf_to_dev(v.tf, t);
@@ -338,6 +345,7 @@ static int commit(const gxy_scene_desc *d, Scene *sc) {
         for (int k = 0; k < v.n_isovalues; k++) V.iso[k] = v.isovalues[k];
         V.volume_render = v.volume_render ? 1 : 0;
         if (v.volume_render || v.n_isovalues > 0) S.integrate = 1;
+        if (v.n_isovalues > 0) S.has_iso = 1;
         // samplingStep = smallest spacing; step = samplingStep / rate (TraceRays.ispc:342-361)
         float ss = fminf(v.deltas[0], fminf(v.deltas[1], v.deltas[2]));
         float st = ss / rate;
@@ -433,7 +441,7 @@ static int commit(const gxy_scene_desc *d, Scene *sc) {
     if ((rc = build_bvh8(S, drad, arena(), 0, sc->bvh))) return rc;
     CK(cudaDeviceSynchronize());
     if ((rc = arena().alloc((void **)&sc->qcount, 16 * sizeof(unsigned int)))) return rc;
-    if ((rc = arena().alloc((void **)&sc->ctr, sizeof(DevCounters)))) return rc;
+    if ((rc = arena().alloc((void **)&sc->ctr, Scene::kMaxLaunch * sizeof(DevCounters)))) return rc;
     return GXY_OK;
 }
 
@@ -528,27 +536,75 @@ __device__ __forceinline__ void put_ray(DRay *q, unsigned idx, V3 o, float t, V3
     p->m = make_int4(x, y, meta, 0);
 }
 
+enum { Q_PRIM = 0, Q_SHADOW = 1, Q_AO = 2, NQ = 3 };
+enum { K_CAMERA = 0, K_PRIMARY = 1, K_SECONDARY = 2 };
+
 struct FrameArgs {
     DevCamera cam;
     DevLights L;
     float *fb;
-    const DRay *qin;
-    unsigned nin;
-    DRay *qout;
-    unsigned *qout_count;
-    unsigned qcap;
-    DevCounters *ctr;
+    const DRay *qin[NQ];
+    unsigned nin[NQ];
+    DRay *qout[NQ];
+    unsigned *qout_count;            // NQ counters
+    unsigned qcap[NQ];
+    DevCounters *ctr;                // this launch's counter slot
 };
 
-// One generation of the wavefront.  PRIMARY: generate camera rays from the
-// pixel index; otherwise read the input queue.
-template <bool PRIMARY, bool ANYSEC>
-__global__ void __launch_bounds__(kThreads) k_frame(DevScene S, FrameArgs A) {
+// Reserve cnt consecutive queue records for this thread: one warp-wide scan
+// and one atomic per warp.  Returns the first index (or ~0u if the queue is
+// full; the overflow flag is then set).  All 32 lanes must call it.
+__device__ __forceinline__ unsigned warp_reserve(unsigned cnt, unsigned *counter, unsigned cap, int &ovf) {
+    unsigned tot;
+    unsigned pre = warp_excl_scan(cnt, tot);
+    unsigned base = 0;
+    if (tot) {
+        if ((threadIdx.x & 31) == 0) base = atomicAdd(counter, tot);
+        base = __shfl_sync(0xffffffffu, base, 0);
+    }
+    if (!cnt) return 0;
+    unsigned idx = base + pre;
+    if (idx + cnt > cap) {
+        ovf = 1;
+        return 0xffffffffu;
+    }
+    return idx;
+}
+
+__device__ __forceinline__ void flush_counters(DevCounters *ctr, const unsigned long long (&vals)[14]) {
+    __shared__ unsigned long long red[16];
+    const int lane = threadIdx.x & 31;
+    if (threadIdx.x < 16) red[threadIdx.x] = 0;
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < 14; k++) {
+        unsigned long long v = vals[k];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0 && v) atomicAdd(&red[k], v);
+    }
+    __syncthreads();
+    if (threadIdx.x < 13 && red[threadIdx.x]) atomicAdd(&(&ctr->primary)[threadIdx.x], red[threadIdx.x]);
+    if (threadIdx.x == 13 && red[13]) atomicExch(&ctr->overflow, 1);
+}
+
+__device__ __forceinline__ void add_pixel(float *fb, int width, int x, int y, float r, float g, float b, float o) {
+    if (r != 0.0f || g != 0.0f || b != 0.0f || o != 0.0f) {
+        float4 *px = reinterpret_cast<float4 *>(fb) + ((size_t)y * width + x);
+        atomicAdd(px, make_float4(r, g, b, o));
+    }
+}
+
+// One generation for primary rays: KIND == K_CAMERA builds the camera ray of
+// each pixel; KIND == K_PRIMARY reads handed-off / kept primaries.  Each ray
+// is traced, shaded if it ends on a surface (ambient, AO spawn, diffuse,
+// shadow spawn), classified and routed; spawned rays go to the shadow and AO
+// queues, continuing primaries to the primary queue.
+template <int KIND>
+__global__ void __launch_bounds__(kThreads) k_primary(DevScene S, FrameArgs A) {
     __shared__ DevTF tfs[kMaxVol];
     load_tfs(S, tfs);
     const DevLights &L = A.L;
-    const int lane = threadIdx.x & 31;
-    const int64_t n_items = PRIMARY ? (int64_t)A.cam.width * A.cam.height : (int64_t)A.nin;
+    const int64_t n_items = KIND == K_CAMERA ? (int64_t)A.cam.width * A.cam.height : (int64_t)A.nin[Q_PRIM];
     RayStats st;
     unsigned long long c_prim = 0, c_sh = 0, c_ao = 0, c_seg = 0, c_hand = 0, c_term = 0, c_drop = 0, c_keep = 0,
                        c_enq = 0;
@@ -561,7 +617,7 @@ __global__ void __launch_bounds__(kThreads) k_frame(DevScene S, FrameArgs A) {
         uint64_t pending = 0;
         int x = 0, y = 0;
         if (valid) {
-            if (PRIMARY) {
+            if (KIND == K_CAMERA) {
                 x = (int)(i % A.cam.width);
                 y = (int)(i / A.cam.width);
                 pending = camera_ray(S, A.cam, x, y, in.org, in.dir);
@@ -570,7 +626,7 @@ __global__ void __launch_bounds__(kThreads) k_frame(DevScene S, FrameArgs A) {
                 in.r = in.g = in.b = in.o = 0.0f;
                 in.type = GXY_RAY_PRIMARY;
             } else {
-                const float4 *src = reinterpret_cast<const float4 *>(A.qin + i);
+                const float4 *src = reinterpret_cast<const float4 *>(A.qin[Q_PRIM] + i);
                 float4 a = __ldg(src), b = __ldg(src + 1), c = __ldg(src + 2);
                 int4 m = __ldg(reinterpret_cast<const int4 *>(src + 3));
                 in.org = v3(a.x, a.y, a.z);
@@ -589,11 +645,10 @@ __global__ void __launch_bounds__(kThreads) k_frame(DevScene S, FrameArgs A) {
             bool act = pending != 0;
             TraceOut T;
             int dest = GXY_DROP_ON_FLOOR;
-            unsigned nspawn = 0;
+            bool spawn = false;
             float ar = 0, ag = 0, ab = 0, o_post = 0;
-            ShadeIn sh;
             if (act) {
-                if (PRIMARY) {
+                if (KIND == K_CAMERA) {
                     int p = __ffsll((long long)pending) - 1;
                     pending &= pending - 1;
                     in.part = p;
@@ -602,7 +657,7 @@ __global__ void __launch_bounds__(kThreads) k_frame(DevScene S, FrameArgs A) {
                     pending = 0;
                 }
                 c_seg++;
-                T = trace_core<ANYSEC>(S, tfs, in, st);
+                T = trace_core<true, false>(S, tfs, in, st);
                 if (in.type == GXY_RAY_PRIMARY && T.surface) {
                     // ambient (TraceRays.ispc:735-761)
                     float s = L.Ka * (1.0f - T.o);
@@ -637,9 +692,8 @@ __global__ void __launch_bounds__(kThreads) k_frame(DevScene S, FrameArgs A) {
                     T.g = T.g + f * tg;
                     T.b = T.b + f * tb;
                     o_post = T.o + f * T.o;
-                    nspawn = L.n_ao + (L.shadows ? L.n : 0);
-                    sh.org = in.org; sh.dir = in.dir; sh.t = T.t; sh.n = T.n; sh.sc = T.sc; sh.x = x; sh.y = y;
                     T.o = o_post;
+                    spawn = true;
                     c_ao += L.n_ao;
                     c_sh += L.shadows ? L.n : 0;
                 }
@@ -647,10 +701,7 @@ __global__ void __launch_bounds__(kThreads) k_frame(DevScene S, FrameArgs A) {
                 dest = assign_destination(S, in.part, in.type, cls, in.org, in.dir);
                 if (dest == GXY_TERMINATED) {
                     c_term++;
-                    if (T.r != 0.0f || T.g != 0.0f || T.b != 0.0f || T.o != 0.0f) {
-                        float4 *px = reinterpret_cast<float4 *>(A.fb) + ((size_t)y * A.cam.width + x);
-                        atomicAdd(px, make_float4(T.r, T.g, T.b, T.o));
-                    }
+                    add_pixel(A.fb, A.cam.width, x, y, T.r, T.g, T.b, T.o);
                 } else if (dest == GXY_DROP_ON_FLOOR) {
                     c_drop++;
                 } else if (dest == GXY_KEEP_HERE) {
@@ -659,79 +710,128 @@ __global__ void __launch_bounds__(kThreads) k_frame(DevScene S, FrameArgs A) {
                     c_hand++;
                 }
             }
+            // continuing primary -> primary queue
             unsigned cont = (act && (dest >= 0 || dest == GXY_KEEP_HERE)) ? 1u : 0u;
-            unsigned cnt = nspawn + cont;
-            unsigned tot;
-            unsigned pre = warp_excl_scan(cnt, tot);
-            unsigned wbase = 0;
-            if (tot) {
-                if (lane == 0) wbase = atomicAdd(A.qout_count, tot);
-                wbase = __shfl_sync(0xffffffffu, wbase, 0);
+            unsigned idx = warp_reserve(cont, A.qout_count + Q_PRIM, A.qcap[Q_PRIM], ovf);
+            if (cont && idx != 0xffffffffu) {
+                int np_ = dest >= 0 ? dest : in.part;
+                put_ray(A.qout[Q_PRIM], idx, in.org, T.t, in.dir, in.tmax, T.r, T.g, T.b, T.o, x, y,
+                        make_meta(in.type, np_, 0));
+                c_enq++;
             }
-            if (cnt) {
-                unsigned idx = wbase + pre;
-                c_enq += cnt;
-                if (idx + cnt > A.qcap) {
-                    ovf = 1;
-                } else {
-                    if (cont) {
-                        int np_ = dest >= 0 ? dest : in.part;
-                        put_ray(A.qout, idx++, in.org, T.t, in.dir, in.tmax, T.r, T.g, T.b, T.o, x, y,
-                                make_meta(in.type, np_, 0));
-                    }
-                    if (nspawn) {
-                        // AO rays (TraceRays.ispc:661-730); payload uses o before diffuse
-                        if (L.n_ao) {
-                            V3 b0, b1;
-                            ao_basis(sh.n, b0, b1);
-                            V3 o = v3(sh.org.x + sh.t * sh.dir.x, sh.org.y + sh.t * sh.dir.y,
-                                      sh.org.z + sh.t * sh.dir.z);
-                            o = v3(o.x + S.epsilon * sh.n.x, o.y + S.epsilon * sh.n.y, o.z + S.epsilon * sh.n.z);
-                            for (int j = 0; j < L.n_ao; j++) {
-                                Spawned s = ao_ray(S, L, sh, j, ar, ag, ab, b0, b1, o);
-                                put_ray(A.qout, idx++, s.o, 0.0f, s.d, s.tmax, s.r, s.g, s.b, 0.0f, x, y,
-                                        make_meta(GXY_RAY_AO, in.part, 0));
-                            }
-                        }
-                        // shadow rays (TraceRays.ispc:813-854); payload uses o after diffuse
-                        if (L.shadows) {
-                            float Kd = -L.Kd / L.n;
-                            for (int k = 0; k < L.n; k++) {
-                                V3 sp = v3(sh.org.x + sh.t * sh.dir.x + S.epsilon * sh.n.x,
-                                           sh.org.y + sh.t * sh.dir.y + S.epsilon * sh.n.y,
-                                           sh.org.z + sh.t * sh.dir.z + S.epsilon * sh.n.z);
-                                V3 lv;
-                                if (L.type[k]) lv = nrm(v3(L.l[k].x, L.l[k].y, L.l[k].z) - sp);
-                                else lv = neg(v3(L.l[k].x, L.l[k].y, L.l[k].z));
-                                lv = nrm(lv);
-                                float dd = dot(sh.n, lv);
-                                if (dd < 0) dd = 0;
-                                float dff = (1.0f - o_post) * Kd * dd;
-                                put_ray(A.qout, idx++, sp, 0.0f, lv, INFINITY, dff * sh.sc.x, dff * sh.sc.y,
-                                        dff * sh.sc.z, 0.0f, x, y, make_meta(GXY_RAY_SHADOW, in.part, 0));
-                            }
-                        }
-                    }
+            // AO rays (TraceRays.ispc:661-730); payload uses o before diffuse
+            unsigned nao = spawn ? (unsigned)L.n_ao : 0u;
+            idx = warp_reserve(nao, A.qout_count + Q_AO, A.qcap[Q_AO], ovf);
+            if (nao && idx != 0xffffffffu) {
+                V3 b0, b1;
+                ao_basis(T.n, b0, b1);
+                V3 o = v3(in.org.x + T.t * in.dir.x, in.org.y + T.t * in.dir.y, in.org.z + T.t * in.dir.z);
+                o = v3(o.x + S.epsilon * T.n.x, o.y + S.epsilon * T.n.y, o.z + S.epsilon * T.n.z);
+                ShadeIn sh;
+                sh.n = T.n; sh.x = x; sh.y = y;
+                for (int j = 0; j < L.n_ao; j++) {
+                    Spawned s = ao_ray(S, L, sh, j, ar, ag, ab, b0, b1, o);
+                    put_ray(A.qout[Q_AO], idx + j, s.o, 0.0f, s.d, s.tmax, s.r, s.g, s.b, 0.0f, x, y,
+                            make_meta(GXY_RAY_AO, in.part, 0));
                 }
+                c_enq += nao;
+            }
+            // shadow rays (TraceRays.ispc:813-854); payload uses o after diffuse
+            unsigned nsh = (spawn && L.shadows) ? (unsigned)L.n : 0u;
+            idx = warp_reserve(nsh, A.qout_count + Q_SHADOW, A.qcap[Q_SHADOW], ovf);
+            if (nsh && idx != 0xffffffffu) {
+                float Kd = -L.Kd / L.n;
+                for (int k = 0; k < L.n; k++) {
+                    V3 sp = v3(in.org.x + T.t * in.dir.x + S.epsilon * T.n.x,
+                               in.org.y + T.t * in.dir.y + S.epsilon * T.n.y,
+                               in.org.z + T.t * in.dir.z + S.epsilon * T.n.z);
+                    V3 lv;
+                    if (L.type[k]) lv = nrm(v3(L.l[k].x, L.l[k].y, L.l[k].z) - sp);
+                    else lv = neg(v3(L.l[k].x, L.l[k].y, L.l[k].z));
+                    lv = nrm(lv);
+                    float dd = dot(T.n, lv);
+                    if (dd < 0) dd = 0;
+                    float dff = (1.0f - o_post) * Kd * dd;
+                    put_ray(A.qout[Q_SHADOW], idx + k, sp, 0.0f, lv, INFINITY, dff * T.sc.x, dff * T.sc.y,
+                            dff * T.sc.z, 0.0f, x, y, make_meta(GXY_RAY_SHADOW, in.part, 0));
+                }
+                c_enq += nsh;
             }
         }
     }
     ovf |= st.ovf;
-    // block-level counter reduction, one atomic per counter per block
-    __shared__ unsigned long long red[16];
-    if (threadIdx.x < 16) red[threadIdx.x] = 0;
-    __syncthreads();
     unsigned long long vals[14] = {c_prim, c_sh, c_ao, c_seg, c_hand, c_term, c_drop, c_keep, st.samples, st.nodes,
                                    st.tris, st.sphs, c_enq, (unsigned long long)ovf};
-#pragma unroll
-    for (int k = 0; k < 14; k++) {
-        unsigned long long v = vals[k];
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-        if (lane == 0 && v) atomicAdd(&red[k], v);
+    flush_counters(A.ctr, vals);
+}
+
+// One generation of shadow and AO rays: the shadow queue, then the AO queue,
+// as one index space.  A ray that ends on a surface adds its payload; a ray
+// leaving its brick goes to the neighbour's queue of the same type; the rest
+// are dropped (reverse lighting).
+__global__ void __launch_bounds__(kThreads) k_secondary(DevScene S, FrameArgs A) {
+    __shared__ DevTF tfs[kMaxVol];
+    load_tfs(S, tfs);
+    const unsigned ns = A.nin[Q_SHADOW];
+    const int64_t n_items = (int64_t)ns + A.nin[Q_AO];
+    RayStats st;
+    unsigned long long c_seg = 0, c_hand = 0, c_term = 0, c_drop = 0, c_enq = 0;
+    int ovf = 0;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n_items; base += stride) {
+        int64_t i = base + threadIdx.x;
+        bool act = i < n_items;
+        TraceIn in;
+        int x = 0, y = 0, q = Q_SHADOW;
+        int dest = GXY_DROP_ON_FLOOR;
+        TraceOut T;
+        if (act) {
+            q = i < ns ? Q_SHADOW : Q_AO;
+            const float4 *src = reinterpret_cast<const float4 *>(A.qin[q] + (i < ns ? i : i - ns));
+            float4 a = __ldg(src), b = __ldg(src + 1), c = __ldg(src + 2);
+            int4 m = __ldg(reinterpret_cast<const int4 *>(src + 3));
+            in.org = v3(a.x, a.y, a.z);
+            in.t = a.w;
+            in.dir = v3(b.x, b.y, b.z);
+            in.tmax = b.w;
+            in.r = c.x; in.g = c.y; in.b = c.z; in.o = c.w;
+            x = m.x;
+            y = m.y;
+            in.type = ray_type(m.z);
+            in.part = ray_part(m.z);
+            c_seg++;
+            T = trace_core<true, true>(S, tfs, in, st);
+            if (T.cull) {
+                dest = GXY_DROP_ON_FLOOR;
+            } else {
+                int cls = classify_ray(in.type, T.term);
+                dest = assign_destination(S, in.part, in.type, cls, in.org, in.dir);
+            }
+            if (dest == GXY_TERMINATED) {
+                c_term++;
+                add_pixel(A.fb, A.cam.width, x, y, T.r, T.g, T.b, T.o);
+            } else if (dest == GXY_DROP_ON_FLOOR) {
+                c_drop++;
+            } else {
+                c_hand++;
+            }
+        }
+        unsigned cs = (act && dest >= 0 && q == Q_SHADOW) ? 1u : 0u;
+        unsigned ca = (act && dest >= 0 && q == Q_AO) ? 1u : 0u;
+        unsigned is = warp_reserve(cs, A.qout_count + Q_SHADOW, A.qcap[Q_SHADOW], ovf);
+        unsigned ia = warp_reserve(ca, A.qout_count + Q_AO, A.qcap[Q_AO], ovf);
+        if (cs && is != 0xffffffffu)
+            put_ray(A.qout[Q_SHADOW], is, in.org, T.t, in.dir, in.tmax, T.r, T.g, T.b, T.o, x, y,
+                    make_meta(in.type, dest, 0));
+        if (ca && ia != 0xffffffffu)
+            put_ray(A.qout[Q_AO], ia, in.org, T.t, in.dir, in.tmax, T.r, T.g, T.b, T.o, x, y,
+                    make_meta(in.type, dest, 0));
+        c_enq += cs + ca;
     }
-    __syncthreads();
-    if (threadIdx.x < 13 && red[threadIdx.x]) atomicAdd(&(&A.ctr->primary)[threadIdx.x], red[threadIdx.x]);
-    if (threadIdx.x == 13 && red[13]) atomicExch(&A.ctr->overflow, 1);
+    ovf |= st.ovf;
+    unsigned long long vals[14] = {0, 0, 0, c_seg, c_hand, c_term, c_drop, 0, st.samples, st.nodes,
+                                   st.tris, st.sphs, c_enq, (unsigned long long)ovf};
+    flush_counters(A.ctr, vals);
 }
 
 // -------------------------------------------------------- RayList kernels
@@ -758,7 +858,7 @@ __global__ void k_rl_trace(DevScene S, int part, RLDev R, DevCounters *ctr) {
         in.r = R.f[F_R][i]; in.g = R.f[F_G][i]; in.b = R.f[F_B][i]; in.o = R.f[F_O][i];
         in.type = R.i[I_TYPE][i];
         in.part = part;
-        TraceOut T = trace_core<false>(S, tfs, in, st);
+        TraceOut T = trace_core<false, false>(S, tfs, in, st);
         R.f[F_R][i] = T.r; R.f[F_G][i] = T.g; R.f[F_B][i] = T.b; R.f[F_O][i] = T.o;
         R.i[I_TERM][i] = T.term;
         R.f[F_T][i] = T.t;
@@ -922,114 +1022,132 @@ static unsigned grid_for(int64_t n) {
     return (unsigned)(want < 1 ? 1 : want);
 }
 
-static int ensure_queues(Scene *sc, size_t need) {
-    if (sc->qcap >= need) return GXY_OK;
-    arena().free(sc->qa);
-    arena().free(sc->qb);
-    sc->qa = sc->qb = nullptr;
-    sc->qcap = 0;
-    int rc;
-    if ((rc = arena().alloc((void **)&sc->qa, need * sizeof(DRay)))) return rc;
-    if ((rc = arena().alloc((void **)&sc->qb, need * sizeof(DRay)))) {
-        arena().free(sc->qa);
-        sc->qa = nullptr;
-        return rc;
+static int ensure_queues(Scene *sc, const size_t need[3]) {
+    for (int k = 0; k < 3; k++) {
+        if (sc->qcap[k] >= need[k]) continue;
+        for (int b = 0; b < 2; b++) {
+            arena().free(sc->q[b][k]);
+            sc->q[b][k] = nullptr;
+        }
+        sc->qcap[k] = 0;
+        for (int b = 0; b < 2; b++) {
+            int rc = arena().alloc((void **)&sc->q[b][k], need[k] * sizeof(DRay));
+            if (rc) return rc;
+        }
+        sc->qcap[k] = need[k];
     }
-    sc->qcap = need;
     return GXY_OK;
 }
 
+static void add_counters(DevCounters &a, const DevCounters &b) {
+    const unsigned long long *pb = &b.primary;
+    unsigned long long *pa = &a.primary;
+    for (int k = 0; k < 13; k++) pa[k] += pb[k];
+    a.overflow |= b.overflow;
+}
+
+// One frame: generation 0 from the camera, then generations of the primary
+// queue and the shadow+AO queues until every queue is empty.  The host reads
+// the three queue counts (12 bytes) after each generation to size the next
+// launches; each launch adds into its own counter slot, and when profiling
+// is on a pair of events brackets each launch, so profiling adds no syncs.
 static int render(Scene *sc, const gxy_camera &cam, const gxy_lighting &lt, float *fb, cudaStream_t st) {
     if (cam.width <= 0 || cam.height <= 0) return set_error(GXY_ERR_INVALID, "bad image size");
     DevScene &S = sc->S;
     FrameArgs A;
+    memset(&A, 0, sizeof A);
     A.cam = setup_camera(cam);
     int rc = setup_lights(lt, A.L);
     if (rc) return rc;
     if (A.L.n == 0) return set_error(GXY_ERR_INVALID, "lighting needs at least one light");
     int64_t npix = (int64_t)cam.width * cam.height;
-    size_t per = 1 + (size_t)A.L.n_ao + (A.L.shadows ? A.L.n : 0);
-    size_t need = (size_t)npix * per + (size_t)npix / 8 + 4096;
+    size_t slack = (size_t)npix / 8 + 4096;
+    size_t need[3] = {(size_t)npix + slack, (size_t)npix * (A.L.shadows ? A.L.n : 0) + slack,
+                      (size_t)npix * A.L.n_ao + slack};
     if ((rc = ensure_queues(sc, need))) return rc;
-    CK(cudaMemsetAsync(sc->ctr, 0, sizeof(DevCounters), st));
+    const int maxl = Scene::kMaxLaunch;
+    CK(cudaMemsetAsync(sc->ctr, 0, maxl * sizeof(DevCounters), st));
     CK(cudaMemsetAsync(sc->qcount, 0, 16 * sizeof(unsigned), st));
-    A.fb = fb;
-    A.ctr = sc->ctr;
-    A.qcap = (unsigned)sc->qcap;
-    bool anysec = !S.integrate;
-    // optional per-generation timing and counter snapshots
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-    DevCounters prev{};
-    sc->gens.clear();
-    if (sc->profile) {
-        CK(cudaEventCreate(&ev0));
-        CK(cudaEventCreate(&ev1));
+    if (sc->profile && (int)sc->events.size() < 2 * maxl) {
+        for (int k = (int)sc->events.size(); k < 2 * maxl; k++) {
+            cudaEvent_t e;
+            CK(cudaEventCreate(&e));
+            sc->events.push_back(e);
+        }
     }
-    auto gen_done = [&](unsigned rays_in) -> int {
-        if (!sc->profile) return GXY_OK;
-        DevCounters now;
-        CK(cudaMemcpyAsync(&now, sc->ctr, sizeof now, cudaMemcpyDeviceToHost, st));
-        CK(cudaStreamSynchronize(st));
-        float ms = 0;
-        CK(cudaEventElapsedTime(&ms, ev0, ev1));
-        gxy_generation_stats g{};
-        g.ms = ms;
-        g.rays_in = rays_in;
-        g.enqueued = (int64_t)(now.enqueued - prev.enqueued);
-        g.segments = (int64_t)(now.segments - prev.segments);
-        g.samples = (int64_t)(now.samples - prev.samples);
-        g.nodes = (int64_t)(now.nodes - prev.nodes);
-        g.tri_tests = (int64_t)(now.tri_tests - prev.tri_tests);
-        g.sph_tests = (int64_t)(now.sph_tests - prev.sph_tests);
-        g.terminated = (int64_t)(now.terminated - prev.terminated);
-        sc->gens.push_back(g);
-        prev = now;
+    A.fb = fb;
+    for (int k = 0; k < 3; k++) A.qcap[k] = (unsigned)sc->qcap[k];
+    struct LaunchRec { int gen, kind; unsigned rays_in; };
+    std::vector<LaunchRec> recs;
+    int nl = 0;
+    auto launch = [&](int kind, int gen, unsigned rays_in, int64_t items) -> int {
+        if (nl >= maxl) return set_error(GXY_ERR_TIMEOUT, "too many launches in one frame");
+        A.ctr = sc->ctr + nl;
+        unsigned g = grid_for(items);
+        if (sc->profile) CK(cudaEventRecord(sc->events[2 * nl], st));
+        if (kind == K_CAMERA) k_primary<K_CAMERA><<<g, kThreads, 0, st>>>(S, A);
+        else if (kind == K_PRIMARY) k_primary<K_PRIMARY><<<g, kThreads, 0, st>>>(S, A);
+        else k_secondary<<<g, kThreads, 0, st>>>(S, A);
+        CK(cudaGetLastError());
+        if (sc->profile) CK(cudaEventRecord(sc->events[2 * nl + 1], st));
+        recs.push_back({gen, kind, rays_in});
+        nl++;
         return GXY_OK;
     };
-    // generation 0: camera rays
-    A.qin = nullptr;
-    A.nin = 0;
-    A.qout = sc->qa;
-    A.qout_count = sc->qcount + 0;
-    unsigned g = grid_for(npix);
-    if (sc->profile) CK(cudaEventRecord(ev0, st));
-    if (anysec) k_frame<true, true><<<g, kThreads, 0, st>>>(S, A);
-    else k_frame<true, false><<<g, kThreads, 0, st>>>(S, A);
-    CK(cudaGetLastError());
-    if (sc->profile) CK(cudaEventRecord(ev1, st));
-    DRay *qin = sc->qa, *qout = sc->qb;
-    unsigned *cin = sc->qcount + 0, *cout = sc->qcount + 1;
-    int64_t gens = 1;
-    unsigned last_in = 0;
+    int cur = 0;   // queue set written by the last generation
+    for (int k = 0; k < 3; k++) A.qout[k] = sc->q[cur][k];
+    A.qout_count = sc->qcount + 3 * cur;
+    if ((rc = launch(K_CAMERA, 0, 0, npix))) return rc;
+    int gen = 1;
     for (;;) {
-        unsigned n = 0;
-        CK(cudaMemcpyAsync(&n, cin, sizeof n, cudaMemcpyDeviceToHost, st));
+        unsigned n[3];
+        CK(cudaMemcpyAsync(n, sc->qcount + 3 * cur, sizeof n, cudaMemcpyDeviceToHost, st));
         CK(cudaStreamSynchronize(st));
-        if ((rc = gen_done(last_in))) return rc;
-        if (n > sc->qcap) n = (unsigned)sc->qcap;   // overflow already flagged
-        if (n == 0) break;
-        CK(cudaMemsetAsync(cout, 0, sizeof(unsigned), st));
-        A.qin = qin;
-        A.nin = n;
-        A.qout = qout;
-        A.qout_count = cout;
-        g = grid_for(n);
-        if (sc->profile) CK(cudaEventRecord(ev0, st));
-        if (anysec) k_frame<false, true><<<g, kThreads, 0, st>>>(S, A);
-        else k_frame<false, false><<<g, kThreads, 0, st>>>(S, A);
-        CK(cudaGetLastError());
-        if (sc->profile) CK(cudaEventRecord(ev1, st));
-        last_in = n;
-        std::swap(qin, qout);
-        std::swap(cin, cout);
-        gens++;
-        if (gens > 10000) return set_error(GXY_ERR_TIMEOUT, "ray queues did not drain");
+        for (int k = 0; k < 3; k++)
+            if (n[k] > sc->qcap[k]) n[k] = (unsigned)sc->qcap[k];   // overflow already flagged
+        if (n[0] + n[1] + n[2] == 0) break;
+        int nxt = cur ^ 1;
+        CK(cudaMemsetAsync(sc->qcount + 3 * nxt, 0, 3 * sizeof(unsigned), st));
+        for (int k = 0; k < 3; k++) {
+            A.qin[k] = sc->q[cur][k];
+            A.nin[k] = n[k];
+            A.qout[k] = sc->q[nxt][k];
+        }
+        A.qout_count = sc->qcount + 3 * nxt;
+        if (n[Q_PRIM] && (rc = launch(K_PRIMARY, gen, n[Q_PRIM], n[Q_PRIM]))) return rc;
+        if (n[Q_SHADOW] + n[Q_AO] &&
+            (rc = launch(K_SECONDARY, gen, n[Q_SHADOW] + n[Q_AO], (int64_t)n[Q_SHADOW] + n[Q_AO])))
+            return rc;
+        cur = nxt;
+        gen++;
     }
-    if (ev0) cudaEventDestroy(ev0);
-    if (ev1) cudaEventDestroy(ev1);
-    CK(cudaMemcpyAsync(&sc->last, sc->ctr, sizeof(DevCounters), cudaMemcpyDeviceToHost, st));
+    std::vector<DevCounters> slots(nl);
+    CK(cudaMemcpyAsync(slots.data(), sc->ctr, nl * sizeof(DevCounters), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
-    sc->bounces = gens;
+    sc->last = DevCounters{};
+    for (int k = 0; k < nl; k++) add_counters(sc->last, slots[k]);
+    sc->bounces = gen;
+    sc->gens.clear();
+    if (sc->profile) {
+        for (int k = 0; k < nl; k++) {
+            gxy_generation_stats g{};
+            float ms = 0;
+            CK(cudaEventElapsedTime(&ms, sc->events[2 * k], sc->events[2 * k + 1]));
+            g.ms = ms;
+            g.generation = recs[k].gen;
+            g.kind = recs[k].kind;
+            g.rays_in = recs[k].kind == K_CAMERA ? 0 : recs[k].rays_in;
+            const DevCounters &c = slots[k];
+            g.enqueued = (int64_t)c.enqueued;
+            g.segments = (int64_t)c.segments;
+            g.samples = (int64_t)c.samples;
+            g.nodes = (int64_t)c.nodes;
+            g.tri_tests = (int64_t)c.tri_tests;
+            g.sph_tests = (int64_t)c.sph_tests;
+            g.terminated = (int64_t)c.terminated;
+            sc->gens.push_back(g);
+        }
+    }
     if (sc->last.overflow) return set_error(GXY_ERR_OVERFLOW, "a ray queue or traversal stack overflowed");
     return GXY_OK;
 }

@@ -29,6 +29,7 @@ struct TraceOut {
     V3 n;               // surface normal (valid when term & SURFACE)
     V3 sc;              // surface colour
     bool surface;
+    bool cull;          // frame path: the ray's framebuffer contribution is provably zero
 };
 
 struct RayStats {
@@ -90,12 +91,25 @@ __device__ __noinline__ void geometry_shade(const DevScene &S, const GeoHit &gh,
 }
 
 // tfs: the volumes' transfer functions (shared-memory copies), indexed by volume.
-// ANY_SECONDARY: shadow/AO rays of a scene without volume integration may
-// stop at the first geometry hit (their fate does not depend on which).
-template <bool ANY_SECONDARY>
+//
+// FRAME = false: the exact per-brick semantics (RayList drop-in).
+// FRAME = true (whole-frame path), for shadow and AO rays only -- their only
+// effect is a framebuffer contribution if they end on a surface, or nothing
+// if they are dropped (reverse lighting):
+//   * without volume integration, the first geometry hit in the brick
+//     decides (any-hit traversal);
+//   * with volume integration, one closest-hit query covers the ray's whole
+//     remaining extent (t0, tMax); the in-brick hit is that hit if it lies
+//     before the brick exit.  If there is no geometry hit, no slice plane and
+//     no isosurface anywhere ahead, every brick the ray would cross finds no
+//     surface and the ray is eventually dropped -- it is culled before the
+//     march.  A ray whose payload is exactly zero adds nothing wherever it
+//     ends and is culled after its query.  Culling never changes a pixel.
+// SECONDARY: the caller guarantees a shadow/AO ray (no shading code).
+template <bool FRAME, bool SECONDARY>
 __device__ __forceinline__ TraceOut trace_core(const DevScene &S, const DevTF *tfs, const TraceIn &R, RayStats &st) {
     const DevPartition &P = S.part[R.part];
-    const bool shade = R.type == GXY_RAY_PRIMARY;
+    const bool shade = !SECONDARY && R.type == GXY_RAY_PRIMARY;
     V3 org = R.org, dir = R.dir;
     if (dir.x == 0.f) dir.x = 1e-6f;
     if (dir.y == 0.f) dir.y = 1e-6f;
@@ -117,8 +131,11 @@ __device__ __forceinline__ TraceOut trace_core(const DevScene &S, const DevTF *t
     ray_t = fmin_(ray_t, tExitVolume);
 
     bool surface_hit = false;
+    bool slice_ahead = false;   // FRAME secondaries: a slice plane in [t0, tMax]
     float hit_t = 0.f, hit_opacity = 0.f, hit_sample = 0.f;
     V3 hit_n = v3(0, 0, 0), hit_c = v3(0, 0, 0);
+    TraceOut out;
+    out.cull = false;
     // slice planes
     {
         int vid = -1;
@@ -130,6 +147,7 @@ __device__ __forceinline__ TraceOut trace_core(const DevScene &S, const DevTF *t
                 float denom = dot(dir, pn);
                 if (fabsf(denom) > 0.0001f) {
                     float t = (pl.w - dot(org, pn)) / denom;
+                    if (FRAME && !shade && t >= ray_t0 && t <= R.tmax) slice_ahead = true;
                     if (t >= ray_t0 && t <= ray_t) {
                         hit_n = denom > 0 ? neg(pn) : pn;
                         hit_opacity = 1.0f;
@@ -149,11 +167,28 @@ __device__ __forceinline__ TraceOut trace_core(const DevScene &S, const DevTF *t
         }
     }
     // geometry
-    if (S.nodes && !(ANY_SECONDARY && !shade && surface_hit)) {
+    if (FRAME && !shade && !S.integrate) {
         GeoHit gh;
-        bool any = ANY_SECONDARY && !shade;
-        bool h = any ? bvh_closest<true>(S, org, dir, ray_t0, ray_t, gh, st.nodes, st.tris, st.sphs, st.ovf)
-                     : bvh_closest<false>(S, org, dir, ray_t0, ray_t, gh, st.nodes, st.tris, st.sphs, st.ovf);
+        if (!surface_hit &&
+            bvh_closest<true>(S, org, dir, ray_t0, ray_t, gh, st.nodes, st.tris, st.sphs, st.ovf)) {
+            ray_t = gh.t;
+            surface_hit = true;
+        }
+    } else if (FRAME && !shade) {
+        GeoHit gh;
+        bool h = bvh_closest<false>(S, org, dir, ray_t0, R.tmax, gh, st.nodes, st.tris, st.sphs, st.ovf);
+        if (h && gh.t < ray_t) {
+            ray_t = gh.t;
+            surface_hit = true;
+        }
+        bool zero = R.r == 0.0f && R.g == 0.0f && R.b == 0.0f && R.o == 0.0f;
+        if (zero || (!h && !surface_hit && !slice_ahead && !S.has_iso)) {
+            out.cull = true;
+            return out;
+        }
+    } else if (S.nodes) {
+        GeoHit gh;
+        bool h = bvh_closest<false>(S, org, dir, ray_t0, ray_t, gh, st.nodes, st.tris, st.sphs, st.ovf);
         if (h) {
             ray_t = gh.t;
             surface_hit = true;
@@ -252,7 +287,6 @@ __device__ __forceinline__ TraceOut trace_core(const DevScene &S, const DevTF *t
         }
         ray_t = tTermination;
     }
-    TraceOut out;
     out.r = cr; out.g = cg; out.b = cb; out.o = ca;
     bool op = fmin_(fmin_(cr, cg), cb) >= 1.0f || ca > S.opaque_alpha;
     int term = op ? GXY_RAY_OPAQUE : 0;

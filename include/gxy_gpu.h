@@ -240,11 +240,13 @@ int gxy_gpu_query_counters(gxy_scene scene, gxy_counters *out);
 int gxy_gpu_query_counters_ex(gxy_scene scene, int64_t *tri_tests, int64_t *sph_tests,
                               int64_t *enqueued);
 
-/* Per-generation statistics of the last gxy_gpu_render, recorded when
- * profiling is on: device time of the generation's kernel (CUDA events on
- * the render stream) and the counters it added. */
+/* Per-launch statistics of the last gxy_gpu_render, recorded when
+ * profiling is on: device time of each kernel launch (CUDA events on the
+ * render stream), its generation and kind, and the counters it added. */
 typedef struct gxy_generation_stats {
     double  ms;
+    int32_t generation;    /* 0 = camera rays                                */
+    int32_t kind;          /* 0 camera, 1 primary queue, 2 shadow+AO queues  */
     int64_t rays_in;       /* queue records read (0 for the camera generation) */
     int64_t enqueued;      /* queue records written                         */
     int64_t segments, samples, nodes, tri_tests, sph_tests, terminated;

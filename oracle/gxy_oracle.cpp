@@ -111,13 +111,15 @@ static const AOTables &ao_tables() {
 // OSPRay 1.8.5 piecewise_linear lookup at the call sites TraceRays.ispc:238,
 // 303,522,529 (OSPRay is not vendored; definition stated here): NaN -> 0;
 // clamp to the first/last entry outside valueRange; otherwise map to
-// [0,255], floor, and interpolate with the next entry.
+// [0,255] as (v - r0) * (255 / (r1 - r0)), floor, and interpolate with the
+// next entry.
 template <class T> static V3<T> tf_color(const gxy_tf &tf, T v) {
     if (std::isnan(v)) return {T(0), T(0), T(0)};
     const float *c = tf.colors;
     if (v <= T(tf.range[0])) return {T(c[0]), T(c[1]), T(c[2])};
     if (v >= T(tf.range[1])) return {T(c[765]), T(c[766]), T(c[767])};
-    T f = (v - T(tf.range[0])) / (T(tf.range[1]) - T(tf.range[0])) * T(255);
+    T k = T(255) / (T(tf.range[1]) - T(tf.range[0]));
+    T f = (v - T(tf.range[0])) * k;
     int i = (int)std::floor(f);
     if (i > 254) i = 254;
     if (i < 0) i = 0;
@@ -131,7 +133,8 @@ template <class T> static T tf_opacity(const gxy_tf &tf, T v) {
     const float *o = tf.opacities;
     if (v <= T(tf.range[0])) return T(o[0]);
     if (v >= T(tf.range[1])) return T(o[255]);
-    T f = (v - T(tf.range[0])) / (T(tf.range[1]) - T(tf.range[0])) * T(255);
+    T k = T(255) / (T(tf.range[1]) - T(tf.range[0]));
+    T f = (v - T(tf.range[0])) * k;
     int i = (int)std::floor(f);
     if (i > 254) i = 254;
     if (i < 0) i = 0;
@@ -141,7 +144,7 @@ template <class T> static T tf_opacity(const gxy_tf &tf, T v) {
 
 // ---------------------------------------------------------------- volume
 // OSPRay shared_structured_volume sample at TraceRays.ispc:234,322 (created at
-// OsprayVolume.cpp:25-52).  Definition: grid coordinate g = (p - origin)/delta
+// OsprayVolume.cpp:25-52).  Definition: grid coordinate g = (p - origin) * (1/delta)
 // over the whole dataset grid, clamped to [0, counts-1) (upper bound the float
 // just below counts-1), lower corner = (int)g, trilinear interpolation in the
 // order x, then y, then z with lerp(a,b,f) = (1-f)*a + f*b -- the same scheme as
@@ -155,11 +158,19 @@ struct Vol {
     int nx, ny, nz;
     float ox, oy, oz, dx, dy, dz;
     float ux, uy, uz;  // clamp upper bounds
+    float ix, iy, iz;  // 1/delta
 };
 template <class T> static T vol_sample(const Vol &v, V3<T> p) {
-    T gx = (p.x - T(v.ox)) / T(v.dx);
-    T gy = (p.y - T(v.oy)) / T(v.dy);
-    T gz = (p.z - T(v.oz)) / T(v.dz);
+    T gx, gy, gz;
+    if (sizeof(T) == sizeof(float)) {
+        gx = (p.x - T(v.ox)) * T(v.ix);
+        gy = (p.y - T(v.oy)) * T(v.iy);
+        gz = (p.z - T(v.oz)) * T(v.iz);
+    } else {
+        gx = (p.x - T(v.ox)) / T(v.dx);
+        gy = (p.y - T(v.oy)) / T(v.dy);
+        gz = (p.z - T(v.oz)) / T(v.dz);
+    }
     if (!(gx >= T(0))) gx = T(0);
     if (!(gy >= T(0))) gy = T(0);
     if (!(gz >= T(0))) gz = T(0);
@@ -565,6 +576,9 @@ static Scene *scene_create(const gxy_scene_desc *d) {
         vol.ux = nextafterf((float)(vol.nx - 1), 0.0f);
         vol.uy = nextafterf((float)(vol.ny - 1), 0.0f);
         vol.uz = nextafterf((float)(vol.nz - 1), 0.0f);
+        vol.ix = 1.0f / vol.dx;
+        vol.iy = 1.0f / vol.dy;
+        vol.iz = 1.0f / vol.dz;
         s->vols.push_back(vol);
         if (v.volume_render || v.n_isovalues > 0) s->integrate = true;
         // samplingStep = smallest spacing; step = samplingStep / samplingRate
