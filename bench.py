@@ -201,6 +201,69 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def run_serve(args):
+    """Serving workload: Poisson arrivals over two resident scenes (the
+    partitioned mixed scene and a 10M-triangle displaced-sphere mesh); each
+    request a random camera on a sphere around the scene and a random light
+    direction, image side log-uniform in [256, 4096].  The requests are
+    served by the continuous-batching loop and, separately, one at a time
+    through the plain path; both report rays/s and p50/p95/p99 latency."""
+    import copy
+    import torch
+    from galaxy_gb300 import gpu, scenes, serve
+    from galaxy_gb300 import scene as S
+    torch.cuda.set_device(0)
+    gpu.init(0)
+    cam_m, vis_m = scenes.mixed_scene()
+    mesh = scenes.displaced_sphere_mesh(10_000_000)
+    L = S.Lighting()
+    L.lights, L.types, L.shadows, L.n_ao, L.ao_radius = [(-0.577, -0.577, -0.577)], [0], True, 2, 0.05
+    vis_t = S.Visualization([S.TrianglesVis(mesh, colormap=scenes.COOLWARM)], L, box=(0, 0, 0, 1, 1, 1))
+    t0 = time.time()
+    table = {"mixed": gpu.Scene(vis_m), "mesh": gpu.Scene(vis_t)}
+    commit_s = time.time() - t0
+    viss = {"mixed": vis_m, "mesh": vis_t}
+    lo, hi = args.side_min, args.side_max
+
+    def make(rng, rid, arrival, key, side):
+        th, ph = rng.uniform(0.2, 1.3), rng.uniform(0, 2 * np.pi)
+        dist = rng.uniform(1.6, 3.0)
+        eye = (0.5 + dist * np.sin(th) * np.cos(ph), 0.5 + dist * np.cos(th), 0.5 + dist * np.sin(th) * np.sin(ph))
+        cam = S.Camera(eye, (0.5 - eye[0], 0.5 - eye[1], 0.5 - eye[2]), (0, 1, 0), 35.0, side, side)
+        lit = copy.copy(viss[key].lighting)
+        d = rng.normal(size=3)
+        d = -np.abs(d) / np.linalg.norm(d)
+        lit.lights, lit.types = [tuple(float(x) for x in d)], [0]
+        return serve.Request(rid, arrival, key, cam, S.resolve_lights(lit, cam).c())
+
+    reqs = serve.poisson_requests(args.rate, args.requests, ["mixed", "mesh"], make, side_range=(lo, hi))
+    # warm-up (not timed): one small request of each scene on both paths
+    warm = [make(np.random.default_rng(1), i, 0.0, k, 256) for i, k in enumerate(["mixed", "mesh"])]
+    serve.serve_plain(table, [copy.copy(w) for w in warm])
+    slot_pixels = hi * hi
+    srv = serve.Server(table, n_slots=args.slots, slot_pixels=slot_pixels, max_jobs=64, max_shadow=1, max_ao=4,
+                       fb_budget=16 << 30, use_graph=True)
+    srv.run([copy.copy(w) for w in warm])
+    served_reqs = [copy.copy(r) for r in reqs]
+    plain_reqs = [copy.copy(r) for r in reqs]
+    served = srv.run(served_reqs, time_limit=args.time_limit)
+    srv.release()
+    torch.cuda.synchronize()
+    plain = serve.serve_plain(table, plain_reqs, time_limit=args.time_limit)
+    out = {"metric": METRIC, "value": served["rays_per_s"], "unit": "rays/s", "n_gpus": 1,
+           "steps": args.requests, "warmup": len(warm), "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+           "config": {"workload": "serving: Poisson %.0f req/s over the partitioned mixed scene and a 10M-triangle "
+                                  "mesh, random camera + light per request, image side log-uniform %d..%d"
+                                  % (args.rate, lo, hi), "rate": args.rate, "requests": args.requests,
+                      "slots": args.slots, "slot_pixels": slot_pixels},
+           "served": served, "plain": plain,
+           "served_over_plain_rays_per_s": served["rays_per_s"] / max(1e-9, plain["rays_per_s"]),
+           "latency_ms": {k: served.get(k + "_ms") for k in ("p50", "p95", "p99")},
+           "scene_commit_s": commit_s}
+    print(json.dumps(out), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -211,9 +274,18 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--image", type=int, default=0, help="override the image side (smaller profiling cases)")
+    ap.add_argument("--mode", default="frame", choices=["frame", "serve"])
+    ap.add_argument("--rate", type=float, default=50.0)
+    ap.add_argument("--requests", type=int, default=200)
+    ap.add_argument("--slots", type=int, default=3)
+    ap.add_argument("--side-min", type=int, default=256)
+    ap.add_argument("--side-max", type=int, default=4096)
+    ap.add_argument("--time-limit", type=float, default=120.0)
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.mode == "serve":
+        return run_serve(args)
     args.warmup = max(3, args.warmup)
 
     import torch

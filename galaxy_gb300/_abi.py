@@ -171,3 +171,8 @@ class RayListArrays:
 class gxy_generation_stats(C.Structure):
     _fields_ = [("ms", C.c_double), ("generation", C.c_int32), ("kind", C.c_int32)] + [(n, C.c_int64) for n in (
         "rays_in", "enqueued", "segments", "samples", "nodes", "tri_tests", "sph_tests", "terminated")]
+
+
+class gxy_job(C.Structure):
+    _fields_ = [("scene", C.c_void_p), ("camera", gxy_camera), ("lighting", gxy_lighting),
+                ("fb_rgba", C.c_void_p)]

@@ -17,6 +17,7 @@
 //
 // RayList path (gxy_gpu_trace_raylist etc.): the same per-ray code over the
 // 25-array RayList layout, one kernel per ISPC export, for ray-level parity.
+#include <cooperative_groups.h>
 #include <cub/cub.cuh>
 
 #include <cfloat>
@@ -25,6 +26,7 @@
 #include <cstring>
 #include <memory>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "gxy_dev.cuh"
@@ -193,6 +195,7 @@ struct Scene {
     std::vector<void *> owned;
     BVHInfo bvh;
     static constexpr int kMaxLaunch = 256;   // counter slots per frame
+    DevScene *d_scene = nullptr;             // device copy of S (batches)
     DRay *q[2][3] = {{nullptr, nullptr, nullptr}, {nullptr, nullptr, nullptr}};   // ping-pong x (primary, shadow, AO)
     size_t qcap[3] = {0, 0, 0};
     unsigned int *qcount = nullptr;     // 2 x 3 queue counters
@@ -440,6 +443,8 @@ static int commit(const gxy_scene_desc *d, Scene *sc) {
     }
     if ((rc = build_bvh8(S, drad, arena(), 0, sc->bvh))) return rc;
     CK(cudaDeviceSynchronize());
+    if ((rc = sc->upload(&S, sizeof S, &p))) return rc;
+    sc->d_scene = (DevScene *)p;
     if ((rc = arena().alloc((void **)&sc->qcount, 16 * sizeof(unsigned int)))) return rc;
     if ((rc = arena().alloc((void **)&sc->ctr, Scene::kMaxLaunch * sizeof(DevCounters)))) return rc;
     return GXY_OK;
@@ -538,17 +543,28 @@ __device__ __forceinline__ void put_ray(DRay *q, unsigned idx, V3 o, float t, V3
 
 enum { Q_PRIM = 0, Q_SHADOW = 1, Q_AO = 2, NQ = 3 };
 enum { K_CAMERA = 0, K_PRIMARY = 1, K_SECONDARY = 2 };
+constexpr int kMaxJobs = 1024;
 
-struct FrameArgs {
+// One render job (a camera x visualization of a RenderingSet).
+struct DevJob {
     DevCamera cam;
     DevLights L;
     float *fb;
+    const DevScene *scene;             // device copy of the job's scene (batches)
+    long long pix0;                    // first global pixel index of the job
+};
+
+struct FrameArgs {
+    DevJob job0;                       // single-job launches
+    const DevJob *jobs;                // batch launches
+    int n_jobs;
+    long long total_pix;
     const DRay *qin[NQ];
     unsigned nin[NQ];
     DRay *qout[NQ];
-    unsigned *qout_count;            // NQ counters
+    unsigned *qout_count;              // NQ counters
     unsigned qcap[NQ];
-    DevCounters *ctr;                // this launch's counter slot
+    DevCounters *ctr;                  // this launch's counter slot
 };
 
 // Reserve cnt consecutive queue records for this thread: one warp-wide scan
@@ -571,9 +587,17 @@ __device__ __forceinline__ unsigned warp_reserve(unsigned cnt, unsigned *counter
     return idx;
 }
 
-__device__ __forceinline__ void flush_counters(DevCounters *ctr, const unsigned long long (&vals)[14]) {
+struct LocalCounters {
+    unsigned long long prim = 0, sh = 0, ao = 0, seg = 0, hand = 0, term = 0, drop = 0, keep = 0, enq = 0;
+    int ovf = 0;
+};
+
+__device__ __forceinline__ void flush_counters(DevCounters *ctr, const LocalCounters &c, const RayStats &st) {
     __shared__ unsigned long long red[16];
     const int lane = threadIdx.x & 31;
+    unsigned long long vals[14] = {c.prim, c.sh, c.ao, c.seg, c.hand, c.term, c.drop, c.keep, st.samples, st.nodes,
+                                   st.tris, st.sphs, c.enq, (unsigned long long)(c.ovf | st.ovf)};
+    __syncthreads();
     if (threadIdx.x < 16) red[threadIdx.x] = 0;
     __syncthreads();
 #pragma unroll
@@ -594,244 +618,354 @@ __device__ __forceinline__ void add_pixel(float *fb, int width, int x, int y, fl
     }
 }
 
-// One generation for primary rays: KIND == K_CAMERA builds the camera ray of
-// each pixel; KIND == K_PRIMARY reads handed-off / kept primaries.  Each ray
-// is traced, shaded if it ends on a surface (ambient, AO spawn, diffuse,
-// shadow spawn), classified and routed; spawned rays go to the shadow and AO
-// queues, continuing primaries to the primary queue.
-template <int KIND>
-__global__ void __launch_bounds__(kThreads) k_primary(DevScene S, FrameArgs A) {
-    __shared__ DevTF tfs[kMaxVol];
-    load_tfs(S, tfs);
-    const DevLights &L = A.L;
-    const int64_t n_items = KIND == K_CAMERA ? (int64_t)A.cam.width * A.cam.height : (int64_t)A.nin[Q_PRIM];
-    RayStats st;
-    unsigned long long c_prim = 0, c_sh = 0, c_ao = 0, c_seg = 0, c_hand = 0, c_term = 0, c_drop = 0, c_keep = 0,
-                       c_enq = 0;
-    int ovf = 0;
-    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n_items; base += stride) {
+__device__ __forceinline__ void load_ray(const DRay *q, int64_t i, TraceIn &in, int &x, int &y, int &job) {
+    const float4 *src = reinterpret_cast<const float4 *>(q + i);
+    float4 a = __ldg(src), b = __ldg(src + 1), c = __ldg(src + 2);
+    int4 m = __ldg(reinterpret_cast<const int4 *>(src + 3));
+    in.org = v3(a.x, a.y, a.z);
+    in.t = a.w;
+    in.dir = v3(b.x, b.y, b.z);
+    in.tmax = b.w;
+    in.r = c.x; in.g = c.y; in.b = c.z; in.o = c.w;
+    x = m.x;
+    y = m.y;
+    in.type = ray_type(m.z);
+    in.part = ray_part(m.z);
+    job = ray_job(m.z);
+}
+
+// Result of tracing one primary ray segment.
+struct PrimOut {
+    TraceOut T;
+    int dest;
+    bool spawn;
+    float ar, ag, ab, o_post;
+};
+
+// Trace, shade (reverse-lighting order of TraceRays.cpp:124-131), classify,
+// route and accumulate one primary ray segment.
+__device__ __forceinline__ void primary_ray(const DevScene &S, const DevTF *tfs, const DevJob &J, const TraceIn &in,
+                                            int x, int y, PrimOut &P, RayStats &st, LocalCounters &c) {
+    const DevLights &L = J.L;
+    P.spawn = false;
+    P.ar = P.ag = P.ab = P.o_post = 0.0f;
+    c.seg++;
+    P.T = trace_core<true, false>(S, tfs, in, st);
+    TraceOut &T = P.T;
+    if (in.type == GXY_RAY_PRIMARY && T.surface) {
+        // ambient (TraceRays.ispc:735-761)
+        float s = L.Ka * (1.0f - T.o);
+        float ka_ao = L.n_ao ? -L.Ka / L.n_ao : 0.0f;
+        float as = ka_ao * (1.0f - T.o);
+        P.ar = as * T.sc.x; P.ag = as * T.sc.y; P.ab = as * T.sc.z;
+        T.r += s * T.sc.x;
+        T.g += s * T.sc.y;
+        T.b += s * T.sc.z;
+        // diffuse (TraceRays.ispc:859-923)
+        float Kd = L.Kd / L.n;
+        float tr = 0, tg = 0, tb = 0;
+        for (int k = 0; k < L.n; k++) {
+            V3 lv;
+            if (L.type[k]) {
+                float t = T.t;
+                V3 sp = v3(in.org.x + t * in.dir.x, in.org.y + t * in.dir.y, in.org.z + t * in.dir.z);
+                lv = nrm(v3(L.l[k].x, L.l[k].y, L.l[k].z) - sp);
+            } else {
+                lv = neg(v3(L.l[k].x, L.l[k].y, L.l[k].z));
+            }
+            float dd = dot(T.n, lv);
+            if (dd > 0) {
+                float dff = (1.0f - T.o) * dd;
+                tr += dff * T.sc.x;
+                tg += dff * T.sc.y;
+                tb += dff * T.sc.z;
+            }
+        }
+        float f = Kd * (1 - T.o);
+        T.r = T.r + f * tr;
+        T.g = T.g + f * tg;
+        T.b = T.b + f * tb;
+        P.o_post = T.o + f * T.o;
+        T.o = P.o_post;
+        P.spawn = true;
+        c.ao += L.n_ao;
+        c.sh += L.shadows ? L.n : 0;
+    }
+    int cls = classify_ray(in.type, T.term);
+    P.dest = assign_destination(S, in.part, in.type, cls, in.org, in.dir);
+    if (P.dest == GXY_TERMINATED) {
+        c.term++;
+        add_pixel(J.fb, J.cam.width, x, y, T.r, T.g, T.b, T.o);
+    } else if (P.dest == GXY_DROP_ON_FLOOR) {
+        c.drop++;
+    } else if (P.dest == GXY_KEEP_HERE) {
+        c.keep++;
+    } else {
+        c.hand++;
+    }
+}
+
+// Warp-collective: write the continuation, AO and shadow rays of the lanes'
+// primary results (act = this lane has a result).
+__device__ __forceinline__ void emit_primary(const DevScene &S, const DevJob &J, int job, bool act, const TraceIn &in,
+                                             int x, int y, const PrimOut &P, const FrameArgs &A, LocalCounters &c) {
+    const DevLights &L = J.L;
+    const TraceOut &T = P.T;
+    // continuing primary -> primary queue
+    unsigned cont = (act && (P.dest >= 0 || P.dest == GXY_KEEP_HERE)) ? 1u : 0u;
+    unsigned idx = warp_reserve(cont, A.qout_count + Q_PRIM, A.qcap[Q_PRIM], c.ovf);
+    if (cont && idx != 0xffffffffu) {
+        int np_ = P.dest >= 0 ? P.dest : in.part;
+        put_ray(A.qout[Q_PRIM], idx, in.org, T.t, in.dir, in.tmax, T.r, T.g, T.b, T.o, x, y,
+                make_meta(in.type, np_, job));
+        c.enq++;
+    }
+    // AO rays (TraceRays.ispc:661-730); payload uses o before diffuse
+    unsigned nao = (act && P.spawn) ? (unsigned)L.n_ao : 0u;
+    idx = warp_reserve(nao, A.qout_count + Q_AO, A.qcap[Q_AO], c.ovf);
+    if (nao && idx != 0xffffffffu) {
+        V3 b0, b1;
+        ao_basis(T.n, b0, b1);
+        V3 o = v3(in.org.x + T.t * in.dir.x, in.org.y + T.t * in.dir.y, in.org.z + T.t * in.dir.z);
+        o = v3(o.x + S.epsilon * T.n.x, o.y + S.epsilon * T.n.y, o.z + S.epsilon * T.n.z);
+        ShadeIn sh;
+        sh.n = T.n; sh.x = x; sh.y = y;
+        for (int j = 0; j < L.n_ao; j++) {
+            Spawned s = ao_ray(S, L, sh, j, P.ar, P.ag, P.ab, b0, b1, o);
+            put_ray(A.qout[Q_AO], idx + j, s.o, 0.0f, s.d, s.tmax, s.r, s.g, s.b, 0.0f, x, y,
+                    make_meta(GXY_RAY_AO, in.part, job));
+        }
+        c.enq += nao;
+    }
+    // shadow rays (TraceRays.ispc:813-854); payload uses o after diffuse
+    unsigned nsh = (act && P.spawn && L.shadows) ? (unsigned)L.n : 0u;
+    idx = warp_reserve(nsh, A.qout_count + Q_SHADOW, A.qcap[Q_SHADOW], c.ovf);
+    if (nsh && idx != 0xffffffffu) {
+        float Kd = -L.Kd / L.n;
+        for (int k = 0; k < L.n; k++) {
+            V3 sp = v3(in.org.x + T.t * in.dir.x + S.epsilon * T.n.x, in.org.y + T.t * in.dir.y + S.epsilon * T.n.y,
+                       in.org.z + T.t * in.dir.z + S.epsilon * T.n.z);
+            V3 lv;
+            if (L.type[k]) lv = nrm(v3(L.l[k].x, L.l[k].y, L.l[k].z) - sp);
+            else lv = neg(v3(L.l[k].x, L.l[k].y, L.l[k].z));
+            lv = nrm(lv);
+            float dd = dot(T.n, lv);
+            if (dd < 0) dd = 0;
+            float dff = (1.0f - P.o_post) * Kd * dd;
+            put_ray(A.qout[Q_SHADOW], idx + k, sp, 0.0f, lv, INFINITY, dff * T.sc.x, dff * T.sc.y, dff * T.sc.z,
+                    0.0f, x, y, make_meta(GXY_RAY_SHADOW, in.part, job));
+        }
+        c.enq += nsh;
+    }
+}
+
+// Trace one shadow/AO ray: a ray that ends on a surface adds its payload, a
+// ray leaving its brick continues in the neighbour, the rest are dropped.
+__device__ __forceinline__ int secondary_ray(const DevScene &S, const DevTF *tfs, const DevJob &J, const TraceIn &in,
+                                             int x, int y, TraceOut &T, RayStats &st, LocalCounters &c) {
+    c.seg++;
+    T = trace_core<true, true>(S, tfs, in, st);
+    int dest;
+    if (T.cull) {
+        dest = GXY_DROP_ON_FLOOR;
+    } else {
+        int cls = classify_ray(in.type, T.term);
+        dest = assign_destination(S, in.part, in.type, cls, in.org, in.dir);
+    }
+    if (dest == GXY_TERMINATED) {
+        c.term++;
+        add_pixel(J.fb, J.cam.width, x, y, T.r, T.g, T.b, T.o);
+    } else if (dest == GXY_DROP_ON_FLOOR) {
+        c.drop++;
+    } else {
+        c.hand++;
+    }
+    return dest;
+}
+
+// Warp-collective: hand shadow/AO rays to their neighbour brick's queue.
+__device__ __forceinline__ void emit_secondary(bool act, int dest, int q, int job, const TraceIn &in, int x, int y,
+                                               const TraceOut &T, const FrameArgs &A, LocalCounters &c) {
+    unsigned cs = (act && dest >= 0 && q == Q_SHADOW) ? 1u : 0u;
+    unsigned ca = (act && dest >= 0 && q == Q_AO) ? 1u : 0u;
+    unsigned is = warp_reserve(cs, A.qout_count + Q_SHADOW, A.qcap[Q_SHADOW], c.ovf);
+    unsigned ia = warp_reserve(ca, A.qout_count + Q_AO, A.qcap[Q_AO], c.ovf);
+    if (cs && is != 0xffffffffu)
+        put_ray(A.qout[Q_SHADOW], is, in.org, T.t, in.dir, in.tmax, T.r, T.g, T.b, T.o, x, y,
+                make_meta(in.type, dest, job));
+    if (ca && ia != 0xffffffffu)
+        put_ray(A.qout[Q_AO], ia, in.org, T.t, in.dir, in.tmax, T.r, T.g, T.b, T.o, x, y, make_meta(in.type, dest, job));
+    c.enq += cs + ca;
+}
+
+// Job of a global camera-pixel index (binary search over the jobs' first pixels).
+__device__ __forceinline__ int find_job(const long long *pix0, int n, long long i) {
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (pix0[mid] <= i) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+// Camera-ray generation over items [0, n_items) of a grid-stride loop.
+// BATCH: pixels of all jobs (job by binary search); USCENE: every job uses
+// the scene Sp (kernel parameter, TFs in shared memory), otherwise each
+// job's scene is read from its device copy and TFs from global memory.
+template <bool BATCH, bool USCENE>
+__device__ __forceinline__ void camera_pass(const DevScene &Sp, const DevTF *tfs_uniform, const FrameArgs &A,
+                                            const long long *pix0_sh, int64_t n_items, int64_t start, int64_t stride,
+                                            RayStats &st, LocalCounters &c) {
+    for (int64_t base = start; base < n_items; base += stride) {
         int64_t i = base + threadIdx.x;
         bool valid = i < n_items;
         TraceIn in;
         uint64_t pending = 0;
-        int x = 0, y = 0;
+        int x = 0, y = 0, job = 0;
+        const DevJob *J = &A.job0;
         if (valid) {
-            if (KIND == K_CAMERA) {
-                x = (int)(i % A.cam.width);
-                y = (int)(i / A.cam.width);
-                pending = camera_ray(S, A.cam, x, y, in.org, in.dir);
-                in.t = 0.0f;
-                in.tmax = FLT_MAX;
-                in.r = in.g = in.b = in.o = 0.0f;
-                in.type = GXY_RAY_PRIMARY;
-            } else {
-                const float4 *src = reinterpret_cast<const float4 *>(A.qin[Q_PRIM] + i);
-                float4 a = __ldg(src), b = __ldg(src + 1), c = __ldg(src + 2);
-                int4 m = __ldg(reinterpret_cast<const int4 *>(src + 3));
-                in.org = v3(a.x, a.y, a.z);
-                in.t = a.w;
-                in.dir = v3(b.x, b.y, b.z);
-                in.tmax = b.w;
-                in.r = c.x; in.g = c.y; in.b = c.z; in.o = c.w;
-                x = m.x;
-                y = m.y;
-                in.type = ray_type(m.z);
-                in.part = ray_part(m.z);
-                pending = 1;
+            if (BATCH) {
+                job = find_job(pix0_sh, A.n_jobs, i);
+                J = A.jobs + job;
             }
+            const DevScene &S = USCENE ? Sp : *J->scene;
+            int w = J->cam.width;
+            int64_t li = i - (BATCH ? J->pix0 : 0);
+            x = (int)(li % w);
+            y = (int)(li / w);
+            pending = camera_ray(S, J->cam, x, y, in.org, in.dir);
+            in.t = 0.0f;
+            in.tmax = FLT_MAX;
+            in.r = in.g = in.b = in.o = 0.0f;
+            in.type = GXY_RAY_PRIMARY;
         }
         while (__any_sync(0xffffffffu, pending != 0)) {
             bool act = pending != 0;
-            TraceOut T;
-            int dest = GXY_DROP_ON_FLOOR;
-            bool spawn = false;
-            float ar = 0, ag = 0, ab = 0, o_post = 0;
+            PrimOut P;
+            const DevScene &S = USCENE ? Sp : *J->scene;
             if (act) {
-                if (KIND == K_CAMERA) {
-                    int p = __ffsll((long long)pending) - 1;
-                    pending &= pending - 1;
-                    in.part = p;
-                    c_prim++;
-                } else {
-                    pending = 0;
-                }
-                c_seg++;
-                T = trace_core<true, false>(S, tfs, in, st);
-                if (in.type == GXY_RAY_PRIMARY && T.surface) {
-                    // ambient (TraceRays.ispc:735-761)
-                    float s = L.Ka * (1.0f - T.o);
-                    float ka_ao = L.n_ao ? -L.Ka / L.n_ao : 0.0f;
-                    float as = ka_ao * (1.0f - T.o);
-                    ar = as * T.sc.x; ag = as * T.sc.y; ab = as * T.sc.z;
-                    T.r += s * T.sc.x;
-                    T.g += s * T.sc.y;
-                    T.b += s * T.sc.z;
-                    // diffuse (TraceRays.ispc:859-923)
-                    float Kd = L.Kd / L.n;
-                    float tr = 0, tg = 0, tb = 0;
-                    for (int k = 0; k < L.n; k++) {
-                        V3 lv;
-                        if (L.type[k]) {
-                            float t = T.t;
-                            V3 sp = v3(in.org.x + t * in.dir.x, in.org.y + t * in.dir.y, in.org.z + t * in.dir.z);
-                            lv = nrm(v3(L.l[k].x, L.l[k].y, L.l[k].z) - sp);
-                        } else {
-                            lv = neg(v3(L.l[k].x, L.l[k].y, L.l[k].z));
-                        }
-                        float dd = dot(T.n, lv);
-                        if (dd > 0) {
-                            float dff = (1.0f - T.o) * dd;
-                            tr += dff * T.sc.x;
-                            tg += dff * T.sc.y;
-                            tb += dff * T.sc.z;
-                        }
-                    }
-                    float f = Kd * (1 - T.o);
-                    T.r = T.r + f * tr;
-                    T.g = T.g + f * tg;
-                    T.b = T.b + f * tb;
-                    o_post = T.o + f * T.o;
-                    T.o = o_post;
-                    spawn = true;
-                    c_ao += L.n_ao;
-                    c_sh += L.shadows ? L.n : 0;
-                }
-                int cls = classify_ray(in.type, T.term);
-                dest = assign_destination(S, in.part, in.type, cls, in.org, in.dir);
-                if (dest == GXY_TERMINATED) {
-                    c_term++;
-                    add_pixel(A.fb, A.cam.width, x, y, T.r, T.g, T.b, T.o);
-                } else if (dest == GXY_DROP_ON_FLOOR) {
-                    c_drop++;
-                } else if (dest == GXY_KEEP_HERE) {
-                    c_keep++;
-                } else {
-                    c_hand++;
-                }
+                int p = __ffsll((long long)pending) - 1;
+                pending &= pending - 1;
+                in.part = p;
+                c.prim++;
+                primary_ray(S, USCENE ? tfs_uniform : S.tfs, *J, in, x, y, P, st, c);
             }
-            // continuing primary -> primary queue
-            unsigned cont = (act && (dest >= 0 || dest == GXY_KEEP_HERE)) ? 1u : 0u;
-            unsigned idx = warp_reserve(cont, A.qout_count + Q_PRIM, A.qcap[Q_PRIM], ovf);
-            if (cont && idx != 0xffffffffu) {
-                int np_ = dest >= 0 ? dest : in.part;
-                put_ray(A.qout[Q_PRIM], idx, in.org, T.t, in.dir, in.tmax, T.r, T.g, T.b, T.o, x, y,
-                        make_meta(in.type, np_, 0));
-                c_enq++;
-            }
-            // AO rays (TraceRays.ispc:661-730); payload uses o before diffuse
-            unsigned nao = spawn ? (unsigned)L.n_ao : 0u;
-            idx = warp_reserve(nao, A.qout_count + Q_AO, A.qcap[Q_AO], ovf);
-            if (nao && idx != 0xffffffffu) {
-                V3 b0, b1;
-                ao_basis(T.n, b0, b1);
-                V3 o = v3(in.org.x + T.t * in.dir.x, in.org.y + T.t * in.dir.y, in.org.z + T.t * in.dir.z);
-                o = v3(o.x + S.epsilon * T.n.x, o.y + S.epsilon * T.n.y, o.z + S.epsilon * T.n.z);
-                ShadeIn sh;
-                sh.n = T.n; sh.x = x; sh.y = y;
-                for (int j = 0; j < L.n_ao; j++) {
-                    Spawned s = ao_ray(S, L, sh, j, ar, ag, ab, b0, b1, o);
-                    put_ray(A.qout[Q_AO], idx + j, s.o, 0.0f, s.d, s.tmax, s.r, s.g, s.b, 0.0f, x, y,
-                            make_meta(GXY_RAY_AO, in.part, 0));
-                }
-                c_enq += nao;
-            }
-            // shadow rays (TraceRays.ispc:813-854); payload uses o after diffuse
-            unsigned nsh = (spawn && L.shadows) ? (unsigned)L.n : 0u;
-            idx = warp_reserve(nsh, A.qout_count + Q_SHADOW, A.qcap[Q_SHADOW], ovf);
-            if (nsh && idx != 0xffffffffu) {
-                float Kd = -L.Kd / L.n;
-                for (int k = 0; k < L.n; k++) {
-                    V3 sp = v3(in.org.x + T.t * in.dir.x + S.epsilon * T.n.x,
-                               in.org.y + T.t * in.dir.y + S.epsilon * T.n.y,
-                               in.org.z + T.t * in.dir.z + S.epsilon * T.n.z);
-                    V3 lv;
-                    if (L.type[k]) lv = nrm(v3(L.l[k].x, L.l[k].y, L.l[k].z) - sp);
-                    else lv = neg(v3(L.l[k].x, L.l[k].y, L.l[k].z));
-                    lv = nrm(lv);
-                    float dd = dot(T.n, lv);
-                    if (dd < 0) dd = 0;
-                    float dff = (1.0f - o_post) * Kd * dd;
-                    put_ray(A.qout[Q_SHADOW], idx + k, sp, 0.0f, lv, INFINITY, dff * T.sc.x, dff * T.sc.y,
-                            dff * T.sc.z, 0.0f, x, y, make_meta(GXY_RAY_SHADOW, in.part, 0));
-                }
-                c_enq += nsh;
-            }
+            emit_primary(S, *J, job, act, in, x, y, P, A, c);
         }
     }
-    ovf |= st.ovf;
-    unsigned long long vals[14] = {c_prim, c_sh, c_ao, c_seg, c_hand, c_term, c_drop, c_keep, st.samples, st.nodes,
-                                   st.tris, st.sphs, c_enq, (unsigned long long)ovf};
-    flush_counters(A.ctr, vals);
 }
 
-// One generation of shadow and AO rays: the shadow queue, then the AO queue,
-// as one index space.  A ray that ends on a surface adds its payload; a ray
-// leaving its brick goes to the neighbour's queue of the same type; the rest
-// are dropped (reverse lighting).
+// Queue pass over items [0, n_prim + n_sec): primaries first, then shadow
+// rays, then AO rays.
+template <bool BATCH, bool USCENE>
+__device__ __forceinline__ void queue_pass(const DevScene &Sp, const DevTF *tfs_uniform, const FrameArgs &A,
+                                           const unsigned n[NQ], int64_t start, int64_t stride, RayStats &st,
+                                           LocalCounters &c) {
+    const int64_t np = n[Q_PRIM], ns = n[Q_SHADOW];
+    const int64_t n_items = np + ns + (int64_t)n[Q_AO];
+    for (int64_t base = start; base < n_items; base += stride) {
+        int64_t i = base + threadIdx.x;
+        bool valid = i < n_items;
+        TraceIn in;
+        int x = 0, y = 0, job = 0;
+        int q = i < np ? Q_PRIM : (i < np + ns ? Q_SHADOW : Q_AO);
+        if (valid) load_ray(A.qin[q], q == Q_PRIM ? i : (q == Q_SHADOW ? i - np : i - np - ns), in, x, y, job);
+        const DevJob &J = BATCH ? A.jobs[valid ? job : 0] : A.job0;
+        const DevScene &S = USCENE ? Sp : *J.scene;
+        const DevTF *tfs = USCENE ? tfs_uniform : S.tfs;
+        bool actp = valid && q == Q_PRIM, acts = valid && q != Q_PRIM;
+        PrimOut P;
+        TraceOut T;
+        int dest = GXY_DROP_ON_FLOOR;
+        if (actp) primary_ray(S, tfs, J, in, x, y, P, st, c);
+        if (acts) dest = secondary_ray(S, tfs, J, in, x, y, T, st, c);
+        if (__any_sync(0xffffffffu, actp)) emit_primary(S, J, job, actp, in, x, y, P, A, c);
+        if (__any_sync(0xffffffffu, acts)) emit_secondary(acts, dest, q, job, in, x, y, T, A, c);
+    }
+}
+
+// Host-driven generations (one launch per kind, counts from the host); the
+// single-frame path and the per-launch profile use these.
+template <int KIND>
+__global__ void __launch_bounds__(kThreads) k_primary(DevScene S, FrameArgs A) {
+    __shared__ DevTF tfs[kMaxVol];
+    load_tfs(S, tfs);
+    RayStats st;
+    LocalCounters c;
+    const int64_t start = (int64_t)blockIdx.x * blockDim.x, stride = (int64_t)gridDim.x * blockDim.x;
+    if (KIND == K_CAMERA) {
+        camera_pass<false, true>(S, tfs, A, nullptr, (int64_t)A.job0.cam.width * A.job0.cam.height, start, stride, st,
+                                 c);
+    } else {
+        unsigned n[NQ] = {A.nin[Q_PRIM], 0u, 0u};
+        queue_pass<false, true>(S, tfs, A, n, start, stride, st, c);
+    }
+    flush_counters(A.ctr, c, st);
+}
+
 __global__ void __launch_bounds__(kThreads) k_secondary(DevScene S, FrameArgs A) {
     __shared__ DevTF tfs[kMaxVol];
     load_tfs(S, tfs);
-    const unsigned ns = A.nin[Q_SHADOW];
-    const int64_t n_items = (int64_t)ns + A.nin[Q_AO];
     RayStats st;
-    unsigned long long c_seg = 0, c_hand = 0, c_term = 0, c_drop = 0, c_enq = 0;
-    int ovf = 0;
-    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n_items; base += stride) {
-        int64_t i = base + threadIdx.x;
-        bool act = i < n_items;
-        TraceIn in;
-        int x = 0, y = 0, q = Q_SHADOW;
-        int dest = GXY_DROP_ON_FLOOR;
-        TraceOut T;
-        if (act) {
-            q = i < ns ? Q_SHADOW : Q_AO;
-            const float4 *src = reinterpret_cast<const float4 *>(A.qin[q] + (i < ns ? i : i - ns));
-            float4 a = __ldg(src), b = __ldg(src + 1), c = __ldg(src + 2);
-            int4 m = __ldg(reinterpret_cast<const int4 *>(src + 3));
-            in.org = v3(a.x, a.y, a.z);
-            in.t = a.w;
-            in.dir = v3(b.x, b.y, b.z);
-            in.tmax = b.w;
-            in.r = c.x; in.g = c.y; in.b = c.z; in.o = c.w;
-            x = m.x;
-            y = m.y;
-            in.type = ray_type(m.z);
-            in.part = ray_part(m.z);
-            c_seg++;
-            T = trace_core<true, true>(S, tfs, in, st);
-            if (T.cull) {
-                dest = GXY_DROP_ON_FLOOR;
-            } else {
-                int cls = classify_ray(in.type, T.term);
-                dest = assign_destination(S, in.part, in.type, cls, in.org, in.dir);
-            }
-            if (dest == GXY_TERMINATED) {
-                c_term++;
-                add_pixel(A.fb, A.cam.width, x, y, T.r, T.g, T.b, T.o);
-            } else if (dest == GXY_DROP_ON_FLOOR) {
-                c_drop++;
-            } else {
-                c_hand++;
-            }
+    LocalCounters c;
+    unsigned n[NQ] = {0u, A.nin[Q_SHADOW], A.nin[Q_AO]};
+    queue_pass<false, true>(S, tfs, A, n, (int64_t)blockIdx.x * blockDim.x, (int64_t)gridDim.x * blockDim.x, st, c);
+    flush_counters(A.ctr, c, st);
+}
+
+// Device-driven wavefront of a batch of jobs: camera generation, then
+// generations of all queues until they are empty or max_gen is reached, in
+// ONE cooperative launch with a grid barrier between generations.  Queue
+// sets ping-pong (2), queue counters rotate over 3 sets so that the set a
+// generation will write is zeroed two barriers after it was last read.
+struct WaveArgs {
+    DRay *q[2][NQ];
+    unsigned *counts;                  // 3 x NQ
+    int max_gen;
+    int *status;                       // [0] generations run, [1] rays left after max_gen
+};
+
+template <bool USCENE>
+__global__ void __launch_bounds__(kThreads) k_wavefront(DevScene Su, FrameArgs A, WaveArgs W) {
+    namespace cg = cooperative_groups;
+    cg::grid_group grid = cg::this_grid();
+    __shared__ DevTF tfs[kMaxVol];
+    __shared__ long long pix0[kMaxJobs];
+    for (int j = threadIdx.x; j < A.n_jobs; j += blockDim.x) pix0[j] = A.jobs[j].pix0;
+    if (USCENE) load_tfs(Su, tfs);
+    else __syncthreads();
+    RayStats st;
+    LocalCounters c;
+    const int64_t start = (int64_t)blockIdx.x * blockDim.x, stride = (int64_t)gridDim.x * blockDim.x;
+    for (int k = 0; k < NQ; k++) A.qout[k] = W.q[0][k];
+    A.qout_count = W.counts + 0;
+    camera_pass<true, USCENE>(Su, tfs, A, pix0, A.total_pix, start, stride, st, c);
+    grid.sync();
+    int g = 1;
+    for (; g < W.max_gen; g++) {
+        const unsigned *cin = W.counts + NQ * ((g - 1) % 3);
+        if (blockIdx.x == 0 && threadIdx.x < NQ) W.counts[NQ * ((g + 1) % 3) + threadIdx.x] = 0;
+        unsigned n[NQ];
+        for (int k = 0; k < NQ; k++) {
+            unsigned v = *((volatile const unsigned *)(cin + k));
+            n[k] = v > A.qcap[k] ? A.qcap[k] : v;
         }
-        unsigned cs = (act && dest >= 0 && q == Q_SHADOW) ? 1u : 0u;
-        unsigned ca = (act && dest >= 0 && q == Q_AO) ? 1u : 0u;
-        unsigned is = warp_reserve(cs, A.qout_count + Q_SHADOW, A.qcap[Q_SHADOW], ovf);
-        unsigned ia = warp_reserve(ca, A.qout_count + Q_AO, A.qcap[Q_AO], ovf);
-        if (cs && is != 0xffffffffu)
-            put_ray(A.qout[Q_SHADOW], is, in.org, T.t, in.dir, in.tmax, T.r, T.g, T.b, T.o, x, y,
-                    make_meta(in.type, dest, 0));
-        if (ca && ia != 0xffffffffu)
-            put_ray(A.qout[Q_AO], ia, in.org, T.t, in.dir, in.tmax, T.r, T.g, T.b, T.o, x, y,
-                    make_meta(in.type, dest, 0));
-        c_enq += cs + ca;
+        if (n[0] + n[1] + n[2] == 0) break;
+        for (int k = 0; k < NQ; k++) {
+            A.qin[k] = W.q[(g - 1) & 1][k];
+            A.qout[k] = W.q[g & 1][k];
+        }
+        A.qout_count = W.counts + NQ * (g % 3);
+        queue_pass<true, USCENE>(Su, tfs, A, n, start, stride, st, c);
+        grid.sync();
     }
-    ovf |= st.ovf;
-    unsigned long long vals[14] = {0, 0, 0, c_seg, c_hand, c_term, c_drop, 0, st.samples, st.nodes,
-                                   st.tris, st.sphs, c_enq, (unsigned long long)ovf};
-    flush_counters(A.ctr, vals);
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        W.status[0] = g;
+        const unsigned *cin = W.counts + NQ * ((g - 1) % 3);
+        W.status[1] = (g >= W.max_gen) ? (int)(cin[0] + cin[1] + cin[2]) : 0;
+    }
+    flush_counters(A.ctr, c, st);
 }
 
 // -------------------------------------------------------- RayList kernels
@@ -1056,14 +1190,14 @@ static int render(Scene *sc, const gxy_camera &cam, const gxy_lighting &lt, floa
     DevScene &S = sc->S;
     FrameArgs A;
     memset(&A, 0, sizeof A);
-    A.cam = setup_camera(cam);
-    int rc = setup_lights(lt, A.L);
+    A.job0.cam = setup_camera(cam);
+    int rc = setup_lights(lt, A.job0.L);
     if (rc) return rc;
-    if (A.L.n == 0) return set_error(GXY_ERR_INVALID, "lighting needs at least one light");
+    if (A.job0.L.n == 0) return set_error(GXY_ERR_INVALID, "lighting needs at least one light");
     int64_t npix = (int64_t)cam.width * cam.height;
     size_t slack = (size_t)npix / 8 + 4096;
-    size_t need[3] = {(size_t)npix + slack, (size_t)npix * (A.L.shadows ? A.L.n : 0) + slack,
-                      (size_t)npix * A.L.n_ao + slack};
+    size_t need[3] = {(size_t)npix + slack, (size_t)npix * (A.job0.L.shadows ? A.job0.L.n : 0) + slack,
+                      (size_t)npix * A.job0.L.n_ao + slack};
     if ((rc = ensure_queues(sc, need))) return rc;
     const int maxl = Scene::kMaxLaunch;
     CK(cudaMemsetAsync(sc->ctr, 0, maxl * sizeof(DevCounters), st));
@@ -1075,7 +1209,11 @@ static int render(Scene *sc, const gxy_camera &cam, const gxy_lighting &lt, floa
             sc->events.push_back(e);
         }
     }
-    A.fb = fb;
+    A.job0.fb = fb;
+    A.job0.scene = sc->d_scene;
+    A.job0.pix0 = 0;
+    A.n_jobs = 1;
+    A.total_pix = npix;
     for (int k = 0; k < 3; k++) A.qcap[k] = (unsigned)sc->qcap[k];
     struct LaunchRec { int gen, kind; unsigned rays_in; };
     std::vector<LaunchRec> recs;
@@ -1561,6 +1699,280 @@ int gxy_gpu_accumulate_terminated(const gxy_raylist *rays, float *fb_rgba, int w
     CK(cudaMemcpy(fb_rgba, fb, bytes, cudaMemcpyDeviceToHost));
     return GXY_OK;
     GUARD_END
+}
+
+}  // extern "C"
+
+// ================================================================ batches
+namespace gxy {
+
+struct Batch {
+    int64_t max_pixels = 0;
+    int max_jobs = 0, max_shadow = 0, max_ao = 0;
+    DRay *q[2][NQ] = {{nullptr, nullptr, nullptr}, {nullptr, nullptr, nullptr}};
+    size_t qcap[NQ] = {0, 0, 0};
+    unsigned *counts = nullptr;        // 3 x NQ
+    DevJob *d_jobs = nullptr;
+    DevJob *h_jobs = nullptr;          // pinned
+    DevCounters *ctr = nullptr;
+    int *d_status = nullptr, *h_status = nullptr;   // pinned host copy of [gens, left]
+    DevCounters *h_ctr = nullptr;                   // pinned
+    cudaStream_t stream = nullptr;
+    cudaEvent_t done = nullptr;
+    cudaGraphExec_t gexec = nullptr;
+    int grid = 0;
+    bool pending = false;
+    int last_rc = GXY_OK;
+    std::vector<void *> dev;
+    ~Batch() {
+        if (stream) cudaStreamSynchronize(stream);
+        for (void *p : dev) arena().free(p);
+        if (h_jobs) cudaFreeHost(h_jobs);
+        if (h_status) cudaFreeHost(h_status);
+        if (h_ctr) cudaFreeHost(h_ctr);
+        if (gexec) cudaGraphExecDestroy(gexec);
+        if (done) cudaEventDestroy(done);
+        if (stream) cudaStreamDestroy(stream);
+    }
+    int dalloc(void **p, size_t bytes) {
+        int rc = arena().alloc(p, bytes ? bytes : 16);
+        if (rc == GXY_OK) dev.push_back(*p);
+        return rc;
+    }
+};
+
+static int batch_grid(bool uniform) {
+    int sms = 152, per = 1;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, g_device);
+    if (uniform) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_wavefront<true>, kThreads, 0);
+    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_wavefront<false>, kThreads, 0);
+    if (per < 1) per = 1;
+    return sms * per;
+}
+
+// Enqueue one submission on the batch stream (captured into a graph or not).
+static int batch_enqueue(Batch *b, const DevScene &Su, bool uniform, const FrameArgs &A, const WaveArgs &W,
+                         int n_jobs) {
+    cudaStream_t st = b->stream;
+    CK(cudaMemcpyAsync(b->d_jobs, b->h_jobs, n_jobs * sizeof(DevJob), cudaMemcpyHostToDevice, st));
+    CK(cudaMemsetAsync(b->counts, 0, 3 * NQ * sizeof(unsigned), st));
+    CK(cudaMemsetAsync(b->ctr, 0, sizeof(DevCounters), st));
+    FrameArgs a = A;
+    WaveArgs w = W;
+    DevScene s = Su;
+    void *args[] = {&s, &a, &w};
+    int grid = batch_grid(uniform);
+    if (uniform)
+        CK(cudaLaunchCooperativeKernel((const void *)k_wavefront<true>, dim3(grid), dim3(kThreads), args, 0, st));
+    else
+        CK(cudaLaunchCooperativeKernel((const void *)k_wavefront<false>, dim3(grid), dim3(kThreads), args, 0, st));
+    CK(cudaMemcpyAsync(b->h_status, b->d_status, 2 * sizeof(int), cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(b->h_ctr, b->ctr, sizeof(DevCounters), cudaMemcpyDeviceToHost, st));
+    return GXY_OK;
+}
+
+}  // namespace gxy
+
+extern "C" {
+
+int gxy_gpu_batch_create(int64_t max_pixels, int max_jobs, int max_shadow, int max_ao, gxy_batch *out) {
+    GUARD_BEGIN
+    if (!g_init) return set_error(GXY_ERR_NOT_INIT, "gxy_gpu_init not called");
+    if (!out || max_pixels <= 0 || max_jobs <= 0 || max_jobs > kMaxJobs || max_shadow < 0 ||
+        max_shadow > GXY_MAX_LIGHTS || max_ao < 0 || max_ao > 64)
+        return set_error(GXY_ERR_INVALID, "bad batch limits");
+    std::unique_ptr<Batch> b(new Batch());
+    b->max_pixels = max_pixels;
+    b->max_jobs = max_jobs;
+    b->max_shadow = max_shadow;
+    b->max_ao = max_ao;
+    size_t slack = (size_t)max_pixels / 8 + 4096;
+    size_t need[NQ] = {(size_t)max_pixels + slack, (size_t)max_pixels * max_shadow + slack,
+                       (size_t)max_pixels * max_ao + slack};
+    size_t bytes = 0;
+    for (int k = 0; k < NQ; k++) bytes += 2 * need[k] * sizeof(DRay);
+    if (!arena().would_fit(bytes + 16 * 1024 * 1024))
+        return set_error(GXY_ERR_ADMISSION, "batch queues (" + std::to_string(bytes) + " bytes) exceed the HBM budget");
+    for (int k = 0; k < NQ; k++) {
+        for (int s = 0; s < 2; s++) {
+            int rc = b->dalloc((void **)&b->q[s][k], need[k] * sizeof(DRay));
+            if (rc) return rc == GXY_ERR_OOM ? set_error(GXY_ERR_ADMISSION, last_error()) : rc;
+        }
+        if (need[k] > 0xffffffffull) return set_error(GXY_ERR_INVALID, "batch too large");
+        b->qcap[k] = need[k];
+    }
+    int rc;
+    if ((rc = b->dalloc((void **)&b->counts, 3 * NQ * sizeof(unsigned)))) return rc;
+    if ((rc = b->dalloc((void **)&b->d_jobs, max_jobs * sizeof(DevJob)))) return rc;
+    if ((rc = b->dalloc((void **)&b->ctr, sizeof(DevCounters)))) return rc;
+    if ((rc = b->dalloc((void **)&b->d_status, 4 * sizeof(int)))) return rc;
+    CK(cudaMallocHost((void **)&b->h_jobs, max_jobs * sizeof(DevJob)));
+    CK(cudaMallocHost((void **)&b->h_status, 4 * sizeof(int)));
+    CK(cudaMallocHost((void **)&b->h_ctr, sizeof(DevCounters)));
+    CK(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
+    CK(cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming));
+    *out = reinterpret_cast<gxy_batch>(b.release());
+    return GXY_OK;
+    GUARD_END
+}
+
+int gxy_gpu_batch_release(gxy_batch batch) {
+    GUARD_BEGIN
+    if (!batch) return set_error(GXY_ERR_INVALID, "null batch");
+    delete reinterpret_cast<Batch *>(batch);
+    return GXY_OK;
+    GUARD_END
+}
+
+int gxy_gpu_batch_stream(gxy_batch batch, void **stream) {
+    if (!batch || !stream) return set_error(GXY_ERR_INVALID, "null argument");
+    *stream = reinterpret_cast<Batch *>(batch)->stream;
+    return GXY_OK;
+}
+
+int gxy_gpu_batch_submit(gxy_batch batch, const gxy_job *jobs, int n_jobs, int use_graph) {
+    GUARD_BEGIN
+    if (!batch || !jobs || n_jobs <= 0) return set_error(GXY_ERR_INVALID, "bad argument");
+    Batch *b = reinterpret_cast<Batch *>(batch);
+    if (b->pending) {
+        cudaError_t q = cudaEventQuery(b->done);
+        if (q == cudaErrorNotReady) return set_error(GXY_ERR_INVALID, "previous submission still running");
+    }
+    if (n_jobs > b->max_jobs) return set_error(GXY_ERR_INVALID, "too many jobs for this batch");
+    long long pix = 0;
+    Scene *first = reinterpret_cast<Scene *>(jobs[0].scene);
+    bool uniform = true;
+    for (int j = 0; j < n_jobs; j++) {
+        const gxy_job &J = jobs[j];
+        if (!J.scene || !J.fb_rgba || J.camera.width <= 0 || J.camera.height <= 0)
+            return set_error(GXY_ERR_INVALID, "bad job " + std::to_string(j));
+        Scene *sc = reinterpret_cast<Scene *>(J.scene);
+        if (sc != first) uniform = false;
+        DevJob &D = b->h_jobs[j];
+        D.cam = setup_camera(J.camera);
+        int rc = setup_lights(J.lighting, D.L);
+        if (rc) return rc;
+        if (D.L.n == 0) return set_error(GXY_ERR_INVALID, "lighting needs at least one light");
+        if ((D.L.shadows ? D.L.n : 0) > b->max_shadow || D.L.n_ao > b->max_ao)
+            return set_error(GXY_ERR_ADMISSION, "job needs more secondary rays per pixel than the batch holds");
+        D.fb = J.fb_rgba;
+        D.scene = sc->d_scene;
+        D.pix0 = pix;
+        pix += (long long)J.camera.width * J.camera.height;
+    }
+    if (pix > b->max_pixels) return set_error(GXY_ERR_ADMISSION, "batch pixel budget exceeded");
+    FrameArgs A;
+    memset(&A, 0, sizeof A);
+    A.jobs = b->d_jobs;
+    A.n_jobs = n_jobs;
+    A.total_pix = pix;
+    A.job0 = b->h_jobs[0];
+    for (int k = 0; k < NQ; k++) A.qcap[k] = (unsigned)b->qcap[k];
+    A.ctr = b->ctr;
+    WaveArgs W;
+    for (int s = 0; s < 2; s++)
+        for (int k = 0; k < NQ; k++) W.q[s][k] = b->q[s][k];
+    W.counts = b->counts;
+    W.max_gen = 64;
+    W.status = b->d_status;
+    const DevScene &Su = first->S;
+    if (use_graph) {
+        cudaGraph_t g;
+        CK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+        int rc = batch_enqueue(b, Su, uniform, A, W, n_jobs);
+        cudaGraph_t gg = nullptr;
+        cudaError_t e = cudaStreamEndCapture(b->stream, &gg);
+        if (rc) return rc;
+        if (e != cudaSuccess) return set_error(GXY_ERR_CUDA, std::string("capture: ") + cudaGetErrorString(e));
+        g = gg;
+        bool updated = false;
+        if (b->gexec) {
+            cudaGraphExecUpdateResultInfo info;
+            if (cudaGraphExecUpdate(b->gexec, g, &info) == cudaSuccess) updated = true;
+            else {
+                cudaGetLastError();
+                cudaGraphExecDestroy(b->gexec);
+                b->gexec = nullptr;
+            }
+        }
+        if (!updated) CK(cudaGraphInstantiate(&b->gexec, g, 0));
+        cudaGraphDestroy(g);
+        CK(cudaGraphLaunch(b->gexec, b->stream));
+    } else {
+        int rc = batch_enqueue(b, Su, uniform, A, W, n_jobs);
+        if (rc) return rc;
+    }
+    CK(cudaEventRecord(b->done, b->stream));
+    b->pending = true;
+    b->last_rc = GXY_OK;
+    return GXY_OK;
+    GUARD_END
+}
+
+static int batch_finish(Batch *b) {
+    b->pending = false;
+    if (b->h_status[1] > 0)
+        return b->last_rc = set_error(GXY_ERR_OVERFLOW, "rays left after the generation limit");
+    if (b->h_ctr->overflow) return b->last_rc = set_error(GXY_ERR_OVERFLOW, "a batch queue overflowed");
+    return b->last_rc = GXY_OK;
+}
+
+int gxy_gpu_batch_poll(gxy_batch batch, int *done) {
+    GUARD_BEGIN
+    if (!batch || !done) return set_error(GXY_ERR_INVALID, "null argument");
+    Batch *b = reinterpret_cast<Batch *>(batch);
+    if (!b->pending) {
+        *done = 1;
+        return b->last_rc;
+    }
+    cudaError_t e = cudaEventQuery(b->done);
+    if (e == cudaErrorNotReady) {
+        *done = 0;
+        return GXY_OK;
+    }
+    if (e != cudaSuccess) return set_error(GXY_ERR_CUDA, cudaGetErrorString(e));
+    *done = 1;
+    return batch_finish(b);
+    GUARD_END
+}
+
+int gxy_gpu_batch_wait(gxy_batch batch, int timeout_ms) {
+    GUARD_BEGIN
+    if (!batch) return set_error(GXY_ERR_INVALID, "null batch");
+    Batch *b = reinterpret_cast<Batch *>(batch);
+    if (!b->pending) return b->last_rc;
+    auto t0 = std::chrono::steady_clock::now();
+    for (;;) {
+        cudaError_t e = cudaEventQuery(b->done);
+        if (e == cudaSuccess) return batch_finish(b);
+        if (e != cudaErrorNotReady) return set_error(GXY_ERR_CUDA, cudaGetErrorString(e));
+        double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        if (timeout_ms >= 0 && ms > timeout_ms) return set_error(GXY_ERR_TIMEOUT, "batch did not finish in time");
+        std::this_thread::sleep_for(std::chrono::microseconds(20));
+    }
+    GUARD_END
+}
+
+int gxy_gpu_batch_counters(gxy_batch batch, gxy_counters *out) {
+    if (!batch || !out) return set_error(GXY_ERR_INVALID, "null argument");
+    Batch *b = reinterpret_cast<Batch *>(batch);
+    const DevCounters &c = *b->h_ctr;
+    memset(out, 0, sizeof *out);
+    out->primary_rays = (int64_t)c.primary;
+    out->shadow_rays = (int64_t)c.shadow;
+    out->ao_rays = (int64_t)c.ao;
+    out->secondary_rays = (int64_t)(c.shadow + c.ao);
+    out->segments = (int64_t)c.segments;
+    out->handoffs = (int64_t)c.handoffs;
+    out->terminated = (int64_t)c.terminated;
+    out->dropped = (int64_t)c.dropped;
+    out->kept = (int64_t)c.kept;
+    out->bounces = b->h_status[0];
+    out->samples = (int64_t)c.samples;
+    out->nodes = (int64_t)c.nodes;
+    out->prim_tests = (int64_t)(c.tri_tests + c.sph_tests);
+    out->overflow = c.overflow;
+    return GXY_OK;
 }
 
 }  // extern "C"

@@ -52,6 +52,13 @@ def lib():
                                   C.POINTER(A.gxy_raylist), C.POINTER(i32)],
         "gxy_gpu_set_profiling": [vp, C.c_int],
         "gxy_gpu_query_generations": [vp, C.POINTER(A.gxy_generation_stats), C.c_int, C.POINTER(i32)],
+        "gxy_gpu_batch_create": [C.c_int64, C.c_int, C.c_int, C.c_int, C.POINTER(vp)],
+        "gxy_gpu_batch_release": [vp],
+        "gxy_gpu_batch_submit": [vp, C.POINTER(A.gxy_job), C.c_int, C.c_int],
+        "gxy_gpu_batch_poll": [vp, C.POINTER(C.c_int)],
+        "gxy_gpu_batch_wait": [vp, C.c_int],
+        "gxy_gpu_batch_counters": [vp, C.POINTER(A.gxy_counters)],
+        "gxy_gpu_batch_stream": [vp, C.POINTER(vp)],
         "gxy_gpu_classify": [C.POINTER(A.gxy_raylist)],
         "gxy_gpu_assign_destinations": [vp, C.c_int, C.POINTER(A.gxy_raylist)],
         "gxy_gpu_accumulate_terminated": [C.POINTER(A.gxy_raylist), A.f32p, C.c_int, C.c_int],
@@ -204,3 +211,59 @@ def accumulate_terminated(rays, fb):
     h, w, _ = fb.shape
     check(lib().gxy_gpu_accumulate_terminated(C.byref(c), A.fptr(fb), w, h))
     return fb
+
+
+class Batch:
+    """A batch slot (gxy_gpu_batch_create): device queues for up to
+    max_pixels camera rays, a job table and its own CUDA stream.  submit()
+    renders many jobs -- (scene, camera, lighting, device framebuffer) -- in
+    one persistent wavefront launch; poll()/wait() report completion."""
+
+    def __init__(self, max_pixels, max_jobs=64, max_shadow=1, max_ao=4):
+        ensure_init()
+        h = C.c_void_p()
+        check(lib().gxy_gpu_batch_create(int(max_pixels), int(max_jobs), int(max_shadow), int(max_ao), C.byref(h)))
+        self.h = h
+        self.max_pixels, self.max_jobs, self.max_shadow, self.max_ao = max_pixels, max_jobs, max_shadow, max_ao
+        self._keep = None
+
+    def release(self):
+        if getattr(self, "h", None) and self.h.value:
+            lib().gxy_gpu_batch_release(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.release()
+        except Exception:
+            pass
+
+    @property
+    def stream(self):
+        s = C.c_void_p()
+        check(lib().gxy_gpu_batch_stream(self.h, C.byref(s)))
+        return s.value
+
+    def submit(self, jobs, use_graph=False):
+        """jobs: list of (Scene, camera, gxy_lighting, device fb pointer)."""
+        arr = (A.gxy_job * len(jobs))()
+        for i, (sc, cam, L, fb) in enumerate(jobs):
+            arr[i].scene = sc.h.value
+            arr[i].camera = cam.c() if hasattr(cam, "c") else cam
+            arr[i].lighting = L if isinstance(L, A.gxy_lighting) else L.c()
+            arr[i].fb_rgba = fb
+        self._keep = (arr, jobs)
+        check(lib().gxy_gpu_batch_submit(self.h, arr, len(jobs), 1 if use_graph else 0))
+
+    def poll(self):
+        d = C.c_int(0)
+        check(lib().gxy_gpu_batch_poll(self.h, C.byref(d)))
+        return bool(d.value)
+
+    def wait(self, timeout_ms=60000):
+        check(lib().gxy_gpu_batch_wait(self.h, int(timeout_ms)))
+
+    def counters(self):
+        c = A.gxy_counters()
+        check(lib().gxy_gpu_batch_counters(self.h, C.byref(c)))
+        return {f: getattr(c, f) for f, _ in A.gxy_counters._fields_ if f != "pad"}

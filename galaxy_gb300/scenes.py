@@ -145,10 +145,23 @@ def vertex_normals(v, t):
     """Area-weighted vertex normals of a triangle mesh."""
     fn = np.cross(v[t[:, 1]] - v[t[:, 0]], v[t[:, 2]] - v[t[:, 0]])
     n = np.zeros_like(v)
-    for k in range(3):
-        np.add.at(n, t[:, k], fn)
+    for a in range(3):
+        for k in range(3):
+            n[:, a] += np.bincount(t[:, k], weights=fn[:, a], minlength=len(v))
     n /= np.maximum(np.linalg.norm(n, axis=1, keepdims=True), 1e-30)
     return n
+
+
+def displaced_sphere_mesh(n_triangles=10_000_000, seed=5, amplitude=0.01, center=(0.5, 0.5, 0.5), radius=0.4):
+    """One displaced UV sphere with about n_triangles triangles (the serving
+    workload's large mesh), per-vertex data = displacement."""
+    n = max(8, int(round(np.sqrt(n_triangles / 2.0))))
+    sv, st = uv_sphere(n, n)
+    g = rng(seed)
+    disp = g.uniform(-amplitude, amplitude, size=len(sv))
+    v = sv * (radius * (1.0 + disp))[:, None] + np.asarray(center)
+    return Triangles(v.astype(f32), st.astype(np.int32), vertex_normals(v, st).astype(f32),
+                     (0.5 + disp / (2 * amplitude)).astype(f32))
 
 
 def triangle_spheres(seed=0, n_seg=105, grid=3, spacing=2.5, amplitude=0.01):

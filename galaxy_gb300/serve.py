@@ -1,0 +1,216 @@
+"""Continuous-batching request loop over device-resident scenes.
+
+This plays the role of Galaxy's serving front ends -- ViewerClientServer's
+`render` command (src/multiserver/ViewerClientServer.cpp:62-253, pixels
+returned per ServerRendering::AddLocalPixels, ServerRendering.cpp:45-66) and
+GuiClientServer's `gui::render` (src/guiserver/GuiClientServer.cpp:375-407)
+-- without their socket transport: a request names a resident scene and
+carries a camera, a light change and an image size; the loop
+
+  * admits waiting requests whenever a batch slot is free and the
+    framebuffers fit the HBM budget (admission control; a request too large
+    for any slot is refused),
+  * packs the admitted requests of one scene into one persistent wavefront
+    launch (gpu.Batch.submit) on that slot's stream, so several batches --
+    requests that arrived while others were already on the GPU -- overlap on
+    the device,
+  * polls the slots, records each request's latency (arrival -> framebuffer
+    complete on the device) and frees its memory.
+
+serve_plain() serves the same requests one at a time through the plain
+single-frame path (gxy_gpu_render) for comparison.
+"""
+import math
+import time
+
+import numpy as np
+
+from . import _abi as A
+from . import gpu
+
+
+class Request:
+    __slots__ = ("id", "arrival", "scene", "camera", "lighting", "pixels", "fb", "t_submit", "t_done", "rays",
+                 "refused")
+
+    def __init__(self, rid, arrival, scene, camera, lighting):
+        self.id = rid
+        self.arrival = arrival
+        self.scene = scene          # key into the scene table
+        self.camera = camera        # scene.Camera
+        self.lighting = lighting    # gxy_lighting (resolved)
+        self.pixels = camera.width * camera.height
+        self.fb = None
+        self.t_submit = None
+        self.t_done = None
+        self.rays = 0
+        self.refused = False
+
+
+class FramebufferPool:
+    """Device framebuffers (torch tensors) under a byte budget."""
+
+    def __init__(self, budget_bytes):
+        import torch
+        self.torch = torch
+        self.budget = budget_bytes
+        self.used = 0
+
+    def try_alloc(self, w, h):
+        nbytes = w * h * 16
+        if self.used + nbytes > self.budget:
+            return None
+        t = self.torch.zeros((h, w, 4), dtype=self.torch.float32, device="cuda")
+        self.used += nbytes
+        return t
+
+    def free(self, t):
+        self.used -= t.numel() * 4
+
+
+class Server:
+    def __init__(self, scenes, n_slots=4, slot_pixels=8 << 20, max_jobs=64, max_shadow=1, max_ao=4,
+                 fb_budget=8 << 30, use_graph=True, keep_results=False):
+        self.scenes = scenes
+        self.slots = [gpu.Batch(slot_pixels, max_jobs, max_shadow, max_ao) for _ in range(n_slots)]
+        self.busy = [None] * n_slots          # list of requests in flight per slot
+        self.slot_pixels = slot_pixels
+        self.max_jobs = max_jobs
+        self.pool = FramebufferPool(fb_budget)
+        self.use_graph = use_graph
+        self.keep_results = keep_results
+
+    def release(self):
+        for s in self.slots:
+            s.release()
+
+    def _finish(self, k, now):
+        for r in self.busy[k]:
+            r.t_done = now
+            if not self.keep_results:
+                self.pool.free(r.fb)
+                r.fb = None
+        c = self.slots[k].counters()
+        per = c["primary_rays"] + c["shadow_rays"] + c["ao_rays"]
+        tot = sum(r.pixels for r in self.busy[k])
+        for r in self.busy[k]:
+            r.rays = per * r.pixels / max(1, tot)
+        self.busy[k] = None
+
+    def run(self, requests, time_limit=120.0):
+        """Serve `requests` (sorted by arrival, seconds from start) in real
+        time; returns a statistics dict."""
+        import torch
+        waiting = []
+        i = 0
+        n = len(requests)
+        t0 = time.perf_counter()
+        done = 0
+        refused = 0
+        while done + refused < n:
+            now = time.perf_counter() - t0
+            if now > time_limit:
+                break
+            while i < n and requests[i].arrival <= now:
+                r = requests[i]
+                if r.pixels > self.slot_pixels:
+                    r.refused = True
+                    refused += 1
+                else:
+                    waiting.append(r)
+                i += 1
+            # completions
+            for k, s in enumerate(self.slots):
+                if self.busy[k] is not None and s.poll():
+                    done += len(self.busy[k])
+                    self._finish(k, time.perf_counter() - t0)
+            # admissions: free slot -> oldest waiting request's scene, FIFO within it
+            for k, s in enumerate(self.slots):
+                if self.busy[k] is not None or not waiting:
+                    continue
+                key = waiting[0].scene
+                batch, pix = [], 0
+                rest = []
+                for r in waiting:
+                    if (r.scene == key and len(batch) < self.max_jobs and pix + r.pixels <= self.slot_pixels):
+                        fb = self.pool.try_alloc(r.camera.width, r.camera.height)
+                        if fb is None:
+                            rest.append(r)
+                            continue
+                        r.fb = fb
+                        batch.append(r)
+                        pix += r.pixels
+                    else:
+                        rest.append(r)
+                if not batch:
+                    continue
+                waiting = rest
+                tnow = time.perf_counter() - t0
+                for r in batch:
+                    r.t_submit = tnow
+                torch.cuda.current_stream().synchronize()   # framebuffers zeroed before the batch stream uses them
+                s.submit([(self.scenes[r.scene], r.camera, r.lighting, r.fb.data_ptr()) for r in batch],
+                         use_graph=self.use_graph)
+                self.busy[k] = batch
+            if not any(b is not None for b in self.busy):
+                nxt = requests[i].arrival if i < n else None
+                if nxt is not None:
+                    dt = nxt - (time.perf_counter() - t0)
+                    if dt > 0:
+                        time.sleep(min(dt, 0.002))
+            else:
+                time.sleep(0.00005)
+        makespan = time.perf_counter() - t0
+        return summarize(requests, makespan)
+
+
+def summarize(requests, makespan):
+    lat = np.array([r.t_done - r.arrival for r in requests if r.t_done is not None])
+    rays = sum(r.rays for r in requests if r.t_done is not None)
+    out = {"requests": len(requests), "completed": int(len(lat)),
+           "refused": int(sum(1 for r in requests if r.refused)), "makespan_s": makespan,
+           "rays": float(rays), "rays_per_s": float(rays / makespan) if makespan > 0 else 0.0}
+    if len(lat):
+        out.update(p50_ms=float(np.percentile(lat, 50) * 1e3), p95_ms=float(np.percentile(lat, 95) * 1e3),
+                   p99_ms=float(np.percentile(lat, 99) * 1e3), mean_ms=float(lat.mean() * 1e3))
+    return out
+
+
+def serve_plain(scenes, requests, time_limit=120.0):
+    """The same requests, one at a time through the plain single-frame path
+    (gxy_gpu_render on the default stream), in arrival order."""
+    import torch
+    t0 = time.perf_counter()
+    stream = torch.cuda.current_stream()
+    for r in requests:
+        now = time.perf_counter() - t0
+        if now > time_limit:
+            break
+        if r.arrival > now:
+            time.sleep(r.arrival - now)
+        fb = torch.zeros((r.camera.height, r.camera.width, 4), dtype=torch.float32, device="cuda")
+        sc = scenes[r.scene]
+        r.t_submit = time.perf_counter() - t0
+        sc.render(r.camera, r.lighting, fb.data_ptr(), stream.cuda_stream)
+        stream.synchronize()
+        r.t_done = time.perf_counter() - t0
+        c = sc.counters()
+        r.rays = c["primary_rays"] + c["shadow_rays"] + c["ao_rays"]
+        del fb
+    return summarize(requests, time.perf_counter() - t0)
+
+
+def poisson_requests(rate, count, scene_keys, make_request, seed=7, side_range=(256, 4096)):
+    """Poisson arrivals at `rate` per second; image side log-uniform in
+    side_range; make_request(rng, rid, arrival, scene_key, side) builds one
+    request (random camera, light or transfer-function change)."""
+    rng = np.random.Generator(np.random.Philox(seed))
+    t = 0.0
+    out = []
+    lo, hi = math.log(side_range[0]), math.log(side_range[1])
+    for rid in range(count):
+        t += rng.exponential(1.0 / rate)
+        side = int(round(math.exp(rng.uniform(lo, hi))))
+        key = scene_keys[int(rng.integers(0, len(scene_keys)))]
+        out.append(make_request(rng, rid, t, key, side))
+    return out

@@ -254,6 +254,40 @@ typedef struct gxy_generation_stats {
 int gxy_gpu_set_profiling(gxy_scene scene, int on);
 int gxy_gpu_query_generations(gxy_scene scene, gxy_generation_stats *out, int max, int32_t *n);
 
+/* ---- batched frames (many Renderings in one launch) --------------------
+ *
+ * Replaces RenderingSet's per-Rendering processing (RenderingSet.cpp:700-738)
+ * and gxywriter's camera x visualization loop (gxywriter.cpp:181-219) with
+ * one persistent, cooperative wavefront launch per batch: every job's camera
+ * rays and every later generation of shadow, AO and handed-off rays of all
+ * jobs share the device queues, with a grid barrier between generations and
+ * no host round trip.  A batch slot owns its queues, job table and stream;
+ * several slots run concurrently (continuous batching in the serving loop). */
+typedef struct gxy_job {
+    gxy_scene    scene;
+    gxy_camera   camera;
+    gxy_lighting lighting;   /* resolved (no camera-relative lights) */
+    float       *fb_rgba;    /* device framebuffer, width*height*4 fp32; contributions added */
+} gxy_job;
+
+typedef struct gxy_batch_s *gxy_batch;
+/* Queue memory for max_pixels camera rays per submission with up to
+ * max_shadow (lights) and max_ao secondary rays per pixel; GXY_ERR_ADMISSION
+ * if it does not fit the HBM budget. */
+int gxy_gpu_batch_create(int64_t max_pixels, int max_jobs, int max_shadow, int max_ao, gxy_batch *out);
+int gxy_gpu_batch_release(gxy_batch batch);
+/* Asynchronous submission on the batch's own stream.  use_graph != 0 replays
+ * the submission (job-table upload, counter reset, wavefront launch, status
+ * read-back) as a CUDA graph, updated in place between submissions. */
+int gxy_gpu_batch_submit(gxy_batch batch, const gxy_job *jobs, int n_jobs, int use_graph);
+/* *done = 1 once the last submission finished (its status is then checked). */
+int gxy_gpu_batch_poll(gxy_batch batch, int *done);
+/* Bounded host wait for the last submission (GXY_ERR_TIMEOUT after timeout_ms). */
+int gxy_gpu_batch_wait(gxy_batch batch, int timeout_ms);
+int gxy_gpu_batch_counters(gxy_batch batch, gxy_counters *out);
+/* The cudaStream_t of the batch (for events and framebuffer copies). */
+int gxy_gpu_batch_stream(gxy_batch batch, void **stream);
+
 /* ---- RayList-level drop-in (host buffers) ------------------------------ */
 
 /* Camera::generate_initial_rays for partition `partition`: fills `out`
