@@ -242,7 +242,7 @@ def run_serve(args):
     serve.serve_plain(table, [copy.copy(w) for w in warm])
     slot_pixels = hi * hi
     srv = serve.Server(table, n_slots=args.slots, slot_pixels=slot_pixels, max_jobs=64, max_shadow=1, max_ao=4,
-                       fb_budget=16 << 30, use_graph=True)
+                       fb_budget=16 << 30, use_graph=True, cooperative=args.coop)
     srv.run([copy.copy(w) for w in warm])
     served_reqs = [copy.copy(r) for r in reqs]
     plain_reqs = [copy.copy(r) for r in reqs]
@@ -250,6 +250,19 @@ def run_serve(args):
     srv.release()
     torch.cuda.synchronize()
     plain = serve.serve_plain(table, plain_reqs, time_limit=args.time_limit)
+    # served vs plain images on a sample of the requests (same camera/light)
+    rmse = 0.0
+    chk = gpu.Batch(slot_pixels, 8, 1, 4)
+    for r in reqs[: min(6, len(reqs))]:
+        fa = torch.zeros((r.camera.height, r.camera.width, 4), device="cuda")
+        fb_ = torch.zeros_like(fa)
+        torch.cuda.synchronize()
+        chk.submit([(table[r.scene], r.camera, r.lighting, fa.data_ptr())], use_graph=True, cooperative=args.coop)
+        chk.wait(120000)
+        table[r.scene].render(r.camera, r.lighting, fb_.data_ptr(), torch.cuda.current_stream().cuda_stream)
+        torch.cuda.synchronize()
+        rmse = max(rmse, float(torch.sqrt(torch.mean((fa[..., :3] - fb_[..., :3]) ** 2)).item()))
+    chk.release()
     out = {"metric": METRIC, "value": served["rays_per_s"], "unit": "rays/s", "n_gpus": 1,
            "steps": args.requests, "warmup": len(warm), "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
@@ -260,6 +273,7 @@ def run_serve(args):
            "served": served, "plain": plain,
            "served_over_plain_rays_per_s": served["rays_per_s"] / max(1e-9, plain["rays_per_s"]),
            "latency_ms": {k: served.get(k + "_ms") for k in ("p50", "p95", "p99")},
+           "rmse_served_vs_plain": rmse,
            "scene_commit_s": commit_s}
     print(json.dumps(out), flush=True)
 
@@ -281,6 +295,7 @@ def main():
     ap.add_argument("--side-min", type=int, default=256)
     ap.add_argument("--side-max", type=int, default=4096)
     ap.add_argument("--time-limit", type=float, default=120.0)
+    ap.add_argument("--coop", action="store_true", help="serve with cooperative single-launch batches")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

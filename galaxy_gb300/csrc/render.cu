@@ -968,6 +968,36 @@ __global__ void __launch_bounds__(kThreads) k_wavefront(DevScene Su, FrameArgs A
     flush_counters(A.ctr, c, st);
 }
 
+// Per-generation batch kernel (no grid barrier, so batches on different
+// streams run concurrently): generation g reads the queue counts that
+// generation g-1 left in device memory (counts + 3*(g-1)) and appends to
+// counts + 3*g.  KIND: K_CAMERA (all jobs' pixels) or K_SECONDARY, which
+// here takes the primary, shadow and AO queues in one index space.
+template <int KIND, bool USCENE>
+__global__ void __launch_bounds__(kThreads) k_batch_gen(DevScene Su, FrameArgs A, const unsigned *cin) {
+    __shared__ DevTF tfs[kMaxVol];
+    __shared__ long long pix0[kMaxJobs];
+    if (KIND == K_CAMERA)
+        for (int j = threadIdx.x; j < A.n_jobs; j += blockDim.x) pix0[j] = A.jobs[j].pix0;
+    if (USCENE) load_tfs(Su, tfs);
+    else __syncthreads();
+    RayStats st;
+    LocalCounters c;
+    const int64_t start = (int64_t)blockIdx.x * blockDim.x, stride = (int64_t)gridDim.x * blockDim.x;
+    if (KIND == K_CAMERA) {
+        camera_pass<true, USCENE>(Su, tfs, A, pix0, A.total_pix, start, stride, st, c);
+    } else {
+        unsigned n[NQ];
+        for (int k = 0; k < NQ; k++) {
+            unsigned v = __ldg(cin + k);
+            n[k] = v > A.qcap[k] ? A.qcap[k] : v;
+        }
+        if (n[0] + n[1] + n[2] == 0) return;   // uniform over the grid: no barrier below is skipped partially
+        queue_pass<true, USCENE>(Su, tfs, A, n, start, stride, st, c);
+    }
+    flush_counters(A.ctr, c, st);
+}
+
 // -------------------------------------------------------- RayList kernels
 struct RLDev {
     float *f[20];
@@ -1711,7 +1741,7 @@ struct Batch {
     int max_jobs = 0, max_shadow = 0, max_ao = 0;
     DRay *q[2][NQ] = {{nullptr, nullptr, nullptr}, {nullptr, nullptr, nullptr}};
     size_t qcap[NQ] = {0, 0, 0};
-    unsigned *counts = nullptr;        // 3 x NQ
+    unsigned *counts = nullptr;        // kMaxGen x NQ (cooperative mode uses the first 3 x NQ)
     DevJob *d_jobs = nullptr;
     DevJob *h_jobs = nullptr;          // pinned
     DevCounters *ctr = nullptr;
@@ -1722,6 +1752,7 @@ struct Batch {
     cudaGraphExec_t gexec = nullptr;
     int grid = 0;
     bool pending = false;
+    int cooperative = 0;
     int last_rc = GXY_OK;
     std::vector<void *> dev;
     ~Batch() {
@@ -1741,6 +1772,17 @@ struct Batch {
     }
 };
 
+constexpr int kBatchGens = 10;   // generations per submission in per-generation mode
+
+static int gen_grid(bool uniform) {
+    int sms = 152, per = 1;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, g_device);
+    if (uniform) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_batch_gen<K_SECONDARY, true>, kThreads, 0);
+    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_batch_gen<K_SECONDARY, false>, kThreads, 0);
+    if (per < 1) per = 1;
+    return sms * per;
+}
+
 static int batch_grid(bool uniform) {
     int sms = 152, per = 1;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, g_device);
@@ -1752,11 +1794,39 @@ static int batch_grid(bool uniform) {
 
 // Enqueue one submission on the batch stream (captured into a graph or not).
 static int batch_enqueue(Batch *b, const DevScene &Su, bool uniform, const FrameArgs &A, const WaveArgs &W,
-                         int n_jobs) {
+                         int n_jobs, int cooperative) {
     cudaStream_t st = b->stream;
     CK(cudaMemcpyAsync(b->d_jobs, b->h_jobs, n_jobs * sizeof(DevJob), cudaMemcpyHostToDevice, st));
-    CK(cudaMemsetAsync(b->counts, 0, 3 * NQ * sizeof(unsigned), st));
+    CK(cudaMemsetAsync(b->counts, 0, (kBatchGens + 1) * NQ * sizeof(unsigned), st));
     CK(cudaMemsetAsync(b->ctr, 0, sizeof(DevCounters), st));
+    if (!cooperative) {
+        // generation g reads counts[g-1], writes counts[g] and queue set g&1
+        int grid = gen_grid(uniform);
+        for (int g = 0; g < kBatchGens; g++) {
+            FrameArgs a = A;
+            for (int k = 0; k < NQ; k++) {
+                a.qin[k] = W.q[(g + 1) & 1][k];
+                a.qout[k] = W.q[g & 1][k];
+            }
+            a.qout_count = b->counts + NQ * g;
+            const unsigned *cin = g ? b->counts + NQ * (g - 1) : nullptr;
+            if (g == 0) {
+                if (uniform) k_batch_gen<K_CAMERA, true><<<grid, kThreads, 0, st>>>(Su, a, cin);
+                else k_batch_gen<K_CAMERA, false><<<grid, kThreads, 0, st>>>(Su, a, cin);
+            } else {
+                if (uniform) k_batch_gen<K_SECONDARY, true><<<grid, kThreads, 0, st>>>(Su, a, cin);
+                else k_batch_gen<K_SECONDARY, false><<<grid, kThreads, 0, st>>>(Su, a, cin);
+            }
+            CK(cudaGetLastError());
+        }
+        // status: generations run, rays left after the last one
+        CK(cudaMemsetAsync(b->d_status, 0, 4 * sizeof(int), st));
+        CK(cudaMemcpyAsync(b->d_status + 2, b->counts + NQ * (kBatchGens - 1), NQ * sizeof(unsigned),
+                           cudaMemcpyDeviceToDevice, st));
+        CK(cudaMemcpyAsync(b->h_status, b->d_status, 4 * sizeof(int), cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(b->h_ctr, b->ctr, sizeof(DevCounters), cudaMemcpyDeviceToHost, st));
+        return GXY_OK;
+    }
     FrameArgs a = A;
     WaveArgs w = W;
     DevScene s = Su;
@@ -1802,12 +1872,12 @@ int gxy_gpu_batch_create(int64_t max_pixels, int max_jobs, int max_shadow, int m
         b->qcap[k] = need[k];
     }
     int rc;
-    if ((rc = b->dalloc((void **)&b->counts, 3 * NQ * sizeof(unsigned)))) return rc;
+    if ((rc = b->dalloc((void **)&b->counts, (kBatchGens + 1) * NQ * sizeof(unsigned)))) return rc;
     if ((rc = b->dalloc((void **)&b->d_jobs, max_jobs * sizeof(DevJob)))) return rc;
     if ((rc = b->dalloc((void **)&b->ctr, sizeof(DevCounters)))) return rc;
-    if ((rc = b->dalloc((void **)&b->d_status, 4 * sizeof(int)))) return rc;
+    if ((rc = b->dalloc((void **)&b->d_status, 8 * sizeof(int)))) return rc;
     CK(cudaMallocHost((void **)&b->h_jobs, max_jobs * sizeof(DevJob)));
-    CK(cudaMallocHost((void **)&b->h_status, 4 * sizeof(int)));
+    CK(cudaMallocHost((void **)&b->h_status, 8 * sizeof(int)));
     CK(cudaMallocHost((void **)&b->h_ctr, sizeof(DevCounters)));
     CK(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
     CK(cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming));
@@ -1830,7 +1900,9 @@ int gxy_gpu_batch_stream(gxy_batch batch, void **stream) {
     return GXY_OK;
 }
 
-int gxy_gpu_batch_submit(gxy_batch batch, const gxy_job *jobs, int n_jobs, int use_graph) {
+int gxy_gpu_batch_submit(gxy_batch batch, const gxy_job *jobs, int n_jobs, int flags) {
+    const int use_graph = flags & GXY_BATCH_GRAPH;
+    const int cooperative = flags & GXY_BATCH_COOPERATIVE;
     GUARD_BEGIN
     if (!batch || !jobs || n_jobs <= 0) return set_error(GXY_ERR_INVALID, "bad argument");
     Batch *b = reinterpret_cast<Batch *>(batch);
@@ -1879,7 +1951,7 @@ int gxy_gpu_batch_submit(gxy_batch batch, const gxy_job *jobs, int n_jobs, int u
     if (use_graph) {
         cudaGraph_t g;
         CK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
-        int rc = batch_enqueue(b, Su, uniform, A, W, n_jobs);
+        int rc = batch_enqueue(b, Su, uniform, A, W, n_jobs, cooperative);
         cudaGraph_t gg = nullptr;
         cudaError_t e = cudaStreamEndCapture(b->stream, &gg);
         if (rc) return rc;
@@ -1899,9 +1971,10 @@ int gxy_gpu_batch_submit(gxy_batch batch, const gxy_job *jobs, int n_jobs, int u
         cudaGraphDestroy(g);
         CK(cudaGraphLaunch(b->gexec, b->stream));
     } else {
-        int rc = batch_enqueue(b, Su, uniform, A, W, n_jobs);
+        int rc = batch_enqueue(b, Su, uniform, A, W, n_jobs, cooperative);
         if (rc) return rc;
     }
+    b->cooperative = cooperative;
     CK(cudaEventRecord(b->done, b->stream));
     b->pending = true;
     b->last_rc = GXY_OK;
@@ -1911,8 +1984,8 @@ int gxy_gpu_batch_submit(gxy_batch batch, const gxy_job *jobs, int n_jobs, int u
 
 static int batch_finish(Batch *b) {
     b->pending = false;
-    if (b->h_status[1] > 0)
-        return b->last_rc = set_error(GXY_ERR_OVERFLOW, "rays left after the generation limit");
+    int left = b->cooperative ? b->h_status[1] : (b->h_status[2] + b->h_status[3] + b->h_status[4]);
+    if (left > 0) return b->last_rc = set_error(GXY_ERR_OVERFLOW, "rays left after the generation limit");
     if (b->h_ctr->overflow) return b->last_rc = set_error(GXY_ERR_OVERFLOW, "a batch queue overflowed");
     return b->last_rc = GXY_OK;
 }
@@ -1967,7 +2040,7 @@ int gxy_gpu_batch_counters(gxy_batch batch, gxy_counters *out) {
     out->terminated = (int64_t)c.terminated;
     out->dropped = (int64_t)c.dropped;
     out->kept = (int64_t)c.kept;
-    out->bounces = b->h_status[0];
+    out->bounces = b->cooperative ? b->h_status[0] : kBatchGens;
     out->samples = (int64_t)c.samples;
     out->nodes = (int64_t)c.nodes;
     out->prim_tests = (int64_t)(c.tri_tests + c.sph_tests);

@@ -244,8 +244,11 @@ class Batch:
         check(lib().gxy_gpu_batch_stream(self.h, C.byref(s)))
         return s.value
 
-    def submit(self, jobs, use_graph=False):
-        """jobs: list of (Scene, camera, gxy_lighting, device fb pointer)."""
+    def submit(self, jobs, use_graph=False, cooperative=False):
+        """jobs: list of (Scene, camera, gxy_lighting, device fb pointer).
+        use_graph: replay the submission as a CUDA graph; cooperative: run
+        every generation in one cooperative launch (else one launch per
+        generation, so slots on different streams overlap)."""
         arr = (A.gxy_job * len(jobs))()
         for i, (sc, cam, L, fb) in enumerate(jobs):
             arr[i].scene = sc.h.value
@@ -253,7 +256,8 @@ class Batch:
             arr[i].lighting = L if isinstance(L, A.gxy_lighting) else L.c()
             arr[i].fb_rgba = fb
         self._keep = (arr, jobs)
-        check(lib().gxy_gpu_batch_submit(self.h, arr, len(jobs), 1 if use_graph else 0))
+        flags = (1 if use_graph else 0) | (2 if cooperative else 0)
+        check(lib().gxy_gpu_batch_submit(self.h, arr, len(jobs), flags))
 
     def poll(self):
         d = C.c_int(0)

@@ -69,9 +69,22 @@ class FramebufferPool:
 
 
 class Server:
+    """Batch slots over resident scenes.  Admission policy: requests up to
+    `small_pixels` are "small" and are packed together (same scene, FIFO) up to
+    `small_batch_pixels` per launch; a larger request runs in a slot of its
+    own.  The oldest waiting request goes first, except that small requests
+    may pass a large one that has waited less than `big_wait_s` (short jobs
+    first, bounded by age, so latency of small requests is not held behind
+    large frames and large frames are not starved)."""
+
     def __init__(self, scenes, n_slots=4, slot_pixels=8 << 20, max_jobs=64, max_shadow=1, max_ao=4,
-                 fb_budget=8 << 30, use_graph=True, keep_results=False):
+                 fb_budget=8 << 30, use_graph=True, keep_results=False, cooperative=False,
+                 small_pixels=1 << 20, small_batch_pixels=4 << 20, big_wait_s=0.05):
         self.scenes = scenes
+        self.cooperative = cooperative
+        self.small_pixels = small_pixels
+        self.small_batch_pixels = min(small_batch_pixels, slot_pixels)
+        self.big_wait_s = big_wait_s
         self.slots = [gpu.Batch(slot_pixels, max_jobs, max_shadow, max_ao) for _ in range(n_slots)]
         self.busy = [None] * n_slots          # list of requests in flight per slot
         self.slot_pixels = slot_pixels
@@ -124,33 +137,37 @@ class Server:
                 if self.busy[k] is not None and s.poll():
                     done += len(self.busy[k])
                     self._finish(k, time.perf_counter() - t0)
-            # admissions: free slot -> oldest waiting request's scene, FIFO within it
+            # admissions
             for k, s in enumerate(self.slots):
                 if self.busy[k] is not None or not waiting:
                     continue
-                key = waiting[0].scene
+                tnow = time.perf_counter() - t0
+                head = waiting[0]
+                smalls = [r for r in waiting if r.pixels <= self.small_pixels]
+                if head.pixels > self.small_pixels and (not smalls or tnow - head.arrival >= self.big_wait_s):
+                    cand, cap = [head], self.slot_pixels
+                else:
+                    key = smalls[0].scene
+                    cand, cap = [r for r in smalls if r.scene == key], self.small_batch_pixels
                 batch, pix = [], 0
-                rest = []
-                for r in waiting:
-                    if (r.scene == key and len(batch) < self.max_jobs and pix + r.pixels <= self.slot_pixels):
-                        fb = self.pool.try_alloc(r.camera.width, r.camera.height)
-                        if fb is None:
-                            rest.append(r)
-                            continue
-                        r.fb = fb
-                        batch.append(r)
-                        pix += r.pixels
-                    else:
-                        rest.append(r)
+                for r in cand:
+                    if len(batch) >= self.max_jobs or pix + r.pixels > cap:
+                        break
+                    fb = self.pool.try_alloc(r.camera.width, r.camera.height)
+                    if fb is None:
+                        break
+                    r.fb = fb
+                    batch.append(r)
+                    pix += r.pixels
                 if not batch:
                     continue
-                waiting = rest
-                tnow = time.perf_counter() - t0
+                chosen = set(id(r) for r in batch)
+                waiting = [r for r in waiting if id(r) not in chosen]
                 for r in batch:
                     r.t_submit = tnow
                 torch.cuda.current_stream().synchronize()   # framebuffers zeroed before the batch stream uses them
                 s.submit([(self.scenes[r.scene], r.camera, r.lighting, r.fb.data_ptr()) for r in batch],
-                         use_graph=self.use_graph)
+                         use_graph=self.use_graph, cooperative=self.cooperative)
                 self.busy[k] = batch
             if not any(b is not None for b in self.busy):
                 nxt = requests[i].arrival if i < n else None

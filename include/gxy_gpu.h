@@ -276,10 +276,17 @@ typedef struct gxy_batch_s *gxy_batch;
  * if it does not fit the HBM budget. */
 int gxy_gpu_batch_create(int64_t max_pixels, int max_jobs, int max_shadow, int max_ao, gxy_batch *out);
 int gxy_gpu_batch_release(gxy_batch batch);
-/* Asynchronous submission on the batch's own stream.  use_graph != 0 replays
- * the submission (job-table upload, counter reset, wavefront launch, status
- * read-back) as a CUDA graph, updated in place between submissions. */
-int gxy_gpu_batch_submit(gxy_batch batch, const gxy_job *jobs, int n_jobs, int use_graph);
+/* Asynchronous submission on the batch's own stream.  flags:
+ * GXY_BATCH_GRAPH replays the submission (job-table upload, counter reset,
+ * launches, status read-back) as a CUDA graph updated in place between
+ * submissions; GXY_BATCH_COOPERATIVE runs all generations in one cooperative
+ * launch with grid barriers (lowest launch overhead, but the launch holds the
+ * whole GPU), otherwise each generation is its own launch reading the
+ * previous generation's queue counts from device memory (up to 10
+ * generations), so batches on different streams overlap. */
+#define GXY_BATCH_GRAPH        1
+#define GXY_BATCH_COOPERATIVE  2
+int gxy_gpu_batch_submit(gxy_batch batch, const gxy_job *jobs, int n_jobs, int flags);
 /* *done = 1 once the last submission finished (its status is then checked). */
 int gxy_gpu_batch_poll(gxy_batch batch, int *done);
 /* Bounded host wait for the last submission (GXY_ERR_TIMEOUT after timeout_ms). */

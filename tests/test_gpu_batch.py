@@ -42,9 +42,10 @@ def jobs_for(env, n, seed=0):
     return jobs
 
 
+@pytest.mark.parametrize("coop", [False, True])
 @pytest.mark.parametrize("graph", [False, True])
 @pytest.mark.parametrize("uniform", [False, True])
-def test_batch_equals_alone(env, graph, uniform):
+def test_batch_equals_alone(env, graph, uniform, coop):
     torch, gpu, sc = env
     jobs = jobs_for(env, 12)
     if uniform:
@@ -52,7 +53,7 @@ def test_batch_equals_alone(env, graph, uniform):
     b = gpu.Batch(max_pixels=200000, max_jobs=64, max_shadow=1, max_ao=2)
     fbs = [torch.zeros((c.height, c.width, 4), dtype=torch.float32, device="cuda") for _, _, c, _ in jobs]
     torch.cuda.synchronize()
-    b.submit([(s, c, L, fb.data_ptr()) for (_, s, c, L), fb in zip(jobs, fbs)], use_graph=graph)
+    b.submit([(s, c, L, fb.data_ptr()) for (_, s, c, L), fb in zip(jobs, fbs)], use_graph=graph, cooperative=coop)
     b.wait(60000)
     cnt = b.counters()
     total_primary = 0
@@ -66,7 +67,7 @@ def test_batch_equals_alone(env, graph, uniform):
     for fb in fbs:
         fb.zero_()
     torch.cuda.synchronize()
-    b.submit([(s, c, L, fb.data_ptr()) for (_, s, c, L), fb in zip(jobs, fbs)], use_graph=graph)
+    b.submit([(s, c, L, fb.data_ptr()) for (_, s, c, L), fb in zip(jobs, fbs)], use_graph=graph, cooperative=coop)
     b.wait(60000)
     for (_, s, c, L), fb in zip(jobs, fbs):
         assert np.abs(fb.cpu().numpy() - alone(torch, s, c, L)).max() <= 1e-5
@@ -95,7 +96,8 @@ def test_serving_results_match_alone(env):
     jobs = jobs_for(env, 24, seed=3)
     reqs = [serve.Request(i, 0.0005 * i, key, cam, L) for i, (key, _, cam, L) in enumerate(jobs)]
     srv = serve.Server(table, n_slots=3, slot_pixels=30000, max_jobs=8, max_shadow=1, max_ao=2,
-                       fb_budget=1 << 28, use_graph=True, keep_results=True)
+                       fb_budget=1 << 28, use_graph=True, keep_results=True, small_pixels=4000,
+                       small_batch_pixels=20000)
     st = srv.run(reqs, time_limit=60)
     assert st["completed"] == len(reqs) and st["refused"] == 0
     assert st["p99_ms"] >= st["p50_ms"] > 0
