@@ -296,6 +296,7 @@ def main():
     ap.add_argument("--side-max", type=int, default=4096)
     ap.add_argument("--time-limit", type=float, default=120.0)
     ap.add_argument("--coop", action="store_true", help="serve with cooperative single-launch batches")
+    ap.add_argument("--autotune", action="store_true", help="pick kernel occupancy and grid size before timing")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -327,6 +328,10 @@ def main():
         fb.zero_()
         sc.render(cam_c, L, fb.data_ptr(), stream.cuda_stream)
 
+    tuning = None
+    if args.autotune:
+        from galaxy_gb300 import autotune
+        tuning = autotune.tune(sc, cam_c, L, frames=2)
     sc.set_profiling(True)
     for _ in range(args.warmup):
         frame()
@@ -413,7 +418,9 @@ def main():
            "generations": [{k: (round(v, 4) if isinstance(v, float) else v) for k, v in g.items()}
                            for g in sc_last_gens],
            "scene_commit_s": commit_s, "bvh": sc.bvh_info(),
-           "gpu_launches": launches, "roofline": roof, "e2e": e2e, "clocks": clk}
+           "gpu_launches": launches, "roofline": roof, "e2e": e2e, "clocks": clk,
+           "tuning": tuning if tuning else {"best": {"blocks_per_sm": gpu.get_tuning(gpu.TUNE_BLOCKS_PER_SM),
+                                                     "grid_per_sm": gpu.get_tuning(gpu.TUNE_GRID_PER_SM)}}}
     if rank == 0 and not args.no_cpu_baseline:
         base, _, _ = cpu_baseline(cam, vis, target_s=args.cpu_seconds)
         base.pop("seconds", None)

@@ -887,8 +887,8 @@ __device__ __forceinline__ void queue_pass(const DevScene &Sp, const DevTF *tfs_
 
 // Host-driven generations (one launch per kind, counts from the host); the
 // single-frame path and the per-launch profile use these.
-template <int KIND>
-__global__ void __launch_bounds__(kThreads) k_primary(DevScene S, FrameArgs A) {
+template <int KIND, int MINB>
+__global__ void __launch_bounds__(kThreads, MINB) k_primary(DevScene S, FrameArgs A) {
     __shared__ DevTF tfs[kMaxVol];
     load_tfs(S, tfs);
     RayStats st;
@@ -904,7 +904,8 @@ __global__ void __launch_bounds__(kThreads) k_primary(DevScene S, FrameArgs A) {
     flush_counters(A.ctr, c, st);
 }
 
-__global__ void __launch_bounds__(kThreads) k_secondary(DevScene S, FrameArgs A) {
+template <int MINB>
+__global__ void __launch_bounds__(kThreads, MINB) k_secondary(DevScene S, FrameArgs A) {
     __shared__ DevTF tfs[kMaxVol];
     load_tfs(S, tfs);
     RayStats st;
@@ -973,8 +974,8 @@ __global__ void __launch_bounds__(kThreads) k_wavefront(DevScene Su, FrameArgs A
 // generation g-1 left in device memory (counts + 3*(g-1)) and appends to
 // counts + 3*g.  KIND: K_CAMERA (all jobs' pixels) or K_SECONDARY, which
 // here takes the primary, shadow and AO queues in one index space.
-template <int KIND, bool USCENE>
-__global__ void __launch_bounds__(kThreads) k_batch_gen(DevScene Su, FrameArgs A, const unsigned *cin) {
+template <int KIND, bool USCENE, int MINB>
+__global__ void __launch_bounds__(kThreads, MINB) k_batch_gen(DevScene Su, FrameArgs A, const unsigned *cin) {
     __shared__ DevTF tfs[kMaxVol];
     __shared__ long long pix0[kMaxJobs];
     if (KIND == K_CAMERA)
@@ -1177,11 +1178,17 @@ __global__ void k_rl_camera_write(DevScene S, DevCamera C, int part, const int *
 }
 
 // ============================================================ frame driver
+// Run-time tuning knobs (gxy_gpu_set_tuning): resident blocks per SM the
+// kernels are compiled for (register budget 2 -> 128, 3 -> 80 registers per
+// thread) and the grid-stride grid size in blocks per SM.
+static int g_tune_minb = 2;
+static int g_tune_grid_per_sm = 8;
+
 static unsigned grid_for(int64_t n) {
     int sms = 152;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, g_device);
     int64_t want = (n + kThreads - 1) / kThreads;
-    int64_t cap = (int64_t)sms * 8;   // persistent-style grid-stride cap
+    int64_t cap = (int64_t)sms * g_tune_grid_per_sm;   // grid-stride grid cap
     if (want > cap) want = cap;
     return (unsigned)(want < 1 ? 1 : want);
 }
@@ -1253,9 +1260,15 @@ static int render(Scene *sc, const gxy_camera &cam, const gxy_lighting &lt, floa
         A.ctr = sc->ctr + nl;
         unsigned g = grid_for(items);
         if (sc->profile) CK(cudaEventRecord(sc->events[2 * nl], st));
-        if (kind == K_CAMERA) k_primary<K_CAMERA><<<g, kThreads, 0, st>>>(S, A);
-        else if (kind == K_PRIMARY) k_primary<K_PRIMARY><<<g, kThreads, 0, st>>>(S, A);
-        else k_secondary<<<g, kThreads, 0, st>>>(S, A);
+        if (g_tune_minb == 3) {
+            if (kind == K_CAMERA) k_primary<K_CAMERA, 3><<<g, kThreads, 0, st>>>(S, A);
+            else if (kind == K_PRIMARY) k_primary<K_PRIMARY, 3><<<g, kThreads, 0, st>>>(S, A);
+            else k_secondary<3><<<g, kThreads, 0, st>>>(S, A);
+        } else {
+            if (kind == K_CAMERA) k_primary<K_CAMERA, 2><<<g, kThreads, 0, st>>>(S, A);
+            else if (kind == K_PRIMARY) k_primary<K_PRIMARY, 2><<<g, kThreads, 0, st>>>(S, A);
+            else k_secondary<2><<<g, kThreads, 0, st>>>(S, A);
+        }
         CK(cudaGetLastError());
         if (sc->profile) CK(cudaEventRecord(sc->events[2 * nl + 1], st));
         recs.push_back({gen, kind, rays_in});
@@ -1565,6 +1578,28 @@ int gxy_gpu_query_counters_ex(gxy_scene scene, int64_t *tri_tests, int64_t *sph_
     return GXY_OK;
 }
 
+int gxy_gpu_set_tuning(int knob, int value) {
+    if (knob == GXY_TUNE_BLOCKS_PER_SM) {
+        if (value != 2 && value != 3) return set_error(GXY_ERR_INVALID, "blocks per SM must be 2 or 3");
+        g_tune_minb = value;
+        return GXY_OK;
+    }
+    if (knob == GXY_TUNE_GRID_PER_SM) {
+        if (value < 1 || value > 64) return set_error(GXY_ERR_INVALID, "grid blocks per SM must be 1..64");
+        g_tune_grid_per_sm = value;
+        return GXY_OK;
+    }
+    return set_error(GXY_ERR_INVALID, "unknown tuning knob");
+}
+
+int gxy_gpu_get_tuning(int knob, int *value) {
+    if (!value) return set_error(GXY_ERR_INVALID, "null argument");
+    if (knob == GXY_TUNE_BLOCKS_PER_SM) *value = g_tune_minb;
+    else if (knob == GXY_TUNE_GRID_PER_SM) *value = g_tune_grid_per_sm;
+    else return set_error(GXY_ERR_INVALID, "unknown tuning knob");
+    return GXY_OK;
+}
+
 int gxy_gpu_set_profiling(gxy_scene scene, int on) {
     if (!scene) return set_error(GXY_ERR_INVALID, "null scene");
     reinterpret_cast<Scene *>(scene)->profile = on ? 1 : 0;
@@ -1777,8 +1812,13 @@ constexpr int kBatchGens = 10;   // generations per submission in per-generation
 static int gen_grid(bool uniform) {
     int sms = 152, per = 1;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, g_device);
-    if (uniform) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_batch_gen<K_SECONDARY, true>, kThreads, 0);
-    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_batch_gen<K_SECONDARY, false>, kThreads, 0);
+    if (g_tune_minb == 3) {
+        if (uniform) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_batch_gen<K_SECONDARY, true, 3>, kThreads, 0);
+        else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_batch_gen<K_SECONDARY, false, 3>, kThreads, 0);
+    } else {
+        if (uniform) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_batch_gen<K_SECONDARY, true, 2>, kThreads, 0);
+        else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_batch_gen<K_SECONDARY, false, 2>, kThreads, 0);
+    }
     if (per < 1) per = 1;
     return sms * per;
 }
@@ -1810,13 +1850,19 @@ static int batch_enqueue(Batch *b, const DevScene &Su, bool uniform, const Frame
             }
             a.qout_count = b->counts + NQ * g;
             const unsigned *cin = g ? b->counts + NQ * (g - 1) : nullptr;
-            if (g == 0) {
-                if (uniform) k_batch_gen<K_CAMERA, true><<<grid, kThreads, 0, st>>>(Su, a, cin);
-                else k_batch_gen<K_CAMERA, false><<<grid, kThreads, 0, st>>>(Su, a, cin);
-            } else {
-                if (uniform) k_batch_gen<K_SECONDARY, true><<<grid, kThreads, 0, st>>>(Su, a, cin);
-                else k_batch_gen<K_SECONDARY, false><<<grid, kThreads, 0, st>>>(Su, a, cin);
-            }
+#define GXY_GEN_LAUNCH(MB)                                                                          \
+    do {                                                                                            \
+        if (g == 0) {                                                                               \
+            if (uniform) k_batch_gen<K_CAMERA, true, MB><<<grid, kThreads, 0, st>>>(Su, a, cin);    \
+            else k_batch_gen<K_CAMERA, false, MB><<<grid, kThreads, 0, st>>>(Su, a, cin);           \
+        } else {                                                                                    \
+            if (uniform) k_batch_gen<K_SECONDARY, true, MB><<<grid, kThreads, 0, st>>>(Su, a, cin); \
+            else k_batch_gen<K_SECONDARY, false, MB><<<grid, kThreads, 0, st>>>(Su, a, cin);        \
+        }                                                                                           \
+    } while (0)
+            if (g_tune_minb == 3) GXY_GEN_LAUNCH(3);
+            else GXY_GEN_LAUNCH(2);
+#undef GXY_GEN_LAUNCH
             CK(cudaGetLastError());
         }
         // status: generations run, rays left after the last one

@@ -59,6 +59,8 @@ def lib():
         "gxy_gpu_batch_wait": [vp, C.c_int],
         "gxy_gpu_batch_counters": [vp, C.POINTER(A.gxy_counters)],
         "gxy_gpu_batch_stream": [vp, C.POINTER(vp)],
+        "gxy_gpu_set_tuning": [C.c_int, C.c_int],
+        "gxy_gpu_get_tuning": [C.c_int, C.POINTER(C.c_int)],
         "gxy_gpu_classify": [C.POINTER(A.gxy_raylist)],
         "gxy_gpu_assign_destinations": [vp, C.c_int, C.POINTER(A.gxy_raylist)],
         "gxy_gpu_accumulate_terminated": [C.POINTER(A.gxy_raylist), A.f32p, C.c_int, C.c_int],
@@ -93,6 +95,20 @@ def ensure_init():
 def hbm_in_use():
     v = C.c_size_t(0)
     check(lib().gxy_gpu_hbm_in_use(C.byref(v)))
+    return v.value
+
+
+TUNE_BLOCKS_PER_SM = 1
+TUNE_GRID_PER_SM = 2
+
+
+def set_tuning(knob, value):
+    check(lib().gxy_gpu_set_tuning(int(knob), int(value)))
+
+
+def get_tuning(knob):
+    v = C.c_int(0)
+    check(lib().gxy_gpu_get_tuning(int(knob), C.byref(v)))
     return v.value
 
 
