@@ -1181,8 +1181,8 @@ __global__ void k_rl_camera_write(DevScene S, DevCamera C, int part, const int *
 // Run-time tuning knobs (gxy_gpu_set_tuning): resident blocks per SM the
 // kernels are compiled for (register budget 2 -> 128, 3 -> 80 registers per
 // thread) and the grid-stride grid size in blocks per SM.
-static int g_tune_minb = 2;
-static int g_tune_grid_per_sm = 8;
+static int g_tune_minb = 3;
+static int g_tune_grid_per_sm = 16;
 
 static unsigned grid_for(int64_t n) {
     int sms = 152;
