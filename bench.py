@@ -401,7 +401,7 @@ def main():
         traffic = t.get("bytes_per_launch")
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "traffic": traffic, "peak_source": peak_kind,
-            "kernel": ["k_primary<camera>", "k_primary<queue>", "k_secondary"][dom],
+            "kernel": ["k_primary<camera>", "k_primary<queue>", "k_secondary", "k_sec_march"][dom],
             "kernel_ms": dom_ms, "algorithmic_bytes": dom_bytes, "share_of_frame_kernel_time": share}
 
     out = {"metric": METRIC, "value": value, "unit": "rays/s", "n_gpus": world, "steps": args.steps,
@@ -420,7 +420,8 @@ def main():
            "scene_commit_s": commit_s, "bvh": sc.bvh_info(),
            "gpu_launches": launches, "roofline": roof, "e2e": e2e, "clocks": clk,
            "tuning": tuning if tuning else {"best": {"blocks_per_sm": gpu.get_tuning(gpu.TUNE_BLOCKS_PER_SM),
-                                                     "grid_per_sm": gpu.get_tuning(gpu.TUNE_GRID_PER_SM)}}}
+                                                     "grid_per_sm": gpu.get_tuning(gpu.TUNE_GRID_PER_SM),
+                                                     "split": gpu.get_tuning(gpu.TUNE_SPLIT_SECONDARY)}}}
     if rank == 0 and not args.no_cpu_baseline:
         base, _, _ = cpu_baseline(cam, vis, target_s=args.cpu_seconds)
         base.pop("seconds", None)

@@ -89,6 +89,8 @@ struct DevScene {
     int integrate;                   // some volume is rendered or has isovalues
     int has_iso;                     // some volume has isovalues
     float step, march_eps, epsilon, opaque_alpha, rate;
+    int rate_pow2;                   // rate is a power of two: x / rate == x * inv_rate exactly
+    float inv_rate;
     // geometry
     const BVH8Node *nodes;
     const float4 *slots;
@@ -131,7 +133,7 @@ struct DevLights {
 
 struct DevCounters {
     unsigned long long primary, shadow, ao, segments, handoffs, terminated, dropped, kept, samples, nodes, tri_tests,
-        sph_tests, enqueued;
+        sph_tests, enqueued, marched;
     int overflow;        // a queue or a traversal stack ran out of room
     int pad;
 };
@@ -183,6 +185,38 @@ __device__ __forceinline__ V3 tf_color(const DevTF &tf, float v) {
     float a = 1.0f - rem;
     return v3(a * c[3 * i] + rem * c[3 * i + 3], a * c[3 * i + 1] + rem * c[3 * i + 4],
               a * c[3 * i + 2] + rem * c[3 * i + 5]);
+}
+
+// Opacity and colour of one value with a single index computation (the
+// same arithmetic as tf_opacity and tf_color).  Returns the opacity; the
+// colour is only evaluated when want_color and the opacity is positive.
+__device__ __forceinline__ float tf_lookup(const DevTF &tf, float v, bool want_color, V3 &col) {
+    if (isnan(v)) {
+        col = v3(0, 0, 0);
+        return 0.0f;
+    }
+    const float *c = tf.colors;
+    float op;
+    if (v <= tf.r0) {
+        op = tf.opac[0];
+        if (want_color && op > 0.0f) col = v3(c[0], c[1], c[2]);
+        return op;
+    }
+    if (v >= tf.r1) {
+        op = tf.opac[255];
+        if (want_color && op > 0.0f) col = v3(c[765], c[766], c[767]);
+        return op;
+    }
+    float f = (v - tf.r0) * tf.k;
+    int i = (int)floorf(f);
+    i = i > 254 ? 254 : (i < 0 ? 0 : i);
+    float rem = f - (float)i;
+    float a = 1.0f - rem;
+    op = a * tf.opac[i] + rem * tf.opac[i + 1];
+    if (want_color && op > 0.0f)
+        col = v3(a * c[3 * i] + rem * c[3 * i + 3], a * c[3 * i + 1] + rem * c[3 * i + 4],
+                 a * c[3 * i + 2] + rem * c[3 * i + 5]);
+    return op;
 }
 
 // ---------------------------------------------------------------- volume

@@ -196,6 +196,8 @@ struct Scene {
     BVHInfo bvh;
     static constexpr int kMaxLaunch = 256;   // counter slots per frame
     DevScene *d_scene = nullptr;             // device copy of S (batches)
+    DRay *qmarch = nullptr;                  // split-path march queue
+    size_t qmarch_cap = 0;
     DRay *q[2][3] = {{nullptr, nullptr, nullptr}, {nullptr, nullptr, nullptr}};   // ping-pong x (primary, shadow, AO)
     size_t qcap[3] = {0, 0, 0};
     unsigned int *qcount = nullptr;     // 2 x 3 queue counters
@@ -212,6 +214,7 @@ struct Scene {
         for (void *p : owned) arena().free(p);
         for (int b = 0; b < 2; b++)
             for (int k = 0; k < 3; k++) arena().free(q[b][k]);
+        arena().free(qmarch);
         arena().free(qcount);
         arena().free(ctr);
         arena().free(fbtmp);
@@ -312,6 +315,12 @@ static int commit(const gxy_scene_desc *d, Scene *sc) {
     if (np > kMaxPart) return set_error(GXY_ERR_INVALID, "too many partitions");
     float rate = d->sampling_rate > 0 ? d->sampling_rate : 1.0f;
     S.rate = rate;
+    {
+        int e;
+        float m = frexpf(rate, &e);
+        S.rate_pow2 = (m == 0.5f) ? 1 : 0;
+        S.inv_rate = 1.0f / rate;
+    }
     S.opaque_alpha = d->opaque_alpha > 0 ? d->opaque_alpha : 0.999f;
     S.epsilon = d->epsilon;
     std::vector<DevTF> tfs;
@@ -542,7 +551,7 @@ __device__ __forceinline__ void put_ray(DRay *q, unsigned idx, V3 o, float t, V3
 }
 
 enum { Q_PRIM = 0, Q_SHADOW = 1, Q_AO = 2, NQ = 3 };
-enum { K_CAMERA = 0, K_PRIMARY = 1, K_SECONDARY = 2 };
+enum { K_CAMERA = 0, K_PRIMARY = 1, K_SECONDARY = 2, K_MARCH = 3 };
 constexpr int kMaxJobs = 1024;
 
 // One render job (a camera x visualization of a RenderingSet).
@@ -565,6 +574,11 @@ struct FrameArgs {
     unsigned *qout_count;              // NQ counters
     unsigned qcap[NQ];
     DevCounters *ctr;                  // this launch's counter slot
+    // split shadow/AO tracing (volume scenes): query pass -> march queue -> march pass
+    int split;
+    DRay *qmarch;
+    unsigned *qmarch_count;            // [0] records, [1] fetch cursor of the march pass
+    unsigned qmarch_cap;
 };
 
 // Reserve cnt consecutive queue records for this thread: one warp-wide scan
@@ -588,27 +602,26 @@ __device__ __forceinline__ unsigned warp_reserve(unsigned cnt, unsigned *counter
 }
 
 struct LocalCounters {
-    unsigned long long prim = 0, sh = 0, ao = 0, seg = 0, hand = 0, term = 0, drop = 0, keep = 0, enq = 0;
+    unsigned long long prim = 0, sh = 0, ao = 0, seg = 0, hand = 0, term = 0, drop = 0, keep = 0, enq = 0, march = 0;
     int ovf = 0;
 };
 
+// Warp-level reduction of the counters, one atomic per counter per warp (no
+// block barrier, so warps retire as soon as their own rays are done).
 __device__ __forceinline__ void flush_counters(DevCounters *ctr, const LocalCounters &c, const RayStats &st) {
-    __shared__ unsigned long long red[16];
     const int lane = threadIdx.x & 31;
-    unsigned long long vals[14] = {c.prim, c.sh, c.ao, c.seg, c.hand, c.term, c.drop, c.keep, st.samples, st.nodes,
-                                   st.tris, st.sphs, c.enq, (unsigned long long)(c.ovf | st.ovf)};
-    __syncthreads();
-    if (threadIdx.x < 16) red[threadIdx.x] = 0;
-    __syncthreads();
+    unsigned long long vals[15] = {c.prim, c.sh,  c.ao,  c.seg, c.hand,  c.term,  c.drop,  c.keep,
+                                   st.samples, st.nodes, st.tris, st.sphs, c.enq, c.march,
+                                   (unsigned long long)(c.ovf | st.ovf)};
 #pragma unroll
-    for (int k = 0; k < 14; k++) {
+    for (int k = 0; k < 15; k++) {
         unsigned long long v = vals[k];
         for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-        if (lane == 0 && v) atomicAdd(&red[k], v);
+        if (lane == 0 && v) {
+            if (k < 14) atomicAdd(&(&ctr->primary)[k], v);
+            else atomicExch(&ctr->overflow, 1);
+        }
     }
-    __syncthreads();
-    if (threadIdx.x < 13 && red[threadIdx.x]) atomicAdd(&(&ctr->primary)[threadIdx.x], red[threadIdx.x]);
-    if (threadIdx.x == 13 && red[13]) atomicExch(&ctr->overflow, 1);
 }
 
 __device__ __forceinline__ void add_pixel(float *fb, int width, int x, int y, float r, float g, float b, float o) {
@@ -878,10 +891,33 @@ __device__ __forceinline__ void queue_pass(const DevScene &Sp, const DevTF *tfs_
         PrimOut P;
         TraceOut T;
         int dest = GXY_DROP_ON_FLOOR;
+        bool to_march = false;
+        SecQuery sq;
         if (actp) primary_ray(S, tfs, J, in, x, y, P, st, c);
-        if (acts) dest = secondary_ray(S, tfs, J, in, x, y, T, st, c);
+        if (acts) {
+            if (A.split) {
+                c.seg++;
+                sq = sec_query(S, in, st);
+                if (sq.cull) c.drop++;
+                else to_march = true;
+                acts = false;
+            } else {
+                dest = secondary_ray(S, tfs, J, in, x, y, T, st, c);
+            }
+        }
         if (__any_sync(0xffffffffu, actp)) emit_primary(S, J, job, actp, in, x, y, P, A, c);
         if (__any_sync(0xffffffffu, acts)) emit_secondary(acts, dest, q, job, in, x, y, T, A, c);
+        if (A.split && __any_sync(0xffffffffu, to_march)) {
+            unsigned idx = warp_reserve(to_march ? 1u : 0u, A.qmarch_count, A.qmarch_cap, c.ovf);
+            if (to_march && idx != 0xffffffffu) {
+                int meta = make_meta(in.type | (sq.surface ? 8 : 0), in.part, job);
+                DRay *p = A.qmarch + idx;
+                p->o = make_float4(in.org.x, in.org.y, in.org.z, in.t);
+                p->d = make_float4(in.dir.x, in.dir.y, in.dir.z, in.tmax);
+                p->c = make_float4(in.r, in.g, in.b, in.o);
+                p->m = make_int4(x, y, meta, __float_as_int(sq.t_term));
+            }
+        }
     }
 }
 
@@ -995,6 +1031,72 @@ __global__ void __launch_bounds__(kThreads, MINB) k_batch_gen(DevScene Su, Frame
         }
         if (n[0] + n[1] + n[2] == 0) return;   // uniform over the grid: no barrier below is skipped partially
         queue_pass<true, USCENE>(Su, tfs, A, n, start, stride, st, c);
+    }
+    flush_counters(A.ctr, c, st);
+}
+
+// March pass of split shadow/AO tracing with per-lane refill: a lane whose
+// ray has finished takes the next record of the march queue while the other
+// lanes keep marching, so warps stay full across rays of different march
+// lengths.  Each record carries the query pass's stop distance and surface
+// flag.  USCENE / batch as for the other frame kernels (uniform scene only).
+template <bool BATCH, int MINB>
+__global__ void __launch_bounds__(kThreads, MINB) k_sec_march(DevScene S, FrameArgs A) {
+    __shared__ DevTF tfs[kMaxVol];
+    load_tfs(S, tfs);
+    RayStats st;
+    LocalCounters c;
+    const int lane = threadIdx.x & 31;
+    const unsigned n = min(*((volatile unsigned *)A.qmarch_count), A.qmarch_cap);
+    unsigned *cursor = A.qmarch_count + 1;
+    SecMarch M;
+    TraceIn in;
+    int x = 0, y = 0, job = 0, q = Q_SHADOW;
+    bool have = false;
+    for (;;) {
+        bool need = !have;
+        unsigned mask = __ballot_sync(0xffffffffu, need);
+        unsigned base = 0;
+        if (mask) {
+            if (lane == 0) base = atomicAdd(cursor, (unsigned)__popc(mask));
+            base = __shfl_sync(0xffffffffu, base, 0);
+        }
+        if (need) {
+            unsigned idx = base + __popc(mask & ((1u << lane) - 1u));
+            if (idx < n) {
+                load_ray(A.qmarch, idx, in, x, y, job);
+                int4 m = __ldg(reinterpret_cast<const int4 *>(A.qmarch + idx) + 3);
+                bool surface = (in.type & 8) != 0;
+                in.type &= 7;
+                q = in.type == GXY_RAY_SHADOW ? Q_SHADOW : Q_AO;
+                sec_march_init(S, in, __int_as_float(m.w), surface, M);
+                have = true;
+                c.march++;
+            }
+        }
+        if (!__any_sync(0xffffffffu, have)) break;
+        if (have && !M.done) sec_march_steps(S, tfs[0], M, 16, st);
+        bool fin = have && M.done;
+        int dest = GXY_DROP_ON_FLOOR;
+        TraceOut T;
+        if (fin) {
+            const DevJob &J = BATCH ? A.jobs[job] : A.job0;
+            int term = sec_march_term(S, M);
+            int cls = classify_ray(in.type, term);
+            dest = assign_destination(S, in.part, in.type, cls, in.org, in.dir);
+            T.t = M.tTerm;
+            T.r = M.cr; T.g = M.cg; T.b = M.cb; T.o = M.ca;
+            if (dest == GXY_TERMINATED) {
+                c.term++;
+                add_pixel(J.fb, J.cam.width, x, y, T.r, T.g, T.b, T.o);
+            } else if (dest == GXY_DROP_ON_FLOOR) {
+                c.drop++;
+            } else {
+                c.hand++;
+            }
+        }
+        if (__any_sync(0xffffffffu, fin && dest >= 0)) emit_secondary(fin, dest, q, job, in, x, y, T, A, c);
+        if (fin) have = false;
     }
     flush_counters(A.ctr, c, st);
 }
@@ -1183,6 +1285,13 @@ __global__ void k_rl_camera_write(DevScene S, DevCamera C, int part, const int *
 // thread) and the grid-stride grid size in blocks per SM.
 static int g_tune_minb = 3;
 static int g_tune_grid_per_sm = 16;
+static int g_tune_split = 1;   // split shadow/AO tracing into query + refill-march passes
+
+// The split path applies to volume-rendered scenes with one volume and no
+// isovalues (the march pass keeps one sample value per lane).
+static bool split_eligible(const DevScene &S) {
+    return g_tune_split && S.integrate && !S.has_iso && S.n_vol == 1;
+}
 
 static unsigned grid_for(int64_t n) {
     int sms = 152;
@@ -1193,7 +1302,26 @@ static unsigned grid_for(int64_t n) {
     return (unsigned)(want < 1 ? 1 : want);
 }
 
+// The refill march keeps every resident warp busy until its queue is empty:
+// one wave of resident blocks.
+static unsigned march_grid(int minb) {
+    int sms = 152, per = 1;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, g_device);
+    if (minb == 3) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_sec_march<false, 3>, kThreads, 0);
+    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_sec_march<false, 2>, kThreads, 0);
+    return (unsigned)(sms * (per < 1 ? 1 : per));
+}
+
 static int ensure_queues(Scene *sc, const size_t need[3]) {
+    size_t mneed = need[1] + need[2];
+    if (sc->qmarch_cap < mneed) {
+        arena().free(sc->qmarch);
+        sc->qmarch = nullptr;
+        sc->qmarch_cap = 0;
+        int rc = arena().alloc((void **)&sc->qmarch, mneed * sizeof(DRay));
+        if (rc) return rc;
+        sc->qmarch_cap = mneed;
+    }
     for (int k = 0; k < 3; k++) {
         if (sc->qcap[k] >= need[k]) continue;
         for (int b = 0; b < 2; b++) {
@@ -1213,7 +1341,7 @@ static int ensure_queues(Scene *sc, const size_t need[3]) {
 static void add_counters(DevCounters &a, const DevCounters &b) {
     const unsigned long long *pb = &b.primary;
     unsigned long long *pa = &a.primary;
-    for (int k = 0; k < 13; k++) pa[k] += pb[k];
+    for (int k = 0; k < 14; k++) pa[k] += pb[k];
     a.overflow |= b.overflow;
 }
 
@@ -1251,6 +1379,10 @@ static int render(Scene *sc, const gxy_camera &cam, const gxy_lighting &lt, floa
     A.job0.pix0 = 0;
     A.n_jobs = 1;
     A.total_pix = npix;
+    A.split = split_eligible(S) ? 1 : 0;
+    A.qmarch = sc->qmarch;
+    A.qmarch_count = sc->qcount + 12;
+    A.qmarch_cap = (unsigned)sc->qmarch_cap;
     for (int k = 0; k < 3; k++) A.qcap[k] = (unsigned)sc->qcap[k];
     struct LaunchRec { int gen, kind; unsigned rays_in; };
     std::vector<LaunchRec> recs;
@@ -1260,14 +1392,17 @@ static int render(Scene *sc, const gxy_camera &cam, const gxy_lighting &lt, floa
         A.ctr = sc->ctr + nl;
         unsigned g = grid_for(items);
         if (sc->profile) CK(cudaEventRecord(sc->events[2 * nl], st));
+        if (kind == K_SECONDARY && A.split) CK(cudaMemsetAsync(A.qmarch_count, 0, 2 * sizeof(unsigned), st));
         if (g_tune_minb == 3) {
             if (kind == K_CAMERA) k_primary<K_CAMERA, 3><<<g, kThreads, 0, st>>>(S, A);
             else if (kind == K_PRIMARY) k_primary<K_PRIMARY, 3><<<g, kThreads, 0, st>>>(S, A);
-            else k_secondary<3><<<g, kThreads, 0, st>>>(S, A);
+            else if (kind == K_SECONDARY) k_secondary<3><<<g, kThreads, 0, st>>>(S, A);
+            else k_sec_march<false, 3><<<march_grid(3), kThreads, 0, st>>>(S, A);
         } else {
             if (kind == K_CAMERA) k_primary<K_CAMERA, 2><<<g, kThreads, 0, st>>>(S, A);
             else if (kind == K_PRIMARY) k_primary<K_PRIMARY, 2><<<g, kThreads, 0, st>>>(S, A);
-            else k_secondary<2><<<g, kThreads, 0, st>>>(S, A);
+            else if (kind == K_SECONDARY) k_secondary<2><<<g, kThreads, 0, st>>>(S, A);
+            else k_sec_march<false, 2><<<march_grid(2), kThreads, 0, st>>>(S, A);
         }
         CK(cudaGetLastError());
         if (sc->profile) CK(cudaEventRecord(sc->events[2 * nl + 1], st));
@@ -1299,6 +1434,7 @@ static int render(Scene *sc, const gxy_camera &cam, const gxy_lighting &lt, floa
         if (n[Q_SHADOW] + n[Q_AO] &&
             (rc = launch(K_SECONDARY, gen, n[Q_SHADOW] + n[Q_AO], (int64_t)n[Q_SHADOW] + n[Q_AO])))
             return rc;
+        if (n[Q_SHADOW] + n[Q_AO] && A.split && (rc = launch(K_MARCH, gen, 0, 1 << 30))) return rc;
         cur = nxt;
         gen++;
     }
@@ -1317,7 +1453,9 @@ static int render(Scene *sc, const gxy_camera &cam, const gxy_lighting &lt, floa
             g.ms = ms;
             g.generation = recs[k].gen;
             g.kind = recs[k].kind;
-            g.rays_in = recs[k].kind == K_CAMERA ? 0 : recs[k].rays_in;
+            g.rays_in = recs[k].kind == K_CAMERA ? 0
+                        : recs[k].kind == K_MARCH ? (int64_t)slots[k].marched
+                                                  : recs[k].rays_in;
             const DevCounters &c = slots[k];
             g.enqueued = (int64_t)c.enqueued;
             g.segments = (int64_t)c.segments;
@@ -1589,6 +1727,10 @@ int gxy_gpu_set_tuning(int knob, int value) {
         g_tune_grid_per_sm = value;
         return GXY_OK;
     }
+    if (knob == GXY_TUNE_SPLIT_SECONDARY) {
+        g_tune_split = value ? 1 : 0;
+        return GXY_OK;
+    }
     return set_error(GXY_ERR_INVALID, "unknown tuning knob");
 }
 
@@ -1596,6 +1738,7 @@ int gxy_gpu_get_tuning(int knob, int *value) {
     if (!value) return set_error(GXY_ERR_INVALID, "null argument");
     if (knob == GXY_TUNE_BLOCKS_PER_SM) *value = g_tune_minb;
     else if (knob == GXY_TUNE_GRID_PER_SM) *value = g_tune_grid_per_sm;
+    else if (knob == GXY_TUNE_SPLIT_SECONDARY) *value = g_tune_split;
     else return set_error(GXY_ERR_INVALID, "unknown tuning knob");
     return GXY_OK;
 }

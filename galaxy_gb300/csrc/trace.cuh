@@ -252,13 +252,13 @@ __device__ __forceinline__ TraceOut trace_core(const DevScene &S, const DevTF *t
                     const DevVolume &vv = S.vol[m];
                     if (vv.volume_render) {
                         float sv = (sLast[m] + sThis[m]) / 2.0f;
-                        float so = tf_opacity(tfs[m], sv);
+                        V3 sc;
+                        float so = tf_lookup(tfs[m], sv, shade, sc);
                         if (so > 0.0f) {
-                            float wo = so / rate;
+                            float wo = S.rate_pow2 ? so * S.inv_rate : so / rate;
                             if (wo > 1.0f) wo = 1.0f;
                             if (wo < 0.0f) wo = 0.0f;
                             if (shade) {
-                                V3 sc = tf_color(tfs[m], sv);
                                 float f = 1.0f - ca;
                                 cr = cr + f * (wo * sc.x);
                                 cg = cg + f * (wo * sc.y);
@@ -384,6 +384,159 @@ __device__ __forceinline__ void ao_basis(V3 n, V3 &b0, V3 &b1) {
     if (fabsf(dot(b0, n)) > 0.95f) b0 = v3(0.f, 1.f, 0.f);
     b1 = nrm(cross(b0, n));
     b0 = nrm(cross(b1, n));
+}
+
+}  // namespace gxy
+
+namespace gxy {
+
+// ------------------------------------------------------------------------
+// Split tracing of shadow/AO rays in volume scenes (whole-frame path):
+//   sec_query  -- box clip, slice planes and the full-extent geometry query
+//                 of trace_core<true, true>; returns whether the ray is culled
+//                 and otherwise the distance the march stops at
+//                 (tTermination) and whether a surface ends the ray;
+//   SecMarch   -- the march of trace_core (one volume, no isovalues) as a
+//                 resumable state, so a lane whose ray is done can take the
+//                 next ray while the others keep marching.
+// The arithmetic is that of trace_core statement for statement.
+
+struct SecQuery {
+    float t_term;
+    bool surface;
+    bool cull;
+};
+
+__device__ __forceinline__ void sec_clip(const DevScene &S, const TraceIn &R, V3 &dir, float &ray_t0, float &ray_t,
+                                         float &tEntry, float &tExitVolume) {
+    const DevPartition &P = S.part[R.part];
+    dir = R.dir;
+    if (dir.x == 0.f) dir.x = 1e-6f;
+    if (dir.y == 0.f) dir.y = 1e-6f;
+    if (dir.z == 0.f) dir.z = 1e-6f;
+    ray_t0 = R.t;
+    ray_t = R.tmax;
+    V3 org = R.org;
+    float rx = 1.0f / dir.x, ry = 1.0f / dir.y, rz = 1.0f / dir.z;
+    float mnx = (P.lo[0] - org.x) * rx, mxx = (P.hi[0] - org.x) * rx;
+    float mny = (P.lo[1] - org.y) * ry, mxy = (P.hi[1] - org.y) * ry;
+    float mnz = (P.lo[2] - org.z) * rz, mxz = (P.hi[2] - org.z) * rz;
+    tEntry = fmax_(fmin_(mnx, mxx), fmax_(fmin_(mny, mxy), fmin_(mnz, mxz)));
+    tExitVolume = fmin_(fmax_(mnx, mxx), fmin_(fmax_(mny, mxy), fmax_(mnz, mxz)));
+    if (tEntry < ray_t0) tEntry = ray_t0;
+    else if (tEntry > ray_t0) ray_t0 = tEntry;
+    ray_t = fmin_(ray_t, tExitVolume);
+}
+
+__device__ __forceinline__ SecQuery sec_query(const DevScene &S, const TraceIn &R, RayStats &st) {
+    SecQuery q;
+    V3 dir;
+    float ray_t0, ray_t, tEntry, tExitVolume;
+    sec_clip(S, R, dir, ray_t0, ray_t, tEntry, tExitVolume);
+    const V3 org = R.org;
+    bool surface_hit = false, slice_ahead = false;
+    for (int m = 0; m < S.n_vol; m++) {
+        const DevVolume &vv = S.vol[m];
+        for (int k = 0; k < vv.n_slices; k++) {
+            float4 pl = vv.slices[k];
+            V3 pn = v3(pl.x, pl.y, pl.z);
+            float denom = dot(dir, pn);
+            if (fabsf(denom) > 0.0001f) {
+                float t = (pl.w - dot(org, pn)) / denom;
+                if (t >= ray_t0 && t <= R.tmax) slice_ahead = true;
+                if (t >= ray_t0 && t <= ray_t) {
+                    ray_t = t;
+                    surface_hit = true;
+                }
+            }
+        }
+    }
+    GeoHit gh;
+    bool h = bvh_closest<false>(S, org, dir, ray_t0, R.tmax, gh, st.nodes, st.tris, st.sphs, st.ovf);
+    if (h && gh.t < ray_t) {
+        ray_t = gh.t;
+        surface_hit = true;
+    }
+    bool zero = R.r == 0.0f && R.g == 0.0f && R.b == 0.0f && R.o == 0.0f;
+    q.cull = zero || (!h && !surface_hit && !slice_ahead && !S.has_iso);
+    q.t_term = ray_t;
+    q.surface = surface_hit;
+    return q;
+}
+
+struct SecMarch {
+    V3 org, dir;
+    float tEntry, tExitVolume, tTimeout, tTerm, tThis, tLast, sLast;
+    float cr, cg, cb, ca;
+    bool surface, opaque, done;
+    CellCache cc;
+};
+
+__device__ __forceinline__ void sec_march_init(const DevScene &S, const TraceIn &R, float t_term, bool surface,
+                                               SecMarch &M) {
+    float ray_t0, ray_t;
+    sec_clip(S, R, M.dir, ray_t0, ray_t, M.tEntry, M.tExitVolume);
+    M.org = R.org;
+    M.tTimeout = R.tmax;
+    M.tTerm = t_term;
+    M.surface = surface;
+    M.cr = R.r; M.cg = R.g; M.cb = R.b; M.ca = R.o;
+    M.tLast = M.tEntry + S.march_eps;
+    M.opaque = (fmin_(fmin_(M.cr, M.cg), M.cb) >= 1.0f || M.ca > S.opaque_alpha);
+    M.tThis = M.tEntry;
+    M.sLast = 0.0f;
+    M.cc.ix = -1; M.cc.iy = -1; M.cc.iz = -1;
+    M.done = !(M.tThis <= M.tTerm && !M.opaque);
+}
+
+// Up to `steps` iterations of the march loop (TraceRays.ispc:470-556 for a
+// shadow/AO ray: compositing `color *= 1 - (dt/step) * clamp(alpha/rate)`).
+__device__ __forceinline__ void sec_march_steps(const DevScene &S, const DevTF &tf, SecMarch &M, int steps,
+                                                RayStats &st) {
+    const DevVolume &vv = S.vol[0];
+    const float step = S.step, epsilon = S.march_eps, oa = S.opaque_alpha;
+    for (int it = 0; it < steps && !M.done; it++) {
+        float tThis = M.tThis;
+        V3 coord = M.org + tThis * M.dir;
+        float sThis = vol_sample_cached(vv, coord, M.cc);
+        st.samples++;
+        if (tThis > M.tEntry && M.tLast >= epsilon) {
+            if (vv.volume_render) {
+                float sv = (M.sLast + sThis) / 2.0f;
+                V3 unused;
+                float so = tf_lookup(tf, sv, false, unused);
+                if (so > 0.0f) {
+                    float wo = S.rate_pow2 ? so * S.inv_rate : so / S.rate;
+                    if (wo > 1.0f) wo = 1.0f;
+                    if (wo < 0.0f) wo = 0.0f;
+                    float w = ((tThis - M.tLast) / step) * wo;
+                    float f = 1.0f - w;
+                    M.cr = M.cr * f;
+                    M.cg = M.cg * f;
+                    M.cb = M.cb * f;
+                    M.ca = M.ca * f;
+                }
+            }
+        }
+        M.sLast = sThis;
+        M.opaque = (fmin_(fmin_(M.cr, M.cg), M.cb) >= 1.0f || M.ca > oa);
+        if (M.opaque) M.tTerm = tThis;
+        M.tLast = tThis;
+        M.tThis = (tThis == M.tEntry) ? (M.tEntry + epsilon)
+                  : (((tThis + step) > M.tTerm) && (tThis < M.tTerm)) ? M.tTerm
+                                                                      : tThis + step;
+        M.done = !(M.tThis <= M.tTerm && !M.opaque);
+    }
+}
+
+// Termination flags of a finished march (TraceRays.ispc:574-617, shadow/AO).
+__device__ __forceinline__ int sec_march_term(const DevScene &S, const SecMarch &M) {
+    bool op = fmin_(fmin_(M.cr, M.cg), M.cb) >= 1.0f || M.ca > S.opaque_alpha;
+    int term = op ? GXY_RAY_OPAQUE : 0;
+    if (M.surface) term |= GXY_RAY_SURFACE;
+    else if (M.tTerm == M.tExitVolume) term |= GXY_RAY_BOUNDARY;
+    else if (M.tTerm == M.tTimeout) term |= GXY_RAY_TIMEOUT;
+    return term;
 }
 
 }  // namespace gxy

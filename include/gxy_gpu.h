@@ -256,9 +256,12 @@ int gxy_gpu_set_profiling(gxy_scene scene, int on);
 /* Process-wide tuning knobs chosen by galaxy_gb300.autotune:
  * GXY_TUNE_BLOCKS_PER_SM: 2 (128 registers per thread) or 3 (80 registers)
  *   -- the register budget the wavefront kernels are compiled for;
- * GXY_TUNE_GRID_PER_SM: blocks per SM of the grid-stride frame kernels. */
+ * GXY_TUNE_GRID_PER_SM: blocks per SM of the grid-stride frame kernels;
+ * GXY_TUNE_SPLIT_SECONDARY: see below. */
 #define GXY_TUNE_BLOCKS_PER_SM 1
 #define GXY_TUNE_GRID_PER_SM   2
+#define GXY_TUNE_SPLIT_SECONDARY 3   /* 1: shadow/AO rays of volume scenes traced as a query
+                                        pass plus a march pass with per-lane refill */
 int gxy_gpu_set_tuning(int knob, int value);
 int gxy_gpu_get_tuning(int knob, int *value);
 int gxy_gpu_query_generations(gxy_scene scene, gxy_generation_stats *out, int max, int32_t *n);
