@@ -476,4 +476,147 @@ __device__ __noinline__ bool bvh_closest(const DevScene &S, V3 org, V3 dir, floa
     return found;
 }
 
+// ------------------------------------------------------------------------
+// Resumable form of bvh_closest<false> (same node order, same tests, same
+// tie rule): trav_step visits one wide node per call, so a persistent lane
+// can interleave traversal steps of successive rays.
+struct TravState {
+    V3 org, dir;
+    float idx, idy, idz;
+    float t0, tfar, cur_tn;
+    uint32_t cur;
+    int sp;
+    GeoHit h;
+    bool found;
+    uint2 stack[64];
+};
+
+__device__ __forceinline__ bool trav_init(const DevScene &S, TravState &T, V3 org, V3 dir, float t0, float tfar) {
+    T.org = org;
+    T.dir = dir;
+    T.idx = 1.0f / dir.x;
+    T.idy = 1.0f / dir.y;
+    T.idz = 1.0f / dir.z;
+    T.t0 = t0;
+    T.tfar = tfar;
+    T.h.t = tfar;
+    T.h.prim = 0xffffffffu;
+    T.found = false;
+    T.sp = 0;
+    T.cur = 0;
+    T.cur_tn = t0;
+    return S.nodes == nullptr;   // done at once without geometry
+}
+
+// One node visit; returns true when the traversal is complete.
+__device__ __forceinline__ bool trav_step(const DevScene &S, TravState &T, unsigned &nodes, unsigned &tris,
+                                          unsigned &sphs, int &ovf) {
+    while (!(T.cur_tn <= T.h.t)) {
+        if (T.sp == 0) return true;
+        uint2 e = T.stack[--T.sp];
+        T.cur = e.x;
+        T.cur_tn = __uint_as_float(e.y);
+    }
+    const V3 org = T.org, dir = T.dir;
+    const float idx = T.idx, idy = T.idy, idz = T.idz, t0 = T.t0, tfar = T.tfar;
+    const bool sx = idx < 0.0f, sy = idy < 0.0f, sz = idz < 0.0f;
+    const float4 *np = reinterpret_cast<const float4 *>(S.nodes + T.cur);
+    float4 n0 = __ldg(np), n1 = __ldg(np + 1);
+    uint32_t child_base = __float_as_uint(n0.w);
+    uint32_t prim_base = __float_as_uint(n1.x);
+    uint32_t e4 = __float_as_uint(n1.y);
+    uint32_t meta_lo = __float_as_uint(n1.z), meta_hi = __float_as_uint(n1.w);
+    uint4 q[6];
+#pragma unroll
+    for (int k = 0; k < 6; k++) q[k] = __ldg(reinterpret_cast<const uint4 *>(np + 2 + k));
+    nodes++;
+    float scx = __uint_as_float((e4 & 0xffu) << 23);
+    float scy = __uint_as_float(((e4 >> 8) & 0xffu) << 23);
+    float scz = __uint_as_float(((e4 >> 16) & 0xffu) << 23);
+    uint32_t imask = e4 >> 24;
+    float ax = scx * idx, bx = (n0.x - org.x) * idx;
+    float ay = scy * idy, by = (n0.y - org.y) * idy;
+    float az = scz * idz, bz = (n0.z - org.z) * idz;
+    uint32_t key[8];
+    uint32_t leafhits = 0;
+    int n_inner = 0;
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+        uint32_t mb = (i < 4 ? meta_lo >> (8 * i) : meta_hi >> (8 * (i - 4))) & 0xffu;
+        uint32_t wl0 = (&q[0].x)[(0 * 8 + i) >> 1], wl1 = (&q[0].x)[(1 * 8 + i) >> 1], wl2 = (&q[0].x)[(2 * 8 + i) >> 1];
+        uint32_t wh0 = (&q[0].x)[(24 + 0 * 8 + i) >> 1], wh1 = (&q[0].x)[(24 + 1 * 8 + i) >> 1],
+                 wh2 = (&q[0].x)[(24 + 2 * 8 + i) >> 1];
+        const int sh = (i & 1) * 16;
+        float lx = (float)((wl0 >> sh) & 0xffffu), ly = (float)((wl1 >> sh) & 0xffffu),
+              lz = (float)((wl2 >> sh) & 0xffffu);
+        float hx = (float)((wh0 >> sh) & 0xffffu), hy = (float)((wh1 >> sh) & 0xffffu),
+              hz = (float)((wh2 >> sh) & 0xffffu);
+        float txa = __fmaf_rn(sx ? hx : lx, ax, bx), txb = __fmaf_rn(sx ? lx : hx, ax, bx);
+        float tya = __fmaf_rn(sy ? hy : ly, ay, by), tyb = __fmaf_rn(sy ? ly : hy, ay, by);
+        float tza = __fmaf_rn(sz ? hz : lz, az, bz), tzb = __fmaf_rn(sz ? lz : hz, az, bz);
+        float tn = fmaxf(fmaxf(txa, tya), fmaxf(tza, t0));
+        float tf = fminf(fminf(txb, tyb), fminf(tzb, T.h.t));
+        bool hit = mb != 0xffu && tn <= tf * 1.00000048f + 1e-30f;
+        bool inner = hit && ((imask >> i) & 1u);
+        key[i] = inner ? ((__float_as_uint(tn) & ~7u) | (uint32_t)i) : 0xffffffffu;
+        n_inner += inner ? 1 : 0;
+        if (hit && !((imask >> i) & 1u)) leafhits |= 1u << i;
+    }
+    while (leafhits) {
+        int i = __ffs(leafhits) - 1;
+        leafhits &= leafhits - 1;
+        uint32_t mb = (i < 4 ? meta_lo >> (8 * i) : meta_hi >> (8 * (i - 4))) & 0xffu;
+        uint32_t s = prim_base + (mb & 31u);
+        uint32_t cnt = (mb >> 5) + 1;
+        for (uint32_t k = 0; k < cnt; k++, s++) {
+            const float4 *rp = S.slots + 3 * (size_t)s;
+            float4 r0 = __ldg(rp), r1 = __ldg(rp + 1);
+            uint32_t id = __float_as_uint(r0.w);
+            float t, u = 0.0f, v = 0.0f;
+            bool ok;
+            if (id & kSphereBit) {
+                sphs++;
+                ok = sph_test(org, dir, v3(r0.x, r0.y, r0.z), r1.x, r1.y, t0, tfar, t);
+            } else {
+                tris++;
+                float4 r2 = __ldg(rp + 2);
+                ok = tri_test(org, dir, v3(r0.x, r0.y, r0.z), v3(r1.x, r1.y, r1.z), v3(r2.x, r2.y, r2.z), t, u, v) &&
+                     t > t0 && t < tfar;
+            }
+            if (ok && (t < T.h.t || (t == T.h.t && id < T.h.prim))) {
+                T.h.t = t; T.h.u = u; T.h.v = v; T.h.prim = id;
+                T.found = true;
+            }
+        }
+    }
+    if (n_inner) {
+        cas(key[0], key[1]); cas(key[2], key[3]); cas(key[4], key[5]); cas(key[6], key[7]);
+        cas(key[0], key[2]); cas(key[1], key[3]); cas(key[4], key[6]); cas(key[5], key[7]);
+        cas(key[1], key[2]); cas(key[5], key[6]); cas(key[0], key[4]); cas(key[3], key[7]);
+        cas(key[1], key[5]); cas(key[2], key[6]);
+        cas(key[1], key[4]); cas(key[3], key[6]);
+        cas(key[2], key[4]); cas(key[3], key[5]);
+        cas(key[3], key[4]);
+#pragma unroll
+        for (int j = 7; j >= 1; j--) {
+            if (j < n_inner) {
+                uint32_t slot = key[j] & 7u;
+                uint32_t mb = (slot < 4 ? meta_lo >> (8 * slot) : meta_hi >> (8 * (slot - 4))) & 0xffu;
+                if (T.sp < 64) T.stack[T.sp++] = make_uint2(child_base + mb, key[j] & ~7u);
+                else ovf = 1;
+            }
+        }
+        uint32_t slot = key[0] & 7u;
+        uint32_t mb = (slot < 4 ? meta_lo >> (8 * slot) : meta_hi >> (8 * (slot - 4))) & 0xffu;
+        T.cur = child_base + mb;
+        T.cur_tn = __uint_as_float(key[0] & ~7u);
+        return false;
+    }
+    if (T.sp == 0) return true;
+    uint2 e = T.stack[--T.sp];
+    T.cur = e.x;
+    T.cur_tn = __uint_as_float(e.y);
+    return false;
+}
+
 }  // namespace gxy

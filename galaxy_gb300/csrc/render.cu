@@ -1035,6 +1035,94 @@ __global__ void __launch_bounds__(kThreads, MINB) k_batch_gen(DevScene Su, Frame
     flush_counters(A.ctr, c, st);
 }
 
+// Query pass of split shadow/AO tracing with per-lane refill: each lane
+// runs the box clip and slice test of its ray, then steps the resumable
+// BVH8 traversal a few nodes at a time; a lane whose traversal is complete
+// finishes the query (cull, or append to the march queue with the stop
+// distance and surface flag) and takes the next ray of the shadow+AO input,
+// so warps stay full while traversals of different lengths proceed.
+template <bool BATCH, int MINB>
+__global__ void __launch_bounds__(kThreads, MINB) k_sec_query(DevScene S, FrameArgs A) {
+    RayStats st;
+    LocalCounters c;
+    const int lane = threadIdx.x & 31;
+    const unsigned ns = A.nin[Q_SHADOW];
+    const unsigned n = ns + A.nin[Q_AO];
+    unsigned *cursor = A.qmarch_count + 2;
+    TravState T;
+    TraceIn in;
+    int x = 0, y = 0, job = 0;
+    float ray_t = 0.0f;
+    bool have = false, done = false, surface = false, slice_ahead = false, zero = false;
+    for (;;) {
+        bool need = !have;
+        unsigned mask = __ballot_sync(0xffffffffu, need);
+        unsigned base = 0;
+        if (mask) {
+            if (lane == 0) base = atomicAdd(cursor, (unsigned)__popc(mask));
+            base = __shfl_sync(0xffffffffu, base, 0);
+        }
+        if (need) {
+            unsigned idx = base + __popc(mask & ((1u << lane) - 1u));
+            if (idx < n) {
+                load_ray(idx < ns ? A.qin[Q_SHADOW] : A.qin[Q_AO], idx < ns ? idx : idx - ns, in, x, y, job);
+                c.seg++;
+                V3 dir;
+                float ray_t0, tEntry, tExitVolume;
+                sec_clip(S, in, dir, ray_t0, ray_t, tEntry, tExitVolume);
+                surface = false;
+                slice_ahead = false;
+                for (int m = 0; m < S.n_vol; m++) {
+                    const DevVolume &vv = S.vol[m];
+                    for (int k = 0; k < vv.n_slices; k++) {
+                        float4 pl = vv.slices[k];
+                        V3 pn = v3(pl.x, pl.y, pl.z);
+                        float denom = dot(dir, pn);
+                        if (fabsf(denom) > 0.0001f) {
+                            float t = (pl.w - dot(in.org, pn)) / denom;
+                            if (t >= ray_t0 && t <= in.tmax) slice_ahead = true;
+                            if (t >= ray_t0 && t <= ray_t) {
+                                ray_t = t;
+                                surface = true;
+                            }
+                        }
+                    }
+                }
+                zero = in.r == 0.0f && in.g == 0.0f && in.b == 0.0f && in.o == 0.0f;
+                done = trav_init(S, T, in.org, dir, ray_t0, in.tmax);
+                have = true;
+            }
+        }
+        if (!__any_sync(0xffffffffu, have)) break;
+        for (int k = 0; k < 4 && have && !done; k++) done = trav_step(S, T, st.nodes, st.tris, st.sphs, st.ovf);
+        bool fin = have && done;
+        bool to_march = false;
+        if (fin) {
+            bool h = T.found;
+            if (h && T.h.t < ray_t) {
+                ray_t = T.h.t;
+                surface = true;
+            }
+            bool cull = zero || (!h && !surface && !slice_ahead && !S.has_iso);
+            if (cull) c.drop++;
+            else to_march = true;
+        }
+        if (__any_sync(0xffffffffu, to_march)) {
+            unsigned idx = warp_reserve(to_march ? 1u : 0u, A.qmarch_count, A.qmarch_cap, c.ovf);
+            if (to_march && idx != 0xffffffffu) {
+                int meta = make_meta(in.type | (surface ? 8 : 0), in.part, job);
+                DRay *p = A.qmarch + idx;
+                p->o = make_float4(in.org.x, in.org.y, in.org.z, in.t);
+                p->d = make_float4(in.dir.x, in.dir.y, in.dir.z, in.tmax);
+                p->c = make_float4(in.r, in.g, in.b, in.o);
+                p->m = make_int4(x, y, meta, __float_as_int(ray_t));
+            }
+        }
+        if (fin) have = false;
+    }
+    flush_counters(A.ctr, c, st);
+}
+
 // March pass of split shadow/AO tracing with per-lane refill: a lane whose
 // ray has finished takes the next record of the march queue while the other
 // lanes keep marching, so warps stay full across rays of different march
@@ -1381,7 +1469,7 @@ static int render(Scene *sc, const gxy_camera &cam, const gxy_lighting &lt, floa
     A.total_pix = npix;
     A.split = split_eligible(S) ? 1 : 0;
     A.qmarch = sc->qmarch;
-    A.qmarch_count = sc->qcount + 12;
+    A.qmarch_count = sc->qcount + 12;   // [0] records, [1] march cursor, [2] query cursor
     A.qmarch_cap = (unsigned)sc->qmarch_cap;
     for (int k = 0; k < 3; k++) A.qcap[k] = (unsigned)sc->qcap[k];
     struct LaunchRec { int gen, kind; unsigned rays_in; };
@@ -1392,15 +1480,17 @@ static int render(Scene *sc, const gxy_camera &cam, const gxy_lighting &lt, floa
         A.ctr = sc->ctr + nl;
         unsigned g = grid_for(items);
         if (sc->profile) CK(cudaEventRecord(sc->events[2 * nl], st));
-        if (kind == K_SECONDARY && A.split) CK(cudaMemsetAsync(A.qmarch_count, 0, 2 * sizeof(unsigned), st));
+        if (kind == K_SECONDARY && A.split) CK(cudaMemsetAsync(A.qmarch_count, 0, 3 * sizeof(unsigned), st));
         if (g_tune_minb == 3) {
             if (kind == K_CAMERA) k_primary<K_CAMERA, 3><<<g, kThreads, 0, st>>>(S, A);
             else if (kind == K_PRIMARY) k_primary<K_PRIMARY, 3><<<g, kThreads, 0, st>>>(S, A);
+            else if (kind == K_SECONDARY && A.split) k_sec_query<false, 3><<<march_grid(3), kThreads, 0, st>>>(S, A);
             else if (kind == K_SECONDARY) k_secondary<3><<<g, kThreads, 0, st>>>(S, A);
             else k_sec_march<false, 3><<<march_grid(3), kThreads, 0, st>>>(S, A);
         } else {
             if (kind == K_CAMERA) k_primary<K_CAMERA, 2><<<g, kThreads, 0, st>>>(S, A);
             else if (kind == K_PRIMARY) k_primary<K_PRIMARY, 2><<<g, kThreads, 0, st>>>(S, A);
+            else if (kind == K_SECONDARY && A.split) k_sec_query<false, 2><<<march_grid(2), kThreads, 0, st>>>(S, A);
             else if (kind == K_SECONDARY) k_secondary<2><<<g, kThreads, 0, st>>>(S, A);
             else k_sec_march<false, 2><<<march_grid(2), kThreads, 0, st>>>(S, A);
         }
