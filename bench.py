@@ -296,7 +296,8 @@ def main():
     ap.add_argument("--side-max", type=int, default=4096)
     ap.add_argument("--time-limit", type=float, default=120.0)
     ap.add_argument("--coop", action="store_true", help="serve with cooperative single-launch batches")
-    ap.add_argument("--autotune", action="store_true", help="pick kernel occupancy and grid size before timing")
+    ap.add_argument("--no-autotune", dest="autotune", action="store_false",
+                    help="skip the autotuner (occupancy, grid size, split tracing) before timing")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

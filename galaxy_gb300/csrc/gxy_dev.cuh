@@ -480,7 +480,7 @@ __device__ __noinline__ bool bvh_closest(const DevScene &S, V3 org, V3 dir, floa
 // Resumable form of bvh_closest<false> (same node order, same tests, same
 // tie rule): trav_step visits one wide node per call, so a persistent lane
 // can interleave traversal steps of successive rays.
-struct TravState {
+struct TravState {                   // scalars only, so it lives in registers
     V3 org, dir;
     float idx, idy, idz;
     float t0, tfar, cur_tn;
@@ -488,7 +488,6 @@ struct TravState {
     int sp;
     GeoHit h;
     bool found;
-    uint2 stack[64];
 };
 
 __device__ __forceinline__ bool trav_init(const DevScene &S, TravState &T, V3 org, V3 dir, float t0, float tfar) {
@@ -509,11 +508,11 @@ __device__ __forceinline__ bool trav_init(const DevScene &S, TravState &T, V3 or
 }
 
 // One node visit; returns true when the traversal is complete.
-__device__ __forceinline__ bool trav_step(const DevScene &S, TravState &T, unsigned &nodes, unsigned &tris,
-                                          unsigned &sphs, int &ovf) {
+__device__ __forceinline__ bool trav_step(const DevScene &S, TravState &T, uint2 *stack, unsigned &nodes,
+                                          unsigned &tris, unsigned &sphs, int &ovf) {
     while (!(T.cur_tn <= T.h.t)) {
         if (T.sp == 0) return true;
-        uint2 e = T.stack[--T.sp];
+        uint2 e = stack[--T.sp];
         T.cur = e.x;
         T.cur_tn = __uint_as_float(e.y);
     }
@@ -602,7 +601,7 @@ __device__ __forceinline__ bool trav_step(const DevScene &S, TravState &T, unsig
             if (j < n_inner) {
                 uint32_t slot = key[j] & 7u;
                 uint32_t mb = (slot < 4 ? meta_lo >> (8 * slot) : meta_hi >> (8 * (slot - 4))) & 0xffu;
-                if (T.sp < 64) T.stack[T.sp++] = make_uint2(child_base + mb, key[j] & ~7u);
+                if (T.sp < 64) stack[T.sp++] = make_uint2(child_base + mb, key[j] & ~7u);
                 else ovf = 1;
             }
         }
@@ -613,7 +612,7 @@ __device__ __forceinline__ bool trav_step(const DevScene &S, TravState &T, unsig
         return false;
     }
     if (T.sp == 0) return true;
-    uint2 e = T.stack[--T.sp];
+    uint2 e = stack[--T.sp];
     T.cur = e.x;
     T.cur_tn = __uint_as_float(e.y);
     return false;

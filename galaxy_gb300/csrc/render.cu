@@ -1050,6 +1050,7 @@ __global__ void __launch_bounds__(kThreads, MINB) k_sec_query(DevScene S, FrameA
     const unsigned n = ns + A.nin[Q_AO];
     unsigned *cursor = A.qmarch_count + 2;
     TravState T;
+    uint2 stack[64];
     TraceIn in;
     int x = 0, y = 0, job = 0;
     float ray_t = 0.0f;
@@ -1094,7 +1095,8 @@ __global__ void __launch_bounds__(kThreads, MINB) k_sec_query(DevScene S, FrameA
             }
         }
         if (!__any_sync(0xffffffffu, have)) break;
-        for (int k = 0; k < 4 && have && !done; k++) done = trav_step(S, T, st.nodes, st.tris, st.sphs, st.ovf);
+        for (int k = 0; k < 4 && have && !done; k++)
+            done = trav_step(S, T, stack, st.nodes, st.tris, st.sphs, st.ovf);
         bool fin = have && done;
         bool to_march = false;
         if (fin) {
@@ -1709,6 +1711,53 @@ int gxy_gpu_scene_partition_info(gxy_scene scene, int partition, gxy_partition_i
     return GXY_OK;
 }
 
+int gxy_scene_partition_layout(const gxy_scene_desc *desc, int partition, gxy_partition_info *out) {
+    GUARD_BEGIN
+    if (!desc || !out) return set_error(GXY_ERR_INVALID, "null argument");
+    int np = (desc->partitions[0] < 1 ? 1 : desc->partitions[0]) * (desc->partitions[1] < 1 ? 1 : desc->partitions[1]) *
+             (desc->partitions[2] < 1 ? 1 : desc->partitions[2]);
+    if (np > kMaxPart || partition < 0 || partition >= np) return set_error(GXY_ERR_INVALID, "bad partition");
+    // geometry box as the commit computes it
+    std::vector<float> g = {FLT_MAX, FLT_MAX, FLT_MAX, -FLT_MAX, -FLT_MAX, -FLT_MAX};
+    bool any = false;
+    for (int s = 0; s < desc->n_triangle_sets; s++) {
+        const gxy_triangles_vis &t = desc->triangles[s];
+        for (int64_t i = 0; i < t.n_vertices; i++)
+            for (int a = 0; a < 3; a++) {
+                g[a] = fminf(g[a], t.vertices[3 * i + a]);
+                g[3 + a] = fmaxf(g[3 + a], t.vertices[3 * i + a]);
+                any = true;
+            }
+    }
+    for (int s = 0; s < desc->n_particle_sets; s++) {
+        const gxy_particles_vis &q = desc->particles[s];
+        for (int64_t i = 0; i < q.n; i++) {
+            float r = sphere_radius(q, i);
+            for (int a = 0; a < 3; a++) {
+                g[a] = fminf(g[a], q.centers[3 * i + a] - r);
+                g[3 + a] = fmaxf(g[3 + a], q.centers[3 * i + a] + r);
+                any = true;
+            }
+        }
+    }
+    if (desc->has_box) g.assign(desc->box, desc->box + 6);
+    else if (!any) g = {-1, -1, -1, 1, 1, 1};
+    DevScene S;
+    memset(&S, 0, sizeof S);
+    make_partitions(*desc, g, S);
+    const DevPartition &P = S.part[partition];
+    for (int a = 0; a < 3; a++) {
+        out->global_box[a] = S.glo[a];
+        out->global_box[3 + a] = S.ghi[a];
+        out->local_box[a] = P.lo[a];
+        out->local_box[3 + a] = P.hi[a];
+    }
+    for (int k = 0; k < 6; k++) out->neighbors[k] = P.nb[k];
+    out->n_partitions = S.np;
+    return GXY_OK;
+    GUARD_END
+}
+
 int gxy_gpu_scene_bvh_info(gxy_scene scene, int64_t *n_nodes, int64_t *n_prim_refs, double *build_ms) {
     if (!scene) return set_error(GXY_ERR_INVALID, "null scene");
     Scene *sc = reinterpret_cast<Scene *>(scene);
@@ -2010,6 +2059,9 @@ struct Batch {
     DRay *q[2][NQ] = {{nullptr, nullptr, nullptr}, {nullptr, nullptr, nullptr}};
     size_t qcap[NQ] = {0, 0, 0};
     unsigned *counts = nullptr;        // kMaxGen x NQ (cooperative mode uses the first 3 x NQ)
+    unsigned *mcounts = nullptr;       // kBatchGens x 4: march records, march cursor (split path)
+    DRay *qmarch = nullptr;
+    size_t qmarch_cap = 0;
     DevJob *d_jobs = nullptr;
     DevJob *h_jobs = nullptr;          // pinned
     DevCounters *ctr = nullptr;
@@ -2071,8 +2123,10 @@ static int batch_enqueue(Batch *b, const DevScene &Su, bool uniform, const Frame
     cudaStream_t st = b->stream;
     CK(cudaMemcpyAsync(b->d_jobs, b->h_jobs, n_jobs * sizeof(DevJob), cudaMemcpyHostToDevice, st));
     CK(cudaMemsetAsync(b->counts, 0, (kBatchGens + 1) * NQ * sizeof(unsigned), st));
+    CK(cudaMemsetAsync(b->mcounts, 0, (kBatchGens + 1) * 4 * sizeof(unsigned), st));
     CK(cudaMemsetAsync(b->ctr, 0, sizeof(DevCounters), st));
     if (!cooperative) {
+        const bool split = uniform && split_eligible(Su);
         // generation g reads counts[g-1], writes counts[g] and queue set g&1
         int grid = gen_grid(uniform);
         for (int g = 0; g < kBatchGens; g++) {
@@ -2082,6 +2136,10 @@ static int batch_enqueue(Batch *b, const DevScene &Su, bool uniform, const Frame
                 a.qout[k] = W.q[g & 1][k];
             }
             a.qout_count = b->counts + NQ * g;
+            a.split = (split && g > 0) ? 1 : 0;
+            a.qmarch = b->qmarch;
+            a.qmarch_count = b->mcounts + 4 * g;
+            a.qmarch_cap = (unsigned)b->qmarch_cap;
             const unsigned *cin = g ? b->counts + NQ * (g - 1) : nullptr;
 #define GXY_GEN_LAUNCH(MB)                                                                          \
     do {                                                                                            \
@@ -2096,6 +2154,10 @@ static int batch_enqueue(Batch *b, const DevScene &Su, bool uniform, const Frame
             if (g_tune_minb == 3) GXY_GEN_LAUNCH(3);
             else GXY_GEN_LAUNCH(2);
 #undef GXY_GEN_LAUNCH
+            if (a.split) {
+                if (g_tune_minb == 3) k_sec_march<true, 3><<<march_grid(3), kThreads, 0, st>>>(Su, a);
+                else k_sec_march<true, 2><<<march_grid(2), kThreads, 0, st>>>(Su, a);
+            }
             CK(cudaGetLastError());
         }
         // status: generations run, rays left after the last one
@@ -2152,6 +2214,9 @@ int gxy_gpu_batch_create(int64_t max_pixels, int max_jobs, int max_shadow, int m
     }
     int rc;
     if ((rc = b->dalloc((void **)&b->counts, (kBatchGens + 1) * NQ * sizeof(unsigned)))) return rc;
+    if ((rc = b->dalloc((void **)&b->mcounts, (kBatchGens + 1) * 4 * sizeof(unsigned)))) return rc;
+    b->qmarch_cap = need[1] + need[2];
+    if ((rc = b->dalloc((void **)&b->qmarch, b->qmarch_cap * sizeof(DRay)))) return rc;
     if ((rc = b->dalloc((void **)&b->d_jobs, max_jobs * sizeof(DevJob)))) return rc;
     if ((rc = b->dalloc((void **)&b->ctr, sizeof(DevCounters)))) return rc;
     if ((rc = b->dalloc((void **)&b->d_status, 8 * sizeof(int)))) return rc;

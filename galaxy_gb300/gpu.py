@@ -41,6 +41,7 @@ def lib():
         "gxy_gpu_scene_release": [vp],
         "gxy_gpu_scene_partition_info": [vp, C.c_int, C.POINTER(A.gxy_partition_info)],
         "gxy_gpu_scene_bvh_info": [vp, C.POINTER(i64), C.POINTER(i64), C.POINTER(C.c_double)],
+        "gxy_scene_partition_layout": [C.POINTER(A.gxy_scene_desc), C.c_int, C.POINTER(A.gxy_partition_info)],
         "gxy_resolve_lights": [C.POINTER(A.gxy_lighting), C.POINTER(A.gxy_camera), C.POINTER(A.gxy_lighting)],
         "gxy_gpu_render": [vp, C.POINTER(A.gxy_camera), C.POINTER(A.gxy_lighting), vp, vp],
         "gxy_gpu_render_host": [vp, C.POINTER(A.gxy_camera), C.POINTER(A.gxy_lighting), A.f32p, vp],
@@ -111,6 +112,14 @@ def get_tuning(knob):
     v = C.c_int(0)
     check(lib().gxy_gpu_get_tuning(int(knob), C.byref(v)))
     return v.value
+
+
+def partition_layout(vis, p):
+    """Brick p's boxes and neighbours for a Visualization (host only)."""
+    d = vis.desc()
+    pi = A.gxy_partition_info()
+    check(lib().gxy_scene_partition_layout(C.byref(d), p, C.byref(pi)))
+    return pi
 
 
 def resolve_lights(lighting, camera):

@@ -212,6 +212,8 @@ int gxy_gpu_hbm_in_use(size_t *bytes);
 int gxy_gpu_scene_commit(const gxy_scene_desc *desc, gxy_scene *out);
 int gxy_gpu_scene_release(gxy_scene scene);
 int gxy_gpu_scene_partition_info(gxy_scene scene, int partition, gxy_partition_info *out);
+/* Host-only: the brick boxes and neighbours a commit of desc would use. */
+int gxy_scene_partition_layout(const gxy_scene_desc *desc, int partition, gxy_partition_info *out);
 /* BVH statistics: wide nodes, leaf primitive references, build time (ms). */
 int gxy_gpu_scene_bvh_info(gxy_scene scene, int64_t *n_nodes, int64_t *n_prim_refs,
                            double *build_ms);

@@ -1,0 +1,106 @@
+"""Host-side logic without a GPU: Galaxy's JSON semantics for lights and
+cameras, light resolution, brick partitions (product vs oracle), state-file
+loading, scene generators and the AO tables."""
+import ctypes as C
+import json
+import os
+
+import numpy as np
+import pytest
+
+import oracle_lib as O
+from galaxy_gb300 import _abi as A
+from galaxy_gb300 import gpu, scenes
+from galaxy_gb300 import scene as S
+
+
+def test_lighting_json_defaults_and_normalisation():
+    L = S.Lighting.from_json({"Sources": [[0, 3, 4], [1, 2, 3, 2]], "shadows": True})
+    assert L.types == [0, 2]
+    np.testing.assert_allclose(L.lights[0], (0, 0.6, 0.8), rtol=1e-6)   # directional normalised (Lighting.cpp:76-90)
+    assert L.lights[1] == (1.0, 2.0, 3.0)
+    assert (L.Ka, L.Kd, L.n_ao, L.ao_radius, L.shadows) == (0.5, 0.5, 0, 1.0, True)
+    Z = S.Lighting.from_json({"Sources": [[0, 0, 0]]})
+    np.testing.assert_allclose(Z.lights[0], (0.57735,) * 3, rtol=1e-5)
+
+
+def test_camera_json_quirks():
+    c = S.Camera.from_json({"viewpoint": [1, 2, 3], "viewcenter": [0, 0, 0], "viewup": [0, 1, 0], "aov": 30,
+                            "dimensions": [640, 480]})
+    assert c.dir == (-1.0, -2.0, -3.0)
+    assert (c.width, c.height) == (640, 640)   # height from dimensions[0] (Camera.cpp:267-271)
+    with pytest.raises(ValueError):
+        S.Camera.from_json({"viewpoint": [0, 0, 1], "viewup": [0, 1, 0], "aov": 30})
+
+
+def test_resolve_lights_python_matches_c_abi():
+    L = S.Lighting.from_json({"Sources": [[1, 2, 3, 1], [-1, -1, 0, 0], [4, 5, 6, 2]]})
+    cam = S.Camera((1, 3, -3), (-1, -3, 3), (0, 1, 0), 30)
+    a = S.resolve_lights(L, cam).c()
+    b = gpu.resolve_lights(L, cam)
+    assert list(a.types)[:3] == list(b.types)[:3] == [2, 0, 2]
+    for i in range(3):
+        assert list(a.lights[i]) == list(b.lights[i])
+
+
+@pytest.mark.parametrize("parts", [(1, 1, 1), (2, 1, 1), (2, 2, 2), (3, 2, 1)])
+def test_partitions_product_equals_oracle(parts):
+    vol = scenes.radial_volume("oneBall", 40)
+    vis = S.Visualization([S.VolumeVis(vol, isovalues=[0.3])], partitions=parts)
+    osc = O.OracleScene(vis)
+    n = parts[0] * parts[1] * parts[2]
+    for p in range(n):
+        a = gpu.partition_layout(vis, p)
+        b = osc.partition_info(p)
+        assert list(a.local_box) == list(b.local_box)
+        assert list(a.global_box) == list(b.global_box)
+        assert list(a.neighbors) == list(b.neighbors)
+        assert a.n_partitions == n
+
+
+def test_geometry_partitions_product_equals_oracle():
+    cam, vis = scenes.triangle_spheres_scene(width=8, height=8, n_seg=8, partitions=(2, 1, 2))
+    vis.box = None
+    osc = O.OracleScene(vis)
+    for p in range(4):
+        a, b = gpu.partition_layout(vis, p), osc.partition_info(p)
+        assert list(a.local_box) == list(b.local_box) and list(a.neighbors) == list(b.neighbors)
+
+
+def test_load_state_file(tmp_path):
+    f = scenes.radial_fields(16)["oneBall"]
+    f.tofile(str(tmp_path / "ball.raw"))
+    (tmp_path / "ball.vol").write_text("float\n-1 -1 -1\n16 16 16\n0.133333 0.133333 0.133333\nball.raw\n")
+    state = {"Datasets": [{"name": "b", "type": "Volume", "filename": "ball.vol"}],
+             "Renderer": {"epsilon": 0.002},
+             "Visualizations": [{"Lighting": {"Sources": [[1, 0, 0, 1]], "ao count": 2},
+                                 "operators": [{"type": "Volume", "dataset": "b", "isovalues": [0.5],
+                                                "colormap": [[0, 1, 0, 0], [1, 0, 0, 1]]}]}],
+             "Cameras": [{"viewpoint": [0, 0, 4], "viewcenter": [0, 0, 0], "viewup": [0, 1, 0], "aov": 30},
+                         {"viewpoint": [4, 0, 0], "viewdirection": [-1, 0, 0], "viewup": [0, 1, 0], "aov": 45}]}
+    (tmp_path / "s.state").write_text(json.dumps(state))
+    rend, eps = S.load_state(str(tmp_path / "s.state"))
+    assert eps == 0.002 and len(rend) == 2
+    cam, vis = rend[1]
+    assert vis.epsilon == 0.002 and vis.lighting.n_ao == 2 and vis.lighting.types == [1]
+    d = vis.desc()
+    assert d.n_volumes == 1 and d.volumes[0].n_isovalues == 1 and list(d.volumes[0].counts) == [16, 16, 16]
+    assert np.array_equal(vis.operators[0].dataset.samples.reshape(-1), f.reshape(-1))
+
+
+def test_generators_are_seeded():
+    a = scenes.sphere_cloud(1000, seed=4)
+    b = scenes.sphere_cloud(1000, seed=4)
+    assert np.array_equal(a.centers, b.centers) and np.array_equal(a.data, b.data)
+    v1 = scenes.blob_field(24, 5, 9)
+    v2 = scenes.blob_field(24, 5, 9)
+    assert np.array_equal(v1, v2)
+    m = scenes.triangle_spheres(seed=0, n_seg=12)
+    assert len(m.indices) == 9 * 2 * 12 * 11 and np.isfinite(m.normals).all()
+
+
+def test_tf_resample_edges():
+    tf = S.resample_tf([(0.0, 0, 0, 0), (1.0, 1, 1, 1)], [(0.0, 0.0), (0.5, 1.0), (1.0, 0.0)])
+    op = np.ctypeslib.as_array(tf.opacities)
+    assert op[0] == 0.0 and op[-1] == 0.0 and abs(op[127] - 0.996) < 0.01
+    assert list(tf.range) == [0.0, 1.0]
