@@ -298,6 +298,7 @@ def main():
     ap.add_argument("--coop", action="store_true", help="serve with cooperative single-launch batches")
     ap.add_argument("--no-autotune", dest="autotune", action="store_false",
                     help="skip the autotuner (occupancy, grid size, split tracing) before timing")
+    ap.add_argument("--tune", default="", help="fixed tuning 'blocks_per_sm,grid_per_sm,split' (implies --no-autotune)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -330,7 +331,13 @@ def main():
         sc.render(cam_c, L, fb.data_ptr(), stream.cuda_stream)
 
     tuning = None
-    if args.autotune:
+    if args.tune:
+        vals = [int(x) for x in args.tune.split(",")] + [1]
+        gpu.set_tuning(gpu.TUNE_BLOCKS_PER_SM, vals[0])
+        gpu.set_tuning(gpu.TUNE_GRID_PER_SM, vals[1])
+        gpu.set_tuning(gpu.TUNE_SPLIT_SECONDARY, vals[2])
+        gpu.set_tuning(gpu.TUNE_SPLIT_PRIMARY, vals[3])
+    elif args.autotune:
         from galaxy_gb300 import autotune
         tuning = autotune.tune(sc, cam_c, L, frames=2)
     sc.set_profiling(True)
@@ -402,7 +409,9 @@ def main():
         traffic = t.get("bytes_per_launch")
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "traffic": traffic, "peak_source": peak_kind,
-            "kernel": ["k_primary<camera>", "k_primary<queue>", "k_secondary", "k_sec_march"][dom],
+            "kernel": ["k_primary<camera>", "k_primary<queue>",
+                       "k_sec_query" if gpu.get_tuning(gpu.TUNE_SPLIT_SECONDARY) else "k_secondary",
+                       "k_sec_march", "k_prim_march"][dom],
             "kernel_ms": dom_ms, "algorithmic_bytes": dom_bytes, "share_of_frame_kernel_time": share}
 
     out = {"metric": METRIC, "value": value, "unit": "rays/s", "n_gpus": world, "steps": args.steps,
@@ -422,7 +431,8 @@ def main():
            "gpu_launches": launches, "roofline": roof, "e2e": e2e, "clocks": clk,
            "tuning": tuning if tuning else {"best": {"blocks_per_sm": gpu.get_tuning(gpu.TUNE_BLOCKS_PER_SM),
                                                      "grid_per_sm": gpu.get_tuning(gpu.TUNE_GRID_PER_SM),
-                                                     "split": gpu.get_tuning(gpu.TUNE_SPLIT_SECONDARY)}}}
+                                                     "split": gpu.get_tuning(gpu.TUNE_SPLIT_SECONDARY),
+                                                     "split_primary": gpu.get_tuning(gpu.TUNE_SPLIT_PRIMARY)}}}
     if rank == 0 and not args.no_cpu_baseline:
         base, _, _ = cpu_baseline(cam, vis, target_s=args.cpu_seconds)
         base.pop("seconds", None)

@@ -9,7 +9,8 @@ candidate setting and keeps the fastest:
   * grid-stride grid size: 4, 8 or 16 blocks per SM (a smaller grid keeps
     rays of a block spatially closer; a larger one balances the tail);
   * split shadow/AO tracing: one combined kernel, or a query pass plus a
-    march pass whose lanes refill from the march queue (volume scenes).
+    march pass whose lanes refill from the march queue (volume scenes);
+  * split camera-ray tracing, likewise.
 
 Frames are timed with CUDA events on the render stream after one warm-up
 frame per setting.  The result can be cached in a JSON file keyed by GPU
@@ -22,18 +23,19 @@ from . import gpu
 
 
 def tune(scene, camera, lighting, frames=3, blocks_per_sm=(2, 3), grid_per_sm=(8, 16, 32), split=(0, 1),
-         verbose=False):
+         split_primary=(0, 1), verbose=False):
     import torch
     stream = torch.cuda.current_stream()
     cam = camera.c() if hasattr(camera, "c") else camera
     fb = torch.zeros((cam.height, cam.width, 4), dtype=torch.float32, device="cuda")
     results = []
-    combos = [(mb, gp, sp) for mb in blocks_per_sm for gp in grid_per_sm for sp in split]
-    for mb, gp, sp in combos:
+    combos = [(mb, gp, sp, pp) for mb in blocks_per_sm for gp in grid_per_sm for sp in split for pp in split_primary]
+    for mb, gp, sp, pp in combos:
         if True:
             gpu.set_tuning(gpu.TUNE_BLOCKS_PER_SM, mb)
             gpu.set_tuning(gpu.TUNE_GRID_PER_SM, gp)
             gpu.set_tuning(gpu.TUNE_SPLIT_SECONDARY, sp)
+            gpu.set_tuning(gpu.TUNE_SPLIT_PRIMARY, pp)
             fb.zero_()
             scene.render(cam, lighting, fb.data_ptr(), stream.cuda_stream)
             torch.cuda.synchronize()
@@ -45,13 +47,15 @@ def tune(scene, camera, lighting, frames=3, blocks_per_sm=(2, 3), grid_per_sm=(8
             e1.record(stream)
             torch.cuda.synchronize()
             ms = e0.elapsed_time(e1) / frames
-            results.append({"blocks_per_sm": mb, "grid_per_sm": gp, "split": sp, "ms_per_frame": ms})
+            results.append({"blocks_per_sm": mb, "grid_per_sm": gp, "split": sp, "split_primary": pp,
+                            "ms_per_frame": ms})
             if verbose:
                 print("autotune", results[-1], flush=True)
     best = min(results, key=lambda r: r["ms_per_frame"])
     gpu.set_tuning(gpu.TUNE_BLOCKS_PER_SM, best["blocks_per_sm"])
     gpu.set_tuning(gpu.TUNE_GRID_PER_SM, best["grid_per_sm"])
     gpu.set_tuning(gpu.TUNE_SPLIT_SECONDARY, best["split"])
+    gpu.set_tuning(gpu.TUNE_SPLIT_PRIMARY, best["split_primary"])
     return {"best": best, "candidates": results}
 
 
@@ -68,6 +72,7 @@ def load(path, workload):
         gpu.set_tuning(gpu.TUNE_BLOCKS_PER_SM, d["blocks_per_sm"])
         gpu.set_tuning(gpu.TUNE_GRID_PER_SM, d["grid_per_sm"])
         gpu.set_tuning(gpu.TUNE_SPLIT_SECONDARY, d.get("split", 1))
+        gpu.set_tuning(gpu.TUNE_SPLIT_PRIMARY, d.get("split_primary", 1))
     return d
 
 

@@ -198,6 +198,9 @@ struct Scene {
     DevScene *d_scene = nullptr;             // device copy of S (batches)
     DRay *qmarch = nullptr;                  // split-path march queue
     size_t qmarch_cap = 0;
+    DRay *pmarch = nullptr;                  // split primary march queue
+    float4 *pmarch_hit = nullptr;
+    size_t pmarch_cap = 0;
     DRay *q[2][3] = {{nullptr, nullptr, nullptr}, {nullptr, nullptr, nullptr}};   // ping-pong x (primary, shadow, AO)
     size_t qcap[3] = {0, 0, 0};
     unsigned int *qcount = nullptr;     // 2 x 3 queue counters
@@ -215,6 +218,8 @@ struct Scene {
         for (int b = 0; b < 2; b++)
             for (int k = 0; k < 3; k++) arena().free(q[b][k]);
         arena().free(qmarch);
+        arena().free(pmarch);
+        arena().free(pmarch_hit);
         arena().free(qcount);
         arena().free(ctr);
         arena().free(fbtmp);
@@ -551,7 +556,7 @@ __device__ __forceinline__ void put_ray(DRay *q, unsigned idx, V3 o, float t, V3
 }
 
 enum { Q_PRIM = 0, Q_SHADOW = 1, Q_AO = 2, NQ = 3 };
-enum { K_CAMERA = 0, K_PRIMARY = 1, K_SECONDARY = 2, K_MARCH = 3 };
+enum { K_CAMERA = 0, K_PRIMARY = 1, K_SECONDARY = 2, K_MARCH = 3, K_PMARCH = 4 };
 constexpr int kMaxJobs = 1024;
 
 // One render job (a camera x visualization of a RenderingSet).
@@ -579,6 +584,12 @@ struct FrameArgs {
     DRay *qmarch;
     unsigned *qmarch_count;            // [0] records, [1] fetch cursor of the march pass
     unsigned qmarch_cap;
+    // split primary tracing: camera query pass -> primary march queue -> march pass
+    int split_prim;
+    DRay *pmarch;
+    float4 *pmarch_hit;                // 2 per record: (n, c.x), (c.y, c.z, -, -)
+    unsigned *pmarch_count;            // [0] records, [1] fetch cursor
+    unsigned pmarch_cap;
 };
 
 // Reserve cnt consecutive queue records for this thread: one warp-wide scan
@@ -655,15 +666,13 @@ struct PrimOut {
     float ar, ag, ab, o_post;
 };
 
-// Trace, shade (reverse-lighting order of TraceRays.cpp:124-131), classify,
-// route and accumulate one primary ray segment.
-__device__ __forceinline__ void primary_ray(const DevScene &S, const DevTF *tfs, const DevJob &J, const TraceIn &in,
-                                            int x, int y, PrimOut &P, RayStats &st, LocalCounters &c) {
+// Shade (reverse-lighting order of TraceRays.cpp:124-131), classify, route
+// and accumulate one traced primary ray segment (P.T holds the trace).
+__device__ __forceinline__ void primary_finish(const DevScene &S, const DevJob &J, const TraceIn &in, int x, int y,
+                                               PrimOut &P, LocalCounters &c) {
     const DevLights &L = J.L;
     P.spawn = false;
     P.ar = P.ag = P.ab = P.o_post = 0.0f;
-    c.seg++;
-    P.T = trace_core<true, false>(S, tfs, in, st);
     TraceOut &T = P.T;
     if (in.type == GXY_RAY_PRIMARY && T.surface) {
         // ambient (TraceRays.ispc:735-761)
@@ -716,6 +725,14 @@ __device__ __forceinline__ void primary_ray(const DevScene &S, const DevTF *tfs,
     } else {
         c.hand++;
     }
+}
+
+// Trace then finish one primary ray segment.
+__device__ __forceinline__ void primary_ray(const DevScene &S, const DevTF *tfs, const DevJob &J, const TraceIn &in,
+                                            int x, int y, PrimOut &P, RayStats &st, LocalCounters &c) {
+    c.seg++;
+    P.T = trace_core<true, false>(S, tfs, in, st);
+    primary_finish(S, J, in, x, y, P, c);
 }
 
 // Warp-collective: write the continuation, AO and shadow rays of the lanes'
@@ -856,15 +873,35 @@ __device__ __forceinline__ void camera_pass(const DevScene &Sp, const DevTF *tfs
         while (__any_sync(0xffffffffu, pending != 0)) {
             bool act = pending != 0;
             PrimOut P;
+            PrimQuery pq;
             const DevScene &S = USCENE ? Sp : *J->scene;
             if (act) {
                 int p = __ffsll((long long)pending) - 1;
                 pending &= pending - 1;
                 in.part = p;
                 c.prim++;
-                primary_ray(S, USCENE ? tfs_uniform : S.tfs, *J, in, x, y, P, st, c);
+                if (A.split_prim) {
+                    c.seg++;
+                    pq = prim_query(S, USCENE ? tfs_uniform : S.tfs, in, st);
+                } else {
+                    primary_ray(S, USCENE ? tfs_uniform : S.tfs, *J, in, x, y, P, st, c);
+                }
             }
-            emit_primary(S, *J, job, act, in, x, y, P, A, c);
+            if (A.split_prim) {
+                unsigned idx = warp_reserve(act ? 1u : 0u, A.pmarch_count, A.pmarch_cap, c.ovf);
+                if (act && idx != 0xffffffffu) {
+                    DRay *r = A.pmarch + idx;
+                    r->o = make_float4(in.org.x, in.org.y, in.org.z, in.t);
+                    r->d = make_float4(in.dir.x, in.dir.y, in.dir.z, in.tmax);
+                    r->c = make_float4(in.r, in.g, in.b, in.o);
+                    r->m = make_int4(x, y, make_meta(in.type | (pq.surface ? 8 : 0), in.part, job),
+                                     __float_as_int(pq.t_term));
+                    A.pmarch_hit[2 * (size_t)idx] = make_float4(pq.n.x, pq.n.y, pq.n.z, pq.c.x);
+                    A.pmarch_hit[2 * (size_t)idx + 1] = make_float4(pq.c.y, pq.c.z, 0.0f, 0.0f);
+                }
+            } else {
+                emit_primary(S, *J, job, act, in, x, y, P, A, c);
+            }
         }
     }
 }
@@ -1125,6 +1162,68 @@ __global__ void __launch_bounds__(kThreads, MINB) k_sec_query(DevScene S, FrameA
     flush_counters(A.ctr, c, st);
 }
 
+// March pass of split primary tracing with per-lane refill: composite the
+// volume up to the query pass's stop distance, then shade (ambient, AO spawn,
+// diffuse, shadow spawn), classify, route and accumulate as primary_ray does.
+template <bool BATCH, int MINB>
+__global__ void __launch_bounds__(kThreads, MINB) k_prim_march(DevScene S, FrameArgs A) {
+    __shared__ DevTF tfs[kMaxVol];
+    load_tfs(S, tfs);
+    RayStats st;
+    LocalCounters c;
+    const int lane = threadIdx.x & 31;
+    const unsigned n = min(*((volatile unsigned *)A.pmarch_count), A.pmarch_cap);
+    unsigned *cursor = A.pmarch_count + 1;
+    SecMarch M;
+    TraceIn in;
+    V3 hn = v3(0, 0, 0), hc = v3(0, 0, 0);
+    int x = 0, y = 0, job = 0;
+    bool have = false;
+    for (;;) {
+        bool need = !have;
+        unsigned mask = __ballot_sync(0xffffffffu, need);
+        unsigned base = 0;
+        if (mask) {
+            if (lane == 0) base = atomicAdd(cursor, (unsigned)__popc(mask));
+            base = __shfl_sync(0xffffffffu, base, 0);
+        }
+        if (need) {
+            unsigned idx = base + __popc(mask & ((1u << lane) - 1u));
+            if (idx < n) {
+                load_ray(A.pmarch, idx, in, x, y, job);
+                int4 m = __ldg(reinterpret_cast<const int4 *>(A.pmarch + idx) + 3);
+                float4 h0 = __ldg(A.pmarch_hit + 2 * (size_t)idx), h1 = __ldg(A.pmarch_hit + 2 * (size_t)idx + 1);
+                hn = v3(h0.x, h0.y, h0.z);
+                hc = v3(h0.w, h1.x, h1.y);
+                bool surface = (in.type & 8) != 0;
+                in.type &= 7;
+                sec_march_init(S, in, __int_as_float(m.w), surface, M);
+                have = true;
+                c.march++;
+            }
+        }
+        if (!__any_sync(0xffffffffu, have)) break;
+        if (have && !M.done) prim_march_steps(S, tfs[0], M, 16, st);
+        bool fin = have && M.done;
+        PrimOut P;
+        const DevJob &J = BATCH ? A.jobs[fin ? job : 0] : A.job0;
+        if (fin) {
+            TraceOut &T = P.T;
+            T.t = M.tTerm;
+            T.term = prim_march_term(S, M);
+            T.r = M.cr; T.g = M.cg; T.b = M.cb; T.o = M.ca;
+            T.surface = M.surface;
+            T.n = hn;
+            T.sc = hc;
+            T.cull = false;
+            primary_finish(S, J, in, x, y, P, c);
+        }
+        if (__any_sync(0xffffffffu, fin)) emit_primary(S, J, job, fin, in, x, y, P, A, c);
+        if (fin) have = false;
+    }
+    flush_counters(A.ctr, c, st);
+}
+
 // March pass of split shadow/AO tracing with per-lane refill: a lane whose
 // ray has finished takes the next record of the march queue while the other
 // lanes keep marching, so warps stay full across rays of different march
@@ -1376,6 +1475,7 @@ __global__ void k_rl_camera_write(DevScene S, DevCamera C, int part, const int *
 static int g_tune_minb = 3;
 static int g_tune_grid_per_sm = 16;
 static int g_tune_split = 1;   // split shadow/AO tracing into query + refill-march passes
+static int g_tune_split_prim = 1;   // split camera rays into query + refill-march passes
 
 // The split path applies to volume-rendered scenes with one volume and no
 // isovalues (the march pass keeps one sample value per lane).
@@ -1403,6 +1503,19 @@ static unsigned march_grid(int minb) {
 }
 
 static int ensure_queues(Scene *sc, const size_t need[3]) {
+    size_t pneed = need[0];
+    if (sc->pmarch_cap < pneed) {
+        arena().free(sc->pmarch);
+        arena().free(sc->pmarch_hit);
+        sc->pmarch = nullptr;
+        sc->pmarch_hit = nullptr;
+        sc->pmarch_cap = 0;
+        int rc = arena().alloc((void **)&sc->pmarch, pneed * sizeof(DRay));
+        if (rc) return rc;
+        rc = arena().alloc((void **)&sc->pmarch_hit, 2 * pneed * sizeof(float4));
+        if (rc) return rc;
+        sc->pmarch_cap = pneed;
+    }
     size_t mneed = need[1] + need[2];
     if (sc->qmarch_cap < mneed) {
         arena().free(sc->qmarch);
@@ -1473,6 +1586,11 @@ static int render(Scene *sc, const gxy_camera &cam, const gxy_lighting &lt, floa
     A.qmarch = sc->qmarch;
     A.qmarch_count = sc->qcount + 12;   // [0] records, [1] march cursor, [2] query cursor
     A.qmarch_cap = (unsigned)sc->qmarch_cap;
+    A.split_prim = (split_eligible(S) && g_tune_split_prim) ? 1 : 0;
+    A.pmarch = sc->pmarch;
+    A.pmarch_hit = sc->pmarch_hit;
+    A.pmarch_count = sc->qcount + 8;    // [0] records, [1] cursor
+    A.pmarch_cap = (unsigned)sc->pmarch_cap;
     for (int k = 0; k < 3; k++) A.qcap[k] = (unsigned)sc->qcap[k];
     struct LaunchRec { int gen, kind; unsigned rays_in; };
     std::vector<LaunchRec> recs;
@@ -1483,17 +1601,20 @@ static int render(Scene *sc, const gxy_camera &cam, const gxy_lighting &lt, floa
         unsigned g = grid_for(items);
         if (sc->profile) CK(cudaEventRecord(sc->events[2 * nl], st));
         if (kind == K_SECONDARY && A.split) CK(cudaMemsetAsync(A.qmarch_count, 0, 3 * sizeof(unsigned), st));
+        if (kind == K_CAMERA && A.split_prim) CK(cudaMemsetAsync(A.pmarch_count, 0, 2 * sizeof(unsigned), st));
         if (g_tune_minb == 3) {
             if (kind == K_CAMERA) k_primary<K_CAMERA, 3><<<g, kThreads, 0, st>>>(S, A);
             else if (kind == K_PRIMARY) k_primary<K_PRIMARY, 3><<<g, kThreads, 0, st>>>(S, A);
             else if (kind == K_SECONDARY && A.split) k_sec_query<false, 3><<<march_grid(3), kThreads, 0, st>>>(S, A);
             else if (kind == K_SECONDARY) k_secondary<3><<<g, kThreads, 0, st>>>(S, A);
+            else if (kind == K_PMARCH) k_prim_march<false, 3><<<march_grid(3), kThreads, 0, st>>>(S, A);
             else k_sec_march<false, 3><<<march_grid(3), kThreads, 0, st>>>(S, A);
         } else {
             if (kind == K_CAMERA) k_primary<K_CAMERA, 2><<<g, kThreads, 0, st>>>(S, A);
             else if (kind == K_PRIMARY) k_primary<K_PRIMARY, 2><<<g, kThreads, 0, st>>>(S, A);
             else if (kind == K_SECONDARY && A.split) k_sec_query<false, 2><<<march_grid(2), kThreads, 0, st>>>(S, A);
             else if (kind == K_SECONDARY) k_secondary<2><<<g, kThreads, 0, st>>>(S, A);
+            else if (kind == K_PMARCH) k_prim_march<false, 2><<<march_grid(2), kThreads, 0, st>>>(S, A);
             else k_sec_march<false, 2><<<march_grid(2), kThreads, 0, st>>>(S, A);
         }
         CK(cudaGetLastError());
@@ -1506,6 +1627,8 @@ static int render(Scene *sc, const gxy_camera &cam, const gxy_lighting &lt, floa
     for (int k = 0; k < 3; k++) A.qout[k] = sc->q[cur][k];
     A.qout_count = sc->qcount + 3 * cur;
     if ((rc = launch(K_CAMERA, 0, 0, npix))) return rc;
+    if (A.split_prim && (rc = launch(K_PMARCH, 0, 0, 1 << 30))) return rc;
+    A.split_prim = 0;   // later generations trace handed-off primaries in one pass
     int gen = 1;
     for (;;) {
         unsigned n[3];
@@ -1546,8 +1669,8 @@ static int render(Scene *sc, const gxy_camera &cam, const gxy_lighting &lt, floa
             g.generation = recs[k].gen;
             g.kind = recs[k].kind;
             g.rays_in = recs[k].kind == K_CAMERA ? 0
-                        : recs[k].kind == K_MARCH ? (int64_t)slots[k].marched
-                                                  : recs[k].rays_in;
+                        : (recs[k].kind == K_MARCH || recs[k].kind == K_PMARCH) ? (int64_t)slots[k].marched
+                                                                                  : recs[k].rays_in;
             const DevCounters &c = slots[k];
             g.enqueued = (int64_t)c.enqueued;
             g.segments = (int64_t)c.segments;
@@ -1870,6 +1993,10 @@ int gxy_gpu_set_tuning(int knob, int value) {
         g_tune_split = value ? 1 : 0;
         return GXY_OK;
     }
+    if (knob == GXY_TUNE_SPLIT_PRIMARY) {
+        g_tune_split_prim = value ? 1 : 0;
+        return GXY_OK;
+    }
     return set_error(GXY_ERR_INVALID, "unknown tuning knob");
 }
 
@@ -1878,6 +2005,7 @@ int gxy_gpu_get_tuning(int knob, int *value) {
     if (knob == GXY_TUNE_BLOCKS_PER_SM) *value = g_tune_minb;
     else if (knob == GXY_TUNE_GRID_PER_SM) *value = g_tune_grid_per_sm;
     else if (knob == GXY_TUNE_SPLIT_SECONDARY) *value = g_tune_split;
+    else if (knob == GXY_TUNE_SPLIT_PRIMARY) *value = g_tune_split_prim;
     else return set_error(GXY_ERR_INVALID, "unknown tuning knob");
     return GXY_OK;
 }

@@ -540,3 +540,120 @@ __device__ __forceinline__ int sec_march_term(const DevScene &S, const SecMarch 
 }
 
 }  // namespace gxy
+
+namespace gxy {
+
+// ------------------------------------------------------------------------
+// Split tracing of primary rays in volume scenes (whole-frame path), the
+// primary-ray counterpart of sec_query / SecMarch:
+//   prim_query -- box clip, slice planes with their surface colour, and the
+//                 in-brick closest geometry hit with its normal and colour
+//                 (trace_core<true,false> up to the march);
+//   PrimMarch  -- the front-to-back compositing march (one volume, no
+//                 isovalues) as a resumable state.
+
+struct PrimQuery {
+    float t_term;
+    bool surface;
+    V3 n, c;
+};
+
+__device__ __forceinline__ PrimQuery prim_query(const DevScene &S, const DevTF *tfs, const TraceIn &R, RayStats &st) {
+    PrimQuery q;
+    V3 dir;
+    float ray_t0, ray_t, tEntry, tExitVolume;
+    sec_clip(S, R, dir, ray_t0, ray_t, tEntry, tExitVolume);
+    const V3 org = R.org;
+    bool surface_hit = false;
+    float hit_t = 0.f;
+    V3 hit_n = v3(0, 0, 0), hit_c = v3(0, 0, 0);
+    int vid = -1;
+    for (int m = 0; m < S.n_vol; m++) {
+        const DevVolume &vv = S.vol[m];
+        for (int k = 0; k < vv.n_slices; k++) {
+            float4 pl = vv.slices[k];
+            V3 pn = v3(pl.x, pl.y, pl.z);
+            float denom = dot(dir, pn);
+            if (fabsf(denom) > 0.0001f) {
+                float t = (pl.w - dot(org, pn)) / denom;
+                if (t >= ray_t0 && t <= ray_t) {
+                    hit_n = denom > 0 ? neg(pn) : pn;
+                    hit_t = t;
+                    vid = m;
+                    ray_t = t;
+                    surface_hit = true;
+                }
+            }
+        }
+    }
+    if (surface_hit) {
+        V3 p = org + hit_t * dir;
+        float smp = vol_sample(S.vol[vid], p);
+        hit_c = tf_color(tfs[vid], smp);
+    }
+    if (S.nodes) {
+        GeoHit gh;
+        if (bvh_closest<false>(S, org, dir, ray_t0, ray_t, gh, st.nodes, st.tris, st.sphs, st.ovf)) {
+            ray_t = gh.t;
+            surface_hit = true;
+            geometry_shade(S, gh, org, dir, hit_n, hit_c);
+        }
+    }
+    q.t_term = ray_t;
+    q.surface = surface_hit;
+    q.n = hit_n;
+    q.c = hit_c;
+    return q;
+}
+
+// Compositing march of a primary ray (TraceRays.ispc:470-556 with the
+// primary-ray weight `color += (1 - color.a) * clamp(alpha/rate) * [rgb, 1]`).
+__device__ __forceinline__ void prim_march_steps(const DevScene &S, const DevTF &tf, SecMarch &M, int steps,
+                                                 RayStats &st) {
+    const DevVolume &vv = S.vol[0];
+    const float step = S.step, epsilon = S.march_eps, oa = S.opaque_alpha;
+    for (int it = 0; it < steps && !M.done; it++) {
+        float tThis = M.tThis;
+        V3 coord = M.org + tThis * M.dir;
+        float sThis = vol_sample_cached(vv, coord, M.cc);
+        st.samples++;
+        if (tThis > M.tEntry && M.tLast >= epsilon) {
+            if (vv.volume_render) {
+                float sv = (M.sLast + sThis) / 2.0f;
+                V3 sc;
+                float so = tf_lookup(tf, sv, true, sc);
+                if (so > 0.0f) {
+                    float wo = S.rate_pow2 ? so * S.inv_rate : so / S.rate;
+                    if (wo > 1.0f) wo = 1.0f;
+                    if (wo < 0.0f) wo = 0.0f;
+                    float f = 1.0f - M.ca;
+                    M.cr = M.cr + f * (wo * sc.x);
+                    M.cg = M.cg + f * (wo * sc.y);
+                    M.cb = M.cb + f * (wo * sc.z);
+                    M.ca = M.ca + f * wo;
+                }
+            }
+        }
+        M.sLast = sThis;
+        M.opaque = (fmin_(fmin_(M.cr, M.cg), M.cb) >= 1.0f || M.ca > oa);
+        if (M.opaque) M.tTerm = tThis;
+        M.tLast = tThis;
+        M.tThis = (tThis == M.tEntry) ? (M.tEntry + epsilon)
+                  : (((tThis + step) > M.tTerm) && (tThis < M.tTerm)) ? M.tTerm
+                                                                      : tThis + step;
+        M.done = !(M.tThis <= M.tTerm && !M.opaque);
+    }
+}
+
+// Termination flags of a finished primary march: a surface found with
+// shading has opacity 1 (TraceRays.ispc:195,240,304; postIntersect colour w=1).
+__device__ __forceinline__ int prim_march_term(const DevScene &S, const SecMarch &M) {
+    bool op = fmin_(fmin_(M.cr, M.cg), M.cb) >= 1.0f || M.ca > S.opaque_alpha;
+    int term = op ? GXY_RAY_OPAQUE : 0;
+    if (M.surface) term |= GXY_RAY_SURFACE | GXY_RAY_OPAQUE;
+    else if (M.tTerm == M.tExitVolume) term |= GXY_RAY_BOUNDARY;
+    else if (M.tTerm == M.tTimeout) term |= GXY_RAY_TIMEOUT;
+    return term;
+}
+
+}  // namespace gxy

@@ -102,6 +102,7 @@ def hbm_in_use():
 TUNE_BLOCKS_PER_SM = 1
 TUNE_GRID_PER_SM = 2
 TUNE_SPLIT_SECONDARY = 3
+TUNE_SPLIT_PRIMARY = 4
 
 
 def set_tuning(knob, value):

@@ -264,6 +264,7 @@ int gxy_gpu_set_profiling(gxy_scene scene, int on);
 #define GXY_TUNE_GRID_PER_SM   2
 #define GXY_TUNE_SPLIT_SECONDARY 3   /* 1: shadow/AO rays of volume scenes traced as a query
                                         pass plus a march pass with per-lane refill */
+#define GXY_TUNE_SPLIT_PRIMARY   4   /* 1: camera rays of volume scenes likewise */
 int gxy_gpu_set_tuning(int knob, int value);
 int gxy_gpu_get_tuning(int knob, int *value);
 int gxy_gpu_query_generations(gxy_scene scene, gxy_generation_stats *out, int max, int32_t *n);
