@@ -299,6 +299,8 @@ def main():
     ap.add_argument("--no-autotune", dest="autotune", action="store_false",
                     help="skip the autotuner (occupancy, grid size, split tracing) before timing")
     ap.add_argument("--tune", default="", help="fixed tuning 'blocks_per_sm,grid_per_sm,split' (implies --no-autotune)")
+    ap.add_argument("--bvh", default="sah", choices=["sah", "lbvh"],
+                    help="BVH binary tree: binned SAH along the Morton order, or radix-tree (LBVH) splits")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -314,6 +316,8 @@ def main():
     from galaxy_gb300 import scene as S
 
     cam, vis, cfg = make_workload(args.workload)
+    gpu.set_tuning(gpu.TUNE_BVH_SAH, 1 if args.bvh == "sah" else 0)
+    cfg = dict(cfg, bvh=args.bvh)
     if args.image:
         cam.width = cam.height = args.image
         cfg = dict(cfg, image=[args.image, args.image], workload=cfg["workload"] + " (image %d^2)" % args.image)

@@ -211,6 +211,106 @@ __global__ void k_refit(int n, const uint32_t *ids, const float4 *plo, const flo
     }
 }
 
+// ---------------------------------------------------------------------
+// Morton-ordered binned SAH binary tree (replaces the radix-tree splits of
+// k_karras): top down, one warp per node of the current level.  A node
+// covers a contiguous range [first, last] of Morton-sorted primitives; its
+// range is cut into B = min(32, count) equal bins, lane k reduces the box of
+// bin k, warp scans give the boxes and counts left and right of every bin
+// boundary, and the node splits at the boundary with the smallest
+// surface-area cost area(L)*n(L) + area(R)*n(R).  Children with one
+// primitive are leaves (~position); the others go to the next level.
+__device__ __forceinline__ float4 f4min(float4 a, float4 b) {
+    return make_float4(fminf(a.x, b.x), fminf(a.y, b.y), fminf(a.z, b.z), 0.0f);
+}
+__device__ __forceinline__ float4 f4max(float4 a, float4 b) {
+    return make_float4(fmaxf(a.x, b.x), fmaxf(a.y, b.y), fmaxf(a.z, b.z), 0.0f);
+}
+__device__ __forceinline__ float4 shfl_up4(float4 v, int o) {
+    return make_float4(__shfl_up_sync(0xffffffffu, v.x, o), __shfl_up_sync(0xffffffffu, v.y, o),
+                       __shfl_up_sync(0xffffffffu, v.z, o), 0.0f);
+}
+__device__ __forceinline__ float4 shfl_down4(float4 v, int o) {
+    return make_float4(__shfl_down_sync(0xffffffffu, v.x, o), __shfl_down_sync(0xffffffffu, v.y, o),
+                       __shfl_down_sync(0xffffffffu, v.z, o), 0.0f);
+}
+
+__global__ void k_sah_level(int nq, const int *q, int *qout, unsigned *ctr, const uint32_t *ids, const float4 *plo,
+                            const float4 *phi, int *left, int *right, int *first, int *last, float4 *nlo,
+                            float4 *nhi) {
+    int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    int lane = threadIdx.x & 31;
+    if (w >= nq) return;   // whole warp exits together
+    int node = q[w];
+    int f = first[node], l = last[node];
+    int cnt = l - f + 1;
+    int B = cnt < 32 ? cnt : 32;
+    float4 lo = make_float4(FLT_MAX, FLT_MAX, FLT_MAX, 0), hi = make_float4(-FLT_MAX, -FLT_MAX, -FLT_MAX, 0);
+    int b0 = f + (int)(((long long)lane * cnt) / B), b1 = f + (int)(((long long)(lane + 1) * cnt) / B);
+    int n = 0;
+    if (lane < B) {
+        for (int i = b0; i < b1; i++) {
+            uint32_t p = ids[i];
+            lo = f4min(lo, plo[p]);
+            hi = f4max(hi, phi[p]);
+        }
+        n = b1 - b0;
+    }
+    // inclusive prefix (boxes and counts) and inclusive suffix
+    float4 plo_ = lo, phi_ = hi, slo = lo, shi = hi;
+    int pn = n, sn = n;
+    for (int o = 1; o < 32; o <<= 1) {
+        float4 a = shfl_up4(plo_, o), b = shfl_up4(phi_, o);
+        int c = __shfl_up_sync(0xffffffffu, pn, o);
+        if (lane >= o) { plo_ = f4min(plo_, a); phi_ = f4max(phi_, b); pn += c; }
+        float4 d = shfl_down4(slo, o), e = shfl_down4(shi, o);
+        int g = __shfl_down_sync(0xffffffffu, sn, o);
+        if (lane + o < 32) { slo = f4min(slo, d); shi = f4max(shi, e); sn += g; }
+    }
+    // candidate: split after bin `lane` (lane < B-1): left = prefix(lane), right = suffix(lane+1)
+    float4 rlo = shfl_down4(slo, 1), rhi = shfl_down4(shi, 1);
+    int rn = __shfl_down_sync(0xffffffffu, sn, 1);
+    float cost = FLT_MAX;
+    if (lane < B - 1) {
+        float la = (phi_.x - plo_.x) * (phi_.y - plo_.y) + (phi_.y - plo_.y) * (phi_.z - plo_.z) +
+                   (phi_.z - plo_.z) * (phi_.x - plo_.x);
+        float ra = (rhi.x - rlo.x) * (rhi.y - rlo.y) + (rhi.y - rlo.y) * (rhi.z - rlo.z) +
+                   (rhi.z - rlo.z) * (rhi.x - rlo.x);
+        cost = la * (float)pn + ra * (float)rn;
+    }
+    int best = lane;
+    for (int o = 16; o > 0; o >>= 1) {
+        float oc = __shfl_xor_sync(0xffffffffu, cost, o);
+        int ob = __shfl_xor_sync(0xffffffffu, best, o);
+        if (oc < cost || (oc == cost && ob < best)) { cost = oc; best = ob; }
+    }
+    float4 alo = make_float4(__shfl_sync(0xffffffffu, plo_.x, B - 1), __shfl_sync(0xffffffffu, plo_.y, B - 1),
+                             __shfl_sync(0xffffffffu, plo_.z, B - 1), 0.0f);
+    float4 ahi = make_float4(__shfl_sync(0xffffffffu, phi_.x, B - 1), __shfl_sync(0xffffffffu, phi_.y, B - 1),
+                             __shfl_sync(0xffffffffu, phi_.z, B - 1), 0.0f);
+    if (lane == 0) {
+        nlo[node] = alo;
+        nhi[node] = ahi;
+        int split = f + (int)(((long long)(best + 1) * cnt) / B);   // first primitive of the right child
+        int rng[2][2] = {{f, split - 1}, {split, l}};
+        int ref[2];
+        for (int k = 0; k < 2; k++) {
+            int a = rng[k][0], b = rng[k][1];
+            if (a == b) {
+                ref[k] = ~a;
+            } else {
+                int id = (int)atomicAdd(&ctr[0], 1u);
+                first[id] = a;
+                last[id] = b;
+                qout[atomicAdd(&ctr[1], 1u)] = id;
+                ref[k] = id;
+            }
+        }
+        left[node] = ref[0];
+        right[node] = ref[1];
+    }
+}
+
 __device__ __forceinline__ float half_area(float4 lo, float4 hi) {
     float x = hi.x - lo.x, y = hi.y - lo.y, z = hi.z - lo.z;
     return x * y + y * z + z * x;
@@ -396,7 +496,32 @@ int build_bvh8(DevScene &S, const float *sph_radius, DeviceArena &arena, cudaStr
     unsigned char *tmp;
     ALLOC(tmp, tmp_bytes);
     CK(cub::DeviceRadixSort::SortPairs(tmp, tmp_bytes, B.keys, B.keys2, B.ids, B.ids2, n, 0, 63, st));
-    if (n > 1) {
+    if (n > 1 && sah_builder()) {
+        // binned-SAH splits along the Morton order, level by level
+        int zero_first[2] = {0, n - 1};
+        CK(cudaMemcpyAsync(B.first, &zero_first[0], sizeof(int), cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(B.last, &zero_first[1], sizeof(int), cudaMemcpyHostToDevice, st));
+        int root = 0;
+        unsigned c2[2] = {1, 0};
+        CK(cudaMemcpyAsync(B.qa, &root, sizeof(int), cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(B.ctr + 4, c2, sizeof c2, cudaMemcpyHostToDevice, st));
+        int nq = 1, lev = 0;
+        int *qa = (int *)B.qa, *qb = (int *)B.qb;
+        while (nq > 0) {
+            CK(cudaMemsetAsync(B.ctr + 5, 0, sizeof(unsigned), st));
+            k_sah_level<<<blocks_for((int64_t)nq * 32, 256), 256, 0, st>>>(nq, qa, qb, B.ctr + 4, B.ids2, B.plo, B.phi,
+                                                                       B.left, B.right, B.first, B.last, B.nlo,
+                                                                       B.nhi);
+            CK(cudaGetLastError());
+            unsigned c[2];
+            CK(cudaMemcpyAsync(c, B.ctr + 4, sizeof c, cudaMemcpyDeviceToHost, st));
+            CK(cudaStreamSynchronize(st));
+            nq = (int)c[1];
+            std::swap(qa, qb);
+            if (++lev > 4096) return set_error(GXY_ERR_INVALID, "SAH build did not converge");
+        }
+        info.sah_levels = lev;
+    } else if (n > 1) {
         CK(cudaMemsetAsync(B.flags, 0, sizeof(int) * ni, st));
         k_karras<<<blocks_for(n - 1, 256), 256, 0, st>>>(n, B.keys2, B.left, B.right, B.parent, B.first, B.last,
                                                          leaf_parent);

@@ -63,11 +63,13 @@ class ScratchList {
 
 struct BVHInfo {
     unsigned n_nodes = 0, n_slots = 0;
-    int levels = 0;
+    int levels = 0, sah_levels = 0;
     double build_ms = 0;
     void *nodes_ptr = nullptr, *slots_ptr = nullptr;
 };
 
 int build_bvh8(DevScene &S, const float *sph_radius, DeviceArena &arena, cudaStream_t st, BVHInfo &info);
+// 1: binary tree by binned SAH along the Morton order; 0: radix-tree (LBVH) splits.
+bool sah_builder();
 
 }  // namespace gxy

@@ -1476,6 +1476,8 @@ static int g_tune_minb = 3;
 static int g_tune_grid_per_sm = 16;
 static int g_tune_split = 1;   // split shadow/AO tracing into query + refill-march passes
 static int g_tune_split_prim = 1;   // split camera rays into query + refill-march passes
+static int g_tune_sah = 1;          // BVH binary tree by binned SAH (else radix-tree splits)
+bool sah_builder() { return g_tune_sah != 0; }
 
 // The split path applies to volume-rendered scenes with one volume and no
 // isovalues (the march pass keeps one sample value per lane).
@@ -1997,6 +1999,10 @@ int gxy_gpu_set_tuning(int knob, int value) {
         g_tune_split_prim = value ? 1 : 0;
         return GXY_OK;
     }
+    if (knob == GXY_TUNE_BVH_SAH) {
+        g_tune_sah = value ? 1 : 0;
+        return GXY_OK;
+    }
     return set_error(GXY_ERR_INVALID, "unknown tuning knob");
 }
 
@@ -2006,6 +2012,7 @@ int gxy_gpu_get_tuning(int knob, int *value) {
     else if (knob == GXY_TUNE_GRID_PER_SM) *value = g_tune_grid_per_sm;
     else if (knob == GXY_TUNE_SPLIT_SECONDARY) *value = g_tune_split;
     else if (knob == GXY_TUNE_SPLIT_PRIMARY) *value = g_tune_split_prim;
+    else if (knob == GXY_TUNE_BVH_SAH) *value = g_tune_sah;
     else return set_error(GXY_ERR_INVALID, "unknown tuning knob");
     return GXY_OK;
 }

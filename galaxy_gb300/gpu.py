@@ -103,6 +103,7 @@ TUNE_BLOCKS_PER_SM = 1
 TUNE_GRID_PER_SM = 2
 TUNE_SPLIT_SECONDARY = 3
 TUNE_SPLIT_PRIMARY = 4
+TUNE_BVH_SAH = 5
 
 
 def set_tuning(knob, value):

@@ -73,18 +73,34 @@ def test_triangle_scene(gpu):
     assert c["shadow_rays"] == cnt["shadow"]
 
 
-def test_mixed_partitioned_scene(gpu):
+@pytest.mark.parametrize("split", [(0, 0), (1, 0), (0, 1), (1, 1)])
+def test_mixed_partitioned_scene(gpu, split):
+    """Every tracing variant (one pass, split shadow/AO, split camera rays)."""
+    gpu.set_tuning(gpu.TUNE_SPLIT_SECONDARY, split[0])
+    gpu.set_tuning(gpu.TUNE_SPLIT_PRIMARY, split[1])
     cam, vis = scenes.mixed_scene(n=64, n_spheres=20000, width=128, height=128, partitions=(2, 2, 2), n_ao=4)
-    img, ref, sc, cnt = render_both(gpu, cam, vis)
+    try:
+        img, ref, sc, cnt = render_both(gpu, cam, vis)
+    finally:
+        gpu.set_tuning(gpu.TUNE_SPLIT_SECONDARY, 1)
+        gpu.set_tuning(gpu.TUNE_SPLIT_PRIMARY, 1)
     image_close(img, ref)
     c = sc.counters()
     assert c["primary_rays"] == cnt["primary"]
     assert abs(c["ao_rays"] - cnt["ao"]) <= 0.001 * cnt["ao"] + 8
 
 
-def test_volume_scene(gpu):
+@pytest.mark.parametrize("split_primary", [0, 1])
+@pytest.mark.parametrize("blocks", [2, 3])
+def test_volume_scene(gpu, split_primary, blocks):
+    gpu.set_tuning(gpu.TUNE_SPLIT_PRIMARY, split_primary)
+    gpu.set_tuning(gpu.TUNE_BLOCKS_PER_SM, blocks)
     cam, vis = scenes.volume_scene(n=96, width=128, height=128)
-    img, ref, sc, cnt = render_both(gpu, cam, vis)
+    try:
+        img, ref, sc, cnt = render_both(gpu, cam, vis)
+    finally:
+        gpu.set_tuning(gpu.TUNE_SPLIT_PRIMARY, 1)
+        gpu.set_tuning(gpu.TUNE_BLOCKS_PER_SM, 3)
     image_close(img, ref)
     assert sc.counters()["samples"] == cnt["samples"]
 
