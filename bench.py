@@ -299,7 +299,7 @@ def main():
     ap.add_argument("--no-autotune", dest="autotune", action="store_false",
                     help="skip the autotuner (occupancy, grid size, split tracing) before timing")
     ap.add_argument("--tune", default="", help="fixed tuning 'blocks_per_sm,grid_per_sm,split' (implies --no-autotune)")
-    ap.add_argument("--bvh", default="sah", choices=["sah", "lbvh"],
+    ap.add_argument("--bvh", default="lbvh", choices=["sah", "lbvh"],
                     help="BVH binary tree: binned SAH along the Morton order, or radix-tree (LBVH) splits")
     args = ap.parse_args()
     if args.impl == "reference":

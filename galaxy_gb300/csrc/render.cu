@@ -1476,7 +1476,7 @@ static int g_tune_minb = 3;
 static int g_tune_grid_per_sm = 16;
 static int g_tune_split = 1;   // split shadow/AO tracing into query + refill-march passes
 static int g_tune_split_prim = 1;   // split camera rays into query + refill-march passes
-static int g_tune_sah = 1;          // BVH binary tree by binned SAH (else radix-tree splits)
+static int g_tune_sah = 0;          // BVH binary tree by binned SAH (else radix-tree splits)
 bool sah_builder() { return g_tune_sah != 0; }
 
 // The split path applies to volume-rendered scenes with one volume and no

@@ -266,7 +266,7 @@ int gxy_gpu_set_profiling(gxy_scene scene, int on);
                                         pass plus a march pass with per-lane refill */
 #define GXY_TUNE_SPLIT_PRIMARY   4   /* 1: camera rays of volume scenes likewise */
 #define GXY_TUNE_BVH_SAH         5   /* 1: BVH binary tree by binned SAH along the Morton
-                                        order (else radix-tree splits); applies to
+                                        order; 0 (default): radix-tree splits. Applies to
                                         scenes committed afterwards */
 int gxy_gpu_set_tuning(int knob, int value);
 int gxy_gpu_get_tuning(int knob, int *value);
