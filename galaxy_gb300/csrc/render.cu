@@ -2528,3 +2528,126 @@ int gxy_gpu_batch_counters(gxy_batch batch, gxy_counters *out) {
 }
 
 }  // extern "C"
+
+// ===================================================== allocation-free entry
+// gxy_gpu_generate_initial_rays_noalloc: the camera-ray pass of
+// gxy_gpu_generate_initial_rays for callers that may not allocate device
+// memory, writing into a RayList the caller already holds in GPU-addressable
+// memory.  Its scratch -- one flag and one output offset per pixel plus the
+// scan's temporary storage -- is the fixed array below, part of this
+// library's device image: every GPU that loads the library holds it until the
+// process exits, and every call on that GPU shares it.
+namespace gxy {
+
+constexpr int64_t kNoAllocMaxPixels = int64_t(1) << 20;   // 1024 x 1024 camera pixels
+constexpr size_t kNoAllocPosOffset = (size_t)kNoAllocMaxPixels * sizeof(int);
+constexpr size_t kNoAllocScanOffset = 2 * (size_t)kNoAllocMaxPixels * sizeof(int);
+constexpr size_t kNoAllocScanBytes = size_t(256) << 10;   // CUB scan temporary storage
+constexpr size_t kNoAllocScratchBytes = kNoAllocScanOffset + kNoAllocScanBytes;   // 8.25 MiB
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+constexpr int kNoAllocMaxDevices = 64;
+static std::mutex g_noalloc_mu;
+static unsigned char *g_noalloc_addr[kNoAllocMaxDevices];
+
+// Device address of g_noalloc_scratch on the current device.  In host code
+// the symbol names a host-side stand-in, not device memory, so the address is
+// looked up with cudaGetSymbolAddress, once per device with that device
+// current, on the first call there.
+static int noalloc_scratch(unsigned char **out) {
+    int dev = -1;
+    CK(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kNoAllocMaxDevices) return set_error(GXY_ERR_INVALID, "device ordinal out of range");
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_addr[dev]) {
+        void *p = nullptr;
+        CK(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+        if (!p) return set_error(GXY_ERR_CUDA, "cudaGetSymbolAddress gave a null scratch address");
+        g_noalloc_addr[dev] = static_cast<unsigned char *>(p);
+    }
+    *out = g_noalloc_addr[dev];
+    return GXY_OK;
+}
+
+// True if a kernel on device `dev` may write through `p`: memory of that
+// device, managed memory, or pinned host memory mapped at the same address.
+static bool gpu_addressable(const void *p, int dev) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    if (a.type == cudaMemoryTypeDevice) return a.device == dev;
+    if (a.type == cudaMemoryTypeManaged) return true;
+    if (a.type == cudaMemoryTypeHost) return a.devicePointer == p;
+    return false;
+}
+
+}  // namespace gxy
+
+extern "C" int gxy_gpu_generate_initial_rays_noalloc(gxy_scene scene, int partition, const gxy_camera *camera,
+                                                     gxy_raylist *out, int32_t *n_out) {
+    GUARD_BEGIN
+    if (!scene || !camera || !out || !n_out) return set_error(GXY_ERR_INVALID, "null argument");
+    Scene *sc = reinterpret_cast<Scene *>(scene);
+    if (partition < 0 || partition >= sc->S.np) return set_error(GXY_ERR_INVALID, "bad partition");
+    if (camera->width <= 0 || camera->height <= 0) return set_error(GXY_ERR_INVALID, "bad image size");
+    int64_t n = (int64_t)camera->width * camera->height;
+    if (n > kNoAllocMaxPixels)
+        return set_error(GXY_ERR_INVALID, "image of " + std::to_string(n) +
+                                              " pixels exceeds the 1048576-pixel limit of the allocation-free "
+                                              "camera-ray entry point");
+    if (out->n < 0) return set_error(GXY_ERR_INVALID, "negative RayList capacity");
+    int dev = -1;
+    CK(cudaGetDevice(&dev));
+    float *of[20];
+    int32_t *oi[5];
+    host_f(*out, of);
+    host_i(*out, oi);
+    for (int k = 0; k < 20; k++)
+        if (!of[k] || !gpu_addressable(of[k], dev))
+            return set_error(GXY_ERR_INVALID, "output RayList float array " + std::to_string(k) +
+                                                  " is not memory the GPU can address");
+    for (int k = 0; k < 5; k++)
+        if (!oi[k] || !gpu_addressable(oi[k], dev))
+            return set_error(GXY_ERR_INVALID, "output RayList int array " + std::to_string(k) +
+                                                  " is not memory the GPU can address");
+    unsigned char *scratch = nullptr;
+    int rc = noalloc_scratch(&scratch);
+    if (rc) return rc;
+    int *flag = reinterpret_cast<int *>(scratch);
+    int *pos = reinterpret_cast<int *>(scratch + kNoAllocPosOffset);
+    void *scan_tmp = scratch + kNoAllocScanOffset;
+    size_t scan_bytes = 0;
+    CK(cub::DeviceScan::ExclusiveSum(nullptr, scan_bytes, flag, pos, (int)n));
+    if (scan_bytes > kNoAllocScanBytes)
+        return set_error(GXY_ERR_OVERFLOW, "scan temporary storage does not fit the fixed scratch");
+    // The flag pass writes flag[0, n), the scan writes pos[0, n) and sets up
+    // its own temporary storage, so nothing left by an earlier call is read.
+    DevCamera C = setup_camera(*camera);
+    unsigned g = (unsigned)((n + 255) / 256);
+    k_rl_camera_flags<<<g, 256>>>(sc->S, C, partition, flag);
+    CK(cudaGetLastError());
+    CK(cub::DeviceScan::ExclusiveSum(scan_tmp, scan_bytes, flag, pos, (int)n));
+    int last_pos = 0, last_flag = 0;
+    CK(cudaMemcpy(&last_pos, pos + n - 1, sizeof(int), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(&last_flag, flag + n - 1, sizeof(int), cudaMemcpyDeviceToHost));
+    int total = last_pos + last_flag;
+    *n_out = total;
+    if (total > out->n) return set_error(GXY_ERR_OVERFLOW, "output RayList too small");
+    if (total) {
+        // fields the camera pass leaves unset read as zero, as in gxy_gpu_generate_initial_rays
+        for (int k = 0; k < 20; k++) CK(cudaMemset(of[k], 0, (size_t)total * sizeof(float)));
+        for (int k = 0; k < 5; k++) CK(cudaMemset(oi[k], 0, (size_t)total * sizeof(int32_t)));
+        RLDev O{};
+        for (int k = 0; k < 20; k++) O.f[k] = of[k];
+        for (int k = 0; k < 5; k++) O.i[k] = oi[k];
+        O.n = total;
+        k_rl_camera_write<<<g, 256>>>(sc->S, C, partition, flag, pos, O);
+        CK(cudaGetLastError());
+    }
+    CK(cudaStreamSynchronize(0));
+    return GXY_OK;
+    GUARD_END
+}

@@ -330,6 +330,25 @@ int gxy_gpu_assign_destinations(gxy_scene scene, int partition, gxy_raylist *ray
 /* Adds every TERMINATED ray's (r,g,b,o) to host framebuffer fb (w*h*4). */
 int gxy_gpu_accumulate_terminated(const gxy_raylist *rays, float *fb_rgba, int width, int height);
 
+/* ---- Allocation-free camera rays ----------------------------------------
+ * No counterpart in the reference.  gxy_gpu_generate_initial_rays with no
+ * device allocation, for callers that must not call cudaMalloc or cudaFree:
+ * e.g. a visualization step run in situ inside a simulation whose own
+ * allocator holds the GPU's memory, where a cudaFree would synchronise the
+ * whole device and stall the simulation's streams.  The caller passes the
+ * output RayList in memory the GPU can address (device memory of the current
+ * device, managed memory, or mapped pinned host memory; all 25 arrays,
+ * capacity out->n); the result equals gxy_gpu_generate_initial_rays's.
+ * Scratch is a fixed 8.25 MiB array in this library's device image, held on
+ * every GPU that loads the library until the process exits.  Images above
+ * 1048576 pixels (1024 x 1024) are refused with GXY_ERR_INVALID.  The first
+ * call on each device looks up the array's device address (with that device
+ * current); make that first call before any stream capture.  All calls on a
+ * device share the array, so calls that overlap on the GPU (from several
+ * host threads) race: serialise them.  Returns after the rays are written. */
+int gxy_gpu_generate_initial_rays_noalloc(gxy_scene scene, int partition, const gxy_camera *camera,
+                                          gxy_raylist *out, int32_t *n_out);
+
 #ifdef __cplusplus
 }
 #endif
