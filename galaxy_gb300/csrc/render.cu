@@ -588,7 +588,7 @@ struct FrameArgs {
     int split_prim;
     DRay *pmarch;
     float4 *pmarch_hit;                // 2 per record: (n, c.x), (c.y, c.z, -, -)
-    unsigned *pmarch_count;            // [0] records, [1] fetch cursor
+    unsigned *pmarch_count;            // [0] records, [1] fetch cursor, [2] camera query cursor
     unsigned pmarch_cap;
 };
 
@@ -1132,6 +1132,8 @@ __global__ void __launch_bounds__(kThreads, MINB) k_sec_query(DevScene S, FrameA
             }
         }
         if (!__any_sync(0xffffffffu, have)) break;
+        // one copy of the step body: unrolled copies overflow the instruction cache
+#pragma unroll 1
         for (int k = 0; k < 4 && have && !done; k++)
             done = trav_step(S, T, stack, st.nodes, st.tris, st.sphs, st.ovf);
         bool fin = have && done;
@@ -1162,6 +1164,129 @@ __global__ void __launch_bounds__(kThreads, MINB) k_sec_query(DevScene S, FrameA
     flush_counters(A.ctr, c, st);
 }
 
+// Query pass of split camera-ray tracing with per-lane refill (single-frame
+// path): a lane takes the next pixel from a device cursor, and for each brick
+// its camera ray enters first (Camera.cpp:431-441) clips to the brick, tests
+// the slices, then steps the resumable BVH8 traversal a few nodes at a time;
+// a finished query writes the same march record as the camera pass's split
+// branch (prim_query), and the lane moves to its next brick or pixel.  The
+// first record of pixel i goes to slot i and a pixel whose ray enters no
+// brick leaves a hole record (meta -1) there, so the march pass reads the
+// records in pixel order; further bricks of one pixel go after slot npix.
+template <int MINB>
+__global__ void __launch_bounds__(kThreads, MINB) k_cam_query(DevScene S, FrameArgs A) {
+    __shared__ DevTF tfs[kMaxVol];
+    load_tfs(S, tfs);
+    RayStats st;
+    LocalCounters c;
+    const int lane = threadIdx.x & 31;
+    const DevCamera &cam = A.job0.cam;
+    const unsigned npix = (unsigned)cam.width * (unsigned)cam.height;
+    unsigned *cursor = A.pmarch_count + 2;
+    TravState T;
+    uint2 stack[64];
+    V3 org = v3(0, 0, 0), dir0 = v3(0, 0, 0), hit_n = v3(0, 0, 0), hit_c = v3(0, 0, 0);
+    int x = 0, y = 0, part = 0;
+    uint64_t pending = 0;
+    float ray_t = 0.0f;
+    bool have = false, done = false, surface = false, exhausted = false, first = false;
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(A.pmarch_count, npix);   // slots [0, npix)
+    for (;;) {
+        bool need = !have && pending == 0 && !exhausted;
+        unsigned mask = __ballot_sync(0xffffffffu, need);
+        unsigned base = 0;
+        if (mask) {
+            if (lane == 0) base = atomicAdd(cursor, (unsigned)__popc(mask));
+            base = __shfl_sync(0xffffffffu, base, 0);
+        }
+        if (need) {
+            unsigned idx = base + __popc(mask & ((1u << lane) - 1u));
+            if (idx < npix) {
+                x = (int)(idx % (unsigned)cam.width);
+                y = (int)(idx / (unsigned)cam.width);
+                pending = camera_ray(S, cam, x, y, org, dir0);
+                first = true;
+                if (!pending) A.pmarch[idx].m = make_int4(x, y, -1, 0);
+            } else {
+                exhausted = true;
+            }
+        }
+        if (!have && pending) {
+            part = __ffsll((long long)pending) - 1;
+            pending &= pending - 1;
+            c.prim++;
+            c.seg++;
+            TraceIn in;
+            in.org = org;
+            in.dir = dir0;
+            in.t = 0.0f;
+            in.tmax = FLT_MAX;
+            in.part = part;
+            V3 dir;
+            float ray_t0, tEntry, tExitVolume;
+            sec_clip(S, in, dir, ray_t0, ray_t, tEntry, tExitVolume);
+            surface = false;
+            hit_n = v3(0, 0, 0);
+            hit_c = v3(0, 0, 0);
+            float hit_t = 0.f;
+            int vid = -1;
+            for (int m = 0; m < S.n_vol; m++) {
+                const DevVolume &vv = S.vol[m];
+                for (int k = 0; k < vv.n_slices; k++) {
+                    float4 pl = vv.slices[k];
+                    V3 pn = v3(pl.x, pl.y, pl.z);
+                    float denom = dot(dir, pn);
+                    if (fabsf(denom) > 0.0001f) {
+                        float t = (pl.w - dot(org, pn)) / denom;
+                        if (t >= ray_t0 && t <= ray_t) {
+                            hit_n = denom > 0 ? neg(pn) : pn;
+                            hit_t = t;
+                            vid = m;
+                            ray_t = t;
+                            surface = true;
+                        }
+                    }
+                }
+            }
+            if (surface) hit_c = tf_color(tfs[vid], vol_sample(S.vol[vid], org + hit_t * dir));
+            done = trav_init(S, T, org, dir, ray_t0, ray_t);
+            have = true;
+        }
+        if (!__any_sync(0xffffffffu, have || pending != 0 || !exhausted)) break;
+#pragma unroll 1
+        for (int k = 0; k < 4 && have && !done; k++)
+            done = trav_step(S, T, stack, st.nodes, st.tris, st.sphs, st.ovf);
+        bool fin = have && done;
+        if (fin && T.found) {
+            ray_t = T.h.t;
+            surface = true;
+            geometry_shade(S, T.h, T.org, T.dir, hit_n, hit_c);
+        }
+        if (__any_sync(0xffffffffu, fin)) {
+            bool extra = fin && !first;
+            unsigned idx = (unsigned)y * (unsigned)cam.width + (unsigned)x;
+            if (__any_sync(0xffffffffu, extra)) {
+                unsigned e = warp_reserve(extra ? 1u : 0u, A.pmarch_count + 3, A.pmarch_cap - npix, c.ovf);
+                unsigned got = __ballot_sync(0xffffffffu, extra && e != 0xffffffffu);
+                if (lane == 0 && got) atomicAdd(A.pmarch_count, (unsigned)__popc(got));
+                if (extra) idx = e == 0xffffffffu ? e : npix + e;
+            }
+            if (fin && idx != 0xffffffffu) {
+                first = false;
+                DRay *r = A.pmarch + idx;
+                r->o = make_float4(org.x, org.y, org.z, 0.0f);
+                r->d = make_float4(dir0.x, dir0.y, dir0.z, FLT_MAX);
+                r->c = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                r->m = make_int4(x, y, make_meta(GXY_RAY_PRIMARY | (surface ? 8 : 0), part, 0), __float_as_int(ray_t));
+                A.pmarch_hit[2 * (size_t)idx] = make_float4(hit_n.x, hit_n.y, hit_n.z, hit_c.x);
+                A.pmarch_hit[2 * (size_t)idx + 1] = make_float4(hit_c.y, hit_c.z, 0.0f, 0.0f);
+            }
+        }
+        if (fin) have = false;
+    }
+    flush_counters(A.ctr, c, st);
+}
+
 // March pass of split primary tracing with per-lane refill: composite the
 // volume up to the query pass's stop distance, then shade (ambient, AO spawn,
 // diffuse, shadow spawn), classify, route and accumulate as primary_ray does.
@@ -1180,26 +1305,32 @@ __global__ void __launch_bounds__(kThreads, MINB) k_prim_march(DevScene S, Frame
     int x = 0, y = 0, job = 0;
     bool have = false;
     for (;;) {
+        // fetch until every idle lane holds a record or the records are used
+        // up; hole records (meta -1, pixels with no brick) are passed over
         bool need = !have;
-        unsigned mask = __ballot_sync(0xffffffffu, need);
-        unsigned base = 0;
-        if (mask) {
+        while (__any_sync(0xffffffffu, need)) {
+            unsigned mask = __ballot_sync(0xffffffffu, need);
+            unsigned base = 0;
             if (lane == 0) base = atomicAdd(cursor, (unsigned)__popc(mask));
             base = __shfl_sync(0xffffffffu, base, 0);
-        }
-        if (need) {
-            unsigned idx = base + __popc(mask & ((1u << lane) - 1u));
-            if (idx < n) {
-                load_ray(A.pmarch, idx, in, x, y, job);
-                int4 m = __ldg(reinterpret_cast<const int4 *>(A.pmarch + idx) + 3);
-                float4 h0 = __ldg(A.pmarch_hit + 2 * (size_t)idx), h1 = __ldg(A.pmarch_hit + 2 * (size_t)idx + 1);
-                hn = v3(h0.x, h0.y, h0.z);
-                hc = v3(h0.w, h1.x, h1.y);
-                bool surface = (in.type & 8) != 0;
-                in.type &= 7;
-                sec_march_init(S, in, __int_as_float(m.w), surface, M);
-                have = true;
-                c.march++;
+            if (need) {
+                unsigned idx = base + __popc(mask & ((1u << lane) - 1u));
+                need = false;
+                int4 m = make_int4(0, 0, -1, 0);
+                if (idx < n) m = __ldg(reinterpret_cast<const int4 *>(A.pmarch + idx) + 3);
+                if (idx < n && m.z < 0) {
+                    need = true;
+                } else if (idx < n) {
+                    load_ray(A.pmarch, idx, in, x, y, job);
+                    float4 h0 = __ldg(A.pmarch_hit + 2 * (size_t)idx), h1 = __ldg(A.pmarch_hit + 2 * (size_t)idx + 1);
+                    hn = v3(h0.x, h0.y, h0.z);
+                    hc = v3(h0.w, h1.x, h1.y);
+                    bool surface = (in.type & 8) != 0;
+                    in.type &= 7;
+                    sec_march_init(S, in, __int_as_float(m.w), surface, M);
+                    have = true;
+                    c.march++;
+                }
             }
         }
         if (!__any_sync(0xffffffffu, have)) break;
@@ -1591,7 +1722,7 @@ static int render(Scene *sc, const gxy_camera &cam, const gxy_lighting &lt, floa
     A.split_prim = (split_eligible(S) && g_tune_split_prim) ? 1 : 0;
     A.pmarch = sc->pmarch;
     A.pmarch_hit = sc->pmarch_hit;
-    A.pmarch_count = sc->qcount + 8;    // [0] records, [1] cursor
+    A.pmarch_count = sc->qcount + 8;    // [0] records, [1] march cursor, [2] camera query cursor, [3] extra slots
     A.pmarch_cap = (unsigned)sc->pmarch_cap;
     for (int k = 0; k < 3; k++) A.qcap[k] = (unsigned)sc->qcap[k];
     struct LaunchRec { int gen, kind; unsigned rays_in; };
@@ -1603,16 +1734,18 @@ static int render(Scene *sc, const gxy_camera &cam, const gxy_lighting &lt, floa
         unsigned g = grid_for(items);
         if (sc->profile) CK(cudaEventRecord(sc->events[2 * nl], st));
         if (kind == K_SECONDARY && A.split) CK(cudaMemsetAsync(A.qmarch_count, 0, 3 * sizeof(unsigned), st));
-        if (kind == K_CAMERA && A.split_prim) CK(cudaMemsetAsync(A.pmarch_count, 0, 2 * sizeof(unsigned), st));
+        if (kind == K_CAMERA && A.split_prim) CK(cudaMemsetAsync(A.pmarch_count, 0, 4 * sizeof(unsigned), st));
         if (g_tune_minb == 3) {
-            if (kind == K_CAMERA) k_primary<K_CAMERA, 3><<<g, kThreads, 0, st>>>(S, A);
+            if (kind == K_CAMERA && A.split_prim) k_cam_query<3><<<march_grid(3), kThreads, 0, st>>>(S, A);
+            else if (kind == K_CAMERA) k_primary<K_CAMERA, 3><<<g, kThreads, 0, st>>>(S, A);
             else if (kind == K_PRIMARY) k_primary<K_PRIMARY, 3><<<g, kThreads, 0, st>>>(S, A);
             else if (kind == K_SECONDARY && A.split) k_sec_query<false, 3><<<march_grid(3), kThreads, 0, st>>>(S, A);
             else if (kind == K_SECONDARY) k_secondary<3><<<g, kThreads, 0, st>>>(S, A);
             else if (kind == K_PMARCH) k_prim_march<false, 3><<<march_grid(3), kThreads, 0, st>>>(S, A);
             else k_sec_march<false, 3><<<march_grid(3), kThreads, 0, st>>>(S, A);
         } else {
-            if (kind == K_CAMERA) k_primary<K_CAMERA, 2><<<g, kThreads, 0, st>>>(S, A);
+            if (kind == K_CAMERA && A.split_prim) k_cam_query<2><<<march_grid(2), kThreads, 0, st>>>(S, A);
+            else if (kind == K_CAMERA) k_primary<K_CAMERA, 2><<<g, kThreads, 0, st>>>(S, A);
             else if (kind == K_PRIMARY) k_primary<K_PRIMARY, 2><<<g, kThreads, 0, st>>>(S, A);
             else if (kind == K_SECONDARY && A.split) k_sec_query<false, 2><<<march_grid(2), kThreads, 0, st>>>(S, A);
             else if (kind == K_SECONDARY) k_secondary<2><<<g, kThreads, 0, st>>>(S, A);
