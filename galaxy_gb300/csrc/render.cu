@@ -212,6 +212,10 @@ struct Scene {
     int profile = 0;
     std::vector<gxy_generation_stats> gens;
     std::vector<cudaEvent_t> events;
+    // continuing primaries of a generation run on `side`, beside the
+    // shadow/AO passes of the same generation (fork/join events)
+    cudaStream_t side = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
     std::mutex mu;                      // one render at a time per scene
     ~Scene() {
         for (void *p : owned) arena().free(p);
@@ -224,6 +228,9 @@ struct Scene {
         arena().free(ctr);
         arena().free(fbtmp);
         for (cudaEvent_t e : events) cudaEventDestroy(e);
+        if (fork) cudaEventDestroy(fork);
+        if (join) cudaEventDestroy(join);
+        if (side) cudaStreamDestroy(side);
         if (bvh.nodes_ptr) arena().free(bvh.nodes_ptr);
         if (bvh.slots_ptr) arena().free(bvh.slots_ptr);
     }
@@ -1728,7 +1735,12 @@ static int render(Scene *sc, const gxy_camera &cam, const gxy_lighting &lt, floa
     struct LaunchRec { int gen, kind; unsigned rays_in; };
     std::vector<LaunchRec> recs;
     int nl = 0;
-    auto launch = [&](int kind, int gen, unsigned rays_in, int64_t items) -> int {
+    if (!sc->side) {
+        CK(cudaStreamCreateWithFlags(&sc->side, cudaStreamNonBlocking));
+        CK(cudaEventCreateWithFlags(&sc->fork, cudaEventDisableTiming));
+        CK(cudaEventCreateWithFlags(&sc->join, cudaEventDisableTiming));
+    }
+    auto launch = [&](int kind, int gen, unsigned rays_in, int64_t items, cudaStream_t st) -> int {
         if (nl >= maxl) return set_error(GXY_ERR_TIMEOUT, "too many launches in one frame");
         A.ctr = sc->ctr + nl;
         unsigned g = grid_for(items);
@@ -1761,8 +1773,8 @@ static int render(Scene *sc, const gxy_camera &cam, const gxy_lighting &lt, floa
     int cur = 0;   // queue set written by the last generation
     for (int k = 0; k < 3; k++) A.qout[k] = sc->q[cur][k];
     A.qout_count = sc->qcount + 3 * cur;
-    if ((rc = launch(K_CAMERA, 0, 0, npix))) return rc;
-    if (A.split_prim && (rc = launch(K_PMARCH, 0, 0, 1 << 30))) return rc;
+    if ((rc = launch(K_CAMERA, 0, 0, npix, st))) return rc;
+    if (A.split_prim && (rc = launch(K_PMARCH, 0, 0, 1 << 30, st))) return rc;
     A.split_prim = 0;   // later generations trace handed-off primaries in one pass
     int gen = 1;
     for (;;) {
@@ -1780,11 +1792,22 @@ static int render(Scene *sc, const gxy_camera &cam, const gxy_lighting &lt, floa
             A.qout[k] = sc->q[nxt][k];
         }
         A.qout_count = sc->qcount + 3 * nxt;
-        if (n[Q_PRIM] && (rc = launch(K_PRIMARY, gen, n[Q_PRIM], n[Q_PRIM]))) return rc;
-        if (n[Q_SHADOW] + n[Q_AO] &&
-            (rc = launch(K_SECONDARY, gen, n[Q_SHADOW] + n[Q_AO], (int64_t)n[Q_SHADOW] + n[Q_AO])))
+        // Continuing primaries and shadow/AO rays of one generation are
+        // independent (both only append to the next generation's queues), so
+        // the primaries, whose launch is bound by its longest march, run on
+        // the side stream beside the shadow/AO passes.
+        const bool sec = n[Q_SHADOW] + n[Q_AO] != 0;
+        const bool overlap = n[Q_PRIM] && sec;
+        if (overlap) {
+            CK(cudaEventRecord(sc->fork, st));
+            CK(cudaStreamWaitEvent(sc->side, sc->fork, 0));
+        }
+        if (n[Q_PRIM] && (rc = launch(K_PRIMARY, gen, n[Q_PRIM], n[Q_PRIM], overlap ? sc->side : st))) return rc;
+        if (overlap) CK(cudaEventRecord(sc->join, sc->side));
+        if (sec && (rc = launch(K_SECONDARY, gen, n[Q_SHADOW] + n[Q_AO], (int64_t)n[Q_SHADOW] + n[Q_AO], st)))
             return rc;
-        if (n[Q_SHADOW] + n[Q_AO] && A.split && (rc = launch(K_MARCH, gen, 0, 1 << 30))) return rc;
+        if (sec && A.split && (rc = launch(K_MARCH, gen, 0, 1 << 30, st))) return rc;
+        if (overlap) CK(cudaStreamWaitEvent(st, sc->join, 0));
         cur = nxt;
         gen++;
     }
