@@ -338,11 +338,86 @@ struct GeoHit {
     uint32_t prim;   // global primitive id (with kSphereBit for spheres)
 };
 
-// Exact float value of the low (hi = 0) or high (hi = 1) 16-bit field of w:
-// the field placed in the mantissa of 2^23 (bits 0x4B000000 | q) minus 2^23.
-// Two full-rate instructions instead of an integer-to-float conversion.
-__device__ __forceinline__ float q16f(uint32_t w, int hi) {
-    return __uint_as_float(__byte_perm(w, 0x4B000000u, hi ? 0x7632 : 0x7610)) - 8388608.0f;
+// Packed pairs of floats (element 0 in the low word) for the f32x2
+// arithmetic of sm_100-family GPUs: one instruction does two element-wise
+// round-to-nearest operations.
+__device__ __forceinline__ uint64_t f2pack(uint32_t lo, uint32_t hi) { return ((uint64_t)hi << 32) | lo; }
+__device__ __forceinline__ uint64_t f2dup(float a) { return f2pack(__float_as_uint(a), __float_as_uint(a)); }
+__device__ __forceinline__ float f2get(uint64_t v, int h) {
+    return __uint_as_float(h ? (uint32_t)(v >> 32) : (uint32_t)v);
+}
+__device__ __forceinline__ uint64_t f2add(uint64_t a, uint64_t b) {
+    uint64_t d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ uint64_t f2fma(uint64_t a, uint64_t b, uint64_t c) {
+    uint64_t d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+// Both 16-bit fields of w as exact floats, packed: each field placed in the
+// mantissa of 2^23 (bits 0x4B000000 | q) minus 2^23 -- full-rate byte
+// permutes and one packed add instead of integer-to-float conversions.
+__device__ __forceinline__ uint64_t q16x2(uint32_t w) {
+    return f2add(f2pack(__byte_perm(w, 0x4B000000u, 0x7610), __byte_perm(w, 0x4B000000u, 0x7632)),
+                 0xCB000000CB000000ull);   // - 2^23 in both halves
+}
+__device__ __forceinline__ float max3f(float a, float b, float c) {
+    float d;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+__device__ __forceinline__ float min3f(float a, float b, float c) {
+    float d;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+
+// Slab test of the 8 quantised child boxes of one BVH8 node (first two
+// 16-byte words n0, n1 and the 96 bytes of planes q) for a ray with origin
+// org and reciprocal direction (idx, idy, idz) over [t0, tmax].  A plane at
+// quantised position k lies at origin + k * 2^e, so its distance is
+// k * (2^e * id) + (origin - org) * id, one fused multiply-add.  The two
+// children of a slot pair share each 32-bit plane word, so a pair is decoded
+// and tested with packed f32x2 operations (the same round-to-nearest FMA per
+// child).  Outputs: key[i] = entry distance (low 3 bits replaced by the slot)
+// of a hit inner child, else 0xffffffff; leafhits = mask of hit leaf slots.
+__device__ __forceinline__ void node_children(float4 n0, float4 n1, const uint4 *q, V3 org, float idx, float idy,
+                                              float idz, float t0, float tmax, uint32_t key[8], int &n_inner,
+                                              uint32_t &leafhits) {
+    const uint32_t *W = &q[0].x;   // lo x, y, z planes: words 0-11; hi planes: words 12-23
+    const bool sx = idx < 0.0f, sy = idy < 0.0f, sz = idz < 0.0f;
+    const uint32_t e4 = __float_as_uint(n1.y);
+    const uint32_t meta_lo = __float_as_uint(n1.z), meta_hi = __float_as_uint(n1.w);
+    const float scx = __uint_as_float((e4 & 0xffu) << 23);
+    const float scy = __uint_as_float(((e4 >> 8) & 0xffu) << 23);
+    const float scz = __uint_as_float(((e4 >> 16) & 0xffu) << 23);
+    const uint32_t imask = e4 >> 24;
+    const uint64_t Ax = f2dup(scx * idx), Bx = f2dup((n0.x - org.x) * idx);
+    const uint64_t Ay = f2dup(scy * idy), By = f2dup((n0.y - org.y) * idy);
+    const uint64_t Az = f2dup(scz * idz), Bz = f2dup((n0.z - org.z) * idz);
+    leafhits = 0;
+    n_inner = 0;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        const uint32_t lx = W[k], ly = W[4 + k], lz = W[8 + k], hx = W[12 + k], hy = W[16 + k], hz = W[20 + k];
+        const uint64_t txa = f2fma(q16x2(sx ? hx : lx), Ax, Bx), txb = f2fma(q16x2(sx ? lx : hx), Ax, Bx);
+        const uint64_t tya = f2fma(q16x2(sy ? hy : ly), Ay, By), tyb = f2fma(q16x2(sy ? ly : hy), Ay, By);
+        const uint64_t tza = f2fma(q16x2(sz ? hz : lz), Az, Bz), tzb = f2fma(q16x2(sz ? lz : hz), Az, Bz);
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            const int i = 2 * k + h;
+            const uint32_t mb = (i < 4 ? meta_lo >> (8 * i) : meta_hi >> (8 * (i - 4))) & 0xffu;
+            float tn = fmaxf(max3f(f2get(txa, h), f2get(tya, h), f2get(tza, h)), t0);
+            float tf = fminf(min3f(f2get(txb, h), f2get(tyb, h), f2get(tzb, h)), tmax);
+            bool hit = mb != 0xffu && tn <= tf * 1.00000048f + 1e-30f;
+            bool inner = hit && ((imask >> i) & 1u);
+            key[i] = inner ? ((__float_as_uint(tn) & ~7u) | (uint32_t)i) : 0xffffffffu;
+            n_inner += inner ? 1 : 0;
+            if (hit && !((imask >> i) & 1u)) leafhits |= 1u << i;
+        }
+    }
 }
 
 // 32-bit compare-exchange for the sorting network below.
@@ -366,7 +441,6 @@ __device__ __noinline__ bool bvh_closest(const DevScene &S, V3 org, V3 dir, floa
                                          unsigned &nodes, unsigned &tris, unsigned &sphs, int &ovf) {
     if (!S.nodes) return false;
     const float idx = 1.0f / dir.x, idy = 1.0f / dir.y, idz = 1.0f / dir.z;
-    const bool sx = idx < 0.0f, sy = idy < 0.0f, sz = idz < 0.0f;
     h.t = tfar;
     h.prim = 0xffffffffu;
     bool found = false;
@@ -380,45 +454,15 @@ __device__ __noinline__ bool bvh_closest(const DevScene &S, V3 org, V3 dir, floa
             float4 n0 = __ldg(np), n1 = __ldg(np + 1);
             uint32_t child_base = __float_as_uint(n0.w);
             uint32_t prim_base = __float_as_uint(n1.x);
-            uint32_t e4 = __float_as_uint(n1.y);
             uint32_t meta_lo = __float_as_uint(n1.z), meta_hi = __float_as_uint(n1.w);
             uint4 q[6];
 #pragma unroll
             for (int k = 0; k < 6; k++) q[k] = __ldg(reinterpret_cast<const uint4 *>(np + 2 + k));
             nodes++;
-            float scx = __uint_as_float((e4 & 0xffu) << 23);
-            float scy = __uint_as_float(((e4 >> 8) & 0xffu) << 23);
-            float scz = __uint_as_float(((e4 >> 16) & 0xffu) << 23);
-            uint32_t imask = e4 >> 24;
-            // t = (origin + q*s - org) * id = q*(s*id) + (origin-org)*id
-            float ax = scx * idx, bx = (n0.x - org.x) * idx;
-            float ay = scy * idy, by = (n0.y - org.y) * idy;
-            float az = scz * idz, bz = (n0.z - org.z) * idz;
             uint32_t key[8];
-            uint32_t leafhits = 0;
-            int n_inner = 0;
-#pragma unroll
-            for (int i = 0; i < 8; i++) {
-                uint32_t mb = (i < 4 ? meta_lo >> (8 * i) : meta_hi >> (8 * (i - 4))) & 0xffu;
-                // 16-bit planes: qlo axis a at q[a*... ] -- word (a*8+i)/2 of 48 bytes, then qhi at +24 words
-                uint32_t wl0 = (&q[0].x)[(0 * 8 + i) >> 1], wl1 = (&q[0].x)[(1 * 8 + i) >> 1],
-                         wl2 = (&q[0].x)[(2 * 8 + i) >> 1];
-                uint32_t wh0 = (&q[0].x)[(24 + 0 * 8 + i) >> 1], wh1 = (&q[0].x)[(24 + 1 * 8 + i) >> 1],
-                         wh2 = (&q[0].x)[(24 + 2 * 8 + i) >> 1];
-                const int hi16 = i & 1;
-                float lx = q16f(wl0, hi16), ly = q16f(wl1, hi16), lz = q16f(wl2, hi16);
-                float hx = q16f(wh0, hi16), hy = q16f(wh1, hi16), hz = q16f(wh2, hi16);
-                float txa = __fmaf_rn(sx ? hx : lx, ax, bx), txb = __fmaf_rn(sx ? lx : hx, ax, bx);
-                float tya = __fmaf_rn(sy ? hy : ly, ay, by), tyb = __fmaf_rn(sy ? ly : hy, ay, by);
-                float tza = __fmaf_rn(sz ? hz : lz, az, bz), tzb = __fmaf_rn(sz ? lz : hz, az, bz);
-                float tn = fmaxf(fmaxf(txa, tya), fmaxf(tza, t0));
-                float tf = fminf(fminf(txb, tyb), fminf(tzb, h.t));
-                bool hit = mb != 0xffu && tn <= tf * 1.00000048f + 1e-30f;
-                bool inner = hit && ((imask >> i) & 1u);
-                key[i] = inner ? ((__float_as_uint(tn) & ~7u) | (uint32_t)i) : 0xffffffffu;
-                n_inner += inner ? 1 : 0;
-                if (hit && !((imask >> i) & 1u)) leafhits |= 1u << i;
-            }
+            uint32_t leafhits;
+            int n_inner;
+            node_children(n0, n1, q, org, idx, idy, idz, t0, h.t, key, n_inner, leafhits);
             while (leafhits) {
                 int i = __ffs(leafhits) - 1;
                 leafhits &= leafhits - 1;
@@ -523,47 +567,19 @@ __device__ __forceinline__ bool trav_step(const DevScene &S, TravState &T, uint2
     }
     const V3 org = T.org, dir = T.dir;
     const float idx = T.idx, idy = T.idy, idz = T.idz, t0 = T.t0, tfar = T.tfar;
-    const bool sx = idx < 0.0f, sy = idy < 0.0f, sz = idz < 0.0f;
     const float4 *np = reinterpret_cast<const float4 *>(S.nodes + T.cur);
     float4 n0 = __ldg(np), n1 = __ldg(np + 1);
     uint32_t child_base = __float_as_uint(n0.w);
     uint32_t prim_base = __float_as_uint(n1.x);
-    uint32_t e4 = __float_as_uint(n1.y);
     uint32_t meta_lo = __float_as_uint(n1.z), meta_hi = __float_as_uint(n1.w);
     uint4 q[6];
 #pragma unroll
     for (int k = 0; k < 6; k++) q[k] = __ldg(reinterpret_cast<const uint4 *>(np + 2 + k));
     nodes++;
-    float scx = __uint_as_float((e4 & 0xffu) << 23);
-    float scy = __uint_as_float(((e4 >> 8) & 0xffu) << 23);
-    float scz = __uint_as_float(((e4 >> 16) & 0xffu) << 23);
-    uint32_t imask = e4 >> 24;
-    float ax = scx * idx, bx = (n0.x - org.x) * idx;
-    float ay = scy * idy, by = (n0.y - org.y) * idy;
-    float az = scz * idz, bz = (n0.z - org.z) * idz;
     uint32_t key[8];
-    uint32_t leafhits = 0;
-    int n_inner = 0;
-#pragma unroll
-    for (int i = 0; i < 8; i++) {
-        uint32_t mb = (i < 4 ? meta_lo >> (8 * i) : meta_hi >> (8 * (i - 4))) & 0xffu;
-        uint32_t wl0 = (&q[0].x)[(0 * 8 + i) >> 1], wl1 = (&q[0].x)[(1 * 8 + i) >> 1], wl2 = (&q[0].x)[(2 * 8 + i) >> 1];
-        uint32_t wh0 = (&q[0].x)[(24 + 0 * 8 + i) >> 1], wh1 = (&q[0].x)[(24 + 1 * 8 + i) >> 1],
-                 wh2 = (&q[0].x)[(24 + 2 * 8 + i) >> 1];
-        const int hi16 = i & 1;
-        float lx = q16f(wl0, hi16), ly = q16f(wl1, hi16), lz = q16f(wl2, hi16);
-        float hx = q16f(wh0, hi16), hy = q16f(wh1, hi16), hz = q16f(wh2, hi16);
-        float txa = __fmaf_rn(sx ? hx : lx, ax, bx), txb = __fmaf_rn(sx ? lx : hx, ax, bx);
-        float tya = __fmaf_rn(sy ? hy : ly, ay, by), tyb = __fmaf_rn(sy ? ly : hy, ay, by);
-        float tza = __fmaf_rn(sz ? hz : lz, az, bz), tzb = __fmaf_rn(sz ? lz : hz, az, bz);
-        float tn = fmaxf(fmaxf(txa, tya), fmaxf(tza, t0));
-        float tf = fminf(fminf(txb, tyb), fminf(tzb, T.h.t));
-        bool hit = mb != 0xffu && tn <= tf * 1.00000048f + 1e-30f;
-        bool inner = hit && ((imask >> i) & 1u);
-        key[i] = inner ? ((__float_as_uint(tn) & ~7u) | (uint32_t)i) : 0xffffffffu;
-        n_inner += inner ? 1 : 0;
-        if (hit && !((imask >> i) & 1u)) leafhits |= 1u << i;
-    }
+    uint32_t leafhits;
+    int n_inner;
+    node_children(n0, n1, q, org, idx, idy, idz, t0, T.h.t, key, n_inner, leafhits);
     while (leafhits) {
         int i = __ffs(leafhits) - 1;
         leafhits &= leafhits - 1;

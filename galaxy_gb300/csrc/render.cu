@@ -1134,7 +1134,8 @@ __global__ void __launch_bounds__(kThreads, MINB) k_sec_query(DevScene S, FrameA
                     }
                 }
                 zero = in.r == 0.0f && in.g == 0.0f && in.b == 0.0f && in.o == 0.0f;
-                done = trav_init(S, T, in.org, dir, ray_t0, in.tmax);
+                // a zero payload is culled whatever the query finds: no traversal
+                done = zero || trav_init(S, T, in.org, dir, ray_t0, in.tmax);
                 have = true;
             }
         }
@@ -1146,7 +1147,7 @@ __global__ void __launch_bounds__(kThreads, MINB) k_sec_query(DevScene S, FrameA
         bool fin = have && done;
         bool to_march = false;
         if (fin) {
-            bool h = T.found;
+            bool h = !zero && T.found;
             if (h && T.h.t < ray_t) {
                 ray_t = T.h.t;
                 surface = true;

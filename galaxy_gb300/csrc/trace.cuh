@@ -104,7 +104,7 @@ __device__ __noinline__ void geometry_shade(const DevScene &S, const GeoHit &gh,
 //     no isosurface anywhere ahead, every brick the ray would cross finds no
 //     surface and the ray is eventually dropped -- it is culled before the
 //     march.  A ray whose payload is exactly zero adds nothing wherever it
-//     ends and is culled after its query.  Culling never changes a pixel.
+//     ends and is culled before its query.  Culling never changes a pixel.
 // SECONDARY: the caller guarantees a shadow/AO ray (no shading code).
 template <bool FRAME, bool SECONDARY>
 __device__ __forceinline__ TraceOut trace_core(const DevScene &S, const DevTF *tfs, const TraceIn &R, RayStats &st) {
@@ -175,14 +175,18 @@ __device__ __forceinline__ TraceOut trace_core(const DevScene &S, const DevTF *t
             surface_hit = true;
         }
     } else if (FRAME && !shade) {
+        bool zero = R.r == 0.0f && R.g == 0.0f && R.b == 0.0f && R.o == 0.0f;
+        if (zero) {   // culled whatever the query finds: skip the query
+            out.cull = true;
+            return out;
+        }
         GeoHit gh;
         bool h = bvh_closest<false>(S, org, dir, ray_t0, R.tmax, gh, st.nodes, st.tris, st.sphs, st.ovf);
         if (h && gh.t < ray_t) {
             ray_t = gh.t;
             surface_hit = true;
         }
-        bool zero = R.r == 0.0f && R.g == 0.0f && R.b == 0.0f && R.o == 0.0f;
-        if (zero || (!h && !surface_hit && !slice_ahead && !S.has_iso)) {
+        if (!h && !surface_hit && !slice_ahead && !S.has_iso) {
             out.cull = true;
             return out;
         }
@@ -451,13 +455,14 @@ __device__ __forceinline__ SecQuery sec_query(const DevScene &S, const TraceIn &
             }
         }
     }
+    // a zero payload is culled whatever the query finds: skip the query
+    bool zero = R.r == 0.0f && R.g == 0.0f && R.b == 0.0f && R.o == 0.0f;
     GeoHit gh;
-    bool h = bvh_closest<false>(S, org, dir, ray_t0, R.tmax, gh, st.nodes, st.tris, st.sphs, st.ovf);
+    bool h = !zero && bvh_closest<false>(S, org, dir, ray_t0, R.tmax, gh, st.nodes, st.tris, st.sphs, st.ovf);
     if (h && gh.t < ray_t) {
         ray_t = gh.t;
         surface_hit = true;
     }
-    bool zero = R.r == 0.0f && R.g == 0.0f && R.b == 0.0f && R.o == 0.0f;
     q.cull = zero || (!h && !surface_hit && !slice_ahead && !S.has_iso);
     q.t_term = ray_t;
     q.surface = surface_hit;
