@@ -582,6 +582,7 @@ struct FrameArgs {
     long long total_pix;
     const DRay *qin[NQ];
     unsigned nin[NQ];
+    const unsigned *nin_dev;           // batch split passes: input queue counts in device memory
     DRay *qout[NQ];
     unsigned *qout_count;              // NQ counters
     unsigned qcap[NQ];
@@ -595,7 +596,7 @@ struct FrameArgs {
     int split_prim;
     DRay *pmarch;
     float4 *pmarch_hit;                // 2 per record: (n, c.x), (c.y, c.z, -, -)
-    unsigned *pmarch_count;            // [0] records, [1] fetch cursor, [2] camera query cursor
+    unsigned *pmarch_count;            // [0] records, [1] fetch cursor, [2] camera query cursor, [3] extras
     unsigned pmarch_cap;
 };
 
@@ -1052,8 +1053,9 @@ __global__ void __launch_bounds__(kThreads) k_wavefront(DevScene Su, FrameArgs A
 // Per-generation batch kernel (no grid barrier, so batches on different
 // streams run concurrently): generation g reads the queue counts that
 // generation g-1 left in device memory (counts + 3*(g-1)) and appends to
-// counts + 3*g.  KIND: K_CAMERA (all jobs' pixels) or K_SECONDARY, which
-// here takes the primary, shadow and AO queues in one index space.
+// counts + 3*g.  KIND: K_CAMERA (all jobs' pixels), K_SECONDARY, which
+// here takes the primary, shadow and AO queues in one index space, or
+// K_PRIMARY (the primary queue alone, beside the split shadow/AO passes).
 template <int KIND, bool USCENE, int MINB>
 __global__ void __launch_bounds__(kThreads, MINB) k_batch_gen(DevScene Su, FrameArgs A, const unsigned *cin) {
     __shared__ DevTF tfs[kMaxVol];
@@ -1072,6 +1074,7 @@ __global__ void __launch_bounds__(kThreads, MINB) k_batch_gen(DevScene Su, Frame
         for (int k = 0; k < NQ; k++) {
             unsigned v = __ldg(cin + k);
             n[k] = v > A.qcap[k] ? A.qcap[k] : v;
+            if (KIND == K_PRIMARY && k != Q_PRIM) n[k] = 0;   // primaries only
         }
         if (n[0] + n[1] + n[2] == 0) return;   // uniform over the grid: no barrier below is skipped partially
         queue_pass<true, USCENE>(Su, tfs, A, n, start, stride, st, c);
@@ -1090,8 +1093,8 @@ __global__ void __launch_bounds__(kThreads, MINB) k_sec_query(DevScene S, FrameA
     RayStats st;
     LocalCounters c;
     const int lane = threadIdx.x & 31;
-    const unsigned ns = A.nin[Q_SHADOW];
-    const unsigned n = ns + A.nin[Q_AO];
+    const unsigned ns = BATCH ? min(__ldg(A.nin_dev + Q_SHADOW), A.qcap[Q_SHADOW]) : A.nin[Q_SHADOW];
+    const unsigned n = ns + (BATCH ? min(__ldg(A.nin_dev + Q_AO), A.qcap[Q_AO]) : A.nin[Q_AO]);
     unsigned *cursor = A.qmarch_count + 2;
     TravState T;
     uint2 stack[64];
@@ -1172,8 +1175,8 @@ __global__ void __launch_bounds__(kThreads, MINB) k_sec_query(DevScene S, FrameA
     flush_counters(A.ctr, c, st);
 }
 
-// Query pass of split camera-ray tracing with per-lane refill (single-frame
-// path): a lane takes the next pixel from a device cursor, and for each brick
+// Query pass of split camera-ray tracing with per-lane refill: a lane takes
+// the next pixel (BATCH: of all jobs, job by binary search) from a device cursor, and for each brick
 // its camera ray enters first (Camera.cpp:431-441) clips to the brick, tests
 // the slices, then steps the resumable BVH8 traversal a few nodes at a time;
 // a finished query writes the same march record as the camera pass's split
@@ -1181,20 +1184,24 @@ __global__ void __launch_bounds__(kThreads, MINB) k_sec_query(DevScene S, FrameA
 // first record of pixel i goes to slot i and a pixel whose ray enters no
 // brick leaves a hole record (meta -1) there, so the march pass reads the
 // records in pixel order; further bricks of one pixel go after slot npix.
-template <int MINB>
+template <bool BATCH, int MINB>
 __global__ void __launch_bounds__(kThreads, MINB) k_cam_query(DevScene S, FrameArgs A) {
     __shared__ DevTF tfs[kMaxVol];
+    __shared__ long long pix0[BATCH ? kMaxJobs : 1];
+    if (BATCH)
+        for (int j = threadIdx.x; j < A.n_jobs; j += blockDim.x) pix0[j] = A.jobs[j].pix0;
     load_tfs(S, tfs);
     RayStats st;
     LocalCounters c;
     const int lane = threadIdx.x & 31;
-    const DevCamera &cam = A.job0.cam;
-    const unsigned npix = (unsigned)cam.width * (unsigned)cam.height;
+    const unsigned npix =
+        BATCH ? (unsigned)A.total_pix : (unsigned)A.job0.cam.width * (unsigned)A.job0.cam.height;
     unsigned *cursor = A.pmarch_count + 2;
     TravState T;
     uint2 stack[64];
     V3 org = v3(0, 0, 0), dir0 = v3(0, 0, 0), hit_n = v3(0, 0, 0), hit_c = v3(0, 0, 0);
-    int x = 0, y = 0, part = 0;
+    int x = 0, y = 0, part = 0, job = 0;
+    unsigned pix = 0;   // global pixel index (all jobs' pixels in job order)
     uint64_t pending = 0;
     float ray_t = 0.0f;
     bool have = false, done = false, surface = false, exhausted = false, first = false;
@@ -1210,8 +1217,15 @@ __global__ void __launch_bounds__(kThreads, MINB) k_cam_query(DevScene S, FrameA
         if (need) {
             unsigned idx = base + __popc(mask & ((1u << lane) - 1u));
             if (idx < npix) {
-                x = (int)(idx % (unsigned)cam.width);
-                y = (int)(idx / (unsigned)cam.width);
+                pix = idx;
+                unsigned li = idx;
+                if (BATCH) {
+                    job = find_job(pix0, A.n_jobs, idx);
+                    li = idx - (unsigned)pix0[job];
+                }
+                const DevCamera &cam = BATCH ? A.jobs[job].cam : A.job0.cam;
+                x = (int)(li % (unsigned)cam.width);
+                y = (int)(li / (unsigned)cam.width);
                 pending = camera_ray(S, cam, x, y, org, dir0);
                 first = true;
                 if (!pending) A.pmarch[idx].m = make_int4(x, y, -1, 0);
@@ -1272,7 +1286,7 @@ __global__ void __launch_bounds__(kThreads, MINB) k_cam_query(DevScene S, FrameA
         }
         if (__any_sync(0xffffffffu, fin)) {
             bool extra = fin && !first;
-            unsigned idx = (unsigned)y * (unsigned)cam.width + (unsigned)x;
+            unsigned idx = pix;
             if (__any_sync(0xffffffffu, extra)) {
                 unsigned e = warp_reserve(extra ? 1u : 0u, A.pmarch_count + 3, A.pmarch_cap - npix, c.ovf);
                 unsigned got = __ballot_sync(0xffffffffu, extra && e != 0xffffffffu);
@@ -1285,7 +1299,7 @@ __global__ void __launch_bounds__(kThreads, MINB) k_cam_query(DevScene S, FrameA
                 r->o = make_float4(org.x, org.y, org.z, 0.0f);
                 r->d = make_float4(dir0.x, dir0.y, dir0.z, FLT_MAX);
                 r->c = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-                r->m = make_int4(x, y, make_meta(GXY_RAY_PRIMARY | (surface ? 8 : 0), part, 0), __float_as_int(ray_t));
+                r->m = make_int4(x, y, make_meta(GXY_RAY_PRIMARY | (surface ? 8 : 0), part, job), __float_as_int(ray_t));
                 A.pmarch_hit[2 * (size_t)idx] = make_float4(hit_n.x, hit_n.y, hit_n.z, hit_c.x);
                 A.pmarch_hit[2 * (size_t)idx + 1] = make_float4(hit_c.y, hit_c.z, 0.0f, 0.0f);
             }
@@ -1643,6 +1657,16 @@ static unsigned march_grid(int minb) {
     return (unsigned)(sms * (per < 1 ? 1 : per));
 }
 
+// The refill query passes run at 4 resident blocks per SM when the tuning
+// asks for 3 (64 registers: more warps to cover node-fetch latency; measured
+// faster than 80 registers with fewer spills).
+static unsigned query_grid() {
+    int sms = 152, per = 1;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, g_device);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_sec_query<false, 4>, kThreads, 0);
+    return (unsigned)(sms * (per < 1 ? 1 : per));
+}
+
 static int ensure_queues(Scene *sc, const size_t need[3]) {
     size_t pneed = need[0];
     if (sc->pmarch_cap < pneed) {
@@ -1749,15 +1773,15 @@ static int render(Scene *sc, const gxy_camera &cam, const gxy_lighting &lt, floa
         if (kind == K_SECONDARY && A.split) CK(cudaMemsetAsync(A.qmarch_count, 0, 3 * sizeof(unsigned), st));
         if (kind == K_CAMERA && A.split_prim) CK(cudaMemsetAsync(A.pmarch_count, 0, 4 * sizeof(unsigned), st));
         if (g_tune_minb == 3) {
-            if (kind == K_CAMERA && A.split_prim) k_cam_query<3><<<march_grid(3), kThreads, 0, st>>>(S, A);
+            if (kind == K_CAMERA && A.split_prim) k_cam_query<false, 4><<<query_grid(), kThreads, 0, st>>>(S, A);
             else if (kind == K_CAMERA) k_primary<K_CAMERA, 3><<<g, kThreads, 0, st>>>(S, A);
             else if (kind == K_PRIMARY) k_primary<K_PRIMARY, 3><<<g, kThreads, 0, st>>>(S, A);
-            else if (kind == K_SECONDARY && A.split) k_sec_query<false, 3><<<march_grid(3), kThreads, 0, st>>>(S, A);
+            else if (kind == K_SECONDARY && A.split) k_sec_query<false, 4><<<query_grid(), kThreads, 0, st>>>(S, A);
             else if (kind == K_SECONDARY) k_secondary<3><<<g, kThreads, 0, st>>>(S, A);
             else if (kind == K_PMARCH) k_prim_march<false, 3><<<march_grid(3), kThreads, 0, st>>>(S, A);
             else k_sec_march<false, 3><<<march_grid(3), kThreads, 0, st>>>(S, A);
         } else {
-            if (kind == K_CAMERA && A.split_prim) k_cam_query<2><<<march_grid(2), kThreads, 0, st>>>(S, A);
+            if (kind == K_CAMERA && A.split_prim) k_cam_query<false, 2><<<march_grid(2), kThreads, 0, st>>>(S, A);
             else if (kind == K_CAMERA) k_primary<K_CAMERA, 2><<<g, kThreads, 0, st>>>(S, A);
             else if (kind == K_PRIMARY) k_primary<K_PRIMARY, 2><<<g, kThreads, 0, st>>>(S, A);
             else if (kind == K_SECONDARY && A.split) k_sec_query<false, 2><<<march_grid(2), kThreads, 0, st>>>(S, A);
@@ -2354,12 +2378,17 @@ struct Batch {
     unsigned *mcounts = nullptr;       // kBatchGens x 4: march records, march cursor (split path)
     DRay *qmarch = nullptr;
     size_t qmarch_cap = 0;
+    DRay *pmarch = nullptr;            // split camera rays (uniform-scene batches)
+    float4 *pmarch_hit = nullptr;
+    size_t pmarch_cap = 0;
     DevJob *d_jobs = nullptr;
     DevJob *h_jobs = nullptr;          // pinned
     DevCounters *ctr = nullptr;
     int *d_status = nullptr, *h_status = nullptr;   // pinned host copy of [gens, left]
     DevCounters *h_ctr = nullptr;                   // pinned
     cudaStream_t stream = nullptr;
+    cudaStream_t side = nullptr;       // continuing primaries beside the shadow/AO passes
+    cudaEvent_t fork[16] = {}, join[16] = {};   // per generation
     cudaEvent_t done = nullptr;
     cudaGraphExec_t gexec = nullptr;
     int grid = 0;
@@ -2375,6 +2404,12 @@ struct Batch {
         if (h_ctr) cudaFreeHost(h_ctr);
         if (gexec) cudaGraphExecDestroy(gexec);
         if (done) cudaEventDestroy(done);
+        for (int k = 0; k < 16; k++) {
+            if (fork[k]) cudaEventDestroy(fork[k]);
+            if (join[k]) cudaEventDestroy(join[k]);
+        }
+        if (side) cudaStreamSynchronize(side);
+        if (side) cudaStreamDestroy(side);
         if (stream) cudaStreamDestroy(stream);
     }
     int dalloc(void **p, size_t bytes) {
@@ -2417,6 +2452,62 @@ static int batch_enqueue(Batch *b, const DevScene &Su, bool uniform, const Frame
     CK(cudaMemsetAsync(b->counts, 0, (kBatchGens + 1) * NQ * sizeof(unsigned), st));
     CK(cudaMemsetAsync(b->mcounts, 0, (kBatchGens + 1) * 4 * sizeof(unsigned), st));
     CK(cudaMemsetAsync(b->ctr, 0, sizeof(DevCounters), st));
+    if (!cooperative && uniform && split_eligible(Su) && g_tune_split_prim) {
+        // Split passes as in a single frame: camera query + primary march,
+        // then per generation the continuing primaries (side stream) beside
+        // the shadow/AO query and march; counts are read on the device.
+        const int grid = gen_grid(true);
+        for (int g = 0; g < kBatchGens; g++) {
+            FrameArgs a = A;
+            for (int k = 0; k < NQ; k++) {
+                a.qin[k] = W.q[(g + 1) & 1][k];
+                a.qout[k] = W.q[g & 1][k];
+            }
+            a.qout_count = b->counts + NQ * g;
+            const unsigned *cin = g ? b->counts + NQ * (g - 1) : nullptr;
+            a.nin_dev = cin;
+            a.split = 1;
+            a.qmarch = b->qmarch;
+            a.qmarch_count = b->mcounts + 4 * g;
+            a.qmarch_cap = (unsigned)b->qmarch_cap;
+            a.split_prim = 1;
+            a.pmarch = b->pmarch;
+            a.pmarch_hit = b->pmarch_hit;
+            a.pmarch_count = b->mcounts + 4 * kBatchGens;
+            a.pmarch_cap = (unsigned)b->pmarch_cap;
+            const bool mb3 = g_tune_minb == 3;
+            if (g == 0) {
+                if (mb3) {
+                    k_cam_query<true, 4><<<query_grid(), kThreads, 0, st>>>(Su, a);
+                    k_prim_march<true, 3><<<march_grid(3), kThreads, 0, st>>>(Su, a);
+                } else {
+                    k_cam_query<true, 2><<<march_grid(2), kThreads, 0, st>>>(Su, a);
+                    k_prim_march<true, 2><<<march_grid(2), kThreads, 0, st>>>(Su, a);
+                }
+            } else {
+                CK(cudaEventRecord(b->fork[g], st));
+                CK(cudaStreamWaitEvent(b->side, b->fork[g], 0));
+                if (mb3) k_batch_gen<K_PRIMARY, true, 3><<<grid, kThreads, 0, b->side>>>(Su, a, cin);
+                else k_batch_gen<K_PRIMARY, true, 2><<<grid, kThreads, 0, b->side>>>(Su, a, cin);
+                CK(cudaEventRecord(b->join[g], b->side));
+                if (mb3) {
+                    k_sec_query<true, 4><<<query_grid(), kThreads, 0, st>>>(Su, a);
+                    k_sec_march<true, 3><<<march_grid(3), kThreads, 0, st>>>(Su, a);
+                } else {
+                    k_sec_query<true, 2><<<march_grid(2), kThreads, 0, st>>>(Su, a);
+                    k_sec_march<true, 2><<<march_grid(2), kThreads, 0, st>>>(Su, a);
+                }
+                CK(cudaStreamWaitEvent(st, b->join[g], 0));
+            }
+            CK(cudaGetLastError());
+        }
+        CK(cudaMemsetAsync(b->d_status, 0, 4 * sizeof(int), st));
+        CK(cudaMemcpyAsync(b->d_status + 2, b->counts + NQ * (kBatchGens - 1), NQ * sizeof(unsigned),
+                           cudaMemcpyDeviceToDevice, st));
+        CK(cudaMemcpyAsync(b->h_status, b->d_status, 4 * sizeof(int), cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(b->h_ctr, b->ctr, sizeof(DevCounters), cudaMemcpyDeviceToHost, st));
+        return GXY_OK;
+    }
     if (!cooperative) {
         const bool split = uniform && split_eligible(Su);
         // generation g reads counts[g-1], writes counts[g] and queue set g&1
@@ -2494,6 +2585,7 @@ int gxy_gpu_batch_create(int64_t max_pixels, int max_jobs, int max_shadow, int m
                        (size_t)max_pixels * max_ao + slack};
     size_t bytes = 0;
     for (int k = 0; k < NQ; k++) bytes += 2 * need[k] * sizeof(DRay);
+    bytes += (need[1] + need[2]) * sizeof(DRay) + need[0] * (sizeof(DRay) + 2 * sizeof(float4));   // march queues
     if (!arena().would_fit(bytes + 16 * 1024 * 1024))
         return set_error(GXY_ERR_ADMISSION, "batch queues (" + std::to_string(bytes) + " bytes) exceed the HBM budget");
     for (int k = 0; k < NQ; k++) {
@@ -2509,6 +2601,9 @@ int gxy_gpu_batch_create(int64_t max_pixels, int max_jobs, int max_shadow, int m
     if ((rc = b->dalloc((void **)&b->mcounts, (kBatchGens + 1) * 4 * sizeof(unsigned)))) return rc;
     b->qmarch_cap = need[1] + need[2];
     if ((rc = b->dalloc((void **)&b->qmarch, b->qmarch_cap * sizeof(DRay)))) return rc;
+    b->pmarch_cap = need[0];
+    if ((rc = b->dalloc((void **)&b->pmarch, b->pmarch_cap * sizeof(DRay)))) return rc;
+    if ((rc = b->dalloc((void **)&b->pmarch_hit, 2 * b->pmarch_cap * sizeof(float4)))) return rc;
     if ((rc = b->dalloc((void **)&b->d_jobs, max_jobs * sizeof(DevJob)))) return rc;
     if ((rc = b->dalloc((void **)&b->ctr, sizeof(DevCounters)))) return rc;
     if ((rc = b->dalloc((void **)&b->d_status, 8 * sizeof(int)))) return rc;
@@ -2516,7 +2611,12 @@ int gxy_gpu_batch_create(int64_t max_pixels, int max_jobs, int max_shadow, int m
     CK(cudaMallocHost((void **)&b->h_status, 8 * sizeof(int)));
     CK(cudaMallocHost((void **)&b->h_ctr, sizeof(DevCounters)));
     CK(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
+    CK(cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking));
     CK(cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming));
+    for (int k = 0; k < 16; k++) {
+        CK(cudaEventCreateWithFlags(&b->fork[k], cudaEventDisableTiming));
+        CK(cudaEventCreateWithFlags(&b->join[k], cudaEventDisableTiming));
+    }
     *out = reinterpret_cast<gxy_batch>(b.release());
     return GXY_OK;
     GUARD_END
