@@ -12,7 +12,8 @@
 //     starts from a binary node's two children and repeatedly opens the child
 //     with the largest surface area (the surface-area-heuristic greedy
 //     choice) until it has 8 children; subtrees of at most kLeafMax
-//     primitives become leaves.  Child boxes are quantised to 16 bits
+//     primitives (leaf_max(): 1-4, so 8 leaves fit the 5-bit primitive
+//     offset of a meta byte) become leaves.  Child boxes are quantised to 16 bits
 //     against a power-of-two grid so a node fills one 128-byte line.
 #include <cub/cub.cuh>
 
@@ -24,8 +25,6 @@
 #include "gxy_host.h"
 
 namespace gxy {
-
-constexpr int kLeafMax = 4;
 
 __device__ __forceinline__ void prim_box(const DevScene &S, uint32_t p, float3 &lo, float3 &hi) {
     if (p < S.n_tri) {
@@ -355,7 +354,8 @@ __device__ void write_slot(const DevScene &S, const float *sph_radius, uint32_t 
 __global__ void k_collapse(DevScene S, const float *sph_radius, int n, const int2 *qin, int nq, int2 *qout,
                            unsigned int *ctr, const int *left, const int *right, const int *first, const int *last,
                            const uint32_t *ids, const float4 *plo, const float4 *phi, const float4 *nlo,
-                           const float4 *nhi, BVH8Node *nodes, float4 *slots, int max_nodes, int max_slots) {
+                           const float4 *nhi, BVH8Node *nodes, float4 *slots, int max_nodes, int max_slots,
+                           int kLeafMax) {
     int w = blockIdx.x * blockDim.x + threadIdx.x;
     if (w >= nq) return;
     int2 item = qin[w];
@@ -546,7 +546,7 @@ int build_bvh8(DevScene &S, const float *sph_radius, DeviceArena &arena, cudaStr
         CK(cudaMemsetAsync(B.ctr + 2, 0, sizeof(unsigned int), st));
         k_collapse<<<blocks_for(nq, 128), 128, 0, st>>>(S, sph_radius, n, B.qa, nq, B.qb, B.ctr, B.left, B.right,
                                                         B.first, B.last, B.ids2, B.plo, B.phi, B.nlo, B.nhi, nodes,
-                                                        slots, max_nodes, max_slots);
+                                                        slots, max_nodes, max_slots, leaf_max());
         CK(cudaGetLastError());
         unsigned int hc[4];
         CK(cudaMemcpyAsync(hc, B.ctr, sizeof hc, cudaMemcpyDeviceToHost, st));

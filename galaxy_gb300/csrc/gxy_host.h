@@ -71,5 +71,7 @@ struct BVHInfo {
 int build_bvh8(DevScene &S, const float *sph_radius, DeviceArena &arena, cudaStream_t st, BVHInfo &info);
 // 1: binary tree by binned SAH along the Morton order; 0: radix-tree (LBVH) splits.
 bool sah_builder();
+// Largest subtree (primitives) stored as one leaf of a wide node, 1-4.
+int leaf_max();
 
 }  // namespace gxy

@@ -1631,6 +1631,8 @@ static int g_tune_split = 1;   // split shadow/AO tracing into query + refill-ma
 static int g_tune_split_prim = 1;   // split camera rays into query + refill-march passes
 static int g_tune_sah = 0;          // BVH binary tree by binned SAH (else radix-tree splits)
 bool sah_builder() { return g_tune_sah != 0; }
+static int g_tune_leaf = 1;         // primitives per BVH8 leaf (at most)
+int leaf_max() { return g_tune_leaf; }
 
 // The split path applies to volume-rendered scenes with one volume and no
 // isovalues (the march pass keeps one sample value per lane).
@@ -2184,6 +2186,11 @@ int gxy_gpu_set_tuning(int knob, int value) {
         g_tune_sah = value ? 1 : 0;
         return GXY_OK;
     }
+    if (knob == GXY_TUNE_LEAF_MAX) {
+        if (value < 1 || value > 4) return set_error(GXY_ERR_INVALID, "leaf size must be 1-4");
+        g_tune_leaf = value;
+        return GXY_OK;
+    }
     return set_error(GXY_ERR_INVALID, "unknown tuning knob");
 }
 
@@ -2194,6 +2201,7 @@ int gxy_gpu_get_tuning(int knob, int *value) {
     else if (knob == GXY_TUNE_SPLIT_SECONDARY) *value = g_tune_split;
     else if (knob == GXY_TUNE_SPLIT_PRIMARY) *value = g_tune_split_prim;
     else if (knob == GXY_TUNE_BVH_SAH) *value = g_tune_sah;
+    else if (knob == GXY_TUNE_LEAF_MAX) *value = g_tune_leaf;
     else return set_error(GXY_ERR_INVALID, "unknown tuning knob");
     return GXY_OK;
 }

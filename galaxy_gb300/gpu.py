@@ -104,6 +104,7 @@ TUNE_GRID_PER_SM = 2
 TUNE_SPLIT_SECONDARY = 3
 TUNE_SPLIT_PRIMARY = 4
 TUNE_BVH_SAH = 5
+TUNE_LEAF_MAX = 6
 
 
 def set_tuning(knob, value):

@@ -268,6 +268,8 @@ int gxy_gpu_set_profiling(gxy_scene scene, int on);
 #define GXY_TUNE_BVH_SAH         5   /* 1: BVH binary tree by binned SAH along the Morton
                                         order; 0 (default): radix-tree splits. Applies to
                                         scenes committed afterwards */
+#define GXY_TUNE_LEAF_MAX        6   /* largest primitive count of a BVH8 leaf, 1-4
+                                        (default 1); scenes committed afterwards */
 int gxy_gpu_set_tuning(int knob, int value);
 int gxy_gpu_get_tuning(int knob, int *value);
 int gxy_gpu_query_generations(gxy_scene scene, gxy_generation_stats *out, int max, int32_t *n);
