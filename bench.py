@@ -300,6 +300,8 @@ def main():
                     help="skip the autotuner (occupancy, grid size, split tracing) before timing")
     ap.add_argument("--tune", default="", help="fixed tuning 'blocks_per_sm,grid_per_sm,split' (implies --no-autotune)")
     ap.add_argument("--leaf-max", type=int, default=0, help="primitives per BVH8 leaf (1-4; 0: library default)")
+    ap.add_argument("--trav-steps", type=int, default=0, help="node visits per refill round (0: library default)")
+    ap.add_argument("--march-steps", type=int, default=0, help="samples per refill round (0: library default)")
     ap.add_argument("--bvh", default="lbvh", choices=["sah", "lbvh"],
                     help="BVH binary tree: binned SAH along the Morton order, or radix-tree (LBVH) splits")
     args = ap.parse_args()
@@ -320,7 +322,12 @@ def main():
     gpu.set_tuning(gpu.TUNE_BVH_SAH, 1 if args.bvh == "sah" else 0)
     if args.leaf_max:
         gpu.set_tuning(gpu.TUNE_LEAF_MAX, args.leaf_max)
-    cfg = dict(cfg, bvh=args.bvh, leaf_max=gpu.get_tuning(gpu.TUNE_LEAF_MAX))
+    if args.trav_steps:
+        gpu.set_tuning(gpu.TUNE_TRAV_STEPS, args.trav_steps)
+    if args.march_steps:
+        gpu.set_tuning(gpu.TUNE_MARCH_STEPS, args.march_steps)
+    cfg = dict(cfg, bvh=args.bvh, leaf_max=gpu.get_tuning(gpu.TUNE_LEAF_MAX),
+               trav_steps=gpu.get_tuning(gpu.TUNE_TRAV_STEPS), march_steps=gpu.get_tuning(gpu.TUNE_MARCH_STEPS))
     if args.image:
         cam.width = cam.height = args.image
         cfg = dict(cfg, image=[args.image, args.image], workload=cfg["workload"] + " (image %d^2)" % args.image)

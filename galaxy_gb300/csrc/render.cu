@@ -593,6 +593,8 @@ struct FrameArgs {
     unsigned *qmarch_count;            // [0] records, [1] fetch cursor of the march pass
     unsigned qmarch_cap;
     // split primary tracing: camera query pass -> primary march queue -> march pass
+    int trav_steps;                    // refill query passes: BVH8 node visits per refill round
+    int march_steps;                   // refill march passes: samples per refill round
     int split_prim;
     DRay *pmarch;
     float4 *pmarch_hit;                // 2 per record: (n, c.x), (c.y, c.z, -, -)
@@ -1145,7 +1147,7 @@ __global__ void __launch_bounds__(kThreads, MINB) k_sec_query(DevScene S, FrameA
         if (!__any_sync(0xffffffffu, have)) break;
         // one copy of the step body: unrolled copies overflow the instruction cache
 #pragma unroll 1
-        for (int k = 0; k < 4 && have && !done; k++)
+        for (int k = 0; k < max(A.trav_steps, 1) && have && !done; k++)
             done = trav_step(S, T, stack, st.nodes, st.tris, st.sphs, st.ovf);
         bool fin = have && done;
         bool to_march = false;
@@ -1276,7 +1278,7 @@ __global__ void __launch_bounds__(kThreads, MINB) k_cam_query(DevScene S, FrameA
         }
         if (!__any_sync(0xffffffffu, have || pending != 0 || !exhausted)) break;
 #pragma unroll 1
-        for (int k = 0; k < 4 && have && !done; k++)
+        for (int k = 0; k < max(A.trav_steps, 1) && have && !done; k++)
             done = trav_step(S, T, stack, st.nodes, st.tris, st.sphs, st.ovf);
         bool fin = have && done;
         if (fin && T.found) {
@@ -1356,7 +1358,7 @@ __global__ void __launch_bounds__(kThreads, MINB) k_prim_march(DevScene S, Frame
             }
         }
         if (!__any_sync(0xffffffffu, have)) break;
-        if (have && !M.done) prim_march_steps(S, tfs[0], M, 16, st);
+        if (have && !M.done) prim_march_steps(S, tfs[0], M, max(A.march_steps, 1), st);
         bool fin = have && M.done;
         PrimOut P;
         const DevJob &J = BATCH ? A.jobs[fin ? job : 0] : A.job0;
@@ -1417,7 +1419,7 @@ __global__ void __launch_bounds__(kThreads, MINB) k_sec_march(DevScene S, FrameA
             }
         }
         if (!__any_sync(0xffffffffu, have)) break;
-        if (have && !M.done) sec_march_steps(S, tfs[0], M, 16, st);
+        if (have && !M.done) sec_march_steps(S, tfs[0], M, max(A.march_steps, 1), st);
         bool fin = have && M.done;
         int dest = GXY_DROP_ON_FLOOR;
         TraceOut T;
@@ -1632,6 +1634,8 @@ static int g_tune_split_prim = 1;   // split camera rays into query + refill-mar
 static int g_tune_sah = 0;          // BVH binary tree by binned SAH (else radix-tree splits)
 bool sah_builder() { return g_tune_sah != 0; }
 static int g_tune_leaf = 1;         // primitives per BVH8 leaf (at most)
+static int g_tune_trav_steps = 8;   // node visits per refill round of the query passes
+static int g_tune_march_steps = 16; // samples per refill round of the march passes
 int leaf_max() { return g_tune_leaf; }
 
 // The split path applies to volume-rendered scenes with one volume and no
@@ -1754,6 +1758,8 @@ static int render(Scene *sc, const gxy_camera &cam, const gxy_lighting &lt, floa
     A.qmarch_count = sc->qcount + 12;   // [0] records, [1] march cursor, [2] query cursor
     A.qmarch_cap = (unsigned)sc->qmarch_cap;
     A.split_prim = (split_eligible(S) && g_tune_split_prim) ? 1 : 0;
+    A.trav_steps = g_tune_trav_steps;
+    A.march_steps = g_tune_march_steps;
     A.pmarch = sc->pmarch;
     A.pmarch_hit = sc->pmarch_hit;
     A.pmarch_count = sc->qcount + 8;    // [0] records, [1] march cursor, [2] camera query cursor, [3] extra slots
@@ -2191,6 +2197,16 @@ int gxy_gpu_set_tuning(int knob, int value) {
         g_tune_leaf = value;
         return GXY_OK;
     }
+    if (knob == GXY_TUNE_TRAV_STEPS) {
+        if (value < 1 || value > 64) return set_error(GXY_ERR_INVALID, "traversal steps must be 1-64");
+        g_tune_trav_steps = value;
+        return GXY_OK;
+    }
+    if (knob == GXY_TUNE_MARCH_STEPS) {
+        if (value < 1 || value > 256) return set_error(GXY_ERR_INVALID, "march steps must be 1-256");
+        g_tune_march_steps = value;
+        return GXY_OK;
+    }
     return set_error(GXY_ERR_INVALID, "unknown tuning knob");
 }
 
@@ -2202,6 +2218,8 @@ int gxy_gpu_get_tuning(int knob, int *value) {
     else if (knob == GXY_TUNE_SPLIT_PRIMARY) *value = g_tune_split_prim;
     else if (knob == GXY_TUNE_BVH_SAH) *value = g_tune_sah;
     else if (knob == GXY_TUNE_LEAF_MAX) *value = g_tune_leaf;
+    else if (knob == GXY_TUNE_TRAV_STEPS) *value = g_tune_trav_steps;
+    else if (knob == GXY_TUNE_MARCH_STEPS) *value = g_tune_march_steps;
     else return set_error(GXY_ERR_INVALID, "unknown tuning knob");
     return GXY_OK;
 }
@@ -2681,6 +2699,8 @@ int gxy_gpu_batch_submit(gxy_batch batch, const gxy_job *jobs, int n_jobs, int f
     memset(&A, 0, sizeof A);
     A.jobs = b->d_jobs;
     A.n_jobs = n_jobs;
+    A.trav_steps = g_tune_trav_steps;
+    A.march_steps = g_tune_march_steps;
     A.total_pix = pix;
     A.job0 = b->h_jobs[0];
     for (int k = 0; k < NQ; k++) A.qcap[k] = (unsigned)b->qcap[k];

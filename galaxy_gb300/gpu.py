@@ -105,6 +105,8 @@ TUNE_SPLIT_SECONDARY = 3
 TUNE_SPLIT_PRIMARY = 4
 TUNE_BVH_SAH = 5
 TUNE_LEAF_MAX = 6
+TUNE_TRAV_STEPS = 7
+TUNE_MARCH_STEPS = 8
 
 
 def set_tuning(knob, value):

@@ -270,6 +270,10 @@ int gxy_gpu_set_profiling(gxy_scene scene, int on);
                                         scenes committed afterwards */
 #define GXY_TUNE_LEAF_MAX        6   /* largest primitive count of a BVH8 leaf, 1-4
                                         (default 1); scenes committed afterwards */
+#define GXY_TUNE_TRAV_STEPS      7   /* BVH8 node visits per refill round of the query
+                                        passes, 1-64 (default 8) */
+#define GXY_TUNE_MARCH_STEPS     8   /* volume samples per refill round of the march
+                                        passes, 1-256 (default 16) */
 int gxy_gpu_set_tuning(int knob, int value);
 int gxy_gpu_get_tuning(int knob, int *value);
 int gxy_gpu_query_generations(gxy_scene scene, gxy_generation_stats *out, int max, int32_t *n);
