@@ -423,7 +423,8 @@ def main():
         traffic = t.get("bytes_per_launch")
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "traffic": traffic, "peak_source": peak_kind,
-            "kernel": ["k_primary<camera>", "k_primary<queue>",
+            "kernel": ["k_cam_query" if gpu.get_tuning(gpu.TUNE_SPLIT_PRIMARY) else "k_primary<camera>",
+                       "k_primary<queue>",
                        "k_sec_query" if gpu.get_tuning(gpu.TUNE_SPLIT_SECONDARY) else "k_secondary",
                        "k_sec_march", "k_prim_march"][dom],
             "kernel_ms": dom_ms, "algorithmic_bytes": dom_bytes, "share_of_frame_kernel_time": share}
