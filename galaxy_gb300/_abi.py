@@ -64,6 +64,13 @@ class gxy_particles_vis(C.Structure):
                 ("value0", C.c_float), ("value1", C.c_float), ("tf", gxy_tf)]
 
 
+class gxy_pathlines_vis(C.Structure):
+    _fields_ = [("vertices", f32p), ("data", f32p), ("n_vertices", C.c_int64),
+                ("indices", i32p), ("n_segments", C.c_int64),
+                ("radius0", C.c_float), ("radius1", C.c_float),
+                ("value0", C.c_float), ("value1", C.c_float), ("tf", gxy_tf)]
+
+
 class gxy_lighting(C.Structure):
     _fields_ = [("n_lights", C.c_int32),
                 ("lights", (C.c_float * 3) * MAX_LIGHTS),
@@ -85,7 +92,8 @@ class gxy_scene_desc(C.Structure):
                 ("partitions", C.c_int32 * 3),
                 ("has_box", C.c_int32), ("box", C.c_float * 6),
                 ("sampling_rate", C.c_float), ("opaque_alpha", C.c_float),
-                ("epsilon", C.c_float)]
+                ("epsilon", C.c_float),
+                ("n_pathline_sets", C.c_int32), ("pathlines", C.POINTER(gxy_pathlines_vis))]
 
 
 RAY_FLOAT_FIELDS = ("ox", "oy", "oz", "dx", "dy", "dz", "nx", "ny", "nz", "sample",

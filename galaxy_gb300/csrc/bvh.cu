@@ -38,12 +38,22 @@ __device__ __forceinline__ void prim_box(const DevScene &S, uint32_t p, float3 &
         float3 c = make_float3(T.vertices[3 * ix[2]], T.vertices[3 * ix[2] + 1], T.vertices[3 * ix[2] + 2]);
         lo = make_float3(fminf(a.x, fminf(b.x, c.x)), fminf(a.y, fminf(b.y, c.y)), fminf(a.z, fminf(b.z, c.z)));
         hi = make_float3(fmaxf(a.x, fmaxf(b.x, c.x)), fmaxf(a.y, fmaxf(b.y, c.y)), fmaxf(a.z, fmaxf(b.z, c.z)));
-    } else {
+    } else if ((int64_t)p < S.n_tri + S.n_sph) {
         int s = 0;
         while (s + 1 < S.n_sph_sets && (int64_t)p >= S.sph_sets[s + 1].prim_base) s++;
         const DevSphSet &P = S.sph_sets[s];
         int64_t lp = (int64_t)p - P.prim_base;
         lo = hi = make_float3(P.centers[3 * lp], P.centers[3 * lp + 1], P.centers[3 * lp + 2]);   // radius added by caller
+    } else {
+        // DataDrivenPathLines_bounds (DataDrivenPathLines.ispc:37-68): segment box grown by radius0
+        int s = 0;
+        while (s + 1 < S.n_line_sets && (int64_t)p >= S.line_sets[s + 1].prim_base) s++;
+        const DevLineSet &L = S.line_sets[s];
+        const int idx = L.indices[(int64_t)p - L.prim_base];
+        const float *a = L.vertices + 3 * idx, *b = a + 3;
+        const float r = L.radius0;
+        lo = make_float3(fminf(a[0], b[0]) - r, fminf(a[1], b[1]) - r, fminf(a[2], b[2]) - r);
+        hi = make_float3(fmaxf(a[0], b[0]) + r, fmaxf(a[1], b[1]) + r, fmaxf(a[2], b[2]) + r);
     }
 }
 
@@ -77,7 +87,7 @@ __global__ void k_prim_bounds(DevScene S, const float *sph_radius, int64_t n, fl
     bool valid = p < n;
     if (valid) {
         prim_box(S, (uint32_t)p, lo, hi);
-        if (p >= S.n_tri) {
+        if (p >= S.n_tri && p < S.n_tri + S.n_sph) {
             float r = sph_radius[p - S.n_tri];
             lo = make_float3(lo.x - r, lo.y - r, lo.z - r);
             hi = make_float3(hi.x + r, hi.y + r, hi.z + r);
@@ -338,7 +348,7 @@ __device__ void write_slot(const DevScene &S, const float *sph_radius, uint32_t 
         r[0] = make_float4(V[3 * ix[0]], V[3 * ix[0] + 1], V[3 * ix[0] + 2], __uint_as_float(p));
         r[1] = make_float4(V[3 * ix[1]], V[3 * ix[1] + 1], V[3 * ix[1] + 2], 0.0f);
         r[2] = make_float4(V[3 * ix[2]], V[3 * ix[2] + 1], V[3 * ix[2] + 2], 0.0f);
-    } else {
+    } else if ((int64_t)p < S.n_tri + S.n_sph) {
         int k = 0;
         while (k + 1 < S.n_sph_sets && (int64_t)p >= S.sph_sets[k + 1].prim_base) k++;
         const DevSphSet &P = S.sph_sets[k];
@@ -346,6 +356,15 @@ __device__ void write_slot(const DevScene &S, const float *sph_radius, uint32_t 
         r[0] = make_float4(P.centers[3 * lp], P.centers[3 * lp + 1], P.centers[3 * lp + 2],
                            __uint_as_float(p | kSphereBit));
         r[1] = make_float4(sph_radius[(int64_t)p - S.n_tri], P.eps, 0.0f, 0.0f);
+        r[2] = make_float4(0, 0, 0, 0);
+    } else {
+        int k = 0;
+        while (k + 1 < S.n_line_sets && (int64_t)p >= S.line_sets[k + 1].prim_base) k++;
+        const DevLineSet &L = S.line_sets[k];
+        const int idx = L.indices[(int64_t)p - L.prim_base];
+        const float *a = L.vertices + 3 * idx, *b = a + 3;
+        r[0] = make_float4(a[0], a[1], a[2], __uint_as_float(p | kSphereBit | kLineBit));
+        r[1] = make_float4(b[0], b[1], b[2], L.radius0);
         r[2] = make_float4(0, 0, 0, 0);
     }
 }
@@ -456,14 +475,15 @@ static inline unsigned blocks_for(int64_t n, int b) { return (unsigned)((n + b -
 // on success).  sph_radius: per-sphere radius (device).
 int build_bvh8(DevScene &S, const float *sph_radius, DeviceArena &arena, cudaStream_t st, BVHInfo &info) {
     auto t_start = std::chrono::steady_clock::now();
-    int64_t n64 = S.n_tri + S.n_sph;
+    int64_t n64 = S.n_tri + S.n_sph + S.n_seg;
     info = BVHInfo{};
     if (n64 == 0) {
         S.nodes = nullptr;
         S.slots = nullptr;
         return GXY_OK;
     }
-    if (n64 >= (int64_t)0x7fffffff) return set_error(GXY_ERR_INVALID, "too many primitives for the BVH");
+    // leaf-slot ids carry kind bits 30 and 31
+    if (n64 >= ((int64_t)1 << 30)) return set_error(GXY_ERR_INVALID, "more than 2^30 primitives for the BVH");
     int n = (int)n64;
     BuildBuffers B;
     ScratchList scratch(arena);

@@ -22,6 +22,7 @@ namespace gxy {
 constexpr int kMaxVol = GXY_MAX_VOLUMES;
 constexpr int kMaxPart = GXY_MAX_PARTITIONS;
 constexpr uint32_t kSphereBit = 0x80000000u;
+constexpr uint32_t kLineBit = 0x40000000u;     // with kSphereBit: a path-line segment
 
 struct DevTF {                       // one resampled transfer function, 4 KB
     float colors[GXY_TF_SIZE * 3];
@@ -65,6 +66,15 @@ struct DevSphSet {                   // spheres [prim_base, prim_base+n)
     float eps;
 };
 
+struct DevLineSet {                  // path-line segments [prim_base, prim_base+n)
+    int64_t prim_base, n;
+    const int32_t *indices;          // first vertex of each segment
+    const float *vertices;           // 3 per vertex
+    const float *radius;             // per vertex, MAP_RADIUS of the data
+    float radius0, radius1, value0, value1;
+    int tf;
+};
+
 // 128-byte wide node: one L2 line.  Child i's box is
 // origin + q * 2^(e-127) per axis, with q the 16-bit lower/upper bounds.
 struct __align__(128) BVH8Node {
@@ -80,6 +90,9 @@ static_assert(sizeof(BVH8Node) == 128, "BVH8 node must fill one 128-byte line");
 
 // Leaf primitive slot: 3 float4.  Triangle: (v0, id) (v1, -) (v2, -).
 // Sphere: (center, id | kSphereBit) (radius, eps, -, -) (-).
+// Path-line segment: (A, id | kSphereBit | kLineBit) (B, radius0) (-).
+// Ids are the primitive's index (triangles, then spheres, then segments)
+// plus these bits, so they order like the index (fewer than 2^30 primitives).
 struct DevScene {
     int n_vol;
     DevVolume vol[kMaxVol];
@@ -94,10 +107,11 @@ struct DevScene {
     // geometry
     const BVH8Node *nodes;
     const float4 *slots;
-    int64_t n_tri, n_sph;
-    int n_tri_sets, n_sph_sets;
+    int64_t n_tri, n_sph, n_seg;
+    int n_tri_sets, n_sph_sets, n_line_sets;
     DevTriSet tri_sets[4];
     DevSphSet sph_sets[4];
+    DevLineSet line_sets[4];
     const DevTF *tfs;
     const float4 *ao;                // 256 x (cos 2pi u, sin 2pi u, sqrt(1-v), sqrt(v))
 };
@@ -332,6 +346,65 @@ __device__ __forceinline__ bool sph_test(V3 org, V3 dir, V3 c, float r, float ep
     return false;
 }
 
+// Path-line segment as DataDrivenPathLines_intersect_kernel intersects it
+// (DataDrivenPathLines.ispc:100-203): a cylinder A-B of radius r clipped at
+// its caps, joined with spheres of radius r at A and B, each with the
+// numerical fix of moving the ray origin to an approximate distance first;
+// rcp/rcpf are taken as exact reciprocals.  Accepted distance: t_in if in
+// (t0, tfar), else t_out if in (t0, tfar).
+__device__ __forceinline__ void line_sphere(V3 org, V3 dir, V3 c, float r, float &t_in, float &t_out) {
+    const float approx = dot(c - org, dir);
+    const V3 close = org + approx * dir;
+    const V3 A = c - close;
+    const float a = dot(dir, dir);
+    const float b = -2.f * dot(dir, A);
+    const float cc = dot(A, A) - r * r;
+    const float rad = b * b - 4.f * a * cc;
+    if (rad < 0.f) return;
+    const float srad = sqrtf(rad);
+    const float r2a = 1.0f / (2.f * a);
+    t_in = fmin_(t_in, approx + (-b - srad) * r2a);
+    t_out = fmax_(t_out, approx + (-b + srad) * r2a);
+}
+__device__ __forceinline__ void line_cylinder(V3 org, V3 dir, V3 A0, V3 B0, float r, float &t_in, float &t_out) {
+    const V3 center = 0.5f * (A0 + B0);
+    const float approx = dot(center - org, dir);
+    const V3 close = org + approx * dir;
+    const V3 A = A0 - close, B = B0 - close;
+    const V3 AB = B - A;
+    const V3 AOxAB = cross(AB, A);
+    const V3 VxAB = cross(dir, AB);
+    const float ab2 = dot(AB, AB);
+    const float a = dot(VxAB, VxAB);
+    if (a == 0.f) return;
+    const float b = 2.f * dot(VxAB, AOxAB);
+    const float c = dot(AOxAB, AOxAB) - ((r * r) * ab2);
+    const float rad = b * b - 4.f * a * c;
+    if (rad < 0.f) return;
+    const float srad = sqrtf(rad);
+    const float dVAB = dot(dir, AB);
+    if (dVAB == 0.f) return;
+    const float rVAB = 1.0f / dVAB;
+    const float tA = dot(AB, A) * rVAB, tB = dot(AB, B) * rVAB;
+    const float r2a = 1.0f / (2.f * a);
+    const float c_in = approx + fmax_((-b - srad) * r2a, fmin_(tA, tB));
+    const float c_out = approx + fmin_((-b + srad) * r2a, fmax_(tA, tB));
+    if (c_in < c_out) {
+        t_in = c_in;
+        t_out = c_out;
+    }
+}
+static __device__ __noinline__ bool line_test(V3 org, V3 dir, V3 A, V3 B, float r, float t0, float tfar, float &t) {
+    float t_in = INFINITY, t_out = -INFINITY;
+    line_cylinder(org, dir, A, B, r, t_in, t_out);
+    line_sphere(org, dir, A, r, t_in, t_out);
+    line_sphere(org, dir, B, r, t_in, t_out);
+    if (!(t_in < t_out)) return false;
+    if (t_in > t0 && t_in < tfar) { t = t_in; return true; }
+    if (t_out > t0 && t_out < tfar) { t = t_out; return true; }
+    return false;
+}
+
 // --------------------------------------------------------- BVH8 traversal
 struct GeoHit {
     float t, u, v;
@@ -475,7 +548,10 @@ __device__ __noinline__ bool bvh_closest(const DevScene &S, V3 org, V3 dir, floa
                     uint32_t id = __float_as_uint(r0.w);
                     float t, u = 0.0f, v = 0.0f;
                     bool ok;
-                    if (id & kSphereBit) {
+                    if (id & kLineBit) {
+                        tris++;   // path-line segments count as primitive tests with triangles
+                        ok = line_test(org, dir, v3(r0.x, r0.y, r0.z), v3(r1.x, r1.y, r1.z), r1.w, t0, tfar, t);
+                    } else if (id & kSphereBit) {
                         sphs++;
                         ok = sph_test(org, dir, v3(r0.x, r0.y, r0.z), r1.x, r1.y, t0, tfar, t);
                     } else {
@@ -592,7 +668,10 @@ __device__ __forceinline__ bool trav_step(const DevScene &S, TravState &T, uint2
             uint32_t id = __float_as_uint(r0.w);
             float t, u = 0.0f, v = 0.0f;
             bool ok;
-            if (id & kSphereBit) {
+            if (id & kLineBit) {
+                tris++;   // path-line segments count as primitive tests with triangles
+                ok = line_test(org, dir, v3(r0.x, r0.y, r0.z), v3(r1.x, r1.y, r1.z), r1.w, t0, tfar, t);
+            } else if (id & kSphereBit) {
                 sphs++;
                 ok = sph_test(org, dir, v3(r0.x, r0.y, r0.z), r1.x, r1.y, t0, tfar, t);
             } else {

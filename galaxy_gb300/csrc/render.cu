@@ -307,6 +307,13 @@ static float sphere_epsilon(float r0) {   // DataDrivenSpheres.ispc:211-220
     return e;
 }
 
+// MAP_RADIUS (DataDrivenPathLines.cpp:11-19): per-vertex path-line radius.
+static float pathline_radius(const gxy_pathlines_vis &q, int64_t i) {
+    if (q.value0 == q.value1 || !q.data) return q.radius0;
+    float R = (q.data[i] - q.value0) / (q.value1 - q.value0);
+    return (R <= 0.0f) ? q.radius0 : (R >= 1.0f) ? q.radius1 : q.radius0 + R * (q.radius1 - q.radius0);
+}
+
 static void tf_to_dev(const gxy_tf &t, DevTF &d) {
     memcpy(d.colors, t.colors, sizeof d.colors);
     memcpy(d.opac, t.opacities, sizeof d.opac);
@@ -320,8 +327,9 @@ static int commit(const gxy_scene_desc *d, Scene *sc) {
     DevScene &S = sc->S;
     memset(&S, 0, sizeof S);
     if (d->n_volumes < 0 || d->n_volumes > kMaxVol) return set_error(GXY_ERR_INVALID, "bad volume count");
-    if (d->n_triangle_sets < 0 || d->n_triangle_sets > 4 || d->n_particle_sets < 0 || d->n_particle_sets > 4)
-        return set_error(GXY_ERR_INVALID, "at most 4 triangle sets and 4 particle sets");
+    if (d->n_triangle_sets < 0 || d->n_triangle_sets > 4 || d->n_particle_sets < 0 || d->n_particle_sets > 4 ||
+        d->n_pathline_sets < 0 || d->n_pathline_sets > 4)
+        return set_error(GXY_ERR_INVALID, "at most 4 triangle, 4 particle and 4 path-line sets");
     int np = (d->partitions[0] < 1 ? 1 : d->partitions[0]) * (d->partitions[1] < 1 ? 1 : d->partitions[1]) *
              (d->partitions[2] < 1 ? 1 : d->partitions[2]);
     if (np > kMaxPart) return set_error(GXY_ERR_INVALID, "too many partitions");
@@ -446,6 +454,44 @@ static int commit(const gxy_scene_desc *d, Scene *sc) {
     }
     S.n_sph = prim - S.n_tri;
     S.n_sph_sets = d->n_particle_sets;
+    for (int s = 0; s < d->n_pathline_sets; s++) {
+        const gxy_pathlines_vis &q = d->pathlines[s];
+        if (!q.vertices || q.n_vertices < 2 || q.n_segments < 0 || (q.n_segments > 0 && !q.indices))
+            return set_error(GXY_ERR_INVALID, "path lines need vertices and segment indices");
+        for (int64_t i = 0; i < q.n_segments; i++)
+            if (q.indices[i] < 0 || (int64_t)q.indices[i] + 1 >= q.n_vertices)
+                return set_error(GXY_ERR_INVALID, "path-line segment index out of range");
+        DevLineSet &L = S.line_sets[s];
+        L.prim_base = prim;
+        L.n = q.n_segments;
+        void *p;
+        if ((rc = sc->upload(q.vertices, sizeof(float) * 3 * q.n_vertices, &p))) return rc;
+        L.vertices = (const float *)p;
+        if ((rc = sc->upload(q.indices, sizeof(int32_t) * q.n_segments, &p))) return rc;
+        L.indices = (const int32_t *)p;
+        std::vector<float> rv((size_t)q.n_vertices);
+        for (int64_t i = 0; i < q.n_vertices; i++) {
+            rv[i] = pathline_radius(q, i);
+            // DataDrivenPathLines::finalize bounds (DataDrivenPathLines.cpp:79-86)
+            for (int a = 0; a < 3; a++) {
+                gbox[a] = fminf(gbox[a], q.vertices[3 * i + a] - rv[i]);
+                gbox[3 + a] = fmaxf(gbox[3 + a], q.vertices[3 * i + a] + rv[i]);
+            }
+        }
+        if ((rc = sc->upload(rv.data(), rv.size() * sizeof(float), &p))) return rc;
+        L.radius = (const float *)p;
+        L.radius0 = q.radius0;
+        L.radius1 = q.radius1;
+        L.value0 = q.value0;
+        L.value1 = q.value1;
+        L.tf = (int)tfs.size();
+        DevTF tt;
+        tf_to_dev(q.tf, tt);
+        tfs.push_back(tt);
+        prim += q.n_segments;
+    }
+    S.n_seg = prim - S.n_tri - S.n_sph;
+    S.n_line_sets = d->n_pathline_sets;
     if (d->has_box) gbox.assign(d->box, d->box + 6);
     else if (prim == 0) gbox = {-1, -1, -1, 1, 1, 1};
     make_partitions(*d, gbox, S);
@@ -2050,6 +2096,18 @@ int gxy_scene_partition_layout(const gxy_scene_desc *desc, int partition, gxy_pa
             for (int a = 0; a < 3; a++) {
                 g[a] = fminf(g[a], q.centers[3 * i + a] - r);
                 g[3 + a] = fmaxf(g[3 + a], q.centers[3 * i + a] + r);
+                any = true;
+            }
+        }
+    }
+    if (desc->n_pathline_sets < 0 || desc->n_pathline_sets > 4) return set_error(GXY_ERR_INVALID, "bad path-line set count");
+    for (int s = 0; s < desc->n_pathline_sets; s++) {
+        const gxy_pathlines_vis &q = desc->pathlines[s];
+        for (int64_t i = 0; i < q.n_vertices; i++) {
+            float r = pathline_radius(q, i);
+            for (int a = 0; a < 3; a++) {
+                g[a] = fminf(g[a], q.vertices[3 * i + a] - r);
+                g[3 + a] = fmaxf(g[3 + a], q.vertices[3 * i + a] + r);
                 any = true;
             }
         }

@@ -40,12 +40,38 @@ struct RayStats {
 // Surface attributes of a geometry hit: normal (normalised, face-forwarded)
 // and colour, as OSPRay postIntersect with DG_NG|DG_NS|DG_NORMALIZE|
 // DG_FACEFORWARD|DG_COLOR over the DataDrivenTriangleMesh /
-// DataDrivenSpheres post-intersect functions.
+// DataDrivenSpheres / DataDrivenPathLines post-intersect functions.
 __device__ __noinline__ void geometry_shade(const DevScene &S, const GeoHit &gh, V3 org, V3 dir, V3 &n_out,
                                             V3 &c_out) {
     V3 Ng, Ns;
     V3 col = v3(1.f, 1.f, 1.f);
-    if (!(gh.prim & kSphereBit)) {
+    if (gh.prim & kLineBit) {
+        // DataDrivenPathLines.ispc:186-196 (u and Ng of the hit) and 213-268
+        int64_t p = gh.prim & ~(kSphereBit | kLineBit);
+        int k = 0;
+        while (k + 1 < S.n_line_sets && p >= S.line_sets[k + 1].prim_base) k++;
+        const DevLineSet &L = S.line_sets[k];
+        const int idx = __ldg(L.indices + (p - L.prim_base));
+        const float *V = L.vertices;
+        V3 A = v3(__ldg(V + 3 * idx), __ldg(V + 3 * idx + 1), __ldg(V + 3 * idx + 2));
+        V3 B = v3(__ldg(V + 3 * idx + 3), __ldg(V + 3 * idx + 4), __ldg(V + 3 * idx + 5));
+        V3 P = org + gh.t * dir;
+        float u = dot(P - A, B - A) * (1.0f / dot(B - A, B - A));
+        u = fmin_(fmax_(u, 0.f), 1.f);
+        V3 PonAxis = A + u * (B - A);
+        Ng = nrm(P - PonAxis);
+        Ns = Ng;
+        float radius = ((1.f - u) * __ldg(L.radius + idx)) + (u * __ldg(L.radius + idx + 1));
+        const float r0 = L.radius0, r1 = L.radius1, v0 = L.value0, v1 = L.value1;
+        float dataval;
+        if (r0 == r1) dataval = v0;
+        else if (r0 < r1 && radius < r0) dataval = v0;
+        else if (r0 < r1 && radius > r1) dataval = v1;
+        else if (r0 > r1 && radius < r1) dataval = v1;
+        else if (r0 > r1 && radius > r0) dataval = v0;
+        else dataval = v0 + ((radius - r0) / (r1 - r0)) * (v1 - v0);
+        col = tf_color(S.tfs[L.tf], dataval);
+    } else if (!(gh.prim & kSphereBit)) {
         int64_t p = gh.prim;
         int k = 0;
         while (k + 1 < S.n_tri_sets && p >= S.tri_sets[k + 1].prim_base) k++;

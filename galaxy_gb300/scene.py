@@ -4,7 +4,8 @@ Class names and JSON semantics follow Galaxy's renderer/data layer:
 Lighting (src/renderer/Lighting.cpp:58-115), Camera (Camera.cpp:165-281),
 MappedVis transfer-function resampling (MappedVis.cpp:86-203, 277-338),
 VolumeVis (VolumeVis.cpp:119-163), ParticlesVis (ParticlesVis.cpp:104-118),
-TrianglesVis, Volume (.vol import, Volume.cpp:195-214) and Visualization
+PathLinesVis (PathLinesVis.cpp:29-112), TrianglesVis, Volume (.vol import,
+Volume.cpp:195-214), PathLines (polylines) and Visualization
 (Visualization.cpp:293-340).  A Visualization turns into the gxy_scene_desc
 the device path consumes; numpy arrays referenced by the descriptor are kept
 alive by the Python objects.
@@ -259,6 +260,24 @@ class ParticlesVis(MappedVis):
         return vis
 
 
+class PathLinesVis(MappedVis):
+    """PathLinesVis (PathLinesVis.cpp:29-36 defaults, :104-112 LoadFromJSON):
+    radius mapped from data between (value0, radius0) and (value1, radius1)."""
+
+    def __init__(self, dataset=None, radius0=-1.0, radius1=1.0, value0=0.0, value1=1.0, **kw):
+        super().__init__(dataset, **kw)
+        self.radius0, self.radius1, self.value0, self.value1 = radius0, radius1, value0, value1
+
+    @classmethod
+    def from_json(cls, v, datasets):
+        vis = cls(datasets[v["dataset"]])
+        for k in ("radius0", "radius1", "value0", "value1"):
+            if k in v:
+                setattr(vis, k, float(v[k]))
+        vis.load_mapped_json(v)
+        return vis
+
+
 # ---------------------------------------------------------------- datasets
 class Volume:
     """Structured fp32 grid, x fastest (Volume.cpp:195-214 for .vol)."""
@@ -301,6 +320,32 @@ class Particles:
         self.data = None if data is None else np.ascontiguousarray(data, np.float32).reshape(-1)
 
 
+class PathLines:
+    """Polylines: vertices (n, 3), per-vertex data and segment first-vertex
+    indices (segment i joins indices[i] and indices[i] + 1), as
+    PathLines::load_from_vtkPointSet builds them from polyline cells
+    (PathLines.cpp:74-126)."""
+
+    def __init__(self, vertices, indices, data=None):
+        self.vertices = np.ascontiguousarray(vertices, np.float32).reshape(-1, 3)
+        self.indices = np.ascontiguousarray(indices, np.int32).reshape(-1)
+        self.data = None if data is None else np.ascontiguousarray(data, np.float32).reshape(-1)
+
+    @classmethod
+    def from_polylines(cls, lines, data=None):
+        """lines: list of (k_i, 3) vertex arrays; data: matching list of (k_i,)
+        arrays or None.  Each polyline contributes its k_i - 1 segments."""
+        verts, idx, dat, base = [], [], [], 0
+        for j, ln in enumerate(lines):
+            ln = np.asarray(ln, np.float32).reshape(-1, 3)
+            verts.append(ln)
+            idx.append(np.arange(base, base + len(ln) - 1, dtype=np.int32))
+            if data is not None:
+                dat.append(np.asarray(data[j], np.float32).reshape(-1))
+            base += len(ln)
+        return cls(np.concatenate(verts), np.concatenate(idx), np.concatenate(dat) if data is not None else None)
+
+
 # ----------------------------------------------------------- Visualization
 class Visualization:
     """A Visualization (Visualization.cpp:293-340): operators plus lighting,
@@ -320,7 +365,7 @@ class Visualization:
     def desc(self):
         """Build the gxy_scene_desc; the returned object keeps every array
         it points at alive (attribute _keep)."""
-        vols, tris, parts = [], [], []
+        vols, tris, parts, lines = [], [], [], []
         keep = []
         for op in self.operators:
             if isinstance(op, VolumeVis):
@@ -361,6 +406,16 @@ class Visualization:
                 p.tf = op.tf()
                 keep += [ds.centers, ds.data]
                 parts.append(p)
+            elif isinstance(op, PathLinesVis):
+                ds = op.dataset
+                q = A.gxy_pathlines_vis()
+                q.vertices, q.n_vertices = A.fptr(ds.vertices), len(ds.vertices)
+                q.indices, q.n_segments = A.iptr(ds.indices), len(ds.indices)
+                q.data = A.fptr(ds.data)
+                q.radius0, q.radius1, q.value0, q.value1 = op.radius0, op.radius1, op.value0, op.value1
+                q.tf = op.tf()
+                keep += [ds.vertices, ds.indices, ds.data]
+                lines.append(q)
             else:
                 raise TypeError("unknown operator %r" % (op,))
         if len(vols) > A.MAX_VOLUMES:
@@ -372,6 +427,8 @@ class Visualization:
         d.n_volumes, d.volumes = len(vols), C.cast(va, C.POINTER(A.gxy_volume_vis))
         d.n_triangle_sets, d.triangles = len(tris), C.cast(ta, C.POINTER(A.gxy_triangles_vis))
         d.n_particle_sets, d.particles = len(parts), C.cast(pa, C.POINTER(A.gxy_particles_vis))
+        la = (A.gxy_pathlines_vis * max(1, len(lines)))(*lines)
+        d.n_pathline_sets, d.pathlines = len(lines), C.cast(la, C.POINTER(A.gxy_pathlines_vis))
         d.partitions[:] = list(self.partitions)
         if self.box is not None:
             d.has_box = 1
@@ -379,7 +436,7 @@ class Visualization:
         d.sampling_rate = self.sampling_rate
         d.opaque_alpha = self.opaque_alpha
         d.epsilon = self.epsilon
-        d._keep = (keep, va, ta, pa)
+        d._keep = (keep, va, ta, pa, la)
         return d
 
 
@@ -417,7 +474,7 @@ def load_state(path, partitions=(1, 1, 1)):
             if not t.endswith("Vis"):
                 t = t + "Vis"
             cls = {"VolumeVis": VolumeVis, "TrianglesVis": TrianglesVis,
-                   "ParticlesVis": ParticlesVis}.get(t)
+                   "ParticlesVis": ParticlesVis, "PathLinesVis": PathLinesVis}.get(t)
             if cls is None:
                 raise ValueError("unknown operator type %s" % t)
             ops.append(cls.from_json(o, datasets))

@@ -18,8 +18,8 @@ generator, so a (seed, size) pair always gives the same scene.
 """
 import numpy as np
 
-from .scene import (Camera, Lighting, Particles, ParticlesVis, Triangles, TrianglesVis,
-                    Visualization, Volume, VolumeVis)
+from .scene import (Camera, Lighting, Particles, ParticlesVis, PathLines, PathLinesVis, Triangles,
+                    TrianglesVis, Visualization, Volume, VolumeVis)
 
 f32 = np.float32
 
@@ -224,6 +224,49 @@ def mixed_scene(n=512, n_spheres=4_000_000, width=2048, height=2048, seed=3, par
                          ParticlesVis(parts, radius0=0.002, radius1=0.002, value0=0.0, value1=0.0,
                                       colormap=[(0.0, 0.9, 0.8, 0.2), (1.0, 0.2, 0.8, 0.9)])],
                         L, partitions=partitions, sampling_rate=2.0, opaque_alpha=0.99)
+    cam = Camera(eye=(1.9, 1.4, 2.6), direction=(0.5 - 1.9, 0.5 - 1.4, 0.5 - 2.6), up=(0, 1, 0), aov=35.0,
+                 width=width, height=height)
+    return cam, vis
+
+
+# ---------------------------------------------------------------- path lines
+def abc_pathlines(n_lines=2000, n_vertices=64, seed=5, step=0.004, box=(0.1, 0.9)):
+    """Seeded path lines: forward-Euler streamlines of the ABC flow
+    (A, B, C) = (1, 0.7, 0.43) on the unit cube from uniform seed points;
+    per-vertex data = flow speed scaled to [0, 1]."""
+    g = rng(seed)
+    p = g.uniform(box[0], box[1], size=(n_lines, 3))
+    a, b, c = 1.0, 0.7, 0.43
+    pts = np.empty((n_lines, n_vertices, 3), np.float64)
+    spd = np.empty((n_lines, n_vertices), np.float64)
+    for k in range(n_vertices):
+        x, y, z = (2.0 * np.pi * p).T
+        v = np.stack([a * np.sin(z) + c * np.cos(y), b * np.sin(x) + a * np.cos(z), c * np.sin(y) + b * np.cos(x)], 1)
+        pts[:, k] = p
+        spd[:, k] = np.linalg.norm(v, axis=1)
+        p = p + step * v
+    spd = spd / (a + b + c)
+    return PathLines.from_polylines(list(pts.astype(f32)), list(spd.astype(f32)))
+
+
+def pathlines_scene(n_lines=2000, n_vertices=64, width=512, height=512, seed=5, partitions=(1, 1, 1),
+                    n_ao=2, ao_radius=0.05, radius0=0.003, radius1=0.008, volume=False):
+    """Path-line workload: (camera, visualization).  volume=True adds a 64^3
+    blob volume, so path lines and the volume march interleave."""
+    lines = abc_pathlines(n_lines, n_vertices, seed)
+    L = Lighting()
+    L.lights, L.types = [tuple(float(x) for x in -np.ones(3, f32) / f32(np.sqrt(3)))], [0]
+    L.shadows, L.n_ao, L.ao_radius, L.Ka, L.Kd = True, n_ao, ao_radius, 0.5, 0.5
+    ops = [PathLinesVis(lines, radius0=radius0, radius1=radius1, value0=0.0, value1=1.0, colormap=COOLWARM)]
+    kw = {}
+    if volume:
+        n = 64
+        vol = Volume(blob_field(n, 16, seed + 1), origin=(0.0, 0.0, 0.0), deltas=(1.0 / (n - 1),) * 3)
+        ops.insert(0, volume_vis(vol))
+        kw = dict(sampling_rate=2.0, opaque_alpha=0.99)
+    else:
+        kw = dict(box=(0.0, 0.0, 0.0, 1.0, 1.0, 1.0))
+    vis = Visualization(ops, L, partitions=partitions, **kw)
     cam = Camera(eye=(1.9, 1.4, 2.6), direction=(0.5 - 1.9, 0.5 - 1.4, 0.5 - 2.6), up=(0, 1, 0), aov=35.0,
                  width=width, height=height)
     return cam, vis

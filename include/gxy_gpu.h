@@ -122,6 +122,24 @@ typedef struct gxy_particles_vis {
     gxy_tf       tf;
 } gxy_particles_vis;
 
+/* PathLinesVis over polylines (DataDrivenPathLines).  Segment i joins
+ * vertices indices[i] and indices[i]+1 (DataDrivenPathLines.cpp:101-104).
+ * Per-vertex radius from data by MAP_RADIUS (DataDrivenPathLines.cpp:11-19);
+ * a segment is intersected as the capsule of DataDrivenPathLines_intersect_kernel
+ * (DataDrivenPathLines.ispc:100-203: cylinder of radius radius0 with a
+ * sphere at each end) and coloured as DataDrivenPathLines_postIntersect
+ * (DataDrivenPathLines.ispc:213-268: radius interpolated along the segment,
+ * mapped back to a data value, looked up in tf). */
+typedef struct gxy_pathlines_vis {
+    const float   *vertices;    /* 3 * n_vertices */
+    const float   *data;        /* n_vertices, or NULL (every radius radius0) */
+    int64_t        n_vertices;
+    const int32_t *indices;     /* n_segments first-vertex indices */
+    int64_t        n_segments;
+    float          radius0, radius1, value0, value1;
+    gxy_tf         tf;
+} gxy_pathlines_vis;
+
 /* Lighting_ispc (Lighting.ih:23-32).  Directional vectors are normalised on
  * load (Lighting.cpp:76-90); camera lights must be resolved first with
  * gxy_resolve_lights. */
@@ -159,6 +177,8 @@ typedef struct gxy_scene_desc {
     float   sampling_rate;   /* volume samples per voxel; 1.0 in Galaxy                */
     float   opaque_alpha;    /* early-termination alpha; 0.999 in Galaxy               */
     float   epsilon;         /* Renderer.epsilon; 0.001 in Galaxy                      */
+    int32_t                  n_pathline_sets;   /* at most 4 */
+    const gxy_pathlines_vis *pathlines;
 } gxy_scene_desc;
 
 /* RayList_ispc (Rays.ih:21-48): 25 SoA arrays plus the count.  Host memory. */

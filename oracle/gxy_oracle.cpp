@@ -256,18 +256,23 @@ static void my_intersect_box(F3 org, F3 dir, const Box &b, float &t0, float &t1)
 
 // ------------------------------------------------------------- geometry
 // Primitive ids: all triangles of set 0, set 1, ..., then all spheres of
-// particle set 0, 1, ...  Closest hit = smallest t in (t0, tfar), ties broken
-// by the smaller primitive id.
+// particle set 0, 1, ..., then all path-line segments of set 0, 1, ...
+// Closest hit = smallest t in (t0, tfar), ties broken by the smaller
+// primitive id.
 struct Geo {
     struct TriSet { const gxy_triangles_vis *v; int64_t base; };
     struct SphSet { const gxy_particles_vis *v; int64_t base; float eps; };
+    struct LineSet { const gxy_pathlines_vis *v; int64_t base; std::vector<float> rad; };
     std::vector<TriSet> tsets;
     std::vector<SphSet> ssets;
-    int64_t n_tri = 0, n_sph = 0;
+    std::vector<LineSet> lsets;
+    int64_t n_tri = 0, n_sph = 0, n_seg = 0;
     // flat per-primitive arrays
     std::vector<F3> tv0, tv1, tv2;
     std::vector<float> srad;
     std::vector<F3> scen;
+    std::vector<F3> la, lb;      // segment end points
+    std::vector<float> lr;       // segment capsule radius (radius0 of its set)
     // binary BVH
     struct Node { float lo[3], hi[3]; int32_t left, right, first, count; };
     std::vector<Node> nodes;
@@ -284,6 +289,13 @@ static float sphere_radius(const gxy_particles_vis &p, int64_t i) {
     }
     return p.radius0;
 }
+// MAP_RADIUS (DataDrivenPathLines.cpp:11-19): per-vertex path-line radius;
+// without data every vertex has radius0.
+static float pathline_radius(const gxy_pathlines_vis &q, int64_t i) {
+    if (q.value0 == q.value1 || !q.data) return q.radius0;
+    float R = (q.data[i] - q.value0) / (q.value1 - q.value0);
+    return (R <= 0.0f) ? q.radius0 : (R >= 1.0f) ? q.radius1 : q.radius0 + R * (q.radius1 - q.radius0);
+}
 // DataDrivenSpheresGeometry_set (DataDrivenSpheres.ispc:211-220).
 static float sphere_epsilon(float r0) {
     float e = logf(r0);
@@ -298,17 +310,24 @@ static void prim_bounds(const Geo &g, int64_t p, float lo[3], float hi[3]) {
         lo[0] = std::min({a.x, b.x, c.x}); hi[0] = std::max({a.x, b.x, c.x});
         lo[1] = std::min({a.y, b.y, c.y}); hi[1] = std::max({a.y, b.y, c.y});
         lo[2] = std::min({a.z, b.z, c.z}); hi[2] = std::max({a.z, b.z, c.z});
-    } else {
+    } else if (p < g.n_tri + g.n_sph) {
         int64_t s = p - g.n_tri;
         F3 c = g.scen[s];
         float r = g.srad[s];
         lo[0] = c.x - r; lo[1] = c.y - r; lo[2] = c.z - r;
         hi[0] = c.x + r; hi[1] = c.y + r; hi[2] = c.z + r;
+    } else {
+        // DataDrivenPathLines_bounds (DataDrivenPathLines.ispc:37-68)
+        int64_t s = p - g.n_tri - g.n_sph;
+        F3 a = g.la[s], b = g.lb[s];
+        float r = g.lr[s];
+        lo[0] = std::min(a.x, b.x) - r; lo[1] = std::min(a.y, b.y) - r; lo[2] = std::min(a.z, b.z) - r;
+        hi[0] = std::max(a.x, b.x) + r; hi[1] = std::max(a.y, b.y) + r; hi[2] = std::max(a.z, b.z) + r;
     }
 }
 
 static void build_bvh(Geo &g) {
-    int64_t n = g.n_tri + g.n_sph;
+    int64_t n = g.n_tri + g.n_sph + g.n_seg;
     g.order.resize(n);
     for (int64_t i = 0; i < n; i++) g.order[i] = i;
     g.nodes.clear();
@@ -417,6 +436,64 @@ static inline bool sph_test(F3 org, F3 dir, F3 c, float r, float eps, float t0, 
     return false;
 }
 
+// DataDrivenPathLines_intersect_kernel (DataDrivenPathLines.ispc:100-203):
+// cylinder A-B of radius r clipped at its caps, joined with spheres of radius
+// r at A and B, each after moving the origin to an approximate distance;
+// rcp/rcpf taken as exact reciprocals.  Accepted distance: t_in if in
+// (t0, tfar), else t_out if in (t0, tfar).
+static inline void line_sphere(F3 org, F3 dir, F3 c, float r, float &t_in, float &t_out) {
+    const float approx = dot(c - org, dir);
+    const F3 close = org + approx * dir;
+    const F3 A = c - close;
+    const float a = dot(dir, dir);
+    const float b = -2.f * dot(dir, A);
+    const float cc = dot(A, A) - r * r;
+    const float rad = b * b - 4.f * a * cc;
+    if (rad < 0.f) return;
+    const float srad = std::sqrt(rad);
+    const float r2a = 1.0f / (2.f * a);
+    t_in = std::min(t_in, approx + (-b - srad) * r2a);
+    t_out = std::max(t_out, approx + (-b + srad) * r2a);
+}
+static inline void line_cylinder(F3 org, F3 dir, F3 A0, F3 B0, float r, float &t_in, float &t_out) {
+    const F3 center = 0.5f * (A0 + B0);
+    const float approx = dot(center - org, dir);
+    const F3 close = org + approx * dir;
+    const F3 A = A0 - close, B = B0 - close;
+    const F3 AB = B - A;
+    const F3 AOxAB = cross(AB, A);
+    const F3 VxAB = cross(dir, AB);
+    const float ab2 = dot(AB, AB);
+    const float a = dot(VxAB, VxAB);
+    if (a == 0.f) return;
+    const float b = 2.f * dot(VxAB, AOxAB);
+    const float c = dot(AOxAB, AOxAB) - ((r * r) * ab2);
+    const float rad = b * b - 4.f * a * c;
+    if (rad < 0.f) return;
+    const float srad = std::sqrt(rad);
+    const float dVAB = dot(dir, AB);
+    if (dVAB == 0.f) return;
+    const float rVAB = 1.0f / dVAB;
+    const float tA = dot(AB, A) * rVAB, tB = dot(AB, B) * rVAB;
+    const float r2a = 1.0f / (2.f * a);
+    const float c_in = approx + std::max((-b - srad) * r2a, std::min(tA, tB));
+    const float c_out = approx + std::min((-b + srad) * r2a, std::max(tA, tB));
+    if (c_in < c_out) {
+        t_in = c_in;
+        t_out = c_out;
+    }
+}
+static inline bool line_test(F3 org, F3 dir, F3 A, F3 B, float r, float t0, float tfar, float &t) {
+    float t_in = INFINITY, t_out = -INFINITY;
+    line_cylinder(org, dir, A, B, r, t_in, t_out);
+    line_sphere(org, dir, A, r, t_in, t_out);
+    line_sphere(org, dir, B, r, t_in, t_out);
+    if (!(t_in < t_out)) return false;
+    if (t_in > t0 && t_in < tfar) { t = t_in; return true; }
+    if (t_out > t0 && t_out < tfar) { t = t_out; return true; }
+    return false;
+}
+
 static bool geo_closest(const Geo &g, F3 org, F3 dir, float t0, float tfar, GeoHit &h, bool any_hit = false) {
     if (g.nodes.empty()) return false;
     F3 inv = mk(1.0f / dir.x, 1.0f / dir.y, 1.0f / dir.z);
@@ -442,6 +519,9 @@ static bool geo_closest(const Geo &g, F3 org, F3 dir, float t0, float tfar, GeoH
                 bool hit;
                 if (p < g.n_tri) {
                     hit = tri_test(org, dir, g.tv0[p], g.tv1[p], g.tv2[p], t, u, v) && t > t0 && t < tfar;
+                } else if (p >= g.n_tri + g.n_sph) {
+                    int64_t s = p - g.n_tri - g.n_sph;
+                    hit = line_test(org, dir, g.la[s], g.lb[s], g.lr[s], t0, tfar, t);
                 } else {
                     int64_t s = p - g.n_tri;
                     float eps = 0;
@@ -470,6 +550,7 @@ struct Scene {
     std::vector<gxy_volume_vis> vols_desc;
     std::vector<gxy_triangles_vis> tris_desc;
     std::vector<gxy_particles_vis> parts_desc;
+    std::vector<gxy_pathlines_vis> lines_desc;
     std::vector<Vol> vols;
     Geo geo;
     Box gbox;
@@ -524,6 +605,16 @@ static void setup_partitions(Scene &s) {
                 prim_bounds(s.geo, p, a, b);
                 for (int k = 0; k < 3; k++) { lo[k] = std::min(lo[k], a[k]); hi[k] = std::max(hi[k], b[k]); }
             }
+            // path lines: vertices grown by their radius (DataDrivenPathLines.cpp:79-86)
+            for (auto &ls : s.geo.lsets) {
+                const gxy_pathlines_vis &q = *ls.v;
+                for (int64_t i = 0; i < q.n_vertices; i++)
+                    for (int k = 0; k < 3; k++) {
+                        lo[k] = std::min(lo[k], q.vertices[3 * i + k] - ls.rad[i]);
+                        hi[k] = std::max(hi[k], q.vertices[3 * i + k] + ls.rad[i]);
+                    }
+                n += q.n_vertices;
+            }
             if (n == 0) { for (int k = 0; k < 3; k++) { lo[k] = -1; hi[k] = 1; } }
             g.lo = mk(lo[0], lo[1], lo[2]);
             g.hi = mk(hi[0], hi[1], hi[2]);
@@ -561,9 +652,11 @@ static Scene *scene_create(const gxy_scene_desc *d) {
     s->vols_desc.assign(d->volumes, d->volumes + d->n_volumes);
     s->tris_desc.assign(d->triangles, d->triangles + d->n_triangle_sets);
     s->parts_desc.assign(d->particles, d->particles + d->n_particle_sets);
+    if (d->n_pathline_sets > 0) s->lines_desc.assign(d->pathlines, d->pathlines + d->n_pathline_sets);
     s->desc.volumes = s->vols_desc.data();
     s->desc.triangles = s->tris_desc.data();
     s->desc.particles = s->parts_desc.data();
+    s->desc.pathlines = s->lines_desc.data();
     if (!(s->desc.sampling_rate > 0)) s->desc.sampling_rate = 1.0f;
     if (!(s->desc.opaque_alpha > 0)) s->desc.opaque_alpha = 0.999f;
     for (auto &v : s->vols_desc) {
@@ -607,6 +700,18 @@ static Scene *scene_create(const gxy_scene_desc *d) {
             g.srad.push_back(sphere_radius(p, i));
         }
         g.n_sph += p.n;
+    }
+    for (auto &q : s->lines_desc) {
+        Geo::LineSet ls{&q, g.n_tri + g.n_sph + g.n_seg, {}};
+        for (int64_t i = 0; i < q.n_vertices; i++) ls.rad.push_back(pathline_radius(q, i));
+        for (int64_t i = 0; i < q.n_segments; i++) {
+            const float *a = q.vertices + 3 * (int64_t)q.indices[i], *b = a + 3;
+            g.la.push_back(mk(a[0], a[1], a[2]));
+            g.lb.push_back(mk(b[0], b[1], b[2]));
+            g.lr.push_back(q.radius0);
+        }
+        g.n_seg += q.n_segments;
+        g.lsets.push_back(std::move(ls));
     }
     build_bvh(g);
     setup_partitions(*s);
@@ -756,6 +861,31 @@ static void trace_one(const Scene &S, int part, Rays &R, int i, Stats *st, doubl
                         float dv = bx * tv.data[ix[0]] + by * tv.data[ix[1]] + bz * tv.data[ix[2]];
                         colr = tf_color<float>(tv.tf, dv);
                     }
+                } else if (p >= g.n_tri + g.n_sph) {
+                    // DataDrivenPathLines.ispc:186-196 (u, Ng) and 213-268 (colour)
+                    const Geo::LineSet *ls = &g.lsets[0];
+                    for (auto &q : g.lsets)
+                        if (p >= q.base) ls = &q;
+                    const gxy_pathlines_vis &lv = *ls->v;
+                    const int32_t idx = lv.indices[p - ls->base];
+                    const float *va = lv.vertices + 3 * (int64_t)idx;
+                    F3 A = mk(va[0], va[1], va[2]), B = mk(va[3], va[4], va[5]);
+                    F3 P = org + gh.t * dir;
+                    float u = dot(P - A, B - A) * (1.0f / dot(B - A, B - A));
+                    u = std::min(std::max(u, 0.f), 1.f);
+                    F3 PonAxis = A + u * (B - A);
+                    Ng = normalize(P - PonAxis);
+                    Ns = Ng;
+                    float radius = ((1.f - u) * ls->rad[idx]) + (u * ls->rad[idx + 1]);
+                    const float r0 = lv.radius0, r1 = lv.radius1, v0 = lv.value0, v1 = lv.value1;
+                    float dataval;
+                    if (r0 == r1) dataval = v0;
+                    else if (r0 < r1 && radius < r0) dataval = v0;
+                    else if (r0 < r1 && radius > r1) dataval = v1;
+                    else if (r0 > r1 && radius < r1) dataval = v1;
+                    else if (r0 > r1 && radius > r0) dataval = v0;
+                    else dataval = v0 + ((radius - r0) / (r1 - r0)) * (v1 - v0);
+                    colr = tf_color<float>(lv.tf, dataval);
                 } else {
                     int64_t s = p - g.n_tri;
                     const Geo::SphSet *ss = &g.ssets[0];

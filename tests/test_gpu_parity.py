@@ -132,10 +132,12 @@ def _hit_agreement(a, b):
     return float(np.mean(ha == hb)), ha & hb
 
 
-@pytest.mark.parametrize("which", ["triangles", "mixed", "iso"])
+@pytest.mark.parametrize("which", ["triangles", "mixed", "iso", "pathlines"])
 def test_raylist_trace_matches_oracle(gpu, which):
     if which == "triangles":
         cam, vis = scenes.triangle_spheres_scene(width=128, height=128, n_seg=32)
+    elif which == "pathlines":
+        cam, vis = scenes.pathlines_scene(n_lines=600, n_vertices=48, width=128, height=128)
     elif which == "mixed":
         cam, vis = scenes.mixed_scene(n=64, n_spheres=20000, width=96, height=96, partitions=(1, 1, 1), n_ao=4)
     else:
@@ -163,6 +165,26 @@ def test_raylist_trace_matches_oracle(gpu, which):
     ca = gpu.classify(ua)
     cb = o.classify(ub)
     assert np.mean(ca.classification == cb.classification) >= 0.9999
+
+
+@pytest.mark.parametrize("case", ["lines", "lines_bricks", "lines_volume"])
+def test_pathlines_match_oracle(gpu, case):
+    """PathLinesVis: capsule segments (DataDrivenPathLines.ispc:100-203) with
+    the post-intersect colour mapping, alone, across 2x2x1 bricks, and inside
+    a volume (split passes)."""
+    if case == "lines":
+        cam, vis = scenes.pathlines_scene(n_lines=800, n_vertices=48, width=128, height=128)
+    elif case == "lines_bricks":
+        cam, vis = scenes.pathlines_scene(n_lines=800, n_vertices=48, width=128, height=128, partitions=(2, 2, 1))
+    else:
+        cam, vis = scenes.pathlines_scene(n_lines=800, n_vertices=48, width=128, height=128, volume=True,
+                                          partitions=(2, 1, 1))
+    img, ref, sc, cnt = render_both(gpu, cam, vis)
+    image_close(img, ref)
+    c = sc.counters()
+    assert c["primary_rays"] == cnt["primary"]
+    assert c["shadow_rays"] == cnt["shadow"] and c["ao_rays"] == cnt["ao"]
+    assert c["shadow_rays"] > 100   # the lines are hit
 
 
 def test_assign_destinations_identical(gpu):
