@@ -93,7 +93,8 @@ class gxy_scene_desc(C.Structure):
                 ("has_box", C.c_int32), ("box", C.c_float * 6),
                 ("sampling_rate", C.c_float), ("opaque_alpha", C.c_float),
                 ("epsilon", C.c_float),
-                ("n_pathline_sets", C.c_int32), ("pathlines", C.POINTER(gxy_pathlines_vis))]
+                ("n_pathline_sets", C.c_int32), ("pathlines", C.POINTER(gxy_pathlines_vis)),
+                ("n_partition_extents", C.c_int32), ("partition_extents", f32p)]
 
 
 RAY_FLOAT_FIELDS = ("ox", "oy", "oz", "dx", "dy", "dz", "nx", "ny", "nz", "sample",

@@ -394,7 +394,7 @@ __device__ __forceinline__ void line_cylinder(V3 org, V3 dir, V3 A0, V3 B0, floa
         t_out = c_out;
     }
 }
-static __device__ __noinline__ bool line_test(V3 org, V3 dir, V3 A, V3 B, float r, float t0, float tfar, float &t) {
+static __device__ __forceinline__ bool line_test(V3 org, V3 dir, V3 A, V3 B, float r, float t0, float tfar, float &t) {
     float t_in = INFINITY, t_out = -INFINITY;
     line_cylinder(org, dir, A, B, r, t_in, t_out);
     line_sphere(org, dir, A, r, t_in, t_out);
@@ -633,6 +633,9 @@ __device__ __forceinline__ bool trav_init(const DevScene &S, TravState &T, V3 or
 }
 
 // One node visit; returns true when the traversal is complete.
+// LINES: the scene has path-line segments (their test is compiled in only
+// then, so the register budget of the common case is unchanged).
+template <bool LINES>
 __device__ __forceinline__ bool trav_step(const DevScene &S, TravState &T, uint2 *stack, unsigned &nodes,
                                           unsigned &tris, unsigned &sphs, int &ovf) {
     while (!(T.cur_tn <= T.h.t)) {
@@ -668,7 +671,7 @@ __device__ __forceinline__ bool trav_step(const DevScene &S, TravState &T, uint2
             uint32_t id = __float_as_uint(r0.w);
             float t, u = 0.0f, v = 0.0f;
             bool ok;
-            if (id & kLineBit) {
+            if (LINES && (id & kLineBit)) {
                 tris++;   // path-line segments count as primitive tests with triangles
                 ok = line_test(org, dir, v3(r0.x, r0.y, r0.z), v3(r1.x, r1.y, r1.z), r1.w, t0, tfar, t);
             } else if (id & kSphereBit) {

@@ -245,7 +245,70 @@ struct Scene {
 
 // Brick partitions and neighbours: Volume::partition (Volume.cpp:133-172,
 // 371-390) on the first volume's grid, or an even split of the geometry box.
+// Bricks of a scene: a partition document's extents, else the brick grid.
+static int desc_partition_count(const gxy_scene_desc &d) {
+    if (d.n_partition_extents > 0) return d.n_partition_extents;
+    return (d.partitions[0] < 1 ? 1 : d.partitions[0]) * (d.partitions[1] < 1 ? 1 : d.partitions[1]) *
+           (d.partitions[2] < 1 ? 1 : d.partitions[2]);
+}
+static int check_partition_extents(const gxy_scene_desc &d) {
+    if (d.n_partition_extents < 0 || d.n_partition_extents > kMaxPart)
+        return set_error(GXY_ERR_INVALID, "bad partition extent count");
+    if (d.n_partition_extents > 0 && !d.partition_extents)
+        return set_error(GXY_ERR_INVALID, "partition extents missing");
+    for (int p = 0; p < d.n_partition_extents; p++)
+        for (int a = 0; a < 3; a++)
+            if (!(d.partition_extents[6 * p + 2 * a] <= d.partition_extents[6 * p + 2 * a + 1]))
+                return set_error(GXY_ERR_INVALID, "partition extent with min > max");
+    return GXY_OK;
+}
+
 static void make_partitions(const gxy_scene_desc &d, const std::vector<float> &geo_box, DevScene &S) {
+    if (d.n_partition_extents > 0) {
+        // Geometry::get_partitioning (Geometry.cpp:279-350): boxes from the
+        // document, global box their union, neighbour i of brick p on a face
+        // when i's extent touches that face and starts where p starts on the
+        // other two axes (a later match wins, as in Galaxy's loop)
+        const int n = d.n_partition_extents;
+        const float *E = d.partition_extents;
+        S.np = n;
+        float g[6] = {FLT_MAX, -FLT_MAX, FLT_MAX, -FLT_MAX, FLT_MAX, -FLT_MAX};
+        for (int i = 0; i < n; i++) {
+            const float *e = E + 6 * i;
+            if (e[0] < g[0]) g[0] = e[0];
+            if (e[1] > g[1]) g[1] = e[1];
+            if (e[2] < g[2]) g[2] = e[2];
+            if (e[3] > g[3]) g[3] = e[3];
+            if (e[4] < g[4]) g[4] = e[4];
+            if (e[5] > g[5]) g[5] = e[5];
+        }
+        for (int a = 0; a < 3; a++) {
+            S.glo[a] = g[2 * a];
+            S.ghi[a] = g[2 * a + 1];
+        }
+        for (int p = 0; p < n; p++) {
+            const float *l = E + 6 * p;
+            DevPartition &P = S.part[p];
+            for (int a = 0; a < 3; a++) {
+                P.lo[a] = l[2 * a];
+                P.hi[a] = l[2 * a + 1];
+            }
+            for (int k = 0; k < 6; k++) P.nb[k] = -1;
+            for (int i = 0; i < n; i++) {
+                const float *e = E + 6 * i;
+                auto last = [&](int a) { return e[2 * a + 1] == l[2 * a]; };
+                auto next = [&](int a) { return e[2 * a] == l[2 * a + 1]; };
+                auto eq = [&](int a) { return e[2 * a] == l[2 * a]; };
+                if (last(0) && eq(1) && eq(2)) P.nb[0] = i;
+                if (next(0) && eq(1) && eq(2)) P.nb[1] = i;
+                if (eq(0) && last(1) && eq(2)) P.nb[2] = i;
+                if (eq(0) && next(1) && eq(2)) P.nb[3] = i;
+                if (eq(0) && eq(1) && last(2)) P.nb[4] = i;
+                if (eq(0) && eq(1) && next(2)) P.nb[5] = i;
+            }
+        }
+        return;
+    }
     int PX = d.partitions[0] < 1 ? 1 : d.partitions[0];
     int PY = d.partitions[1] < 1 ? 1 : d.partitions[1];
     int PZ = d.partitions[2] < 1 ? 1 : d.partitions[2];
@@ -330,8 +393,9 @@ static int commit(const gxy_scene_desc *d, Scene *sc) {
     if (d->n_triangle_sets < 0 || d->n_triangle_sets > 4 || d->n_particle_sets < 0 || d->n_particle_sets > 4 ||
         d->n_pathline_sets < 0 || d->n_pathline_sets > 4)
         return set_error(GXY_ERR_INVALID, "at most 4 triangle, 4 particle and 4 path-line sets");
-    int np = (d->partitions[0] < 1 ? 1 : d->partitions[0]) * (d->partitions[1] < 1 ? 1 : d->partitions[1]) *
-             (d->partitions[2] < 1 ? 1 : d->partitions[2]);
+    int rc = check_partition_extents(*d);
+    if (rc) return rc;
+    int np = desc_partition_count(*d);
     if (np > kMaxPart) return set_error(GXY_ERR_INVALID, "too many partitions");
     float rate = d->sampling_rate > 0 ? d->sampling_rate : 1.0f;
     S.rate = rate;
@@ -345,7 +409,6 @@ static int commit(const gxy_scene_desc *d, Scene *sc) {
     S.epsilon = d->epsilon;
     std::vector<DevTF> tfs;
     S.step = -1;
-    int rc;
     for (int m = 0; m < d->n_volumes; m++) {
         const gxy_volume_vis &v = d->volumes[m];
         if (!v.samples || v.counts[0] < 2 || v.counts[1] < 2 || v.counts[2] < 2)
@@ -1136,7 +1199,7 @@ __global__ void __launch_bounds__(kThreads, MINB) k_batch_gen(DevScene Su, Frame
 // finishes the query (cull, or append to the march queue with the stop
 // distance and surface flag) and takes the next ray of the shadow+AO input,
 // so warps stay full while traversals of different lengths proceed.
-template <bool BATCH, int MINB>
+template <bool BATCH, int MINB, bool LINES>
 __global__ void __launch_bounds__(kThreads, MINB) k_sec_query(DevScene S, FrameArgs A) {
     RayStats st;
     LocalCounters c;
@@ -1194,7 +1257,7 @@ __global__ void __launch_bounds__(kThreads, MINB) k_sec_query(DevScene S, FrameA
         // one copy of the step body: unrolled copies overflow the instruction cache
 #pragma unroll 1
         for (int k = 0; k < max(A.trav_steps, 1) && have && !done; k++)
-            done = trav_step(S, T, stack, st.nodes, st.tris, st.sphs, st.ovf);
+            done = trav_step<LINES>(S, T, stack, st.nodes, st.tris, st.sphs, st.ovf);
         bool fin = have && done;
         bool to_march = false;
         if (fin) {
@@ -1232,7 +1295,7 @@ __global__ void __launch_bounds__(kThreads, MINB) k_sec_query(DevScene S, FrameA
 // first record of pixel i goes to slot i and a pixel whose ray enters no
 // brick leaves a hole record (meta -1) there, so the march pass reads the
 // records in pixel order; further bricks of one pixel go after slot npix.
-template <bool BATCH, int MINB>
+template <bool BATCH, int MINB, bool LINES>
 __global__ void __launch_bounds__(kThreads, MINB) k_cam_query(DevScene S, FrameArgs A) {
     __shared__ DevTF tfs[kMaxVol];
     __shared__ long long pix0[BATCH ? kMaxJobs : 1];
@@ -1325,7 +1388,7 @@ __global__ void __launch_bounds__(kThreads, MINB) k_cam_query(DevScene S, FrameA
         if (!__any_sync(0xffffffffu, have || pending != 0 || !exhausted)) break;
 #pragma unroll 1
         for (int k = 0; k < max(A.trav_steps, 1) && have && !done; k++)
-            done = trav_step(S, T, stack, st.nodes, st.tris, st.sphs, st.ovf);
+            done = trav_step<LINES>(S, T, stack, st.nodes, st.tris, st.sphs, st.ovf);
         bool fin = have && done;
         if (fin && T.found) {
             ray_t = T.h.t;
@@ -1715,7 +1778,7 @@ static unsigned march_grid(int minb) {
 static unsigned query_grid() {
     int sms = 152, per = 1;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, g_device);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_sec_query<false, 4>, kThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_sec_query<false, 4, false>, kThreads, 0);
     return (unsigned)(sms * (per < 1 ? 1 : per));
 }
 
@@ -1819,6 +1882,7 @@ static int render(Scene *sc, const gxy_camera &cam, const gxy_lighting &lt, floa
         CK(cudaEventCreateWithFlags(&sc->fork, cudaEventDisableTiming));
         CK(cudaEventCreateWithFlags(&sc->join, cudaEventDisableTiming));
     }
+    const bool lines = S.n_seg > 0;
     auto launch = [&](int kind, int gen, unsigned rays_in, int64_t items, cudaStream_t st) -> int {
         if (nl >= maxl) return set_error(GXY_ERR_TIMEOUT, "too many launches in one frame");
         A.ctr = sc->ctr + nl;
@@ -1827,18 +1891,22 @@ static int render(Scene *sc, const gxy_camera &cam, const gxy_lighting &lt, floa
         if (kind == K_SECONDARY && A.split) CK(cudaMemsetAsync(A.qmarch_count, 0, 3 * sizeof(unsigned), st));
         if (kind == K_CAMERA && A.split_prim) CK(cudaMemsetAsync(A.pmarch_count, 0, 4 * sizeof(unsigned), st));
         if (g_tune_minb == 3) {
-            if (kind == K_CAMERA && A.split_prim) k_cam_query<false, 4><<<query_grid(), kThreads, 0, st>>>(S, A);
+            if (kind == K_CAMERA && A.split_prim && lines) k_cam_query<false, 4, true><<<query_grid(), kThreads, 0, st>>>(S, A);
+            else if (kind == K_CAMERA && A.split_prim) k_cam_query<false, 4, false><<<query_grid(), kThreads, 0, st>>>(S, A);
             else if (kind == K_CAMERA) k_primary<K_CAMERA, 3><<<g, kThreads, 0, st>>>(S, A);
             else if (kind == K_PRIMARY) k_primary<K_PRIMARY, 3><<<g, kThreads, 0, st>>>(S, A);
-            else if (kind == K_SECONDARY && A.split) k_sec_query<false, 4><<<query_grid(), kThreads, 0, st>>>(S, A);
+            else if (kind == K_SECONDARY && A.split && lines) k_sec_query<false, 4, true><<<query_grid(), kThreads, 0, st>>>(S, A);
+            else if (kind == K_SECONDARY && A.split) k_sec_query<false, 4, false><<<query_grid(), kThreads, 0, st>>>(S, A);
             else if (kind == K_SECONDARY) k_secondary<3><<<g, kThreads, 0, st>>>(S, A);
             else if (kind == K_PMARCH) k_prim_march<false, 3><<<march_grid(3), kThreads, 0, st>>>(S, A);
             else k_sec_march<false, 3><<<march_grid(3), kThreads, 0, st>>>(S, A);
         } else {
-            if (kind == K_CAMERA && A.split_prim) k_cam_query<false, 2><<<march_grid(2), kThreads, 0, st>>>(S, A);
+            if (kind == K_CAMERA && A.split_prim && lines) k_cam_query<false, 2, true><<<march_grid(2), kThreads, 0, st>>>(S, A);
+            else if (kind == K_CAMERA && A.split_prim) k_cam_query<false, 2, false><<<march_grid(2), kThreads, 0, st>>>(S, A);
             else if (kind == K_CAMERA) k_primary<K_CAMERA, 2><<<g, kThreads, 0, st>>>(S, A);
             else if (kind == K_PRIMARY) k_primary<K_PRIMARY, 2><<<g, kThreads, 0, st>>>(S, A);
-            else if (kind == K_SECONDARY && A.split) k_sec_query<false, 2><<<march_grid(2), kThreads, 0, st>>>(S, A);
+            else if (kind == K_SECONDARY && A.split && lines) k_sec_query<false, 2, true><<<march_grid(2), kThreads, 0, st>>>(S, A);
+            else if (kind == K_SECONDARY && A.split) k_sec_query<false, 2, false><<<march_grid(2), kThreads, 0, st>>>(S, A);
             else if (kind == K_SECONDARY) k_secondary<2><<<g, kThreads, 0, st>>>(S, A);
             else if (kind == K_PMARCH) k_prim_march<false, 2><<<march_grid(2), kThreads, 0, st>>>(S, A);
             else k_sec_march<false, 2><<<march_grid(2), kThreads, 0, st>>>(S, A);
@@ -2074,8 +2142,9 @@ int gxy_gpu_scene_partition_info(gxy_scene scene, int partition, gxy_partition_i
 int gxy_scene_partition_layout(const gxy_scene_desc *desc, int partition, gxy_partition_info *out) {
     GUARD_BEGIN
     if (!desc || !out) return set_error(GXY_ERR_INVALID, "null argument");
-    int np = (desc->partitions[0] < 1 ? 1 : desc->partitions[0]) * (desc->partitions[1] < 1 ? 1 : desc->partitions[1]) *
-             (desc->partitions[2] < 1 ? 1 : desc->partitions[2]);
+    int rc = check_partition_extents(*desc);
+    if (rc) return rc;
+    int np = desc_partition_count(*desc);
     if (np > kMaxPart || partition < 0 || partition >= np) return set_error(GXY_ERR_INVALID, "bad partition");
     // geometry box as the commit computes it
     std::vector<float> g = {FLT_MAX, FLT_MAX, FLT_MAX, -FLT_MAX, -FLT_MAX, -FLT_MAX};
@@ -2541,6 +2610,7 @@ static int batch_enqueue(Batch *b, const DevScene &Su, bool uniform, const Frame
         // then per generation the continuing primaries (side stream) beside
         // the shadow/AO query and march; counts are read on the device.
         const int grid = gen_grid(true);
+        const bool lines = Su.n_seg > 0;
         for (int g = 0; g < kBatchGens; g++) {
             FrameArgs a = A;
             for (int k = 0; k < NQ; k++) {
@@ -2562,10 +2632,12 @@ static int batch_enqueue(Batch *b, const DevScene &Su, bool uniform, const Frame
             const bool mb3 = g_tune_minb == 3;
             if (g == 0) {
                 if (mb3) {
-                    k_cam_query<true, 4><<<query_grid(), kThreads, 0, st>>>(Su, a);
+                    if (lines) k_cam_query<true, 4, true><<<query_grid(), kThreads, 0, st>>>(Su, a);
+                    else k_cam_query<true, 4, false><<<query_grid(), kThreads, 0, st>>>(Su, a);
                     k_prim_march<true, 3><<<march_grid(3), kThreads, 0, st>>>(Su, a);
                 } else {
-                    k_cam_query<true, 2><<<march_grid(2), kThreads, 0, st>>>(Su, a);
+                    if (lines) k_cam_query<true, 2, true><<<march_grid(2), kThreads, 0, st>>>(Su, a);
+                    else k_cam_query<true, 2, false><<<march_grid(2), kThreads, 0, st>>>(Su, a);
                     k_prim_march<true, 2><<<march_grid(2), kThreads, 0, st>>>(Su, a);
                 }
             } else {
@@ -2575,10 +2647,12 @@ static int batch_enqueue(Batch *b, const DevScene &Su, bool uniform, const Frame
                 else k_batch_gen<K_PRIMARY, true, 2><<<grid, kThreads, 0, b->side>>>(Su, a, cin);
                 CK(cudaEventRecord(b->join[g], b->side));
                 if (mb3) {
-                    k_sec_query<true, 4><<<query_grid(), kThreads, 0, st>>>(Su, a);
+                    if (lines) k_sec_query<true, 4, true><<<query_grid(), kThreads, 0, st>>>(Su, a);
+                    else k_sec_query<true, 4, false><<<query_grid(), kThreads, 0, st>>>(Su, a);
                     k_sec_march<true, 3><<<march_grid(3), kThreads, 0, st>>>(Su, a);
                 } else {
-                    k_sec_query<true, 2><<<march_grid(2), kThreads, 0, st>>>(Su, a);
+                    if (lines) k_sec_query<true, 2, true><<<march_grid(2), kThreads, 0, st>>>(Su, a);
+                    else k_sec_query<true, 2, false><<<march_grid(2), kThreads, 0, st>>>(Su, a);
                     k_sec_march<true, 2><<<march_grid(2), kThreads, 0, st>>>(Su, a);
                 }
                 CK(cudaStreamWaitEvent(st, b->join[g], 0));

@@ -292,18 +292,40 @@ class Volume:
 
     @classmethod
     def load_vol(cls, path):
-        toks = open(path).read().split()
-        kind = toks[0]
-        if kind != "float":
-            raise ValueError("only float volumes are supported")
-        origin = [float(x) for x in toks[1:4]]
-        counts = [int(x) for x in toks[4:7]]
-        deltas = [float(x) for x in toks[7:10]]
-        raw = toks[10]
+        """Volume header as Volume::local_import reads it (Volume.cpp:195-297):
+        a .vol text header -- type, origin, counts, deltas, raw file name --
+        or a .json header with "type", "origin", "counts", "delta",
+        "rawdata" and optional "number of components".  Raw data are float32
+        or uchar (read as their float values); the raw file name is
+        relative to the header's directory.  Multi-component volumes are
+        not rendered."""
+        if path.endswith(".json"):
+            import json
+            doc = json.load(open(path))
+            for k in ("type", "origin", "counts", "delta", "rawdata"):
+                if k not in doc:
+                    raise ValueError("volume JSON has no %s field: %s" % (k, path))
+            kind = doc["type"]
+            origin = [float(x) for x in doc["origin"]]
+            counts = [int(x) for x in doc["counts"]]
+            deltas = [float(x) for x in doc["delta"]]
+            raw = doc["rawdata"]
+            if int(doc.get("number of components", 1)) != 1:
+                raise ValueError("multi-component volumes are not rendered")
+        else:
+            toks = open(path).read().split()
+            kind = toks[0]
+            origin = [float(x) for x in toks[1:4]]
+            counts = [int(x) for x in toks[4:7]]
+            deltas = [float(x) for x in toks[7:10]]
+            raw = toks[10]
         if not raw.startswith("/"):
             raw = os.path.join(os.path.dirname(path), raw)
-        a = np.fromfile(raw, np.float32, count=counts[0] * counts[1] * counts[2])
-        return cls(a.reshape(counts[2], counts[1], counts[0]), origin, deltas)
+        n = counts[0] * counts[1] * counts[2]
+        a = np.fromfile(raw, np.float32 if kind == "float" else np.uint8, count=n)
+        if a.size != n:
+            raise ValueError("raw data file %s holds %d of %d samples" % (raw, a.size, n))
+        return cls(a.astype(np.float32).reshape(counts[2], counts[1], counts[0]), origin, deltas)
 
 
 class Triangles:
@@ -353,10 +375,14 @@ class Visualization:
     threshold and Renderer.epsilon."""
 
     def __init__(self, operators=(), lighting=None, partitions=(1, 1, 1), box=None,
-                 sampling_rate=1.0, opaque_alpha=0.999, epsilon=0.001):
+                 sampling_rate=1.0, opaque_alpha=0.999, epsilon=0.001, partition_extents=None):
         self.operators = list(operators)
         self.lighting = lighting if lighting is not None else Lighting()
         self.partitions = tuple(int(p) for p in partitions)
+        # explicit bricks from a partition document (see partition_document);
+        # when given they replace the brick grid
+        self.partition_extents = (None if partition_extents is None
+                                  else np.ascontiguousarray(partition_extents, np.float32).reshape(-1, 6))
         self.box = box
         self.sampling_rate = float(sampling_rate)
         self.opaque_alpha = float(opaque_alpha)
@@ -430,6 +456,10 @@ class Visualization:
         la = (A.gxy_pathlines_vis * max(1, len(lines)))(*lines)
         d.n_pathline_sets, d.pathlines = len(lines), C.cast(la, C.POINTER(A.gxy_pathlines_vis))
         d.partitions[:] = list(self.partitions)
+        if self.partition_extents is not None:
+            d.n_partition_extents = len(self.partition_extents)
+            d.partition_extents = A.fptr(self.partition_extents)
+            keep.append(self.partition_extents)
         if self.box is not None:
             d.has_box = 1
             d.box[:] = [float(x) for x in self.box]
@@ -438,6 +468,26 @@ class Visualization:
         d.epsilon = self.epsilon
         d._keep = (keep, va, ta, pa, la)
         return d
+
+
+def partition_document(doc):
+    """Brick extents of a Galaxy partition document (a dict, JSON text or a
+    path): {"parts": [{"extent": [xmin, xmax, ymin, ymax, zmin, zmax], ...},
+    ...]}, one part per brick, as Geometry::get_partitioning reads it
+    (Geometry.cpp:279-312).  Returns a float32 (n, 6) array for
+    Visualization(partition_extents=...)."""
+    import json
+    if isinstance(doc, str):
+        doc = json.load(open(doc)) if os.path.exists(doc) else json.loads(doc)
+    if "parts" not in doc:
+        raise ValueError("partition document does not have parts")
+    parts = doc["parts"]
+    if not isinstance(parts, list) or not parts:
+        raise ValueError("invalid partition document")
+    ext = np.array([[float(x) for x in p["extent"]] for p in parts], np.float32)
+    if ext.shape[1] != 6:
+        raise ValueError("a partition extent has 6 numbers")
+    return ext
 
 
 def load_state(path, partitions=(1, 1, 1)):

@@ -179,6 +179,12 @@ typedef struct gxy_scene_desc {
     float   epsilon;         /* Renderer.epsilon; 0.001 in Galaxy                      */
     int32_t                  n_pathline_sets;   /* at most 4 */
     const gxy_pathlines_vis *pathlines;
+    /* Galaxy partition document (Geometry::get_partitioning, Geometry.cpp:279-350):
+     * when n_partition_extents > 0, brick p is partition_extents[6p .. 6p+5] =
+     * xmin xmax ymin ymax zmin zmax, face neighbours are found by Galaxy's
+     * matching rules, and partitions[] is ignored.  At most 64. */
+    int32_t                  n_partition_extents;
+    const float             *partition_extents;
 } gxy_scene_desc;
 
 /* RayList_ispc (Rays.ih:21-48): 25 SoA arrays plus the count.  Host memory. */

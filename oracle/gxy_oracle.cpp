@@ -551,6 +551,7 @@ struct Scene {
     std::vector<gxy_triangles_vis> tris_desc;
     std::vector<gxy_particles_vis> parts_desc;
     std::vector<gxy_pathlines_vis> lines_desc;
+    std::vector<float> extents;    // partition document, 6 per brick
     std::vector<Vol> vols;
     Geo geo;
     Box gbox;
@@ -565,6 +566,48 @@ struct Scene {
 // uniform split of the geometry box; neighbours as Volume.cpp:371-376.
 static void setup_partitions(Scene &s) {
     const gxy_scene_desc &d = s.desc;
+    if (d.n_partition_extents > 0) {
+        // Geometry::get_partitioning (Geometry.cpp:279-350)
+        const int n = d.n_partition_extents;
+        const float *E = s.extents.data();
+        s.np = n;
+        s.lbox.resize(n);
+        s.neighbors.assign(6 * n, -1);
+        float g[6] = {FLT_MAX, -FLT_MAX, FLT_MAX, -FLT_MAX, FLT_MAX, -FLT_MAX};
+        for (int i = 0; i < n; i++) {
+            const float *e = E + 6 * i;
+            if (e[0] < g[0]) g[0] = e[0];
+            if (e[1] > g[1]) g[1] = e[1];
+            if (e[2] < g[2]) g[2] = e[2];
+            if (e[3] > g[3]) g[3] = e[3];
+            if (e[4] < g[4]) g[4] = e[4];
+            if (e[5] > g[5]) g[5] = e[5];
+        }
+        s.gbox.lo = mk(g[0], g[2], g[4]);
+        s.gbox.hi = mk(g[1], g[3], g[5]);
+        for (int p = 0; p < n; p++) {
+            const float *l = E + 6 * p;
+            s.lbox[p].lo = mk(l[0], l[2], l[4]);
+            s.lbox[p].hi = mk(l[1], l[3], l[5]);
+            int *nb = &s.neighbors[6 * p];
+            for (int i = 0; i < n; i++) {
+                const float *e = E + 6 * i;
+#define LAST(a) (e[2 * (a) + 1] == l[2 * (a)])
+#define NEXT(a) (e[2 * (a)] == l[2 * (a) + 1])
+#define EQ(a) (e[2 * (a)] == l[2 * (a)])
+                if (LAST(0) && EQ(1) && EQ(2)) nb[0] = i;
+                if (NEXT(0) && EQ(1) && EQ(2)) nb[1] = i;
+                if (EQ(0) && LAST(1) && EQ(2)) nb[2] = i;
+                if (EQ(0) && NEXT(1) && EQ(2)) nb[3] = i;
+                if (EQ(0) && EQ(1) && LAST(2)) nb[4] = i;
+                if (EQ(0) && EQ(1) && NEXT(2)) nb[5] = i;
+#undef LAST
+#undef NEXT
+#undef EQ
+            }
+        }
+        return;
+    }
     int PX = std::max(1, d.partitions[0]), PY = std::max(1, d.partitions[1]), PZ = std::max(1, d.partitions[2]);
     s.np = PX * PY * PZ;
     s.lbox.resize(s.np);
@@ -653,6 +696,9 @@ static Scene *scene_create(const gxy_scene_desc *d) {
     s->tris_desc.assign(d->triangles, d->triangles + d->n_triangle_sets);
     s->parts_desc.assign(d->particles, d->particles + d->n_particle_sets);
     if (d->n_pathline_sets > 0) s->lines_desc.assign(d->pathlines, d->pathlines + d->n_pathline_sets);
+    if (d->n_partition_extents > 0)
+        s->extents.assign(d->partition_extents, d->partition_extents + 6 * d->n_partition_extents);
+    s->desc.partition_extents = s->extents.data();
     s->desc.volumes = s->vols_desc.data();
     s->desc.triangles = s->tris_desc.data();
     s->desc.particles = s->parts_desc.data();

@@ -187,6 +187,26 @@ def test_pathlines_match_oracle(gpu, case):
     assert c["shadow_rays"] > 100   # the lines are hit
 
 
+def test_partition_document_render(gpu):
+    """Bricks from a Galaxy partition document: uneven bricks match the
+    oracle, and a document equal to the 2x2x1 grid renders the grid's image."""
+    doc = {"parts": [{"extent": [0, 0.3, 0, 1, 0, 1]}, {"extent": [0.3, 0.7, 0, 1, 0, 1]},
+                     {"extent": [0.7, 1, 0, 0.5, 0, 1]}, {"extent": [0.7, 1, 0.5, 1, 0, 1]}]}
+    cam, vis = scenes.pathlines_scene(n_lines=800, n_vertices=48, width=128, height=128)
+    vis.partition_extents = S.partition_document(doc)
+    img, ref, sc, cnt = render_both(gpu, cam, vis)
+    image_close(img, ref)
+    assert sc.counters()["primary_rays"] == cnt["primary"]
+    grid = {"parts": [{"extent": [x0, x1, y0, y1, 0, 1]} for (y0, y1) in ((0, 0.5), (0.5, 1))
+                      for (x0, x1) in ((0, 0.5), (0.5, 1))]}
+    cam, vis = scenes.pathlines_scene(n_lines=800, n_vertices=48, width=128, height=128, partitions=(2, 2, 1))
+    L = S.resolve_lights(vis.lighting, cam)
+    a = gpu.Scene(vis).render_host(cam, L)
+    vis.partition_extents = S.partition_document(grid)
+    b = gpu.Scene(vis).render_host(cam, L)
+    np.testing.assert_allclose(a, b, atol=1e-6)
+
+
 def test_assign_destinations_identical(gpu):
     cam, vis = scenes.mixed_scene(n=64, n_spheres=2000, width=64, height=64, partitions=(2, 2, 2))
     L = S.resolve_lights(vis.lighting, cam)
