@@ -1209,8 +1209,7 @@ __global__ void __launch_bounds__(kThreads, MINB) k_sec_query(DevScene S, FrameA
     unsigned *cursor = A.qmarch_count + 2;
     TravState T;
     uint2 stack[64];
-    TraceIn in;
-    int x = 0, y = 0, job = 0;
+    unsigned src = 0;   // the lane's input record (shadow, then AO index space)
     float ray_t = 0.0f;
     bool have = false, done = false, surface = false, slice_ahead = false, zero = false;
     for (;;) {
@@ -1224,6 +1223,9 @@ __global__ void __launch_bounds__(kThreads, MINB) k_sec_query(DevScene S, FrameA
         if (need) {
             unsigned idx = base + __popc(mask & ((1u << lane) - 1u));
             if (idx < n) {
+                TraceIn in;
+                int x, y, job;
+                src = idx;
                 load_ray(idx < ns ? A.qin[Q_SHADOW] : A.qin[Q_AO], idx < ns ? idx : idx - ns, in, x, y, job);
                 c.seg++;
                 V3 dir;
@@ -1273,12 +1275,18 @@ __global__ void __launch_bounds__(kThreads, MINB) k_sec_query(DevScene S, FrameA
         if (__any_sync(0xffffffffu, to_march)) {
             unsigned idx = warp_reserve(to_march ? 1u : 0u, A.qmarch_count, A.qmarch_cap, c.ovf);
             if (to_march && idx != 0xffffffffu) {
-                int meta = make_meta(in.type | (surface ? 8 : 0), in.part, job);
+                // the input record with the surface flag in its type bits
+                // (shadow and AO types leave bit 3 free) and the stop distance
+                // in the spare word; re-read here so no ray fields stay live
+                // through the traversal
+                const float4 *q = reinterpret_cast<const float4 *>(src < ns ? A.qin[Q_SHADOW] + src
+                                                                            : A.qin[Q_AO] + (src - ns));
+                int4 m = __ldg(reinterpret_cast<const int4 *>(q + 3));
                 DRay *p = A.qmarch + idx;
-                p->o = make_float4(in.org.x, in.org.y, in.org.z, in.t);
-                p->d = make_float4(in.dir.x, in.dir.y, in.dir.z, in.tmax);
-                p->c = make_float4(in.r, in.g, in.b, in.o);
-                p->m = make_int4(x, y, meta, __float_as_int(ray_t));
+                p->o = __ldg(q);
+                p->d = __ldg(q + 1);
+                p->c = __ldg(q + 2);
+                p->m = make_int4(m.x, m.y, m.z | (surface ? 8 : 0), __float_as_int(ray_t));
             }
         }
         if (fin) have = false;
@@ -1310,8 +1318,12 @@ __global__ void __launch_bounds__(kThreads, MINB) k_cam_query(DevScene S, FrameA
     unsigned *cursor = A.pmarch_count + 2;
     TravState T;
     uint2 stack[64];
-    V3 org = v3(0, 0, 0), dir0 = v3(0, 0, 0), hit_n = v3(0, 0, 0), hit_c = v3(0, 0, 0);
+    V3 hit_n = v3(0, 0, 0), hit_c = v3(0, 0, 0);
     int x = 0, y = 0, part = 0, job = 0;
+    // The camera ray lives in T between bricks and after the query: T.org is
+    // its origin and T.dir its direction with exact zeros replaced by 1e-6;
+    // bit a of zmask marks a component that was zero (no ray copy stays live).
+    int zmask = 0;
     unsigned pix = 0;   // global pixel index (all jobs' pixels in job order)
     uint64_t pending = 0;
     float ray_t = 0.0f;
@@ -1325,6 +1337,8 @@ __global__ void __launch_bounds__(kThreads, MINB) k_cam_query(DevScene S, FrameA
             if (lane == 0) base = atomicAdd(cursor, (unsigned)__popc(mask));
             base = __shfl_sync(0xffffffffu, base, 0);
         }
+        V3 org, dir0;
+        bool fresh = false;
         if (need) {
             unsigned idx = base + __popc(mask & ((1u << lane) - 1u));
             if (idx < npix) {
@@ -1338,6 +1352,7 @@ __global__ void __launch_bounds__(kThreads, MINB) k_cam_query(DevScene S, FrameA
                 x = (int)(li % (unsigned)cam.width);
                 y = (int)(li / (unsigned)cam.width);
                 pending = camera_ray(S, cam, x, y, org, dir0);
+                fresh = true;
                 first = true;
                 if (!pending) A.pmarch[idx].m = make_int4(x, y, -1, 0);
             } else {
@@ -1345,6 +1360,11 @@ __global__ void __launch_bounds__(kThreads, MINB) k_cam_query(DevScene S, FrameA
             }
         }
         if (!have && pending) {
+            if (!fresh) {   // a further brick of the pixel: its ray from T
+                org = T.org;
+                dir0 = v3((zmask & 1) ? 0.f : T.dir.x, (zmask & 2) ? 0.f : T.dir.y, (zmask & 4) ? 0.f : T.dir.z);
+            }
+            zmask = (dir0.x == 0.f ? 1 : 0) | (dir0.y == 0.f ? 2 : 0) | (dir0.z == 0.f ? 4 : 0);
             part = __ffsll((long long)pending) - 1;
             pending &= pending - 1;
             c.prim++;
@@ -1407,8 +1427,9 @@ __global__ void __launch_bounds__(kThreads, MINB) k_cam_query(DevScene S, FrameA
             if (fin && idx != 0xffffffffu) {
                 first = false;
                 DRay *r = A.pmarch + idx;
-                r->o = make_float4(org.x, org.y, org.z, 0.0f);
-                r->d = make_float4(dir0.x, dir0.y, dir0.z, FLT_MAX);
+                r->o = make_float4(T.org.x, T.org.y, T.org.z, 0.0f);
+                r->d = make_float4((zmask & 1) ? 0.f : T.dir.x, (zmask & 2) ? 0.f : T.dir.y,
+                                   (zmask & 4) ? 0.f : T.dir.z, FLT_MAX);
                 r->c = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
                 r->m = make_int4(x, y, make_meta(GXY_RAY_PRIMARY | (surface ? 8 : 0), part, job), __float_as_int(ray_t));
                 A.pmarch_hit[2 * (size_t)idx] = make_float4(hit_n.x, hit_n.y, hit_n.z, hit_c.x);

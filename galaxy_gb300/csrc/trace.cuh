@@ -41,8 +41,8 @@ struct RayStats {
 // and colour, as OSPRay postIntersect with DG_NG|DG_NS|DG_NORMALIZE|
 // DG_FACEFORWARD|DG_COLOR over the DataDrivenTriangleMesh /
 // DataDrivenSpheres / DataDrivenPathLines post-intersect functions.
-__device__ __noinline__ void geometry_shade(const DevScene &S, const GeoHit &gh, V3 org, V3 dir, V3 &n_out,
-                                            V3 &c_out) {
+__device__ __forceinline__ void geometry_shade_body(const DevScene &S, const GeoHit &gh, V3 org, V3 dir, V3 &n_out,
+                                                    V3 &c_out) {
     V3 Ng, Ns;
     V3 col = v3(1.f, 1.f, 1.f);
     if (gh.prim & kLineBit) {
@@ -114,6 +114,11 @@ __device__ __noinline__ void geometry_shade(const DevScene &S, const GeoHit &gh,
     if (dot(Ng, Ns) < 0.f) Ns = neg(Ns);
     n_out = Ns;
     c_out = col;
+}
+// One out-of-line copy: inlined into the refill query loops it raised spills.
+__device__ __noinline__ void geometry_shade(const DevScene &S, const GeoHit &gh, V3 org, V3 dir, V3 &n_out,
+                                            V3 &c_out) {
+    geometry_shade_body(S, gh, org, dir, n_out, c_out);
 }
 
 // tfs: the volumes' transfer functions (shared-memory copies), indexed by volume.
