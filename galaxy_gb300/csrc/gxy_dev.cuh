@@ -633,14 +633,23 @@ __device__ __forceinline__ bool trav_init(const DevScene &S, TravState &T, V3 or
 }
 
 // One node visit; returns true when the traversal is complete.
+// Traversal stack of (node, entry distance) pairs, 64 entries deep, in the
+// lane's local memory.  (A variant with the first 16 entries in shared
+// memory measured slower: the shared allocation takes L1 capacity that the
+// node fetches use.)
+struct LocalStack {
+    uint2 *p;
+    __device__ __forceinline__ uint2 get(int i) const { return p[i]; }
+    __device__ __forceinline__ void set(int i, uint2 v) { p[i] = v; }
+};
 // LINES: the scene has path-line segments (their test is compiled in only
 // then, so the register budget of the common case is unchanged).
-template <bool LINES>
-__device__ __forceinline__ bool trav_step(const DevScene &S, TravState &T, uint2 *stack, unsigned &nodes,
+template <bool LINES, class STACK>
+__device__ __forceinline__ bool trav_step(const DevScene &S, TravState &T, STACK &stack, unsigned &nodes,
                                           unsigned &tris, unsigned &sphs, int &ovf) {
     while (!(T.cur_tn <= T.h.t)) {
         if (T.sp == 0) return true;
-        uint2 e = stack[--T.sp];
+        uint2 e = stack.get(--T.sp);
         T.cur = e.x;
         T.cur_tn = __uint_as_float(e.y);
     }
@@ -702,7 +711,7 @@ __device__ __forceinline__ bool trav_step(const DevScene &S, TravState &T, uint2
             if (j < n_inner) {
                 uint32_t slot = key[j] & 7u;
                 uint32_t mb = (slot < 4 ? meta_lo >> (8 * slot) : meta_hi >> (8 * (slot - 4))) & 0xffu;
-                if (T.sp < 64) stack[T.sp++] = make_uint2(child_base + mb, key[j] & ~7u);
+                if (T.sp < 64) stack.set(T.sp++, make_uint2(child_base + mb, key[j] & ~7u));
                 else ovf = 1;
             }
         }
@@ -713,7 +722,7 @@ __device__ __forceinline__ bool trav_step(const DevScene &S, TravState &T, uint2
         return false;
     }
     if (T.sp == 0) return true;
-    uint2 e = stack[--T.sp];
+    uint2 e = stack.get(--T.sp);
     T.cur = e.x;
     T.cur_tn = __uint_as_float(e.y);
     return false;

@@ -1208,7 +1208,8 @@ __global__ void __launch_bounds__(kThreads, MINB) k_sec_query(DevScene S, FrameA
     const unsigned n = ns + (BATCH ? min(__ldg(A.nin_dev + Q_AO), A.qcap[Q_AO]) : A.nin[Q_AO]);
     unsigned *cursor = A.qmarch_count + 2;
     TravState T;
-    uint2 stack[64];
+    uint2 stack_mem[64];
+    LocalStack stack{stack_mem};
     unsigned src = 0;   // the lane's input record (shadow, then AO index space)
     float ray_t = 0.0f;
     bool have = false, done = false, surface = false, slice_ahead = false, zero = false;
@@ -1317,7 +1318,8 @@ __global__ void __launch_bounds__(kThreads, MINB) k_cam_query(DevScene S, FrameA
         BATCH ? (unsigned)A.total_pix : (unsigned)A.job0.cam.width * (unsigned)A.job0.cam.height;
     unsigned *cursor = A.pmarch_count + 2;
     TravState T;
-    uint2 stack[64];
+    uint2 stack_mem[64];
+    LocalStack stack{stack_mem};
     V3 hit_n = v3(0, 0, 0), hit_c = v3(0, 0, 0);
     int x = 0, y = 0, part = 0, job = 0;
     // The camera ray lives in T between bricks and after the query: T.org is
