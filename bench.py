@@ -278,6 +278,71 @@ def run_serve(args):
     print(json.dumps(out), flush=True)
 
 
+def run_batch(args):
+    """Batching workload: 64 render jobs at once over the three plain
+    scenes (200k-triangle spheres, 256^3 volume, partitioned mixed scene),
+    image side log-uniform in [128, 2048], camera on a sphere of radius
+    U[4, 12] around the scene centre (in units of the triangle scene; the
+    unit-cube scenes scale it by 1/4), 0-2 shadow/AO levels (none / shadows
+    / shadows + 4 AO).  The jobs go through the batching loop (same-scene
+    jobs packed into CUDA-graph batch submissions on several slot streams,
+    larger frames alone) and, separately, one at a time through the plain
+    path; both report rays/s and per-job latency."""
+    import copy
+    import torch
+    from galaxy_gb300 import gpu, scenes, serve
+    from galaxy_gb300 import scene as S
+    torch.cuda.set_device(0)
+    gpu.init(0)
+    c0, c1, c2 = scenes.triangle_spheres_scene(), scenes.volume_scene(), scenes.mixed_scene()
+    viss = {"triangles": c0[1], "volume": c1[1], "mixed": c2[1]}
+    geom = {"triangles": ((0.0, 0.0, 0.0), 1.0), "volume": ((0.5, 0.5, 0.5), 0.25), "mixed": ((0.5, 0.5, 0.5), 0.25)}
+    t0 = time.time()
+    table = {k: gpu.Scene(v) for k, v in viss.items()}
+    commit_s = time.time() - t0
+    rng = np.random.Generator(np.random.Philox(11))
+
+    def make(rid, side=None):
+        key = ["triangles", "volume", "mixed"][int(rng.integers(0, 3))]
+        if side is None:
+            side = int(round(np.exp(rng.uniform(np.log(128), np.log(2048)))))
+        (cx, cy, cz), scale = geom[key]
+        th, ph = rng.uniform(0.3, 2.8), rng.uniform(0, 2 * np.pi)
+        rad = rng.uniform(4.0, 12.0) * scale
+        eye = (cx + rad * np.sin(th) * np.cos(ph), cy + rad * np.cos(th), cz + rad * np.sin(th) * np.sin(ph))
+        cam = S.Camera(eye, (cx - eye[0], cy - eye[1], cz - eye[2]), (0, 1, 0), 45.0, side, side)
+        lit = copy.copy(viss[key].lighting)
+        level = int(rng.integers(0, 3))
+        lit.lights, lit.types = [(-0.577, -0.577, -0.577)], [0]
+        lit.shadows, lit.n_ao = level >= 1, (4 if level == 2 else 0)
+        lit.ao_radius = 0.1 * scale * 4
+        return serve.Request(rid, 0.0, key, cam, S.resolve_lights(lit, cam).c())
+
+    jobs = [make(j) for j in range(args.jobs)]
+    warm = [make(1000 + j, 256) for j in range(6)]
+    slot_pixels = 2048 * 2048
+    n_slots = max(args.slots, 4)   # 4-8 slot streams measured alike (1.60-1.62x), 2 slower (1.52x)
+    srv = serve.Server(table, n_slots=n_slots, slot_pixels=slot_pixels, max_jobs=64, max_shadow=1, max_ao=4,
+                       fb_budget=16 << 30, use_graph=True, small_pixels=1 << 20, small_batch_pixels=4 << 20)
+    serve.serve_plain(table, [copy.copy(w) for w in warm])
+    srv.run([copy.copy(w) for w in warm])
+    batched = srv.run([copy.copy(r) for r in jobs], time_limit=args.time_limit)
+    srv.release()
+    torch.cuda.synchronize()
+    plain = serve.serve_plain(table, [copy.copy(r) for r in jobs], time_limit=args.time_limit)
+    out = {"metric": "rays/s: batched vs plain GPU path (64 uneven jobs)", "value": batched["rays_per_s"],
+           "unit": "rays/s", "n_gpus": 1, "steps": args.jobs, "warmup": len(warm), "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+           "config": {"workload": "batching: %d jobs over the triangle, volume and mixed scenes, image side "
+                                  "log-uniform 128..2048, 0-2 shadow/AO levels" % args.jobs,
+                      "slots": n_slots, "slot_pixels": slot_pixels, "pixels": int(sum(r.pixels for r in jobs))},
+           "batched": batched, "plain": plain,
+           "batched_over_plain_rays_per_s": batched["rays_per_s"] / max(1e-9, plain["rays_per_s"]),
+           "latency_ms": {k: batched.get(k + "_ms") for k in ("p50", "p95", "p99")},
+           "scene_commit_s": commit_s}
+    print(json.dumps(out), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -288,7 +353,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--image", type=int, default=0, help="override the image side (smaller profiling cases)")
-    ap.add_argument("--mode", default="frame", choices=["frame", "serve"])
+    ap.add_argument("--mode", default="frame", choices=["frame", "serve", "batch"])
+    ap.add_argument("--jobs", type=int, default=64, help="batch mode: number of render jobs")
     ap.add_argument("--rate", type=float, default=50.0)
     ap.add_argument("--requests", type=int, default=200)
     ap.add_argument("--slots", type=int, default=3)
@@ -309,6 +375,8 @@ def main():
         return run_reference(args)
     if args.mode == "serve":
         return run_serve(args)
+    if args.mode == "batch":
+        return run_batch(args)
     args.warmup = max(3, args.warmup)
 
     import torch
