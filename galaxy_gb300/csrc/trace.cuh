@@ -56,7 +56,8 @@ __device__ __forceinline__ void geometry_shade_body(const DevScene &S, const Geo
         V3 A = v3(__ldg(V + 3 * idx), __ldg(V + 3 * idx + 1), __ldg(V + 3 * idx + 2));
         V3 B = v3(__ldg(V + 3 * idx + 3), __ldg(V + 3 * idx + 4), __ldg(V + 3 * idx + 5));
         V3 P = org + gh.t * dir;
-        float u = dot(P - A, B - A) * (1.0f / dot(B - A, B - A));
+        const float ab2 = dot(B - A, B - A);
+        float u = ab2 == 0.f ? 0.f : dot(P - A, B - A) * (1.0f / ab2);   // zero-length segment: its end sphere
         u = fmin_(fmax_(u, 0.f), 1.f);
         V3 PonAxis = A + u * (B - A);
         Ng = nrm(P - PonAxis);

@@ -917,7 +917,8 @@ static void trace_one(const Scene &S, int part, Rays &R, int i, Stats *st, doubl
                     const float *va = lv.vertices + 3 * (int64_t)idx;
                     F3 A = mk(va[0], va[1], va[2]), B = mk(va[3], va[4], va[5]);
                     F3 P = org + gh.t * dir;
-                    float u = dot(P - A, B - A) * (1.0f / dot(B - A, B - A));
+                    const float ab2 = dot(B - A, B - A);
+                    float u = ab2 == 0.f ? 0.f : dot(P - A, B - A) * (1.0f / ab2);  // zero length: end sphere
                     u = std::min(std::max(u, 0.f), 1.f);
                     F3 PonAxis = A + u * (B - A);
                     Ng = normalize(P - PonAxis);
