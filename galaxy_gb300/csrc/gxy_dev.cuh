@@ -30,9 +30,15 @@ struct DevTF {                       // one resampled transfer function, 4 KB
     float r0, r1, k, pad;            // k = 255 / (r1 - r0)
 };
 
+// Voxels are stored in bricks of 4x4x4 cells with a one-voxel apron: brick
+// (bx, by, bz) holds voxels 4b .. 4b+4 on each axis (5^3 floats, padded to
+// 128 = one 512-byte block), so the 8 corners of any cell lie in one brick,
+// within 124 contiguous bytes (at most two 128-byte lines).
+constexpr int kBrick = 4, kBrickSide = 5, kBrickFloats = 128;
 struct DevVolume {
-    const float *data;
+    const float *data;               // bricked
     int nx, ny, nz;
+    int nbx, nby;                    // bricks along x and y
     float ox, oy, oz, dx, dy, dz;
     float ux, uy, uz;                // clamp bounds: float just below n-1
     float ix, iy, iz;                // 1 / delta
@@ -236,6 +242,14 @@ __device__ __forceinline__ float tf_lookup(const DevTF &tf, float v, bool want_c
 // ---------------------------------------------------------------- volume
 // Trilinear sample of the dataset grid at world point p, clamped to the grid;
 // grid coordinate (p - origin) * (1 / delta).
+// Corner (ix, iy, iz) of cell (ix, iy, iz) in the bricked layout; the other
+// corners are at +1 (x), +kBrickSide (y) and +kBrickSide^2 (z).
+__device__ __forceinline__ const float *cell_base(const DevVolume &v, int ix, int iy, int iz) {
+    const int bx = ix >> 2, by = iy >> 2, bz = iz >> 2;
+    const size_t brick = ((size_t)bz * v.nby + by) * v.nbx + bx;
+    return v.data + brick * kBrickFloats + ((iz & 3) * kBrickSide + (iy & 3)) * kBrickSide + (ix & 3);
+}
+
 __device__ __forceinline__ float vol_sample(const DevVolume &v, V3 p) {
     float gx = (p.x - v.ox) * v.ix;
     float gy = (p.y - v.oy) * v.iy;
@@ -248,10 +262,10 @@ __device__ __forceinline__ float vol_sample(const DevVolume &v, V3 p) {
     if (gz > v.uz) gz = v.uz;
     int ix = (int)gx, iy = (int)gy, iz = (int)gz;
     float fx = gx - (float)ix, fy = gy - (float)iy, fz = gz - (float)iz;
-    size_t sy = (size_t)v.nx, sz = (size_t)v.nx * (size_t)v.ny;
-    const float *b = v.data + (size_t)iz * sz + (size_t)iy * sy + (size_t)ix;
-    float v000 = __ldg(b), v100 = __ldg(b + 1), v010 = __ldg(b + sy), v110 = __ldg(b + sy + 1);
-    float v001 = __ldg(b + sz), v101 = __ldg(b + sz + 1), v011 = __ldg(b + sz + sy), v111 = __ldg(b + sz + sy + 1);
+    const float *b = cell_base(v, ix, iy, iz);
+    constexpr int SY = kBrickSide, SZ = kBrickSide * kBrickSide;
+    float v000 = __ldg(b), v100 = __ldg(b + 1), v010 = __ldg(b + SY), v110 = __ldg(b + SY + 1);
+    float v001 = __ldg(b + SZ), v101 = __ldg(b + SZ + 1), v011 = __ldg(b + SZ + SY), v111 = __ldg(b + SZ + SY + 1);
     float ax = 1.0f - fx;
     float v00 = ax * v000 + fx * v100;
     float v10 = ax * v010 + fx * v110;
@@ -281,11 +295,11 @@ __device__ __forceinline__ float vol_sample_cached(const DevVolume &v, V3 p, Cel
     if (gz > v.uz) gz = v.uz;
     int ix = (int)gx, iy = (int)gy, iz = (int)gz;
     if (ix != cc.ix || iy != cc.iy || iz != cc.iz) {
-        size_t sy = (size_t)v.nx, sz = (size_t)v.nx * (size_t)v.ny;
-        const float *b = v.data + (size_t)iz * sz + (size_t)iy * sy + (size_t)ix;
-        cc.c[0] = __ldg(b); cc.c[1] = __ldg(b + 1); cc.c[2] = __ldg(b + sy); cc.c[3] = __ldg(b + sy + 1);
-        cc.c[4] = __ldg(b + sz); cc.c[5] = __ldg(b + sz + 1); cc.c[6] = __ldg(b + sz + sy);
-        cc.c[7] = __ldg(b + sz + sy + 1);
+        const float *b = cell_base(v, ix, iy, iz);
+        constexpr int SY = kBrickSide, SZ = kBrickSide * kBrickSide;
+        cc.c[0] = __ldg(b); cc.c[1] = __ldg(b + 1); cc.c[2] = __ldg(b + SY); cc.c[3] = __ldg(b + SY + 1);
+        cc.c[4] = __ldg(b + SZ); cc.c[5] = __ldg(b + SZ + 1); cc.c[6] = __ldg(b + SZ + SY);
+        cc.c[7] = __ldg(b + SZ + SY + 1);
         cc.ix = ix; cc.iy = iy; cc.iz = iz;
     }
     float fx = gx - (float)ix, fy = gy - (float)iy, fz = gz - (float)iz;

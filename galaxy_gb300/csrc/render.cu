@@ -386,6 +386,22 @@ static void tf_to_dev(const gxy_tf &t, DevTF &d) {
     d.pad = 0;
 }
 
+// Linear x-fastest volume -> bricked layout (DevVolume): one thread per
+// output float; voxel indices past the grid (apron of the last brick, pad
+// floats) read the clamped edge voxel and are never sampled.
+__global__ void k_brick_volume(const float *lin, int nx, int ny, int nz, int nbx, int nby, int64_t n_out,
+                               float *out) {
+    int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e >= n_out) return;
+    int64_t brick = e / kBrickFloats;
+    int o = (int)(e % kBrickFloats);
+    if (o >= kBrickSide * kBrickSide * kBrickSide) o = 0;
+    int lx = o % kBrickSide, ly = (o / kBrickSide) % kBrickSide, lz = o / (kBrickSide * kBrickSide);
+    int bx = (int)(brick % nbx), by = (int)((brick / nbx) % nby), bz = (int)(brick / ((int64_t)nbx * nby));
+    int x = min(bx * kBrick + lx, nx - 1), y = min(by * kBrick + ly, ny - 1), z = min(bz * kBrick + lz, nz - 1);
+    out[e] = lin[((int64_t)z * ny + y) * nx + x];
+}
+
 static int commit(const gxy_scene_desc *d, Scene *sc) {
     DevScene &S = sc->S;
     memset(&S, 0, sizeof S);
@@ -417,10 +433,26 @@ static int commit(const gxy_scene_desc *d, Scene *sc) {
             return set_error(GXY_ERR_INVALID, "too many slices or isovalues");
         DevVolume &V = S.vol[m];
         size_t nvox = (size_t)v.counts[0] * v.counts[1] * v.counts[2];
-        void *p;
-        if ((rc = sc->upload(v.samples, nvox * sizeof(float), &p))) return rc;
-        V.data = (const float *)p;
         V.nx = v.counts[0]; V.ny = v.counts[1]; V.nz = v.counts[2];
+        // cells 0 .. n-2 per axis, kBrick cells per brick
+        V.nbx = (V.nx - 2) / kBrick + 1;
+        V.nby = (V.ny - 2) / kBrick + 1;
+        const int nbz = (V.nz - 2) / kBrick + 1;
+        const int64_t n_out = (int64_t)V.nbx * V.nby * nbz * kBrickFloats;
+        {
+            ScratchList tmp(arena());
+            float *lin;
+            if ((rc = tmp.alloc((void **)&lin, nvox * sizeof(float)))) return rc;
+            CK(cudaMemcpy(lin, v.samples, nvox * sizeof(float), cudaMemcpyHostToDevice));
+            float *bricked;
+            if ((rc = arena().alloc((void **)&bricked, (size_t)n_out * sizeof(float)))) return rc;
+            sc->owned.push_back(bricked);
+            k_brick_volume<<<(unsigned)((n_out + 255) / 256), 256>>>(lin, V.nx, V.ny, V.nz, V.nbx, V.nby, n_out,
+                                                                     bricked);
+            CK(cudaGetLastError());
+            CK(cudaDeviceSynchronize());
+            V.data = bricked;
+        }
         V.ox = v.origin[0]; V.oy = v.origin[1]; V.oz = v.origin[2];
         V.dx = v.deltas[0]; V.dy = v.deltas[1]; V.dz = v.deltas[2];
         V.ux = nextafterf((float)(V.nx - 1), 0.0f);
