@@ -742,4 +742,133 @@ __device__ __forceinline__ bool trav_step(const DevScene &S, TravState &T, STACK
     return false;
 }
 
+
+// ------------------------------------------------------------------------
+// Warp-cooperative closest hit for the 32 rays of a warp (one per lane;
+// active = false gives the lane an empty interval), for coherent rays such
+// as camera rays of an 8x4 pixel tile.  The warp walks one node stack in
+// shared memory (wstack: 64 entries of this warp): every lane tests its own
+// ray against the 8 children of the same node, so each node line is fetched
+// once for the warp; a child any lane enters is visited, nearest first by
+// the smallest entry distance over the lanes; a stacked node is skipped once
+// that distance lies beyond every lane's current hit.  Each lane tests the
+// primitives of the leaves its own ray enters, with the same tests and tie
+// rule as bvh_closest, so it finds the same closest hit.  All 32 lanes call
+// it together.  nodes counts node lines fetched (once per warp).
+template <bool LINES>
+__device__ __forceinline__ bool packet_closest(const DevScene &S, V3 org, V3 dir, float t0, float tfar, bool active,
+                                               uint2 *wstack, GeoHit &h, unsigned &nodes, unsigned &tris,
+                                               unsigned &sphs, int &ovf) {
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    if (!active) {   // an interval no box test passes
+        org = v3(0.f, 0.f, 0.f);
+        dir = v3(1.f, 1.f, 1.f);
+        t0 = 0.f;
+        tfar = -1.f;
+    }
+    const float idx = 1.0f / dir.x, idy = 1.0f / dir.y, idz = 1.0f / dir.z;
+    h.t = tfar;
+    h.u = h.v = 0.f;
+    h.prim = 0xffffffffu;
+    bool found = false;
+    if (!S.nodes) return false;
+    int sp = 0;
+    uint32_t cur = 0;
+    for (;;) {
+        const float4 *np = reinterpret_cast<const float4 *>(S.nodes + cur);
+        float4 n0 = __ldg(np), n1 = __ldg(np + 1);
+        uint4 q[6];
+#pragma unroll
+        for (int k = 0; k < 6; k++) q[k] = __ldg(reinterpret_cast<const uint4 *>(np + 2 + k));
+        if (lane == 0) nodes++;
+        const uint32_t child_base = __float_as_uint(n0.w), prim_base = __float_as_uint(n1.x);
+        const uint32_t meta_lo = __float_as_uint(n1.z), meta_hi = __float_as_uint(n1.w);
+        uint32_t key[8];
+        uint32_t leafhits;
+        int n_inner;
+        node_children(n0, n1, q, org, idx, idy, idz, t0, h.t, key, n_inner, leafhits);
+        while (leafhits) {
+            int i = __ffs(leafhits) - 1;
+            leafhits &= leafhits - 1;
+            uint32_t mb = (i < 4 ? meta_lo >> (8 * i) : meta_hi >> (8 * (i - 4))) & 0xffu;
+            uint32_t s = prim_base + (mb & 31u);
+            uint32_t cnt = (mb >> 5) + 1;
+            for (uint32_t k = 0; k < cnt; k++, s++) {
+                const float4 *rp = S.slots + 3 * (size_t)s;
+                float4 r0 = __ldg(rp), r1 = __ldg(rp + 1);
+                uint32_t id = __float_as_uint(r0.w);
+                float t, u = 0.0f, v = 0.0f;
+                bool ok;
+                if (LINES && (id & kLineBit)) {
+                    tris++;
+                    ok = line_test(org, dir, v3(r0.x, r0.y, r0.z), v3(r1.x, r1.y, r1.z), r1.w, t0, tfar, t);
+                } else if (id & kSphereBit) {
+                    sphs++;
+                    ok = sph_test(org, dir, v3(r0.x, r0.y, r0.z), r1.x, r1.y, t0, tfar, t);
+                } else {
+                    tris++;
+                    float4 r2 = __ldg(rp + 2);
+                    ok = tri_test(org, dir, v3(r0.x, r0.y, r0.z), v3(r1.x, r1.y, r1.z), v3(r2.x, r2.y, r2.z), t, u, v) &&
+                         t > t0 && t < tfar;
+                }
+                if (ok && (t < h.t || (t == h.t && id < h.prim))) {
+                    h.t = t; h.u = u; h.v = v; h.prim = id;
+                    found = true;
+                }
+            }
+        }
+        // children entered by any lane, keyed by the nearest entry over the lanes
+        uint32_t m[8];
+        int cnt = 0;
+#pragma unroll
+        for (int i = 0; i < 8; i++) {
+            m[i] = __reduce_min_sync(FULL, key[i]);
+            cnt += m[i] != 0xffffffffu ? 1 : 0;
+        }
+        if (cnt) {
+            cas(m[0], m[1]); cas(m[2], m[3]); cas(m[4], m[5]); cas(m[6], m[7]);
+            cas(m[0], m[2]); cas(m[1], m[3]); cas(m[4], m[6]); cas(m[5], m[7]);
+            cas(m[1], m[2]); cas(m[5], m[6]); cas(m[0], m[4]); cas(m[3], m[7]);
+            cas(m[1], m[5]); cas(m[2], m[6]);
+            cas(m[1], m[4]); cas(m[3], m[6]);
+            cas(m[2], m[4]); cas(m[3], m[5]);
+            cas(m[3], m[4]);
+            // far-to-near onto the stack: m[cnt-1] deepest ... m[1] on top
+            if (sp + cnt - 1 > 64) {
+                ovf = 1;
+            } else {
+#pragma unroll
+                for (int j = 7; j >= 1; j--) {
+                    if (j < cnt && lane == j) {
+                        uint32_t slot = m[j] & 7u;
+                        uint32_t mb = (slot < 4 ? meta_lo >> (8 * slot) : meta_hi >> (8 * (slot - 4))) & 0xffu;
+                        wstack[sp + (cnt - 1 - j)] = make_uint2(child_base + mb, m[j] & ~7u);
+                    }
+                }
+                sp += cnt - 1;
+            }
+            __syncwarp();
+            uint32_t slot = m[0] & 7u;
+            uint32_t mb = (slot < 4 ? meta_lo >> (8 * slot) : meta_hi >> (8 * (slot - 4))) & 0xffu;
+            cur = child_base + mb;
+            continue;
+        }
+        // pop the nearest stacked node some lane may still need
+        const unsigned far = __reduce_max_sync(FULL, __float_as_uint(fmaxf(h.t, 0.0f)));
+        bool got = false;
+        while (sp > 0) {
+            uint2 e = wstack[--sp];
+            if (e.y <= far) {
+                cur = e.x;
+                got = true;
+                break;
+            }
+        }
+        __syncwarp();
+        if (!got) break;
+    }
+    return found;
+}
+
 }  // namespace gxy

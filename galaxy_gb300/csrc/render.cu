@@ -1475,6 +1475,116 @@ __global__ void __launch_bounds__(kThreads, MINB) k_cam_query(DevScene S, FrameA
     flush_counters(A.ctr, c, st);
 }
 
+// Query pass of split camera-ray tracing, warp-cooperative (single-frame
+// path): a warp takes the next 8x4 pixel tile from a device cursor and, for
+// each brick the lanes' camera rays enter first (Camera.cpp:431-441), clips
+// and tests slices per lane, then finds the closest hits of the 32 coherent
+// rays with one shared traversal (packet_closest).  Records as k_cam_query:
+// pixel i's first record in slot i, a hole record for a pixel whose ray
+// enters no brick, further bricks after slot npix.
+template <int MINB, bool LINES>
+__global__ void __launch_bounds__(kThreads, MINB) k_cam_packet(DevScene S, FrameArgs A) {
+    __shared__ DevTF tfs[kMaxVol];
+    __shared__ uint2 wstacks[kThreads / 32][64];
+    load_tfs(S, tfs);
+    RayStats st;
+    LocalCounters c;
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    uint2 *wstack = wstacks[threadIdx.x >> 5];
+    const DevCamera &cam = A.job0.cam;
+    const int w = cam.width, hgt = cam.height;
+    const unsigned npix = (unsigned)w * (unsigned)hgt;
+    const unsigned tiles_x = (unsigned)(w + 7) / 8, ntiles = tiles_x * (unsigned)((hgt + 3) / 4);
+    unsigned *cursor = A.pmarch_count + 2;
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(A.pmarch_count, npix);   // slots [0, npix)
+    for (;;) {
+        unsigned tile = 0;
+        if (lane == 0) tile = atomicAdd(cursor, 1u);
+        tile = __shfl_sync(FULL, tile, 0);
+        if (tile >= ntiles) break;
+        const int x = (int)(tile % tiles_x) * 8 + (lane & 7), y = (int)(tile / tiles_x) * 4 + (lane >> 3);
+        const bool valid = x < w && y < hgt;
+        const unsigned pix = valid ? (unsigned)y * (unsigned)w + (unsigned)x : 0u;
+        V3 org = v3(0, 0, 0), dir0 = v3(1, 1, 1);
+        uint64_t pending = 0;
+        if (valid) {
+            pending = camera_ray(S, cam, x, y, org, dir0);
+            if (!pending) A.pmarch[pix].m = make_int4(x, y, -1, 0);
+        }
+        bool first = true;
+        while (__any_sync(FULL, pending != 0)) {
+            const bool act = pending != 0;
+            int part = 0;
+            V3 dir = dir0, hit_n = v3(0, 0, 0), hit_c = v3(0, 0, 0);
+            float ray_t0 = 0.f, ray_t = 0.f;
+            bool surface = false;
+            if (act) {
+                part = __ffsll((long long)pending) - 1;
+                pending &= pending - 1;
+                c.prim++;
+                c.seg++;
+                TraceIn in;
+                in.org = org;
+                in.dir = dir0;
+                in.t = 0.0f;
+                in.tmax = FLT_MAX;
+                in.part = part;
+                float tEntry, tExitVolume;
+                sec_clip(S, in, dir, ray_t0, ray_t, tEntry, tExitVolume);
+                float hit_t = 0.f;
+                int vid = -1;
+                for (int m = 0; m < S.n_vol; m++) {
+                    const DevVolume &vv = S.vol[m];
+                    for (int k = 0; k < vv.n_slices; k++) {
+                        float4 pl = vv.slices[k];
+                        V3 pn = v3(pl.x, pl.y, pl.z);
+                        float denom = dot(dir, pn);
+                        if (fabsf(denom) > 0.0001f) {
+                            float t = (pl.w - dot(org, pn)) / denom;
+                            if (t >= ray_t0 && t <= ray_t) {
+                                hit_n = denom > 0 ? neg(pn) : pn;
+                                hit_t = t;
+                                vid = m;
+                                ray_t = t;
+                                surface = true;
+                            }
+                        }
+                    }
+                }
+                if (surface) hit_c = tf_color(tfs[vid], vol_sample(S.vol[vid], org + hit_t * dir));
+            }
+            GeoHit gh;
+            const bool found =
+                packet_closest<LINES>(S, org, dir, ray_t0, ray_t, act, wstack, gh, st.nodes, st.tris, st.sphs, st.ovf);
+            if (act && found) {
+                ray_t = gh.t;
+                surface = true;
+                geometry_shade(S, gh, org, dir, hit_n, hit_c);
+            }
+            const bool extra = act && !first;
+            unsigned idx = pix;
+            if (__any_sync(FULL, extra)) {
+                unsigned e = warp_reserve(extra ? 1u : 0u, A.pmarch_count + 3, A.pmarch_cap - npix, c.ovf);
+                unsigned got = __ballot_sync(FULL, extra && e != 0xffffffffu);
+                if (lane == 0 && got) atomicAdd(A.pmarch_count, (unsigned)__popc(got));
+                if (extra) idx = e == 0xffffffffu ? e : npix + e;
+            }
+            if (act && idx != 0xffffffffu) {
+                first = false;
+                DRay *r = A.pmarch + idx;
+                r->o = make_float4(org.x, org.y, org.z, 0.0f);
+                r->d = make_float4(dir0.x, dir0.y, dir0.z, FLT_MAX);
+                r->c = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                r->m = make_int4(x, y, make_meta(GXY_RAY_PRIMARY | (surface ? 8 : 0), part, 0), __float_as_int(ray_t));
+                A.pmarch_hit[2 * (size_t)idx] = make_float4(hit_n.x, hit_n.y, hit_n.z, hit_c.x);
+                A.pmarch_hit[2 * (size_t)idx + 1] = make_float4(hit_c.y, hit_c.z, 0.0f, 0.0f);
+            }
+        }
+    }
+    flush_counters(A.ctr, c, st);
+}
+
 // March pass of split primary tracing with per-lane refill: composite the
 // volume up to the query pass's stop distance, then shade (ambient, AO spawn,
 // diffuse, shadow spawn), classify, route and accumulate as primary_ray does.
@@ -1800,6 +1910,7 @@ bool sah_builder() { return g_tune_sah != 0; }
 static int g_tune_leaf = 1;         // primitives per BVH8 leaf (at most)
 static int g_tune_trav_steps = 8;   // node visits per refill round of the query passes
 static int g_tune_march_steps = 16; // samples per refill round of the march passes
+static int g_tune_cam_packet = 1;   // single-frame camera query: warp-cooperative (1) or per-lane refill (0)
 int leaf_max() { return g_tune_leaf; }
 
 // The split path applies to volume-rendered scenes with one volume and no
@@ -1946,7 +2057,11 @@ static int render(Scene *sc, const gxy_camera &cam, const gxy_lighting &lt, floa
         if (kind == K_SECONDARY && A.split) CK(cudaMemsetAsync(A.qmarch_count, 0, 3 * sizeof(unsigned), st));
         if (kind == K_CAMERA && A.split_prim) CK(cudaMemsetAsync(A.pmarch_count, 0, 4 * sizeof(unsigned), st));
         if (g_tune_minb == 3) {
-            if (kind == K_CAMERA && A.split_prim && lines) k_cam_query<false, 4, true><<<query_grid(), kThreads, 0, st>>>(S, A);
+            if (kind == K_CAMERA && A.split_prim && g_tune_cam_packet && lines)
+                k_cam_packet<4, true><<<query_grid(), kThreads, 0, st>>>(S, A);
+            else if (kind == K_CAMERA && A.split_prim && g_tune_cam_packet)
+                k_cam_packet<4, false><<<query_grid(), kThreads, 0, st>>>(S, A);
+            else if (kind == K_CAMERA && A.split_prim && lines) k_cam_query<false, 4, true><<<query_grid(), kThreads, 0, st>>>(S, A);
             else if (kind == K_CAMERA && A.split_prim) k_cam_query<false, 4, false><<<query_grid(), kThreads, 0, st>>>(S, A);
             else if (kind == K_CAMERA) k_primary<K_CAMERA, 3><<<g, kThreads, 0, st>>>(S, A);
             else if (kind == K_PRIMARY) k_primary<K_PRIMARY, 3><<<g, kThreads, 0, st>>>(S, A);
@@ -1956,7 +2071,11 @@ static int render(Scene *sc, const gxy_camera &cam, const gxy_lighting &lt, floa
             else if (kind == K_PMARCH) k_prim_march<false, 3><<<march_grid(3), kThreads, 0, st>>>(S, A);
             else k_sec_march<false, 3><<<march_grid(3), kThreads, 0, st>>>(S, A);
         } else {
-            if (kind == K_CAMERA && A.split_prim && lines) k_cam_query<false, 2, true><<<march_grid(2), kThreads, 0, st>>>(S, A);
+            if (kind == K_CAMERA && A.split_prim && g_tune_cam_packet && lines)
+                k_cam_packet<2, true><<<march_grid(2), kThreads, 0, st>>>(S, A);
+            else if (kind == K_CAMERA && A.split_prim && g_tune_cam_packet)
+                k_cam_packet<2, false><<<march_grid(2), kThreads, 0, st>>>(S, A);
+            else if (kind == K_CAMERA && A.split_prim && lines) k_cam_query<false, 2, true><<<march_grid(2), kThreads, 0, st>>>(S, A);
             else if (kind == K_CAMERA && A.split_prim) k_cam_query<false, 2, false><<<march_grid(2), kThreads, 0, st>>>(S, A);
             else if (kind == K_CAMERA) k_primary<K_CAMERA, 2><<<g, kThreads, 0, st>>>(S, A);
             else if (kind == K_PRIMARY) k_primary<K_PRIMARY, 2><<<g, kThreads, 0, st>>>(S, A);
@@ -2379,6 +2498,10 @@ int gxy_gpu_set_tuning(int knob, int value) {
         g_tune_leaf = value;
         return GXY_OK;
     }
+    if (knob == GXY_TUNE_CAMERA_PACKET) {
+        g_tune_cam_packet = value ? 1 : 0;
+        return GXY_OK;
+    }
     if (knob == GXY_TUNE_TRAV_STEPS) {
         if (value < 1 || value > 64) return set_error(GXY_ERR_INVALID, "traversal steps must be 1-64");
         g_tune_trav_steps = value;
@@ -2401,6 +2524,7 @@ int gxy_gpu_get_tuning(int knob, int *value) {
     else if (knob == GXY_TUNE_BVH_SAH) *value = g_tune_sah;
     else if (knob == GXY_TUNE_LEAF_MAX) *value = g_tune_leaf;
     else if (knob == GXY_TUNE_TRAV_STEPS) *value = g_tune_trav_steps;
+    else if (knob == GXY_TUNE_CAMERA_PACKET) *value = g_tune_cam_packet;
     else if (knob == GXY_TUNE_MARCH_STEPS) *value = g_tune_march_steps;
     else return set_error(GXY_ERR_INVALID, "unknown tuning knob");
     return GXY_OK;

@@ -107,6 +107,7 @@ TUNE_BVH_SAH = 5
 TUNE_LEAF_MAX = 6
 TUNE_TRAV_STEPS = 7
 TUNE_MARCH_STEPS = 8
+TUNE_CAMERA_PACKET = 9
 
 
 def set_tuning(knob, value):

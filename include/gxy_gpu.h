@@ -300,6 +300,9 @@ int gxy_gpu_set_profiling(gxy_scene scene, int on);
                                         passes, 1-64 (default 8) */
 #define GXY_TUNE_MARCH_STEPS     8   /* volume samples per refill round of the march
                                         passes, 1-256 (default 16) */
+#define GXY_TUNE_CAMERA_PACKET   9   /* 1 (default): camera rays of a frame queried by
+                                        warps over 8x4 pixel tiles with one shared BVH8
+                                        traversal; 0: per-lane refill traversal */
 int gxy_gpu_set_tuning(int knob, int value);
 int gxy_gpu_get_tuning(int knob, int *value);
 int gxy_gpu_query_generations(gxy_scene scene, gxy_generation_stats *out, int max, int32_t *n);

@@ -73,17 +73,20 @@ def test_triangle_scene(gpu):
     assert c["shadow_rays"] == cnt["shadow"]
 
 
-@pytest.mark.parametrize("split", [(0, 0), (1, 0), (0, 1), (1, 1)])
+@pytest.mark.parametrize("split", [(0, 0, 1), (1, 0, 1), (0, 1, 1), (1, 1, 1), (1, 1, 0)])
 def test_mixed_partitioned_scene(gpu, split):
-    """Every tracing variant (one pass, split shadow/AO, split camera rays)."""
+    """Every tracing variant: one pass, split shadow/AO, split camera rays
+    with the warp-cooperative (third flag 1) or the per-lane camera query."""
     gpu.set_tuning(gpu.TUNE_SPLIT_SECONDARY, split[0])
     gpu.set_tuning(gpu.TUNE_SPLIT_PRIMARY, split[1])
+    gpu.set_tuning(gpu.TUNE_CAMERA_PACKET, split[2])
     cam, vis = scenes.mixed_scene(n=64, n_spheres=20000, width=128, height=128, partitions=(2, 2, 2), n_ao=4)
     try:
         img, ref, sc, cnt = render_both(gpu, cam, vis)
     finally:
         gpu.set_tuning(gpu.TUNE_SPLIT_SECONDARY, 1)
         gpu.set_tuning(gpu.TUNE_SPLIT_PRIMARY, 1)
+        gpu.set_tuning(gpu.TUNE_CAMERA_PACKET, 1)
     image_close(img, ref)
     c = sc.counters()
     assert c["primary_rays"] == cnt["primary"]
@@ -167,7 +170,7 @@ def test_raylist_trace_matches_oracle(gpu, which):
     assert np.mean(ca.classification == cb.classification) >= 0.9999
 
 
-@pytest.mark.parametrize("case", ["lines", "lines_bricks", "lines_volume"])
+@pytest.mark.parametrize("case", ["lines", "lines_bricks", "lines_volume", "lines_volume_refill"])
 def test_pathlines_match_oracle(gpu, case):
     """PathLinesVis: capsule segments (DataDrivenPathLines.ispc:100-203) with
     the post-intersect colour mapping, alone, across 2x2x1 bricks, and inside
@@ -179,7 +182,11 @@ def test_pathlines_match_oracle(gpu, case):
     else:
         cam, vis = scenes.pathlines_scene(n_lines=800, n_vertices=48, width=128, height=128, volume=True,
                                           partitions=(2, 1, 1))
-    img, ref, sc, cnt = render_both(gpu, cam, vis)
+    gpu.set_tuning(gpu.TUNE_CAMERA_PACKET, 0 if case.endswith("refill") else 1)
+    try:
+        img, ref, sc, cnt = render_both(gpu, cam, vis)
+    finally:
+        gpu.set_tuning(gpu.TUNE_CAMERA_PACKET, 1)
     image_close(img, ref)
     c = sc.counters()
     assert c["primary_rays"] == cnt["primary"]
