@@ -1024,35 +1024,15 @@ __device__ __forceinline__ void camera_pass(const DevScene &Sp, const DevTF *tfs
         while (__any_sync(0xffffffffu, pending != 0)) {
             bool act = pending != 0;
             PrimOut P;
-            PrimQuery pq;
             const DevScene &S = USCENE ? Sp : *J->scene;
             if (act) {
                 int p = __ffsll((long long)pending) - 1;
                 pending &= pending - 1;
                 in.part = p;
                 c.prim++;
-                if (A.split_prim) {
-                    c.seg++;
-                    pq = prim_query(S, USCENE ? tfs_uniform : S.tfs, in, st);
-                } else {
-                    primary_ray(S, USCENE ? tfs_uniform : S.tfs, *J, in, x, y, P, st, c);
-                }
+                primary_ray(S, USCENE ? tfs_uniform : S.tfs, *J, in, x, y, P, st, c);
             }
-            if (A.split_prim) {
-                unsigned idx = warp_reserve(act ? 1u : 0u, A.pmarch_count, A.pmarch_cap, c.ovf);
-                if (act && idx != 0xffffffffu) {
-                    DRay *r = A.pmarch + idx;
-                    r->o = make_float4(in.org.x, in.org.y, in.org.z, in.t);
-                    r->d = make_float4(in.dir.x, in.dir.y, in.dir.z, in.tmax);
-                    r->c = make_float4(in.r, in.g, in.b, in.o);
-                    r->m = make_int4(x, y, make_meta(in.type | (pq.surface ? 8 : 0), in.part, job),
-                                     __float_as_int(pq.t_term));
-                    A.pmarch_hit[2 * (size_t)idx] = make_float4(pq.n.x, pq.n.y, pq.n.z, pq.c.x);
-                    A.pmarch_hit[2 * (size_t)idx + 1] = make_float4(pq.c.y, pq.c.z, 0.0f, 0.0f);
-                }
-            } else {
-                emit_primary(S, *J, job, act, in, x, y, P, A, c);
-            }
+            emit_primary(S, *J, job, act, in, x, y, P, A, c);
         }
     }
 }
@@ -1331,8 +1311,9 @@ __global__ void __launch_bounds__(kThreads, MINB) k_sec_query(DevScene S, FrameA
 // the next pixel (BATCH: of all jobs, job by binary search) from a device cursor, and for each brick
 // its camera ray enters first (Camera.cpp:431-441) clips to the brick, tests
 // the slices, then steps the resumable BVH8 traversal a few nodes at a time;
-// a finished query writes the same march record as the camera pass's split
-// branch (prim_query), and the lane moves to its next brick or pixel.  The
+// a finished query writes a march record (origin, direction, stop distance,
+// surface flag; hit normal and colour beside it), and the lane moves to its
+// next brick or pixel.  The
 // first record of pixel i goes to slot i and a pixel whose ray enters no
 // brick leaves a hole record (meta -1) there, so the march pass reads the
 // records in pixel order; further bricks of one pixel go after slot npix.
@@ -1415,27 +1396,7 @@ __global__ void __launch_bounds__(kThreads, MINB) k_cam_query(DevScene S, FrameA
             surface = false;
             hit_n = v3(0, 0, 0);
             hit_c = v3(0, 0, 0);
-            float hit_t = 0.f;
-            int vid = -1;
-            for (int m = 0; m < S.n_vol; m++) {
-                const DevVolume &vv = S.vol[m];
-                for (int k = 0; k < vv.n_slices; k++) {
-                    float4 pl = vv.slices[k];
-                    V3 pn = v3(pl.x, pl.y, pl.z);
-                    float denom = dot(dir, pn);
-                    if (fabsf(denom) > 0.0001f) {
-                        float t = (pl.w - dot(org, pn)) / denom;
-                        if (t >= ray_t0 && t <= ray_t) {
-                            hit_n = denom > 0 ? neg(pn) : pn;
-                            hit_t = t;
-                            vid = m;
-                            ray_t = t;
-                            surface = true;
-                        }
-                    }
-                }
-            }
-            if (surface) hit_c = tf_color(tfs[vid], vol_sample(S.vol[vid], org + hit_t * dir));
+            cam_slices(S, tfs, org, dir, ray_t0, ray_t, surface, hit_n, hit_c);
             done = trav_init(S, T, org, dir, ray_t0, ray_t);
             have = true;
         }
@@ -1532,27 +1493,7 @@ __global__ void __launch_bounds__(kThreads, MINB) k_cam_packet(DevScene S, Frame
                 in.part = part;
                 float tEntry, tExitVolume;
                 sec_clip(S, in, dir, ray_t0, ray_t, tEntry, tExitVolume);
-                float hit_t = 0.f;
-                int vid = -1;
-                for (int m = 0; m < S.n_vol; m++) {
-                    const DevVolume &vv = S.vol[m];
-                    for (int k = 0; k < vv.n_slices; k++) {
-                        float4 pl = vv.slices[k];
-                        V3 pn = v3(pl.x, pl.y, pl.z);
-                        float denom = dot(dir, pn);
-                        if (fabsf(denom) > 0.0001f) {
-                            float t = (pl.w - dot(org, pn)) / denom;
-                            if (t >= ray_t0 && t <= ray_t) {
-                                hit_n = denom > 0 ? neg(pn) : pn;
-                                hit_t = t;
-                                vid = m;
-                                ray_t = t;
-                                surface = true;
-                            }
-                        }
-                    }
-                }
-                if (surface) hit_c = tf_color(tfs[vid], vol_sample(S.vol[vid], org + hit_t * dir));
+                cam_slices(S, tfs, org, dir, ray_t0, ray_t, surface, hit_n, hit_c);
             }
             GeoHit gh;
             const bool found =

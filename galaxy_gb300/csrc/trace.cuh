@@ -581,29 +581,15 @@ __device__ __forceinline__ int sec_march_term(const DevScene &S, const SecMarch 
 namespace gxy {
 
 // ------------------------------------------------------------------------
-// Split tracing of primary rays in volume scenes (whole-frame path), the
-// primary-ray counterpart of sec_query / SecMarch:
-//   prim_query -- box clip, slice planes with their surface colour, and the
-//                 in-brick closest geometry hit with its normal and colour
-//                 (trace_core<true,false> up to the march);
-//   PrimMarch  -- the front-to-back compositing march (one volume, no
-//                 isovalues) as a resumable state.
-
-struct PrimQuery {
-    float t_term;
-    bool surface;
-    V3 n, c;
-};
-
-__device__ __forceinline__ PrimQuery prim_query(const DevScene &S, const DevTF *tfs, const TraceIn &R, RayStats &st) {
-    PrimQuery q;
-    V3 dir;
-    float ray_t0, ray_t, tEntry, tExitVolume;
-    sec_clip(S, R, dir, ray_t0, ray_t, tEntry, tExitVolume);
-    const V3 org = R.org;
-    bool surface_hit = false;
+// Split tracing of primary rays in volume scenes (whole-frame path): the
+// camera queries (k_cam_packet, k_cam_query in render.cu) clip the ray to
+// its brick (sec_clip), take the nearest slice plane with its surface colour
+// (cam_slices) and then the in-brick closest geometry hit with its normal and
+// colour -- trace_core<true,false> up to the march; prim_march_steps then
+// composites the volume up to that distance as a resumable state.
+__device__ __forceinline__ void cam_slices(const DevScene &S, const DevTF *tfs, V3 org, V3 dir, float ray_t0,
+                                           float &ray_t, bool &surface, V3 &hit_n, V3 &hit_c) {
     float hit_t = 0.f;
-    V3 hit_n = v3(0, 0, 0), hit_c = v3(0, 0, 0);
     int vid = -1;
     for (int m = 0; m < S.n_vol; m++) {
         const DevVolume &vv = S.vol[m];
@@ -618,29 +604,12 @@ __device__ __forceinline__ PrimQuery prim_query(const DevScene &S, const DevTF *
                     hit_t = t;
                     vid = m;
                     ray_t = t;
-                    surface_hit = true;
+                    surface = true;
                 }
             }
         }
     }
-    if (surface_hit) {
-        V3 p = org + hit_t * dir;
-        float smp = vol_sample(S.vol[vid], p);
-        hit_c = tf_color(tfs[vid], smp);
-    }
-    if (S.nodes) {
-        GeoHit gh;
-        if (bvh_closest<false>(S, org, dir, ray_t0, ray_t, gh, st.nodes, st.tris, st.sphs, st.ovf)) {
-            ray_t = gh.t;
-            surface_hit = true;
-            geometry_shade(S, gh, org, dir, hit_n, hit_c);
-        }
-    }
-    q.t_term = ray_t;
-    q.surface = surface_hit;
-    q.n = hit_n;
-    q.c = hit_c;
-    return q;
+    if (surface) hit_c = tf_color(tfs[vid], vol_sample(S.vol[vid], org + hit_t * dir));
 }
 
 // Compositing march of a primary ray (TraceRays.ispc:470-556 with the
