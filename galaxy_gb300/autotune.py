@@ -1,16 +1,20 @@
 """Autotuner for the wavefront kernels.
 
-Measures a short run of real frames of the caller's scene for each
-candidate setting and keeps the fastest:
+Measures a short run of real frames of the caller's scene per candidate
+setting and keeps the fastest, one knob at a time (coordinate descent,
+repeated while a pass still changes something):
 
   * register budget / occupancy: the frame kernels compiled for 2 resident
     blocks per SM (128 registers, no spills) or 3 (80 registers, some
-    spills to L1-resident local memory);
-  * grid-stride grid size: 4, 8 or 16 blocks per SM (a smaller grid keeps
-    rays of a block spatially closer; a larger one balances the tail);
+    spills to L1-resident local memory; the refill queries then run at 4);
+  * grid-stride grid size: 8, 16 or 32 blocks per SM;
   * split shadow/AO tracing: one combined kernel, or a query pass plus a
     march pass whose lanes refill from the march queue (volume scenes);
-  * split camera-ray tracing, likewise.
+  * split camera-ray tracing, likewise;
+  * camera-ray traversal per thread (per-lane refill) or per warp (one
+    shared traversal for an 8x4 pixel tile);
+  * queue chunk of the refill queries: BVH8 node visits per refill round;
+  * march tiling: volume samples per refill round of the march passes.
 
 Frames are timed with CUDA events on the render stream after one warm-up
 frame per setting.  The result can be cached in a JSON file keyed by GPU
@@ -21,42 +25,73 @@ import os
 
 from . import gpu
 
+KNOBS = (
+    ("blocks_per_sm", gpu.TUNE_BLOCKS_PER_SM, (2, 3)),
+    ("grid_per_sm", gpu.TUNE_GRID_PER_SM, (8, 16, 32)),
+    ("split", gpu.TUNE_SPLIT_SECONDARY, (0, 1)),
+    ("split_primary", gpu.TUNE_SPLIT_PRIMARY, (0, 1)),
+    ("camera_packet", gpu.TUNE_CAMERA_PACKET, (0, 1)),
+    ("trav_steps", gpu.TUNE_TRAV_STEPS, (4, 8, 16)),
+    ("march_steps", gpu.TUNE_MARCH_STEPS, (8, 16, 32)),
+)
 
-def tune(scene, camera, lighting, frames=3, blocks_per_sm=(2, 3), grid_per_sm=(8, 16, 32), split=(0, 1),
-         split_primary=(0, 1), verbose=False):
+
+def current():
+    return {name: gpu.get_tuning(knob) for name, knob, _ in KNOBS}
+
+
+def apply(setting):
+    for name, knob, _ in KNOBS:
+        if name in setting:
+            gpu.set_tuning(knob, int(setting[name]))
+
+
+def tune(scene, camera, lighting, frames=3, passes=2, knobs=KNOBS, verbose=False):
     import torch
     stream = torch.cuda.current_stream()
     cam = camera.c() if hasattr(camera, "c") else camera
     fb = torch.zeros((cam.height, cam.width, 4), dtype=torch.float32, device="cuda")
+    measured = {}
     results = []
-    combos = [(mb, gp, sp, pp) for mb in blocks_per_sm for gp in grid_per_sm for sp in split for pp in split_primary]
-    for mb, gp, sp, pp in combos:
-        if True:
-            gpu.set_tuning(gpu.TUNE_BLOCKS_PER_SM, mb)
-            gpu.set_tuning(gpu.TUNE_GRID_PER_SM, gp)
-            gpu.set_tuning(gpu.TUNE_SPLIT_SECONDARY, sp)
-            gpu.set_tuning(gpu.TUNE_SPLIT_PRIMARY, pp)
+
+    def measure(setting):
+        key = tuple(sorted(setting.items()))
+        if key in measured:
+            return measured[key]
+        apply(setting)
+        fb.zero_()
+        scene.render(cam, lighting, fb.data_ptr(), stream.cuda_stream)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(frames):
             fb.zero_()
             scene.render(cam, lighting, fb.data_ptr(), stream.cuda_stream)
-            torch.cuda.synchronize()
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            for _ in range(frames):
-                fb.zero_()
-                scene.render(cam, lighting, fb.data_ptr(), stream.cuda_stream)
-            e1.record(stream)
-            torch.cuda.synchronize()
-            ms = e0.elapsed_time(e1) / frames
-            results.append({"blocks_per_sm": mb, "grid_per_sm": gp, "split": sp, "split_primary": pp,
-                            "ms_per_frame": ms})
-            if verbose:
-                print("autotune", results[-1], flush=True)
-    best = min(results, key=lambda r: r["ms_per_frame"])
-    gpu.set_tuning(gpu.TUNE_BLOCKS_PER_SM, best["blocks_per_sm"])
-    gpu.set_tuning(gpu.TUNE_GRID_PER_SM, best["grid_per_sm"])
-    gpu.set_tuning(gpu.TUNE_SPLIT_SECONDARY, best["split"])
-    gpu.set_tuning(gpu.TUNE_SPLIT_PRIMARY, best["split_primary"])
-    return {"best": best, "candidates": results}
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / frames
+        measured[key] = ms
+        results.append(dict(setting, ms_per_frame=ms))
+        if verbose:
+            print("autotune", results[-1], flush=True)
+        return ms
+
+    best = current()
+    best_ms = measure(best)
+    for _ in range(passes):
+        changed = False
+        for name, _, values in knobs:
+            for v in values:
+                if v == best[name]:
+                    continue
+                cand = dict(best, **{name: v})
+                ms = measure(cand)
+                if ms < best_ms:
+                    best, best_ms, changed = cand, ms, True
+        if not changed:
+            break
+    apply(best)
+    return {"best": dict(best, ms_per_frame=best_ms), "candidates": results}
 
 
 def cache_key(workload):
@@ -69,10 +104,7 @@ def load(path, workload):
         return None
     d = json.load(open(path)).get(cache_key(workload))
     if d:
-        gpu.set_tuning(gpu.TUNE_BLOCKS_PER_SM, d["blocks_per_sm"])
-        gpu.set_tuning(gpu.TUNE_GRID_PER_SM, d["grid_per_sm"])
-        gpu.set_tuning(gpu.TUNE_SPLIT_SECONDARY, d.get("split", 1))
-        gpu.set_tuning(gpu.TUNE_SPLIT_PRIMARY, d.get("split_primary", 1))
+        apply(d)
     return d
 
 

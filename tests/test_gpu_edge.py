@@ -1,6 +1,7 @@
 """Edge cases of the device path against the oracle: an empty scene, tiny
 and odd image sizes, empty ray lists, degenerate path-line segments,
-invalid arguments, and a 4096x4096 frame checked on a band of rows."""
+invalid arguments, a 4096x4096 frame checked on a band of rows; and the
+autotuner's coordinate descent."""
 import numpy as np
 import pytest
 
@@ -113,3 +114,27 @@ def test_largest_frame_band_matches_oracle(gpu):
     ref, _ = O.OracleScene(vis).render(cam, L, nthreads=16, rows=(r0, r1))
     close(img[r0:r1], ref[r0:r1])
     assert img[:r0].any() and img[r1:].any()
+
+
+def test_autotuner_coordinate_descent(gpu):
+    """The tuner measures one knob at a time, returns a setting for every
+    knob, and leaves the library set to it."""
+    from galaxy_gb300 import autotune
+    cam, vis = scenes.mixed_scene(n=48, n_spheres=4000, width=96, height=96, partitions=(2, 1, 1), n_ao=2)
+    L = S.resolve_lights(vis.lighting, cam)
+    sc = gpu.Scene(vis)
+    before = autotune.current()
+    try:
+        res = autotune.tune(sc, cam, L, frames=1, passes=1)
+        best = res["best"]
+        assert set(n for n, _, _ in autotune.KNOBS) <= set(best)
+        assert autotune.current() == {n: best[n] for n, _, _ in autotune.KNOBS}
+        assert len(res["candidates"]) >= 1 + sum(len(v) - 1 for _, _, v in autotune.KNOBS) - 1
+        assert best["ms_per_frame"] == min(c["ms_per_frame"] for c in res["candidates"])
+        # every setting renders the same image (within the parity tolerance)
+        img = sc.render_host(cam, L)
+        autotune.apply(before)
+        ref = sc.render_host(cam, L)
+        close(img, ref)
+    finally:
+        autotune.apply(before)
