@@ -1879,9 +1879,10 @@ static unsigned march_grid(int minb) {
     return (unsigned)(sms * (per < 1 ? 1 : per));
 }
 
-// The refill query passes run at 4 resident blocks per SM when the tuning
-// asks for 3 (64 registers: more warps to cover node-fetch latency; measured
-// faster than 80 registers with fewer spills).
+// The refill query passes and the shadow/AO march run at 4 resident blocks
+// per SM when the tuning asks for 3 (64 registers: more warps to cover
+// node-fetch and voxel-gather latency; measured faster than 80 registers
+// with fewer spills; the camera-ray march measured slower and stays at 3).
 static unsigned query_grid() {
     int sms = 152, per = 1;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, g_device);
@@ -2010,7 +2011,7 @@ static int render(Scene *sc, const gxy_camera &cam, const gxy_lighting &lt, floa
             else if (kind == K_SECONDARY && A.split) k_sec_query<false, 4, false><<<query_grid(), kThreads, 0, st>>>(S, A);
             else if (kind == K_SECONDARY) k_secondary<3><<<g, kThreads, 0, st>>>(S, A);
             else if (kind == K_PMARCH) k_prim_march<false, 3><<<march_grid(3), kThreads, 0, st>>>(S, A);
-            else k_sec_march<false, 3><<<march_grid(3), kThreads, 0, st>>>(S, A);
+            else k_sec_march<false, 4><<<query_grid(), kThreads, 0, st>>>(S, A);
         } else {
             if (kind == K_CAMERA && A.split_prim && g_tune_cam_packet && lines)
                 k_cam_packet<2, true><<<march_grid(2), kThreads, 0, st>>>(S, A);
@@ -2769,7 +2770,7 @@ static int batch_enqueue(Batch *b, const DevScene &Su, bool uniform, const Frame
                 if (mb3) {
                     if (lines) k_sec_query<true, 4, true><<<query_grid(), kThreads, 0, st>>>(Su, a);
                     else k_sec_query<true, 4, false><<<query_grid(), kThreads, 0, st>>>(Su, a);
-                    k_sec_march<true, 3><<<march_grid(3), kThreads, 0, st>>>(Su, a);
+                    k_sec_march<true, 4><<<query_grid(), kThreads, 0, st>>>(Su, a);
                 } else {
                     if (lines) k_sec_query<true, 2, true><<<march_grid(2), kThreads, 0, st>>>(Su, a);
                     else k_sec_query<true, 2, false><<<march_grid(2), kThreads, 0, st>>>(Su, a);
@@ -2816,7 +2817,7 @@ static int batch_enqueue(Batch *b, const DevScene &Su, bool uniform, const Frame
             else GXY_GEN_LAUNCH(2);
 #undef GXY_GEN_LAUNCH
             if (a.split) {
-                if (g_tune_minb == 3) k_sec_march<true, 3><<<march_grid(3), kThreads, 0, st>>>(Su, a);
+                if (g_tune_minb == 3) k_sec_march<true, 4><<<query_grid(), kThreads, 0, st>>>(Su, a);
                 else k_sec_march<true, 2><<<march_grid(2), kThreads, 0, st>>>(Su, a);
             }
             CK(cudaGetLastError());
