@@ -490,17 +490,10 @@ def partition_document(doc):
     return ext
 
 
-def load_state(path, partitions=(1, 1, 1)):
-    """Read a Galaxy state file (docs/state_files.md as implemented by
-    gxywriter.cpp:181-219, Datasets.cpp:99-125, Visualization.cpp:293-340,
-    Camera.cpp:165-281, Renderer.cpp:289-296).  Returns (renderings, epsilon):
-    one (camera, visualization) pair per camera x visualization."""
-    import json
-    doc = json.load(open(path))
-    base = os.path.dirname(os.path.abspath(path))
-    eps = 0.001
-    if "Renderer" in doc and "epsilon" in doc["Renderer"]:
-        eps = float(doc["Renderer"]["epsilon"])
+def datasets_from_json(doc, base="."):
+    """The "Datasets" block of a state document (Datasets.cpp:99-125):
+    name -> dataset.  Volumes load from .vol/.json headers relative to
+    base; other types need VTK readers and are refused."""
     datasets = {}
     for d in doc.get("Datasets", []):
         t = d["type"]
@@ -511,23 +504,48 @@ def load_state(path, partitions=(1, 1, 1)):
             datasets[d["name"]] = Volume.load_vol(fn)
         else:
             raise ValueError("dataset type %s needs VTK, which is not supported" % t)
-    viss = []
-    for v in doc.get("Visualizations", []):
-        lighting = Lighting()
-        if "Lighting" in v:
-            lighting = Lighting.from_json(v["Lighting"])
-        elif "lighting" in v:
-            lighting = Lighting.from_json(v["lighting"])
-        ops = []
-        for o in v["operators"]:
-            t = o["type"]
-            if not t.endswith("Vis"):
-                t = t + "Vis"
-            cls = {"VolumeVis": VolumeVis, "TrianglesVis": TrianglesVis,
-                   "ParticlesVis": ParticlesVis, "PathLinesVis": PathLinesVis}.get(t)
-            if cls is None:
-                raise ValueError("unknown operator type %s" % t)
-            ops.append(cls.from_json(o, datasets))
-        viss.append(Visualization(ops, lighting, partitions=partitions, epsilon=eps))
+    return datasets
+
+
+def visualization_from_json(v, datasets, partitions=(1, 1, 1), epsilon=0.001):
+    """One Visualization object (Visualization.cpp:293-340): lighting and
+    operators; an operator type gets "Vis" appended when it lacks it
+    (Visualization.cpp:318-322)."""
+    lighting = Lighting()
+    if "Lighting" in v:
+        lighting = Lighting.from_json(v["Lighting"])
+    elif "lighting" in v:
+        lighting = Lighting.from_json(v["lighting"])
+    ops = []
+    for o in v["operators"]:
+        t = o["type"]
+        if not t.endswith("Vis"):
+            t = t + "Vis"
+        cls = {"VolumeVis": VolumeVis, "TrianglesVis": TrianglesVis,
+               "ParticlesVis": ParticlesVis, "PathLinesVis": PathLinesVis}.get(t)
+        if cls is None:
+            raise ValueError("unknown operator type %s" % t)
+        ops.append(cls.from_json(o, datasets))
+    return Visualization(ops, lighting, partitions=partitions, epsilon=epsilon)
+
+
+def renderer_epsilon(doc, default=0.001):
+    """Renderer.epsilon of a state document (Renderer.cpp:289-296)."""
+    if "Renderer" in doc and "epsilon" in doc["Renderer"]:
+        return float(doc["Renderer"]["epsilon"])
+    return default
+
+
+def load_state(path, partitions=(1, 1, 1)):
+    """Read a Galaxy state file (docs/state_files.md as implemented by
+    gxywriter.cpp:181-219, Datasets.cpp:99-125, Visualization.cpp:293-340,
+    Camera.cpp:165-281, Renderer.cpp:289-296).  Returns (renderings, epsilon):
+    one (camera, visualization) pair per camera x visualization."""
+    import json
+    doc = json.load(open(path))
+    base = os.path.dirname(os.path.abspath(path))
+    eps = renderer_epsilon(doc)
+    datasets = datasets_from_json(doc, base)
+    viss = [visualization_from_json(v, datasets, partitions, eps) for v in doc.get("Visualizations", [])]
     cams = [Camera.from_json(c) for c in doc.get("Cameras", [])]
     return [(c, v) for c in cams for v in viss], eps

@@ -18,7 +18,9 @@ carries a camera, a light change and an image size; the loop
     complete on the device) and frees its memory.
 
 serve_plain() serves the same requests one at a time through the plain
-single-frame path (gxy_gpu_render) for comparison.
+single-frame path (gxy_gpu_render) for comparison.  CommandSession reads a
+viewer client's command lines (json / window / render / renderMany ...) and
+streams each frame's pixels back as AddLocalPixels messages.
 """
 import math
 import time
@@ -27,6 +29,7 @@ import numpy as np
 
 from . import _abi as A
 from . import gpu
+from . import scene as S
 
 
 class Request:
@@ -231,3 +234,145 @@ def poisson_requests(rate, count, scene_keys, make_request, seed=7, side_range=(
         key = scene_keys[int(rng.integers(0, len(scene_keys)))]
         out.append(make_request(rng, rid, t, key, side))
     return out
+
+
+# ------------------------------------------------------- command protocol
+PIXEL_DTYPE = np.dtype([("x", "<i4"), ("y", "<i4"), ("r", "<f4"), ("g", "<f4"), ("b", "<f4"), ("o", "<f4")])
+
+
+class CommandSession:
+    """One viewer client's command stream, as ViewerClientServer::handle
+    (multiserver/ViewerClientServer.cpp:62-253) reads it, over the resident
+    device path (no sockets here: a front end passes each received line to
+    handle() and sends back the reply and the pixel messages).
+
+    Commands: "json <document>" with any of Datasets, Visualization, Camera,
+    Renderer (loaded and committed in that order; error replies as Galaxy
+    words them), "window <w> <h>", "commit", "render", "renderMany <n>",
+    "permute_pixels on|off" and "max_rays_per_packet <n>" (accepted; the
+    device path renders whole frames, so they change nothing).  handle()
+    returns (handled, reply); an unknown command is (False, None).
+
+    Each rendered frame is sent as ServerRendering::AddLocalPixels messages
+    (ServerRendering.cpp:45-66): on_pixels(n, frame, sender, pixels), pixels
+    a PIXEL_DTYPE array (x, y, r, g, b, o) of the frame's non-zero pixels,
+    in chunks of `chunk`."""
+
+    def __init__(self, base_dir=".", on_pixels=None, chunk=1 << 16, partitions=(1, 1, 1), render_fn=None):
+        self.base_dir = base_dir
+        self.on_pixels = on_pixels
+        self.chunk = int(chunk)
+        self.partitions = partitions
+        self.render_fn = render_fn
+        self.datasets = {}
+        self.visualization = None
+        self.camera = None
+        self.epsilon = 0.001
+        self.scene = None
+        self.frame = 0
+        self.permute = True
+        self.max_rays_per_packet = 0
+
+    def _commit(self):
+        self.scene = None
+        if self.visualization is not None:
+            self.scene = gpu.Scene(self.visualization)
+
+    def handle(self, line):
+        import json
+        parts = line.strip().split(None, 1)
+        if not parts:
+            return False, None
+        cmd, rest = parts[0], (parts[1] if len(parts) > 1 else "")
+        if cmd == "permute_pixels":
+            if rest.strip() in ("", "on"):
+                self.permute = True
+            elif rest.strip() == "off":
+                self.permute = False
+            else:
+                return True, "error permute_pixels needs on or off"
+            return True, "ok"
+        if cmd == "max_rays_per_packet":
+            try:
+                self.max_rays_per_packet = int(rest.split()[0])
+            except (ValueError, IndexError):
+                return True, "error max_rays_per_packet needs an integer"
+            return True, "ok"
+        if cmd == "commit":
+            self._commit()
+            return True, "ok"
+        if cmd == "json":
+            try:
+                doc = json.loads(rest)
+            except ValueError:
+                return True, "error parsing json command"
+            if "Datasets" in doc:
+                try:
+                    self.datasets.update(S.datasets_from_json(doc, self.base_dir))
+                except (ValueError, OSError, KeyError):
+                    return True, "error loading datasets from json command"
+            if "Renderer" in doc:
+                self.epsilon = S.renderer_epsilon(doc, self.epsilon)
+            if "Visualization" in doc:
+                try:
+                    self.visualization = S.visualization_from_json(doc["Visualization"], self.datasets,
+                                                                   self.partitions, self.epsilon)
+                except (ValueError, KeyError):
+                    return True, "error loading visualization from json command"
+                try:
+                    self._commit()
+                except gpu.GxyError:
+                    return True, "error committing visualization from json command"
+            if "Camera" in doc:
+                try:
+                    cam = S.Camera.from_json(doc["Camera"])
+                except (ValueError, KeyError):
+                    return True, "error loading camera from json command"
+                if self.camera is not None and "dimensions" not in doc["Camera"]:
+                    cam.width, cam.height = self.camera.width, self.camera.height
+                self.camera = cam
+            return True, "ok"
+        if cmd == "window":
+            try:
+                w, h = (int(x) for x in rest.split()[:2])
+            except ValueError:
+                return True, "error window command needs width and height as integers"
+            if self.camera is None:
+                self.camera = S.Camera((0, 0, 5), (0, 0, -1), (0, 1, 0), 45.0, w, h)
+            self.camera.width, self.camera.height = w, h
+            return True, "ok"
+        if cmd == "render":
+            self.render()
+            return True, "ok"
+        if cmd == "renderMany":
+            try:
+                n = int(rest.split()[0])
+            except (ValueError, IndexError):
+                return True, "error renderMany needs a count"
+            for _ in range(n):
+                self.render()
+            return True, "ok"
+        return False, None
+
+    def render(self):
+        """Render the current camera x visualization and stream its pixels;
+        returns the (h, w, 4) framebuffer."""
+        if self.scene is None or self.camera is None:
+            return None
+        L = S.resolve_lights(self.visualization.lighting, self.camera)
+        if self.render_fn is not None:
+            fb = self.render_fn(self.scene, self.camera, L)
+        else:
+            fb = self.scene.render_host(self.camera, L)
+        frame = self.frame
+        self.frame += 1
+        if self.on_pixels is not None:
+            ys, xs = np.nonzero(np.any(fb != 0, axis=2))
+            px = np.empty(len(xs), PIXEL_DTYPE)
+            px["x"], px["y"] = xs, ys
+            v = fb[ys, xs]
+            px["r"], px["g"], px["b"], px["o"] = v[:, 0], v[:, 1], v[:, 2], v[:, 3]
+            for k in range(0, len(px), self.chunk):
+                part = px[k:k + self.chunk]
+                self.on_pixels(len(part), frame, 0, part)
+        return fb
