@@ -185,3 +185,10 @@ class gxy_generation_stats(C.Structure):
 class gxy_job(C.Structure):
     _fields_ = [("scene", C.c_void_p), ("camera", gxy_camera), ("lighting", gxy_lighting),
                 ("fb_rgba", C.c_void_p)]
+
+
+class gxy_server_config(C.Structure):
+    _fields_ = [("n_slots", C.c_int32), ("slot_pixels", C.c_int64), ("max_jobs", C.c_int32),
+                ("max_shadow", C.c_int32), ("max_ao", C.c_int32), ("fb_budget_bytes", C.c_size_t),
+                ("small_pixels", C.c_int64), ("small_batch_pixels", C.c_int64), ("big_wait_s", C.c_double),
+                ("use_graph", C.c_int32), ("cooperative", C.c_int32)]

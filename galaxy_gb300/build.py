@@ -15,7 +15,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libgxy_gpu.so")
-SOURCES = ["render.cu", "bvh.cu"]
+SOURCES = ["render.cu", "bvh.cu", "server.cu"]
 HEADERS = ["gxy_dev.cuh", "gxy_host.h", "trace.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

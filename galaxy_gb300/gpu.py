@@ -65,6 +65,12 @@ def lib():
         "gxy_gpu_classify": [C.POINTER(A.gxy_raylist)],
         "gxy_gpu_assign_destinations": [vp, C.c_int, C.POINTER(A.gxy_raylist)],
         "gxy_gpu_accumulate_terminated": [C.POINTER(A.gxy_raylist), A.f32p, C.c_int, C.c_int],
+        "gxy_server_create": [C.POINTER(A.gxy_server_config), C.POINTER(vp)],
+        "gxy_server_release": [vp],
+        "gxy_server_submit": [vp, vp, C.POINTER(A.gxy_camera), C.POINTER(A.gxy_lighting), C.POINTER(i64)],
+        "gxy_server_poll": [vp, i64, C.POINTER(C.c_int)],
+        "gxy_server_drain": [vp, C.c_int],
+        "gxy_server_take": [vp, i64, A.f32p, C.POINTER(C.c_double), C.POINTER(i64)],
     }
     for name, args in sig.items():
         f = getattr(L, name)
@@ -303,3 +309,58 @@ class Batch:
         c = A.gxy_counters()
         check(lib().gxy_gpu_batch_counters(self.h, C.byref(c)))
         return {f: getattr(c, f) for f, _ in A.gxy_counters._fields_ if f != "pad"}
+
+
+class NativeServer:
+    """The library's continuous-batching request loop (gxy_server_*): a C++
+    worker thread admits submitted requests into batch slots under a
+    framebuffer budget and completes them by polling."""
+
+    def __init__(self, n_slots=4, slot_pixels=8 << 20, max_jobs=64, max_shadow=1, max_ao=4, fb_budget=8 << 30,
+                 small_pixels=1 << 20, small_batch_pixels=4 << 20, big_wait_s=0.05, use_graph=True,
+                 cooperative=False):
+        ensure_init()
+        cfg = A.gxy_server_config(n_slots=n_slots, slot_pixels=int(slot_pixels), max_jobs=max_jobs,
+                                  max_shadow=max_shadow, max_ao=max_ao, fb_budget_bytes=int(fb_budget),
+                                  small_pixels=int(small_pixels), small_batch_pixels=int(small_batch_pixels),
+                                  big_wait_s=float(big_wait_s), use_graph=1 if use_graph else 0,
+                                  cooperative=1 if cooperative else 0)
+        h = C.c_void_p()
+        check(lib().gxy_server_create(C.byref(cfg), C.byref(h)))
+        self.h = h
+        self._sizes = {}
+
+    def release(self):
+        if getattr(self, "h", None) and self.h.value:
+            lib().gxy_server_release(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.release()
+        except Exception:
+            pass
+
+    def submit(self, scene, camera, lighting):
+        cam = camera.c() if hasattr(camera, "c") else camera
+        L = lighting if isinstance(lighting, A.gxy_lighting) else lighting.c()
+        rid = C.c_int64(0)
+        check(lib().gxy_server_submit(self.h, scene.h, C.byref(cam), C.byref(L), C.byref(rid)))
+        self._sizes[rid.value] = (cam.height, cam.width)
+        return rid.value
+
+    def poll(self, rid):
+        d = C.c_int(0)
+        check(lib().gxy_server_poll(self.h, int(rid), C.byref(d)))
+        return bool(d.value)
+
+    def drain(self, timeout_ms=600000):
+        check(lib().gxy_server_drain(self.h, int(timeout_ms)))
+
+    def take(self, rid, image=True):
+        """(rgba or None, latency seconds, rays) of a finished request."""
+        h, w = self._sizes.pop(rid)
+        out = np.zeros((h, w, 4), np.float32) if image else None
+        lat, rays = C.c_double(0), C.c_int64(0)
+        check(lib().gxy_server_take(self.h, int(rid), A.fptr(out) if image else None, C.byref(lat), C.byref(rays)))
+        return out, lat.value, rays.value

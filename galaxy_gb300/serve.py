@@ -5,17 +5,17 @@ This plays the role of Galaxy's serving front ends -- ViewerClientServer's
 returned per ServerRendering::AddLocalPixels, ServerRendering.cpp:45-66) and
 GuiClientServer's `gui::render` (src/guiserver/GuiClientServer.cpp:375-407)
 -- without their socket transport: a request names a resident scene and
-carries a camera, a light change and an image size; the loop
+carries a camera, a light change and an image size.  The loop itself is the
+library's C++ worker (gxy_server_*, src csrc/server.cu); it
 
   * admits waiting requests whenever a batch slot is free and the
     framebuffers fit the HBM budget (admission control; a request too large
     for any slot is refused),
   * packs the admitted requests of one scene into one persistent wavefront
-    launch (gpu.Batch.submit) on that slot's stream, so several batches --
-    requests that arrived while others were already on the GPU -- overlap on
-    the device,
-  * polls the slots, records each request's latency (arrival -> framebuffer
-    complete on the device) and frees its memory.
+    launch on that slot's stream, so several batches -- requests that
+    arrived while others were already on the GPU -- overlap on the device,
+  * polls the slots and records each request's latency (arrival ->
+    framebuffer complete on the device); the client takes the image.
 
 serve_plain() serves the same requests one at a time through the plain
 single-frame path (gxy_gpu_render) for comparison.  CommandSession reads a
@@ -50,137 +50,58 @@ class Request:
         self.refused = False
 
 
-class FramebufferPool:
-    """Device framebuffers (torch tensors) under a byte budget."""
-
-    def __init__(self, budget_bytes):
-        import torch
-        self.torch = torch
-        self.budget = budget_bytes
-        self.used = 0
-
-    def try_alloc(self, w, h):
-        nbytes = w * h * 16
-        if self.used + nbytes > self.budget:
-            return None
-        t = self.torch.zeros((h, w, 4), dtype=self.torch.float32, device="cuda")
-        self.used += nbytes
-        return t
-
-    def free(self, t):
-        self.used -= t.numel() * 4
-
-
 class Server:
-    """Batch slots over resident scenes.  Admission policy: requests up to
-    `small_pixels` are "small" and are packed together (same scene, FIFO) up to
+    """Continuous batching over resident scenes: the library's C++ request
+    loop (gxy_server_*, gpu.NativeServer) does the admission, packing and
+    completion; run() replays requests at their arrival times and collects
+    latency and rays.  Admission policy: requests up to `small_pixels` are
+    "small" and are packed together (same scene, FIFO) up to
     `small_batch_pixels` per launch; a larger request runs in a slot of its
     own.  The oldest waiting request goes first, except that small requests
-    may pass a large one that has waited less than `big_wait_s` (short jobs
-    first, bounded by age, so latency of small requests is not held behind
-    large frames and large frames are not starved)."""
+    may pass a large one that has waited less than `big_wait_s`; requests
+    are admitted while their framebuffers fit `fb_budget` bytes."""
 
     def __init__(self, scenes, n_slots=4, slot_pixels=8 << 20, max_jobs=64, max_shadow=1, max_ao=4,
                  fb_budget=8 << 30, use_graph=True, keep_results=False, cooperative=False,
                  small_pixels=1 << 20, small_batch_pixels=4 << 20, big_wait_s=0.05):
         self.scenes = scenes
-        self.cooperative = cooperative
-        self.small_pixels = small_pixels
-        self.small_batch_pixels = min(small_batch_pixels, slot_pixels)
-        self.big_wait_s = big_wait_s
-        self.slots = [gpu.Batch(slot_pixels, max_jobs, max_shadow, max_ao) for _ in range(n_slots)]
-        self.busy = [None] * n_slots          # list of requests in flight per slot
-        self.slot_pixels = slot_pixels
-        self.max_jobs = max_jobs
-        self.pool = FramebufferPool(fb_budget)
-        self.use_graph = use_graph
         self.keep_results = keep_results
+        self.slot_pixels = slot_pixels
+        self.native = gpu.NativeServer(n_slots, slot_pixels, max_jobs, max_shadow, max_ao, fb_budget,
+                                       small_pixels, small_batch_pixels, big_wait_s, use_graph, cooperative)
 
     def release(self):
-        for s in self.slots:
-            s.release()
-
-    def _finish(self, k, now):
-        for r in self.busy[k]:
-            r.t_done = now
-            if not self.keep_results:
-                self.pool.free(r.fb)
-                r.fb = None
-        c = self.slots[k].counters()
-        per = c["primary_rays"] + c["shadow_rays"] + c["ao_rays"]
-        tot = sum(r.pixels for r in self.busy[k])
-        for r in self.busy[k]:
-            r.rays = per * r.pixels / max(1, tot)
-        self.busy[k] = None
+        self.native.release()
 
     def run(self, requests, time_limit=120.0):
-        """Serve `requests` (sorted by arrival, seconds from start) in real
-        time; returns a statistics dict."""
-        import torch
-        waiting = []
-        i = 0
-        n = len(requests)
+        """Submit `requests` (sorted by arrival, seconds from start) in real
+        time, wait for all, and return the statistics dict; with
+        keep_results each request's image is left in r.fb (host array)."""
         t0 = time.perf_counter()
-        done = 0
-        refused = 0
-        while done + refused < n:
+        submitted = []
+        for r in requests:
             now = time.perf_counter() - t0
             if now > time_limit:
                 break
-            while i < n and requests[i].arrival <= now:
-                r = requests[i]
-                if r.pixels > self.slot_pixels:
-                    r.refused = True
-                    refused += 1
-                else:
-                    waiting.append(r)
-                i += 1
-            # completions
-            for k, s in enumerate(self.slots):
-                if self.busy[k] is not None and s.poll():
-                    done += len(self.busy[k])
-                    self._finish(k, time.perf_counter() - t0)
-            # admissions
-            for k, s in enumerate(self.slots):
-                if self.busy[k] is not None or not waiting:
-                    continue
-                tnow = time.perf_counter() - t0
-                head = waiting[0]
-                smalls = [r for r in waiting if r.pixels <= self.small_pixels]
-                if head.pixels > self.small_pixels and (not smalls or tnow - head.arrival >= self.big_wait_s):
-                    cand, cap = [head], self.slot_pixels
-                else:
-                    key = smalls[0].scene
-                    cand, cap = [r for r in smalls if r.scene == key], self.small_batch_pixels
-                batch, pix = [], 0
-                for r in cand:
-                    if len(batch) >= self.max_jobs or pix + r.pixels > cap:
-                        break
-                    fb = self.pool.try_alloc(r.camera.width, r.camera.height)
-                    if fb is None:
-                        break
-                    r.fb = fb
-                    batch.append(r)
-                    pix += r.pixels
-                if not batch:
-                    continue
-                chosen = set(id(r) for r in batch)
-                waiting = [r for r in waiting if id(r) not in chosen]
-                for r in batch:
-                    r.t_submit = tnow
-                torch.cuda.current_stream().synchronize()   # framebuffers zeroed before the batch stream uses them
-                s.submit([(self.scenes[r.scene], r.camera, r.lighting, r.fb.data_ptr()) for r in batch],
-                         use_graph=self.use_graph, cooperative=self.cooperative)
-                self.busy[k] = batch
-            if not any(b is not None for b in self.busy):
-                nxt = requests[i].arrival if i < n else None
-                if nxt is not None:
-                    dt = nxt - (time.perf_counter() - t0)
-                    if dt > 0:
-                        time.sleep(min(dt, 0.002))
-            else:
-                time.sleep(0.00005)
+            if r.arrival > now:
+                time.sleep(r.arrival - now)
+            try:
+                rid = self.native.submit(self.scenes[r.scene], r.camera, r.lighting)
+            except gpu.GxyError as e:
+                if e.code != A.GXY_ERR_ADMISSION:
+                    raise
+                r.refused = True
+                continue
+            r.t_submit = time.perf_counter() - t0
+            submitted.append((r, rid))
+        left = max(1.0, time_limit - (time.perf_counter() - t0))
+        self.native.drain(int(left * 1000))
         makespan = time.perf_counter() - t0
+        for r, rid in submitted:
+            img, lat, rays = self.native.take(rid, image=self.keep_results)
+            r.t_done = r.t_submit + lat
+            r.rays = rays
+            r.fb = img
         return summarize(requests, makespan)
 
 

@@ -348,6 +348,43 @@ int gxy_gpu_batch_counters(gxy_batch batch, gxy_counters *out);
 /* The cudaStream_t of the batch (for events and framebuffer copies). */
 int gxy_gpu_batch_stream(gxy_batch batch, void **stream);
 
+/* ---- Serving loop -------------------------------------------------------
+ * Replaces the request handling of Galaxy's serving front ends
+ * (ViewerClientServer::handle `render`, src/multiserver/ViewerClientServer.cpp:
+ * 62-253; GuiClientServer gui::render, src/guiserver/GuiClientServer.cpp:375-407),
+ * which render one request at a time, with continuous batching: a worker
+ * thread admits submitted requests into n_slots batch slots as slots and the
+ * framebuffer budget allow (requests up to small_pixels of one scene packed
+ * up to small_batch_pixels per launch, larger ones alone; a large request
+ * lets smaller ones pass for at most big_wait_s), and finds completions by
+ * polling.  Framebuffers come from a stream-ordered device memory pool. */
+typedef struct gxy_server_s *gxy_server;
+typedef struct gxy_server_config {
+    int32_t n_slots;
+    int64_t slot_pixels;          /* camera rays per slot = largest request */
+    int32_t max_jobs, max_shadow, max_ao;
+    size_t  fb_budget_bytes;      /* device framebuffers of admitted requests */
+    int64_t small_pixels;
+    int64_t small_batch_pixels;
+    double  big_wait_s;
+    int32_t use_graph;            /* GXY_BATCH_GRAPH submissions */
+    int32_t cooperative;          /* GXY_BATCH_COOPERATIVE submissions */
+} gxy_server_config;
+int gxy_server_create(const gxy_server_config *config, gxy_server *out);
+/* Waits (bounded) for running batches, then frees everything. */
+int gxy_server_release(gxy_server server);
+/* Enqueue a request arriving now (lighting resolved); GXY_ERR_ADMISSION if
+ * it can never be admitted (larger than a slot or the framebuffer budget). */
+int gxy_server_submit(gxy_server server, gxy_scene scene, const gxy_camera *camera,
+                      const gxy_lighting *lighting, int64_t *id);
+int gxy_server_poll(gxy_server server, int64_t id, int *done);
+/* Bounded host wait until every submitted request has finished. */
+int gxy_server_drain(gxy_server server, int timeout_ms);
+/* Copy a finished request's image to host rgba (height*width*4 fp32, or
+ * NULL) and release it; latency_s = submission to completion, rays = its
+ * share of the batch's traced rays. */
+int gxy_server_take(gxy_server server, int64_t id, float *rgba, double *latency_s, int64_t *rays);
+
 /* ---- RayList-level drop-in (host buffers) ------------------------------ */
 
 /* Camera::generate_initial_rays for partition `partition`: fills `out`

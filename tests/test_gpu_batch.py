@@ -103,5 +103,5 @@ def test_serving_results_match_alone(env):
     assert st["p99_ms"] >= st["p50_ms"] > 0
     for r in reqs:
         ref = alone(torch, table[r.scene], r.camera, r.lighting)
-        assert np.abs(r.fb.cpu().numpy() - ref).max() <= 1e-5
+        assert np.abs(r.fb - ref).max() <= 1e-5
     srv.release()
