@@ -105,3 +105,31 @@ def test_serving_results_match_alone(env):
         ref = alone(torch, table[r.scene], r.camera, r.lighting)
         assert np.abs(r.fb - ref).max() <= 1e-5
     srv.release()
+
+
+def test_native_server_contract(env):
+    """gxy_server_*: refusals at submission, poll/drain/take, one take per
+    request, images equal to rendering alone."""
+    torch, gpu, sc = env
+    A = gpu.A
+    srv = gpu.NativeServer(n_slots=2, slot_pixels=10000, max_jobs=4, max_shadow=1, max_ao=2, fb_budget=1 << 24,
+                           small_pixels=3000, small_batch_pixels=8000)
+    try:
+        scene, cam0, vis = sc["tri"]
+        big = S.Camera(cam0.eye, cam0.dir, cam0.up, cam0.aov, 200, 100)      # 20000 pixels > slot
+        with pytest.raises(gpu.GxyError) as e:
+            srv.submit(scene, big, S.resolve_lights(vis.lighting, big))
+        assert e.value.code == A.GXY_ERR_ADMISSION
+        ids = []
+        for k, (key, sce, cam, L) in enumerate(jobs_for(env, 6, seed=9)):
+            ids.append((srv.submit(sce, cam, L), sce, cam, L))
+        srv.drain(60000)
+        for rid, sce, cam, L in ids:
+            assert srv.poll(rid)
+            img, lat, rays = srv.take(rid)
+            assert lat > 0 and rays > 0
+            assert np.abs(img - alone(torch, sce, cam, L)).max() <= 1e-5
+            with pytest.raises(gpu.GxyError):
+                srv.poll(rid)   # taken: no longer known
+    finally:
+        srv.release()
