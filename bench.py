@@ -368,8 +368,8 @@ def main():
     ap.add_argument("--leaf-max", type=int, default=0, help="primitives per BVH8 leaf (1-4; 0: library default)")
     ap.add_argument("--trav-steps", type=int, default=0, help="node visits per refill round (0: library default)")
     ap.add_argument("--march-steps", type=int, default=0, help="samples per refill round (0: library default)")
-    ap.add_argument("--bvh", default="lbvh", choices=["sah", "lbvh"],
-                    help="BVH binary tree: binned SAH along the Morton order, or radix-tree (LBVH) splits")
+    ap.add_argument("--bvh", default="", help="BVH binary tree: 'lbvh' (radix tree), 'sah' (binned-SAH top over "
+                                                "radix clusters of 256) or 'sah:C' (clusters of C); default: library")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -387,24 +387,34 @@ def main():
     from galaxy_gb300 import scene as S
 
     cam, vis, cfg = make_workload(args.workload)
-    gpu.set_tuning(gpu.TUNE_BVH_SAH, 1 if args.bvh == "sah" else 0)
+    if args.bvh:
+        gpu.set_tuning(gpu.TUNE_BVH_SAH, 0 if args.bvh == "lbvh" else
+                       (int(args.bvh.split(":")[1]) if ":" in args.bvh else 1))
     if args.leaf_max:
         gpu.set_tuning(gpu.TUNE_LEAF_MAX, args.leaf_max)
     if args.trav_steps:
         gpu.set_tuning(gpu.TUNE_TRAV_STEPS, args.trav_steps)
     if args.march_steps:
         gpu.set_tuning(gpu.TUNE_MARCH_STEPS, args.march_steps)
-    cfg = dict(cfg, bvh=args.bvh, leaf_max=gpu.get_tuning(gpu.TUNE_LEAF_MAX),
+    cfg = dict(cfg, bvh_sah_clusters=gpu.get_tuning(gpu.TUNE_BVH_SAH), leaf_max=gpu.get_tuning(gpu.TUNE_LEAF_MAX),
                trav_steps=gpu.get_tuning(gpu.TUNE_TRAV_STEPS), march_steps=gpu.get_tuning(gpu.TUNE_MARCH_STEPS))
     if args.image:
         cam.width = cam.height = args.image
         cfg = dict(cfg, image=[args.image, args.image], workload=cfg["workload"] + " (image %d^2)" % args.image)
     gpu.init(local)
-    t0 = time.time()
-    sc = gpu.Scene(vis)
-    commit_s = time.time() - t0
     L = S.resolve_lights(vis.lighting, cam)
     cam_c = cam.c()
+    bvh_tuning = None
+    t0 = time.time()
+    if args.autotune and not args.tune and not args.bvh:
+        # scene-level knob first: radix-tree BVH or binned-SAH top over clusters of 64
+        from galaxy_gb300 import autotune
+        sc, v, bvh_out = autotune.tune_bvh(vis, cam_c, L, values=(0, 64))
+        bvh_tuning = {"bvh_sah_clusters": v, "ms_per_frame": dict(bvh_out)}
+        cfg = dict(cfg, bvh_sah_clusters=v)
+    else:
+        sc = gpu.Scene(vis)
+    commit_s = time.time() - t0
     stream = torch.cuda.current_stream()
     fb = torch.zeros((cam.height, cam.width, 4), dtype=torch.float32, device="cuda")
 
@@ -512,10 +522,11 @@ def main():
                            for g in sc_last_gens],
            "scene_commit_s": commit_s, "bvh": sc.bvh_info(),
            "gpu_launches": launches, "roofline": roof, "e2e": e2e, "clocks": clk,
-           "tuning": tuning if tuning else {"best": {"blocks_per_sm": gpu.get_tuning(gpu.TUNE_BLOCKS_PER_SM),
-                                                     "grid_per_sm": gpu.get_tuning(gpu.TUNE_GRID_PER_SM),
-                                                     "split": gpu.get_tuning(gpu.TUNE_SPLIT_SECONDARY),
-                                                     "split_primary": gpu.get_tuning(gpu.TUNE_SPLIT_PRIMARY)}}}
+           "tuning": dict(tuning if tuning else {"best": {"blocks_per_sm": gpu.get_tuning(gpu.TUNE_BLOCKS_PER_SM),
+                                                          "grid_per_sm": gpu.get_tuning(gpu.TUNE_GRID_PER_SM),
+                                                          "split": gpu.get_tuning(gpu.TUNE_SPLIT_SECONDARY),
+                                                          "split_primary": gpu.get_tuning(gpu.TUNE_SPLIT_PRIMARY)}},
+                          bvh=bvh_tuning)}
     if rank == 0 and not args.no_cpu_baseline:
         base, _, _ = cpu_baseline(cam, vis, target_s=args.cpu_seconds)
         base.pop("seconds", None)

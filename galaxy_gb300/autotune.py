@@ -16,6 +16,9 @@ repeated while a pass still changes something):
   * queue chunk of the refill queries: BVH8 node visits per refill round;
   * march tiling: volume samples per refill round of the march passes.
 
+tune_bvh() picks the scene-level BVH builder (radix tree, or a binned-SAH
+top over radix-tree clusters) by committing the scene with each.
+
 Frames are timed with CUDA events on the render stream after one warm-up
 frame per setting.  The result can be cached in a JSON file keyed by GPU
 name and workload.
@@ -92,6 +95,42 @@ def tune(scene, camera, lighting, frames=3, passes=2, knobs=KNOBS, verbose=False
             break
     apply(best)
     return {"best": dict(best, ms_per_frame=best_ms), "candidates": results}
+
+
+def tune_bvh(vis, camera, lighting, values=(0, 64), frames=2, verbose=False):
+    """Scene-level knob: commit `vis` once per BVH binary-tree builder
+    (GXY_TUNE_BVH_SAH: 0 radix tree, C > 1 binned-SAH top over clusters of C
+    primitives), time a few frames of each and keep the faster scene.
+    Returns (scene, value, [(value, ms), ...])."""
+    import torch
+    stream = torch.cuda.current_stream()
+    cam = camera.c() if hasattr(camera, "c") else camera
+    fb = torch.zeros((cam.height, cam.width, 4), dtype=torch.float32, device="cuda")
+    best, best_ms, out = None, float("inf"), []
+    for v in values:
+        gpu.set_tuning(gpu.TUNE_BVH_SAH, v)
+        sc = gpu.Scene(vis)
+        sc.render(cam, lighting, fb.data_ptr(), stream.cuda_stream)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(frames):
+            fb.zero_()
+            sc.render(cam, lighting, fb.data_ptr(), stream.cuda_stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / frames
+        out.append((v, ms))
+        if verbose:
+            print("autotune bvh", v, ms, flush=True)
+        if ms < best_ms:
+            if best is not None:
+                best[0].release()
+            best, best_ms = (sc, v), ms
+        else:
+            sc.release()
+    gpu.set_tuning(gpu.TUNE_BVH_SAH, best[1])
+    return best[0], best[1], out
 
 
 def cache_key(workload):

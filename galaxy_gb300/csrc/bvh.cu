@@ -18,6 +18,8 @@
 #include <cub/cub.cuh>
 
 #include <cfloat>
+#include <cstring>
+#include <algorithm>
 #include <chrono>
 #include <vector>
 
@@ -221,103 +223,41 @@ __global__ void k_refit(int n, const uint32_t *ids, const float4 *plo, const flo
 }
 
 // ---------------------------------------------------------------------
-// Morton-ordered binned SAH binary tree (replaces the radix-tree splits of
-// k_karras): top down, one warp per node of the current level.  A node
-// covers a contiguous range [first, last] of Morton-sorted primitives; its
-// range is cut into B = min(32, count) equal bins, lane k reduces the box of
-// bin k, warp scans give the boxes and counts left and right of every bin
-// boundary, and the node splits at the boundary with the smallest
-// surface-area cost area(L)*n(L) + area(R)*n(R).  Children with one
-// primitive are leaves (~position); the others go to the next level.
-__device__ __forceinline__ float4 f4min(float4 a, float4 b) {
-    return make_float4(fminf(a.x, b.x), fminf(a.y, b.y), fminf(a.z, b.z), 0.0f);
-}
-__device__ __forceinline__ float4 f4max(float4 a, float4 b) {
-    return make_float4(fmaxf(a.x, b.x), fmaxf(a.y, b.y), fmaxf(a.z, b.z), 0.0f);
-}
-__device__ __forceinline__ float4 shfl_up4(float4 v, int o) {
-    return make_float4(__shfl_up_sync(0xffffffffu, v.x, o), __shfl_up_sync(0xffffffffu, v.y, o),
-                       __shfl_up_sync(0xffffffffu, v.z, o), 0.0f);
-}
-__device__ __forceinline__ float4 shfl_down4(float4 v, int o) {
-    return make_float4(__shfl_down_sync(0xffffffffu, v.x, o), __shfl_down_sync(0xffffffffu, v.y, o),
-                       __shfl_down_sync(0xffffffffu, v.z, o), 0.0f);
+// Binned-SAH refinement of the top of the radix tree.  The radix tree is cut
+// into clusters -- maximal subtrees of at most C primitives -- and the tree
+// above them is rebuilt top down by binned SAH over the clusters' boxes
+// (build_top_sah on the host: a few thousand to a hundred thousand
+// clusters), so the levels that every ray visits get surface-area splits
+// while the bottom keeps the Morton structure.
+__global__ void k_clusters(int n, int C, const int *parent, const int *leaf_parent, const int *first, const int *last,
+                           int *refs, unsigned int *count) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n - 1) {   // internal node i
+        int size = last[i] - first[i] + 1;
+        if (size <= C) {
+            int p = i == 0 ? -1 : parent[i];
+            if (p < 0 || last[p] - first[p] + 1 > C) refs[atomicAdd(count, 1u)] = i;
+        }
+    }
+    if (i < n) {       // leaf i (a single primitive) under a node larger than C
+        int p = leaf_parent[i];
+        if (last[p] - first[p] + 1 > C) refs[atomicAdd(count, 1u)] = ~i;
+    }
 }
 
-__global__ void k_sah_level(int nq, const int *q, int *qout, unsigned *ctr, const uint32_t *ids, const float4 *plo,
-                            const float4 *phi, int *left, int *right, int *first, int *last, float4 *nlo,
-                            float4 *nhi) {
-    int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    int lane = threadIdx.x & 31;
-    if (w >= nq) return;   // whole warp exits together
-    int node = q[w];
-    int f = first[node], l = last[node];
-    int cnt = l - f + 1;
-    int B = cnt < 32 ? cnt : 32;
-    float4 lo = make_float4(FLT_MAX, FLT_MAX, FLT_MAX, 0), hi = make_float4(-FLT_MAX, -FLT_MAX, -FLT_MAX, 0);
-    int b0 = f + (int)(((long long)lane * cnt) / B), b1 = f + (int)(((long long)(lane + 1) * cnt) / B);
-    int n = 0;
-    if (lane < B) {
-        for (int i = b0; i < b1; i++) {
-            uint32_t p = ids[i];
-            lo = f4min(lo, plo[p]);
-            hi = f4max(hi, phi[p]);
-        }
-        n = b1 - b0;
-    }
-    // inclusive prefix (boxes and counts) and inclusive suffix
-    float4 plo_ = lo, phi_ = hi, slo = lo, shi = hi;
-    int pn = n, sn = n;
-    for (int o = 1; o < 32; o <<= 1) {
-        float4 a = shfl_up4(plo_, o), b = shfl_up4(phi_, o);
-        int c = __shfl_up_sync(0xffffffffu, pn, o);
-        if (lane >= o) { plo_ = f4min(plo_, a); phi_ = f4max(phi_, b); pn += c; }
-        float4 d = shfl_down4(slo, o), e = shfl_down4(shi, o);
-        int g = __shfl_down_sync(0xffffffffu, sn, o);
-        if (lane + o < 32) { slo = f4min(slo, d); shi = f4max(shi, e); sn += g; }
-    }
-    // candidate: split after bin `lane` (lane < B-1): left = prefix(lane), right = suffix(lane+1)
-    float4 rlo = shfl_down4(slo, 1), rhi = shfl_down4(shi, 1);
-    int rn = __shfl_down_sync(0xffffffffu, sn, 1);
-    float cost = FLT_MAX;
-    if (lane < B - 1) {
-        float la = (phi_.x - plo_.x) * (phi_.y - plo_.y) + (phi_.y - plo_.y) * (phi_.z - plo_.z) +
-                   (phi_.z - plo_.z) * (phi_.x - plo_.x);
-        float ra = (rhi.x - rlo.x) * (rhi.y - rlo.y) + (rhi.y - rlo.y) * (rhi.z - rlo.z) +
-                   (rhi.z - rlo.z) * (rhi.x - rlo.x);
-        cost = la * (float)pn + ra * (float)rn;
-    }
-    int best = lane;
-    for (int o = 16; o > 0; o >>= 1) {
-        float oc = __shfl_xor_sync(0xffffffffu, cost, o);
-        int ob = __shfl_xor_sync(0xffffffffu, best, o);
-        if (oc < cost || (oc == cost && ob < best)) { cost = oc; best = ob; }
-    }
-    float4 alo = make_float4(__shfl_sync(0xffffffffu, plo_.x, B - 1), __shfl_sync(0xffffffffu, plo_.y, B - 1),
-                             __shfl_sync(0xffffffffu, plo_.z, B - 1), 0.0f);
-    float4 ahi = make_float4(__shfl_sync(0xffffffffu, phi_.x, B - 1), __shfl_sync(0xffffffffu, phi_.y, B - 1),
-                             __shfl_sync(0xffffffffu, phi_.z, B - 1), 0.0f);
-    if (lane == 0) {
-        nlo[node] = alo;
-        nhi[node] = ahi;
-        int split = f + (int)(((long long)(best + 1) * cnt) / B);   // first primitive of the right child
-        int rng[2][2] = {{f, split - 1}, {split, l}};
-        int ref[2];
-        for (int k = 0; k < 2; k++) {
-            int a = rng[k][0], b = rng[k][1];
-            if (a == b) {
-                ref[k] = ~a;
-            } else {
-                int id = (int)atomicAdd(&ctr[0], 1u);
-                first[id] = a;
-                last[id] = b;
-                qout[atomicAdd(&ctr[1], 1u)] = id;
-                ref[k] = id;
-            }
-        }
-        left[node] = ref[0];
-        right[node] = ref[1];
-    }
+__global__ void k_cluster_info(int m, const int *refs, const uint32_t *ids, const float4 *plo, const float4 *phi,
+                               const int *first, const int *last, const float4 *nlo, const float4 *nhi,
+                               float4 *clo, float4 *chi) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= m) return;
+    int r = refs[k];
+    float4 a, b;
+    int cnt;
+    if (r >= 0) { a = nlo[r]; b = nhi[r]; cnt = last[r] - first[r] + 1; }
+    else { uint32_t p = ids[~r]; a = plo[p]; b = phi[p]; cnt = 1; }
+    a.w = __int_as_float(cnt);
+    clo[k] = a;
+    chi[k] = b;
 }
 
 __device__ __forceinline__ float half_area(float4 lo, float4 hi) {
@@ -473,6 +413,132 @@ static inline unsigned blocks_for(int64_t n, int b) { return (unsigned)((n + b -
 
 // Build the BVH8 for the geometry described by S (S.nodes/S.slots are set
 // on success).  sph_radius: per-sphere radius (device).
+// Host binned-SAH build over the clusters (box lo/hi, primitive count in
+// lo.w): 32 centroid bins on each axis, cost area(L)*prims(L) +
+// area(R)*prims(R), split at the cheapest bin boundary (by index when every
+// centroid coincides).  Node t of the result is binary node base + t; a
+// child is a cluster ref (refs[k]) or another top node.  A top node's size
+// is stated as at least 5 primitives so that the collapse, which decides
+// leaves by size (at most 4 primitives per leaf), always opens it.
+static inline int __float_as_int_host(float f) {
+    int i;
+    memcpy(&i, &f, sizeof i);
+    return i;
+}
+struct TopNode {
+    int left, right;
+    float lo[3], hi[3];
+    int count;
+};
+static void build_top_sah(const std::vector<float4> &clo, const std::vector<float4> &chi, const std::vector<int> &refs,
+                          int base, std::vector<TopNode> &out) {
+    const int m = (int)refs.size();
+    std::vector<int> idx(m);
+    for (int k = 0; k < m; k++) idx[k] = k;
+    auto cen = [&](int k, int a) {
+        const float *l = &clo[k].x, *h = &chi[k].x;
+        return 0.5f * (l[a] + h[a]);
+    };
+    auto area = [](const float *lo, const float *hi) {
+        float x = hi[0] - lo[0], y = hi[1] - lo[1], z = hi[2] - lo[2];
+        return x * y + y * z + z * x;
+    };
+    struct Task {
+        int node, begin, end;
+    };
+    out.clear();
+    out.reserve(m > 1 ? m - 1 : 1);
+    out.push_back(TopNode{});
+    std::vector<Task> todo{{0, 0, m}};
+    constexpr int NB = 32;
+    while (!todo.empty()) {
+        Task t = todo.back();
+        todo.pop_back();
+        TopNode &nd = out[t.node];
+        float cmin[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, cmax[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+        for (int a = 0; a < 3; a++) { nd.lo[a] = FLT_MAX; nd.hi[a] = -FLT_MAX; }
+        int count = 0;
+        for (int i = t.begin; i < t.end; i++) {
+            int k = idx[i];
+            const float *l = &clo[k].x, *h = &chi[k].x;
+            for (int a = 0; a < 3; a++) {
+                nd.lo[a] = std::min(nd.lo[a], l[a]);
+                nd.hi[a] = std::max(nd.hi[a], h[a]);
+                cmin[a] = std::min(cmin[a], cen(k, a));
+                cmax[a] = std::max(cmax[a], cen(k, a));
+            }
+            count += __float_as_int_host(clo[k].w);
+        }
+        nd.count = count;
+        // best bin boundary over the three axes
+        float best = FLT_MAX;
+        int best_axis = -1, best_bin = 0;
+        for (int a = 0; a < 3; a++) {
+            float ext = cmax[a] - cmin[a];
+            if (!(ext > 0.f)) continue;
+            float blo[NB][3], bhi[NB][3];
+            int bn[NB] = {0}, bc[NB] = {0};
+            for (int b = 0; b < NB; b++)
+                for (int q = 0; q < 3; q++) { blo[b][q] = FLT_MAX; bhi[b][q] = -FLT_MAX; }
+            for (int i = t.begin; i < t.end; i++) {
+                int k = idx[i];
+                int b = std::min(NB - 1, (int)((cen(k, a) - cmin[a]) / ext * NB));
+                const float *l = &clo[k].x, *h = &chi[k].x;
+                for (int q = 0; q < 3; q++) { blo[b][q] = std::min(blo[b][q], l[q]); bhi[b][q] = std::max(bhi[b][q], h[q]); }
+                bn[b] += __float_as_int_host(clo[k].w);
+                bc[b]++;
+            }
+            float llo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, lhi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+            float lcost[NB];
+            int ln = 0, lc = 0;
+            int litems[NB];
+            for (int b = 0; b < NB; b++) {
+                for (int q = 0; q < 3; q++) { llo[q] = std::min(llo[q], blo[b][q]); lhi[q] = std::max(lhi[q], bhi[b][q]); }
+                ln += bn[b];
+                lc += bc[b];
+                litems[b] = lc;
+                lcost[b] = lc ? area(llo, lhi) * ln : 0.f;
+            }
+            float rlo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, rhi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+            int rn = 0;
+            for (int b = NB - 1; b >= 1; b--) {
+                for (int q = 0; q < 3; q++) { rlo[q] = std::min(rlo[q], blo[b][q]); rhi[q] = std::max(rhi[q], bhi[b][q]); }
+                rn += bn[b];
+                int left_items = litems[b - 1];
+                if (left_items == 0 || left_items == t.end - t.begin) continue;
+                float cost = lcost[b - 1] + area(rlo, rhi) * rn;
+                if (cost < best) { best = cost; best_axis = a; best_bin = b - 1; }
+            }
+        }
+        int mid;
+        if (best_axis < 0) {
+            mid = (t.begin + t.end) / 2;
+        } else {
+            const int a = best_axis;
+            const float ext = cmax[a] - cmin[a];
+            auto it = std::partition(idx.begin() + t.begin, idx.begin() + t.end, [&](int k) {
+                return std::min(NB - 1, (int)((cen(k, a) - cmin[a]) / ext * NB)) <= best_bin;
+            });
+            mid = (int)(it - idx.begin());
+            if (mid == t.begin || mid == t.end) mid = (t.begin + t.end) / 2;
+        }
+        int child[2];
+        const int rb[2] = {t.begin, mid}, re[2] = {mid, t.end};
+        for (int c = 0; c < 2; c++) {
+            if (re[c] - rb[c] == 1) {
+                child[c] = refs[idx[rb[c]]];
+            } else {
+                int id = (int)out.size();
+                out.push_back(TopNode{});
+                todo.push_back({id, rb[c], re[c]});
+                child[c] = base + id;
+            }
+        }
+        out[t.node].left = child[0];
+        out[t.node].right = child[1];
+    }
+}
+
 int build_bvh8(DevScene &S, const float *sph_radius, DeviceArena &arena, cudaStream_t st, BVHInfo &info) {
     auto t_start = std::chrono::steady_clock::now();
     int64_t n64 = S.n_tri + S.n_sph + S.n_seg;
@@ -496,8 +562,10 @@ int build_bvh8(DevScene &S, const float *sph_radius, DeviceArena &arena, cudaStr
     ALLOC(B.plo, n); ALLOC(B.phi, n);
     ALLOC(B.keys, n); ALLOC(B.keys2, n); ALLOC(B.ids, n); ALLOC(B.ids2, n);
     int ni = n > 1 ? n - 1 : 1;
-    ALLOC(B.left, ni); ALLOC(B.right, ni); ALLOC(B.parent, ni); ALLOC(B.first, ni); ALLOC(B.last, ni);
-    ALLOC(B.flags, ni); ALLOC(B.nlo, ni); ALLOC(B.nhi, ni);
+    const int C = sah_builder() ? sah_cluster_size() : 0;   // top-level SAH over clusters of <= C primitives
+    const int ncap = (C > 1 && n > C) ? 2 * ni : ni;       // room for the top tree's nodes after the radix tree's
+    ALLOC(B.left, ncap); ALLOC(B.right, ncap); ALLOC(B.parent, ni); ALLOC(B.first, ncap); ALLOC(B.last, ncap);
+    ALLOC(B.flags, ni); ALLOC(B.nlo, ncap); ALLOC(B.nhi, ncap);
     int *leaf_parent;
     ALLOC(leaf_parent, n);
     ALLOC(B.ctr, 8);
@@ -516,32 +584,8 @@ int build_bvh8(DevScene &S, const float *sph_radius, DeviceArena &arena, cudaStr
     unsigned char *tmp;
     ALLOC(tmp, tmp_bytes);
     CK(cub::DeviceRadixSort::SortPairs(tmp, tmp_bytes, B.keys, B.keys2, B.ids, B.ids2, n, 0, 63, st));
-    if (n > 1 && sah_builder()) {
-        // binned-SAH splits along the Morton order, level by level
-        int zero_first[2] = {0, n - 1};
-        CK(cudaMemcpyAsync(B.first, &zero_first[0], sizeof(int), cudaMemcpyHostToDevice, st));
-        CK(cudaMemcpyAsync(B.last, &zero_first[1], sizeof(int), cudaMemcpyHostToDevice, st));
-        int root = 0;
-        unsigned c2[2] = {1, 0};
-        CK(cudaMemcpyAsync(B.qa, &root, sizeof(int), cudaMemcpyHostToDevice, st));
-        CK(cudaMemcpyAsync(B.ctr + 4, c2, sizeof c2, cudaMemcpyHostToDevice, st));
-        int nq = 1, lev = 0;
-        int *qa = (int *)B.qa, *qb = (int *)B.qb;
-        while (nq > 0) {
-            CK(cudaMemsetAsync(B.ctr + 5, 0, sizeof(unsigned), st));
-            k_sah_level<<<blocks_for((int64_t)nq * 32, 256), 256, 0, st>>>(nq, qa, qb, B.ctr + 4, B.ids2, B.plo, B.phi,
-                                                                       B.left, B.right, B.first, B.last, B.nlo,
-                                                                       B.nhi);
-            CK(cudaGetLastError());
-            unsigned c[2];
-            CK(cudaMemcpyAsync(c, B.ctr + 4, sizeof c, cudaMemcpyDeviceToHost, st));
-            CK(cudaStreamSynchronize(st));
-            nq = (int)c[1];
-            std::swap(qa, qb);
-            if (++lev > 4096) return set_error(GXY_ERR_INVALID, "SAH build did not converge");
-        }
-        info.sah_levels = lev;
-    } else if (n > 1) {
+    int root_ref = n > 1 ? 0 : ~0;
+    if (n > 1) {
         CK(cudaMemsetAsync(B.flags, 0, sizeof(int) * ni, st));
         k_karras<<<blocks_for(n - 1, 256), 256, 0, st>>>(n, B.keys2, B.left, B.right, B.parent, B.first, B.last,
                                                          leaf_parent);
@@ -549,14 +593,59 @@ int build_bvh8(DevScene &S, const float *sph_radius, DeviceArena &arena, cudaStr
                                                     B.flags, B.nlo, B.nhi);
         CK(cudaGetLastError());
     }
+    if (C > 1 && n > C) {
+        int *refs;
+        float4 *clo, *chi;
+        ALLOC(refs, n); ALLOC(clo, n); ALLOC(chi, n);
+        CK(cudaMemsetAsync(B.ctr + 6, 0, sizeof(unsigned int), st));
+        k_clusters<<<blocks_for(n, 256), 256, 0, st>>>(n, C, B.parent, leaf_parent, B.first, B.last, refs, B.ctr + 6);
+        unsigned int m = 0;
+        CK(cudaMemcpyAsync(&m, B.ctr + 6, sizeof m, cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        if (m >= 2 && m <= (unsigned)n) {
+            k_cluster_info<<<blocks_for(m, 256), 256, 0, st>>>((int)m, refs, B.ids2, B.plo, B.phi, B.first, B.last,
+                                                               B.nlo, B.nhi, clo, chi);
+            CK(cudaGetLastError());
+            std::vector<int> h_refs(m);
+            std::vector<float4> h_lo(m), h_hi(m);
+            CK(cudaMemcpyAsync(h_refs.data(), refs, m * sizeof(int), cudaMemcpyDeviceToHost, st));
+            CK(cudaMemcpyAsync(h_lo.data(), clo, m * sizeof(float4), cudaMemcpyDeviceToHost, st));
+            CK(cudaMemcpyAsync(h_hi.data(), chi, m * sizeof(float4), cudaMemcpyDeviceToHost, st));
+            CK(cudaStreamSynchronize(st));
+            std::vector<TopNode> top;
+            const int base = ni;
+            build_top_sah(h_lo, h_hi, h_refs, base, top);
+            const int t = (int)top.size();
+            std::vector<int> L(t), R(t), F(t), Z(t);
+            std::vector<float4> LO(t), HI(t);
+            for (int k = 0; k < t; k++) {
+                L[k] = top[k].left;
+                R[k] = top[k].right;
+                F[k] = 0;
+                Z[k] = std::max(top[k].count, 5) - 1;   // stated size >= 5: never a leaf
+                LO[k] = make_float4(top[k].lo[0], top[k].lo[1], top[k].lo[2], 0.f);
+                HI[k] = make_float4(top[k].hi[0], top[k].hi[1], top[k].hi[2], 0.f);
+            }
+            CK(cudaMemcpyAsync(B.left + base, L.data(), t * sizeof(int), cudaMemcpyHostToDevice, st));
+            CK(cudaMemcpyAsync(B.right + base, R.data(), t * sizeof(int), cudaMemcpyHostToDevice, st));
+            CK(cudaMemcpyAsync(B.first + base, F.data(), t * sizeof(int), cudaMemcpyHostToDevice, st));
+            CK(cudaMemcpyAsync(B.last + base, Z.data(), t * sizeof(int), cudaMemcpyHostToDevice, st));
+            CK(cudaMemcpyAsync(B.nlo + base, LO.data(), t * sizeof(float4), cudaMemcpyHostToDevice, st));
+            CK(cudaMemcpyAsync(B.nhi + base, HI.data(), t * sizeof(float4), cudaMemcpyHostToDevice, st));
+            CK(cudaStreamSynchronize(st));   // the host vectors go out of scope
+            root_ref = base;
+            info.sah_levels = (int)m;   // clusters under the SAH top tree
+        }
+    }
     BVH8Node *nodes;
     float4 *slots;
     rc = arena.alloc((void **)&nodes, sizeof(BVH8Node) * (size_t)max_nodes);
     if (rc) return rc;
     rc = arena.alloc((void **)&slots, sizeof(float4) * 3 * (size_t)max_slots);
     if (rc) { arena.free(nodes); return rc; }
-    // root: wide node 0 from binary root 0 (or the single leaf)
-    int2 root = make_int2(n > 1 ? 0 : ~0, 0);
+    // root: wide node 0 from the binary root (radix-tree root 0, the SAH top
+    // tree's root, or the single leaf)
+    int2 root = make_int2(root_ref, 0);
     unsigned int c0[8] = {1, 0, 0, 0, 0, 0, 0, 0};
     CK(cudaMemcpyAsync(B.ctr, c0, sizeof c0, cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(B.qa, &root, sizeof root, cudaMemcpyHostToDevice, st));

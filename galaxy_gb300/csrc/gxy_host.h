@@ -69,8 +69,10 @@ struct BVHInfo {
 };
 
 int build_bvh8(DevScene &S, const float *sph_radius, DeviceArena &arena, cudaStream_t st, BVHInfo &info);
-// 1: binary tree by binned SAH along the Morton order; 0: radix-tree (LBVH) splits.
+// Binned-SAH top tree over radix-tree clusters of at most sah_cluster_size()
+// primitives (sah_builder() true), else the radix tree alone.
 bool sah_builder();
+int sah_cluster_size();
 // Largest subtree (primitives) stored as one leaf of a wide node, 1-4.
 int leaf_max();
 

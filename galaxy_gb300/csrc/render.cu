@@ -1848,6 +1848,7 @@ static int g_tune_split = 1;   // split shadow/AO tracing into query + refill-ma
 static int g_tune_split_prim = 1;   // split camera rays into query + refill-march passes
 static int g_tune_sah = 0;          // BVH binary tree by binned SAH (else radix-tree splits)
 bool sah_builder() { return g_tune_sah != 0; }
+int sah_cluster_size() { return g_tune_sah == 1 ? 256 : g_tune_sah; }
 static int g_tune_leaf = 1;         // primitives per BVH8 leaf (at most)
 static int g_tune_trav_steps = 8;   // node visits per refill round of the query passes
 static int g_tune_march_steps = 16; // samples per refill round of the march passes
@@ -2432,7 +2433,8 @@ int gxy_gpu_set_tuning(int knob, int value) {
         return GXY_OK;
     }
     if (knob == GXY_TUNE_BVH_SAH) {
-        g_tune_sah = value ? 1 : 0;
+        if (value < 0 || value > (1 << 20)) return set_error(GXY_ERR_INVALID, "bad SAH cluster size");
+        g_tune_sah = value;
         return GXY_OK;
     }
     if (knob == GXY_TUNE_LEAF_MAX) {

@@ -291,9 +291,10 @@ int gxy_gpu_set_profiling(gxy_scene scene, int on);
 #define GXY_TUNE_SPLIT_SECONDARY 3   /* 1: shadow/AO rays of volume scenes traced as a query
                                         pass plus a march pass with per-lane refill */
 #define GXY_TUNE_SPLIT_PRIMARY   4   /* 1: camera rays of volume scenes likewise */
-#define GXY_TUNE_BVH_SAH         5   /* 1: BVH binary tree by binned SAH along the Morton
-                                        order; 0 (default): radix-tree splits. Applies to
-                                        scenes committed afterwards */
+#define GXY_TUNE_BVH_SAH         5   /* top of the BVH binary tree rebuilt by binned SAH
+                                        over radix-tree clusters of at most C primitives:
+                                        0 off (radix tree only), 1 C = 256, >= 2 C itself.
+                                        Applies to scenes committed afterwards */
 #define GXY_TUNE_LEAF_MAX        6   /* largest primitive count of a BVH8 leaf, 1-4
                                         (default 1); scenes committed afterwards */
 #define GXY_TUNE_TRAV_STEPS      7   /* BVH8 node visits per refill round of the query

@@ -280,3 +280,24 @@ def test_errors_are_reported(gpu):
     bad.types[0] = 1    # unresolved camera light
     with pytest.raises(GxyError):
         g.render_host(cam, bad)
+
+
+@pytest.mark.parametrize("which", ["triangles", "mixed", "pathlines"])
+def test_sah_top_bvh_matches_oracle(gpu, which):
+    """BVH with the binned-SAH top over radix-tree clusters (small clusters,
+    so the top tree is deep): same images as the oracle."""
+    gpu.set_tuning(gpu.TUNE_BVH_SAH, 16)
+    try:
+        if which == "triangles":
+            cam, vis = scenes.triangle_spheres_scene(width=128, height=128, n_seg=24)
+        elif which == "mixed":
+            cam, vis = scenes.mixed_scene(n=64, n_spheres=20000, width=112, height=112, partitions=(2, 2, 1), n_ao=2)
+        else:
+            cam, vis = scenes.pathlines_scene(n_lines=500, n_vertices=32, width=112, height=112)
+        img, ref, sc, cnt = render_both(gpu, cam, vis)
+        assert sc.bvh_info()["nodes"] > 0
+    finally:
+        gpu.set_tuning(gpu.TUNE_BVH_SAH, 0)
+    image_close(img, ref)
+    c = sc.counters()
+    assert c["primary_rays"] == cnt["primary"] and c["shadow_rays"] == cnt["shadow"]
