@@ -101,10 +101,11 @@ class ClockSampler:
 def algorithmic_bytes(g):
     """Algorithmic bytes of one generation's kernel: 64 B per queue record
     read and written, 128 B per BVH8 node line, 48 B per triangle and 16 B
-    per sphere tested, 4 B per volume sample, 32 B per framebuffer
+    per sphere tested, 4 B per volume sample read (march positions in clear
+    bricks read no voxels and are left out), 32 B per framebuffer
     contribution (read + write of fp32 RGBA)."""
     return (64 * g["rays_in"] + 64 * g["enqueued"] + 128 * g["nodes"] + 48 * g["tri_tests"] +
-            16 * g["sph_tests"] + 4 * g["samples"] + 32 * g["terminated"])
+            16 * g["sph_tests"] + 4 * (g["samples"] - g.get("samples_skipped", 0)) + 32 * g["terminated"])
 
 
 def measured_peaks():
@@ -368,6 +369,11 @@ def main():
     ap.add_argument("--leaf-max", type=int, default=0, help="primitives per BVH8 leaf (1-4; 0: library default)")
     ap.add_argument("--trav-steps", type=int, default=0, help="node visits per refill round (0: library default)")
     ap.add_argument("--march-steps", type=int, default=0, help="samples per refill round (0: library default)")
+    ap.add_argument("--skip-clear", type=int, default=-1,
+                    help="empty-space skipping flags at scene commit: 1 on, 0 off (-1: library default)")
+    ap.add_argument("--skip-mode", type=int, default=-1,
+                    help="clear-brick skipping bits: 1 camera-ray runs, 2 shadow/AO skipping, 4 shadow/AO runs "
+                         "(-1: library default)")
     ap.add_argument("--bvh", default="", help="BVH binary tree: 'lbvh' (radix tree), 'sah' (binned-SAH top over "
                                                 "radix clusters of 256) or 'sah:C' (clusters of C); default: library")
     args = ap.parse_args()
@@ -383,6 +389,7 @@ def main():
     rank, world, local = dist_setup(args.gpus)
     torch.cuda.set_device(local)
     from galaxy_gb300 import _abi as A
+    from galaxy_gb300 import autotune
     from galaxy_gb300 import gpu
     from galaxy_gb300 import scene as S
 
@@ -392,11 +399,16 @@ def main():
                        (int(args.bvh.split(":")[1]) if ":" in args.bvh else 1))
     if args.leaf_max:
         gpu.set_tuning(gpu.TUNE_LEAF_MAX, args.leaf_max)
+    if args.skip_clear >= 0:
+        gpu.set_tuning(gpu.TUNE_SKIP_CLEAR, args.skip_clear)
     if args.trav_steps:
         gpu.set_tuning(gpu.TUNE_TRAV_STEPS, args.trav_steps)
     if args.march_steps:
         gpu.set_tuning(gpu.TUNE_MARCH_STEPS, args.march_steps)
+    if args.skip_mode >= 0:
+        gpu.set_tuning(gpu.TUNE_SKIP_MODE, args.skip_mode)
     cfg = dict(cfg, bvh_sah_clusters=gpu.get_tuning(gpu.TUNE_BVH_SAH), leaf_max=gpu.get_tuning(gpu.TUNE_LEAF_MAX),
+               skip_clear=gpu.get_tuning(gpu.TUNE_SKIP_CLEAR),
                trav_steps=gpu.get_tuning(gpu.TUNE_TRAV_STEPS), march_steps=gpu.get_tuning(gpu.TUNE_MARCH_STEPS))
     if args.image:
         cam.width = cam.height = args.image
@@ -408,7 +420,6 @@ def main():
     t0 = time.time()
     if args.autotune and not args.tune and not args.bvh:
         # scene-level knob first: radix-tree BVH or binned-SAH top over clusters of 64
-        from galaxy_gb300 import autotune
         sc, v, bvh_out = autotune.tune_bvh(vis, cam_c, L, values=(0, 64))
         bvh_tuning = {"bvh_sah_clusters": v, "ms_per_frame": dict(bvh_out)}
         cfg = dict(cfg, bvh_sah_clusters=v)
@@ -430,7 +441,6 @@ def main():
         gpu.set_tuning(gpu.TUNE_SPLIT_SECONDARY, vals[2])
         gpu.set_tuning(gpu.TUNE_SPLIT_PRIMARY, vals[3])
     elif args.autotune:
-        from galaxy_gb300 import autotune
         tuning = autotune.tune(sc, cam_c, L, frames=2)
     sc.set_profiling(True)
     for _ in range(args.warmup):
@@ -517,16 +527,13 @@ def main():
            "rays_per_frame": rays_per_frame,
            "rays": {"primary": c["primary_rays"], "shadow": c["shadow_rays"], "ao": c["ao_rays"],
                     "segments": c["segments"], "handoffs": c["handoffs"], "generations": c["bounces"],
-                    "samples": c["samples"], "bvh_nodes": c["nodes"], "prim_tests": c["prim_tests"]},
+                    "samples": c["samples"], "samples_skipped": c["samples_skipped"], "bvh_nodes": c["nodes"],
+                    "prim_tests": c["prim_tests"]},
            "generations": [{k: (round(v, 4) if isinstance(v, float) else v) for k, v in g.items()}
                            for g in sc_last_gens],
            "scene_commit_s": commit_s, "bvh": sc.bvh_info(),
            "gpu_launches": launches, "roofline": roof, "e2e": e2e, "clocks": clk,
-           "tuning": dict(tuning if tuning else {"best": {"blocks_per_sm": gpu.get_tuning(gpu.TUNE_BLOCKS_PER_SM),
-                                                          "grid_per_sm": gpu.get_tuning(gpu.TUNE_GRID_PER_SM),
-                                                          "split": gpu.get_tuning(gpu.TUNE_SPLIT_SECONDARY),
-                                                          "split_primary": gpu.get_tuning(gpu.TUNE_SPLIT_PRIMARY)}},
-                          bvh=bvh_tuning)}
+           "tuning": dict(tuning if tuning else {"best": autotune.current()}, bvh=bvh_tuning)}
     if rank == 0 and not args.no_cpu_baseline:
         base, _, _ = cpu_baseline(cam, vis, target_s=args.cpu_seconds)
         base.pop("seconds", None)

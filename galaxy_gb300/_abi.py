@@ -116,7 +116,7 @@ class gxy_counters(C.Structure):
     _fields_ = [(n, C.c_int64) for n in (
         "primary_rays", "secondary_rays", "shadow_rays", "ao_rays", "segments",
         "handoffs", "terminated", "dropped", "kept", "bounces", "samples", "nodes",
-        "prim_tests")] + [("overflow", C.c_int32), ("pad", C.c_int32)]
+        "prim_tests")] + [("overflow", C.c_int32), ("pad", C.c_int32), ("samples_skipped", C.c_int64)]
 
 
 def fptr(a):
@@ -179,7 +179,8 @@ class RayListArrays:
 
 class gxy_generation_stats(C.Structure):
     _fields_ = [("ms", C.c_double), ("generation", C.c_int32), ("kind", C.c_int32)] + [(n, C.c_int64) for n in (
-        "rays_in", "enqueued", "segments", "samples", "nodes", "tri_tests", "sph_tests", "terminated")]
+        "rays_in", "enqueued", "segments", "samples", "nodes", "tri_tests", "sph_tests", "terminated",
+        "samples_skipped")]
 
 
 class gxy_job(C.Structure):

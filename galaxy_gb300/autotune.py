@@ -14,7 +14,9 @@ repeated while a pass still changes something):
   * camera-ray traversal per thread (per-lane refill) or per warp (one
     shared traversal for an 8x4 pixel tile);
   * queue chunk of the refill queries: BVH8 node visits per refill round;
-  * march tiling: volume samples per refill round of the march passes.
+  * march tiling: volume samples per refill round of the march passes;
+  * clear-brick skipping: fast runs in the camera-ray march, skipping (and
+    fast runs) in the shadow/AO march.
 
 tune_bvh() picks the scene-level BVH builder (radix tree, or a binned-SAH
 top over radix-tree clusters) by committing the scene with each.
@@ -35,7 +37,8 @@ KNOBS = (
     ("split_primary", gpu.TUNE_SPLIT_PRIMARY, (0, 1)),
     ("camera_packet", gpu.TUNE_CAMERA_PACKET, (0, 1)),
     ("trav_steps", gpu.TUNE_TRAV_STEPS, (4, 8, 16)),
-    ("march_steps", gpu.TUNE_MARCH_STEPS, (8, 16, 32)),
+    ("march_steps", gpu.TUNE_MARCH_STEPS, (8, 16, 32, 64)),
+    ("skip_mode", gpu.TUNE_SKIP_MODE, (0, 1, 3, 7)),
 )
 
 

@@ -48,6 +48,10 @@ struct DevVolume {
     int n_iso;
     float iso[GXY_MAX_ISOVALUES];
     int volume_render;
+    // Per brick, 1 when every trilinear sample inside it lies below the
+    // transfer function's zero-opacity threshold (tf_clear_below), so an
+    // interval between two such samples composites nothing.
+    const unsigned char *clear;
 };
 
 struct DevPartition {
@@ -153,7 +157,7 @@ struct DevLights {
 
 struct DevCounters {
     unsigned long long primary, shadow, ao, segments, handoffs, terminated, dropped, kept, samples, nodes, tri_tests,
-        sph_tests, enqueued, marched;
+        sph_tests, enqueued, marched, skipped;
     int overflow;        // a queue or a traversal stack ran out of room
     int pad;
 };
@@ -283,26 +287,43 @@ struct CellCache {
     int ix, iy, iz;
     float c[8];
 };
-__device__ __forceinline__ float vol_sample_cached(const DevVolume &v, V3 p, CellCache &cc) {
-    float gx = (p.x - v.ox) * v.ix;
-    float gy = (p.y - v.oy) * v.iy;
-    float gz = (p.z - v.oz) * v.iz;
-    if (!(gx >= 0.0f)) gx = 0.0f;
-    if (!(gy >= 0.0f)) gy = 0.0f;
-    if (!(gz >= 0.0f)) gz = 0.0f;
-    if (gx > v.ux) gx = v.ux;
-    if (gy > v.uy) gy = v.uy;
-    if (gz > v.uz) gz = v.uz;
-    int ix = (int)gx, iy = (int)gy, iz = (int)gz;
-    if (ix != cc.ix || iy != cc.iy || iz != cc.iz) {
-        const float *b = cell_base(v, ix, iy, iz);
+
+// Clamped grid coordinate of a world point and its cell, as vol_sample
+// computes them.
+struct VolPos {
+    float gx, gy, gz;
+    int ix, iy, iz;
+};
+__device__ __forceinline__ VolPos vol_pos(const DevVolume &v, V3 p) {
+    VolPos g;
+    g.gx = (p.x - v.ox) * v.ix;
+    g.gy = (p.y - v.oy) * v.iy;
+    g.gz = (p.z - v.oz) * v.iz;
+    if (!(g.gx >= 0.0f)) g.gx = 0.0f;
+    if (!(g.gy >= 0.0f)) g.gy = 0.0f;
+    if (!(g.gz >= 0.0f)) g.gz = 0.0f;
+    if (g.gx > v.ux) g.gx = v.ux;
+    if (g.gy > v.uy) g.gy = v.uy;
+    if (g.gz > v.uz) g.gz = v.uz;
+    g.ix = (int)g.gx; g.iy = (int)g.gy; g.iz = (int)g.gz;
+    return g;
+}
+
+// Linear index of the brick holding the cell of g.
+__device__ __forceinline__ int brick_of(const DevVolume &v, const VolPos &g) {
+    return ((g.iz >> 2) * v.nby + (g.iy >> 2)) * v.nbx + (g.ix >> 2);
+}
+
+__device__ __forceinline__ float vol_sample_at(const DevVolume &v, const VolPos &g, CellCache &cc) {
+    if (g.ix != cc.ix || g.iy != cc.iy || g.iz != cc.iz) {
+        const float *b = cell_base(v, g.ix, g.iy, g.iz);
         constexpr int SY = kBrickSide, SZ = kBrickSide * kBrickSide;
         cc.c[0] = __ldg(b); cc.c[1] = __ldg(b + 1); cc.c[2] = __ldg(b + SY); cc.c[3] = __ldg(b + SY + 1);
         cc.c[4] = __ldg(b + SZ); cc.c[5] = __ldg(b + SZ + 1); cc.c[6] = __ldg(b + SZ + SY);
         cc.c[7] = __ldg(b + SZ + SY + 1);
-        cc.ix = ix; cc.iy = iy; cc.iz = iz;
+        cc.ix = g.ix; cc.iy = g.iy; cc.iz = g.iz;
     }
-    float fx = gx - (float)ix, fy = gy - (float)iy, fz = gz - (float)iz;
+    float fx = g.gx - (float)g.ix, fy = g.gy - (float)g.iy, fz = g.gz - (float)g.iz;
     float ax = 1.0f - fx;
     float v00 = ax * cc.c[0] + fx * cc.c[1];
     float v10 = ax * cc.c[2] + fx * cc.c[3];
@@ -312,6 +333,10 @@ __device__ __forceinline__ float vol_sample_cached(const DevVolume &v, V3 p, Cel
     float v0 = ay * v00 + fy * v10;
     float v1 = ay * v01 + fy * v11;
     return (1.0f - fz) * v0 + fz * v1;
+}
+
+__device__ __forceinline__ float vol_sample_cached(const DevVolume &v, V3 p, CellCache &cc) {
+    return vol_sample_at(v, vol_pos(v, p), cc);
 }
 
 // Central-difference gradient, one grid spacing either side.

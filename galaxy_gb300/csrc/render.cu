@@ -402,6 +402,47 @@ __global__ void k_brick_volume(const float *lin, int nx, int ny, int nz, int nbx
     out[e] = lin[((int64_t)z * ny + y) * nx + x];
 }
 
+// Per brick of a bricked volume: 1 when no trilinear sample inside it can
+// reach `below`.  A sample is a convex combination of the brick's voxels, so
+// it exceeds their maximum by at most a few ulps of rounding in the weights
+// (margin 1e-5 relative); NaN voxels are left out of the maximum because a
+// sample touching one is NaN, whose opacity is zero.  One warp per brick.
+__global__ void k_brick_clear(const float *bricked, int64_t n_bricks, float below, unsigned char *clear) {
+    const int64_t b = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (b >= n_bricks) return;       // uniform per warp: blockDim is a multiple of 32
+    const float *p = bricked + b * kBrickFloats;
+    float m = -INFINITY;
+    for (int o = lane; o < kBrickSide * kBrickSide * kBrickSide; o += 32) m = fmaxf(m, p[o]);
+    for (int s = 16; s > 0; s >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, s));
+    if (lane == 0) clear[b] = (m == -INFINITY) ? (below > -INFINITY) : (m + fabsf(m) * 1e-5f < below);
+}
+
+// Threshold T of a transfer function such that tf_lookup gives opacity
+// exactly 0 for every value v < T (and for NaN): values at or below r0 read
+// opac[0]; inside the range, floor((v - r0) * k) = i interpolates opac[i]
+// and opac[i + 1].  With opac[0 .. z-1] zero, every v below
+// r0 + (z - 1) / k interpolates two zeros; the bound is pulled in by 1e-4
+// relative to cover the rounding of (v - r0) * k.  -inf when opac[0] > 0.
+static float tf_clear_below(const DevTF &t) {
+    int z = 0;
+    while (z < GXY_TF_SIZE && t.opac[z] == 0.0f) z++;
+    if (z == 0) return -INFINITY;
+    if (z == GXY_TF_SIZE) return INFINITY;
+    float T = t.r0;
+    if (z >= 2 && t.k > 0.0f && std::isfinite(t.k)) {
+        double lim = (double)t.r0 + (double)(z - 1) / (double)t.k * (1.0 - 1e-4);
+        float f = (float)lim;
+        if ((double)f > lim) f = nextafterf(f, -INFINITY);
+        if (f > T) T = f;
+    }
+    return T;
+}
+
+// Commit-time knob GXY_TUNE_SKIP_CLEAR: build the per-brick clear flags
+// (empty-space skipping in the march passes) or leave them out.
+static int g_tune_skip_clear = 1;
+
 static int commit(const gxy_scene_desc *d, Scene *sc) {
     DevScene &S = sc->S;
     memset(&S, 0, sizeof S);
@@ -465,6 +506,16 @@ static int commit(const gxy_scene_desc *d, Scene *sc) {
         DevTF t;
         tf_to_dev(v.tf, t);
         tfs.push_back(t);
+        if (g_tune_skip_clear) {
+            const int64_t nb = n_out / kBrickFloats;
+            unsigned char *clear;
+            if ((rc = arena().alloc((void **)&clear, (size_t)nb))) return rc;
+            sc->owned.push_back(clear);
+            k_brick_clear<<<(unsigned)((nb * 32 + 255) / 256), 256>>>(V.data, nb, tf_clear_below(t), clear);
+            CK(cudaGetLastError());
+            CK(cudaDeviceSynchronize());
+            V.clear = clear;
+        }
         V.n_slices = v.n_slices;
         for (int k = 0; k < v.n_slices; k++)
             V.slices[k] = make_float4(v.slices[k][0], v.slices[k][1], v.slices[k][2], v.slices[k][3]);
@@ -736,6 +787,7 @@ struct FrameArgs {
     // split primary tracing: camera query pass -> primary march queue -> march pass
     int trav_steps;                    // refill query passes: BVH8 node visits per refill round
     int march_steps;                   // refill march passes: samples per refill round
+    int skip_mode;                     // GXY_TUNE_SKIP_MODE bits
     int split_prim;
     DRay *pmarch;
     float4 *pmarch_hit;                // 2 per record: (n, c.x), (c.y, c.z, -, -)
@@ -772,15 +824,15 @@ struct LocalCounters {
 // block barrier, so warps retire as soon as their own rays are done).
 __device__ __forceinline__ void flush_counters(DevCounters *ctr, const LocalCounters &c, const RayStats &st) {
     const int lane = threadIdx.x & 31;
-    unsigned long long vals[15] = {c.prim, c.sh,  c.ao,  c.seg, c.hand,  c.term,  c.drop,  c.keep,
-                                   st.samples, st.nodes, st.tris, st.sphs, c.enq, c.march,
+    unsigned long long vals[16] = {c.prim, c.sh,  c.ao,  c.seg, c.hand,  c.term,  c.drop,  c.keep,
+                                   st.samples, st.nodes, st.tris, st.sphs, c.enq, c.march, st.skipped,
                                    (unsigned long long)(c.ovf | st.ovf)};
 #pragma unroll
-    for (int k = 0; k < 15; k++) {
+    for (int k = 0; k < 16; k++) {
         unsigned long long v = vals[k];
         for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
         if (lane == 0 && v) {
-            if (k < 14) atomicAdd(&(&ctr->primary)[k], v);
+            if (k < 15) atomicAdd(&(&ctr->primary)[k], v);
             else atomicExch(&ctr->overflow, 1);
         }
     }
@@ -1529,7 +1581,7 @@ __global__ void __launch_bounds__(kThreads, MINB) k_cam_packet(DevScene S, Frame
 // March pass of split primary tracing with per-lane refill: composite the
 // volume up to the query pass's stop distance, then shade (ambient, AO spawn,
 // diffuse, shadow spawn), classify, route and accumulate as primary_ray does.
-template <bool BATCH, int MINB>
+template <bool BATCH, int MINB, bool SKIP>
 __global__ void __launch_bounds__(kThreads, MINB) k_prim_march(DevScene S, FrameArgs A) {
     __shared__ DevTF tfs[kMaxVol];
     load_tfs(S, tfs);
@@ -1573,7 +1625,7 @@ __global__ void __launch_bounds__(kThreads, MINB) k_prim_march(DevScene S, Frame
             }
         }
         if (!__any_sync(0xffffffffu, have)) break;
-        if (have && !M.done) prim_march_steps(S, tfs[0], M, max(A.march_steps, 1), st);
+        if (have && !M.done) prim_march_steps<SKIP>(S, tfs[0], M, max(A.march_steps, 1), A.skip_mode & 1, st);
         bool fin = have && M.done;
         PrimOut P;
         const DevJob &J = BATCH ? A.jobs[fin ? job : 0] : A.job0;
@@ -1599,7 +1651,7 @@ __global__ void __launch_bounds__(kThreads, MINB) k_prim_march(DevScene S, Frame
 // lanes keep marching, so warps stay full across rays of different march
 // lengths.  Each record carries the query pass's stop distance and surface
 // flag.  USCENE / batch as for the other frame kernels (uniform scene only).
-template <bool BATCH, int MINB>
+template <bool BATCH, int MINB, bool SKIP>
 __global__ void __launch_bounds__(kThreads, MINB) k_sec_march(DevScene S, FrameArgs A) {
     __shared__ DevTF tfs[kMaxVol];
     load_tfs(S, tfs);
@@ -1634,7 +1686,7 @@ __global__ void __launch_bounds__(kThreads, MINB) k_sec_march(DevScene S, FrameA
             }
         }
         if (!__any_sync(0xffffffffu, have)) break;
-        if (have && !M.done) sec_march_steps(S, tfs[0], M, max(A.march_steps, 1), st);
+        if (have && !M.done) sec_march_steps<SKIP>(S, tfs[0], M, max(A.march_steps, 1), A.skip_mode & 4, st);
         bool fin = have && M.done;
         int dest = GXY_DROP_ON_FLOOR;
         TraceOut T;
@@ -1852,6 +1904,7 @@ int sah_cluster_size() { return g_tune_sah == 1 ? 256 : g_tune_sah; }
 static int g_tune_leaf = 1;         // primitives per BVH8 leaf (at most)
 static int g_tune_trav_steps = 8;   // node visits per refill round of the query passes
 static int g_tune_march_steps = 16; // samples per refill round of the march passes
+static int g_tune_skip_mode = 1;    // clear-brick skipping per march pass (GXY_TUNE_SKIP_MODE bits)
 static int g_tune_cam_packet = 1;   // single-frame camera query: warp-cooperative (1) or per-lane refill (0)
 int leaf_max() { return g_tune_leaf; }
 
@@ -1875,9 +1928,23 @@ static unsigned grid_for(int64_t n) {
 static unsigned march_grid(int minb) {
     int sms = 152, per = 1;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, g_device);
-    if (minb == 3) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_sec_march<false, 3>, kThreads, 0);
-    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_sec_march<false, 2>, kThreads, 0);
+    if (minb == 3) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_sec_march<false, 3, false>, kThreads, 0);
+    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_sec_march<false, 2, false>, kThreads, 0);
     return (unsigned)(sms * (per < 1 ? 1 : per));
+}
+
+// The march passes with or without clear-brick skipping: the camera-ray
+// march skips whenever the scene has the flags, the shadow/AO march when
+// GXY_TUNE_SKIP_MODE bit 1 also asks for it.
+template <bool BATCH, int MINB>
+static void launch_prim_march(unsigned grid, cudaStream_t st, const DevScene &S, const FrameArgs &A) {
+    if (S.vol[0].clear) k_prim_march<BATCH, MINB, true><<<grid, kThreads, 0, st>>>(S, A);
+    else k_prim_march<BATCH, MINB, false><<<grid, kThreads, 0, st>>>(S, A);
+}
+template <bool BATCH, int MINB>
+static void launch_sec_march(unsigned grid, cudaStream_t st, const DevScene &S, const FrameArgs &A) {
+    if (S.vol[0].clear && (A.skip_mode & 2)) k_sec_march<BATCH, MINB, true><<<grid, kThreads, 0, st>>>(S, A);
+    else k_sec_march<BATCH, MINB, false><<<grid, kThreads, 0, st>>>(S, A);
 }
 
 // The refill query passes and the shadow/AO march run at 4 resident blocks
@@ -1933,7 +2000,7 @@ static int ensure_queues(Scene *sc, const size_t need[3]) {
 static void add_counters(DevCounters &a, const DevCounters &b) {
     const unsigned long long *pb = &b.primary;
     unsigned long long *pa = &a.primary;
-    for (int k = 0; k < 14; k++) pa[k] += pb[k];
+    for (int k = 0; k < 15; k++) pa[k] += pb[k];
     a.overflow |= b.overflow;
 }
 
@@ -1978,6 +2045,7 @@ static int render(Scene *sc, const gxy_camera &cam, const gxy_lighting &lt, floa
     A.split_prim = (split_eligible(S) && g_tune_split_prim) ? 1 : 0;
     A.trav_steps = g_tune_trav_steps;
     A.march_steps = g_tune_march_steps;
+    A.skip_mode = g_tune_skip_mode;
     A.pmarch = sc->pmarch;
     A.pmarch_hit = sc->pmarch_hit;
     A.pmarch_count = sc->qcount + 8;    // [0] records, [1] march cursor, [2] camera query cursor, [3] extra slots
@@ -2011,8 +2079,8 @@ static int render(Scene *sc, const gxy_camera &cam, const gxy_lighting &lt, floa
             else if (kind == K_SECONDARY && A.split && lines) k_sec_query<false, 4, true><<<query_grid(), kThreads, 0, st>>>(S, A);
             else if (kind == K_SECONDARY && A.split) k_sec_query<false, 4, false><<<query_grid(), kThreads, 0, st>>>(S, A);
             else if (kind == K_SECONDARY) k_secondary<3><<<g, kThreads, 0, st>>>(S, A);
-            else if (kind == K_PMARCH) k_prim_march<false, 3><<<march_grid(3), kThreads, 0, st>>>(S, A);
-            else k_sec_march<false, 4><<<query_grid(), kThreads, 0, st>>>(S, A);
+            else if (kind == K_PMARCH) launch_prim_march<false, 3>(march_grid(3), st, S, A);
+            else launch_sec_march<false, 4>(query_grid(), st, S, A);
         } else {
             if (kind == K_CAMERA && A.split_prim && g_tune_cam_packet && lines)
                 k_cam_packet<2, true><<<march_grid(2), kThreads, 0, st>>>(S, A);
@@ -2025,8 +2093,8 @@ static int render(Scene *sc, const gxy_camera &cam, const gxy_lighting &lt, floa
             else if (kind == K_SECONDARY && A.split && lines) k_sec_query<false, 2, true><<<march_grid(2), kThreads, 0, st>>>(S, A);
             else if (kind == K_SECONDARY && A.split) k_sec_query<false, 2, false><<<march_grid(2), kThreads, 0, st>>>(S, A);
             else if (kind == K_SECONDARY) k_secondary<2><<<g, kThreads, 0, st>>>(S, A);
-            else if (kind == K_PMARCH) k_prim_march<false, 2><<<march_grid(2), kThreads, 0, st>>>(S, A);
-            else k_sec_march<false, 2><<<march_grid(2), kThreads, 0, st>>>(S, A);
+            else if (kind == K_PMARCH) launch_prim_march<false, 2>(march_grid(2), st, S, A);
+            else launch_sec_march<false, 2>(march_grid(2), st, S, A);
         }
         CK(cudaGetLastError());
         if (sc->profile) CK(cudaEventRecord(sc->events[2 * nl + 1], st));
@@ -2097,6 +2165,7 @@ static int render(Scene *sc, const gxy_camera &cam, const gxy_lighting &lt, floa
             g.enqueued = (int64_t)c.enqueued;
             g.segments = (int64_t)c.segments;
             g.samples = (int64_t)c.samples;
+            g.samples_skipped = (int64_t)c.skipped;
             g.nodes = (int64_t)c.nodes;
             g.tri_tests = (int64_t)c.tri_tests;
             g.sph_tests = (int64_t)c.sph_tests;
@@ -2400,6 +2469,7 @@ int gxy_gpu_query_counters(gxy_scene scene, gxy_counters *out) {
     out->nodes = (int64_t)c.nodes;
     out->prim_tests = (int64_t)(c.tri_tests + c.sph_tests);
     out->overflow = c.overflow;
+    out->samples_skipped = (int64_t)c.skipped;
     return GXY_OK;
 }
 
@@ -2456,6 +2526,15 @@ int gxy_gpu_set_tuning(int knob, int value) {
         g_tune_march_steps = value;
         return GXY_OK;
     }
+    if (knob == GXY_TUNE_SKIP_CLEAR) {
+        g_tune_skip_clear = value ? 1 : 0;
+        return GXY_OK;
+    }
+    if (knob == GXY_TUNE_SKIP_MODE) {
+        if (value < 0 || value > 7) return set_error(GXY_ERR_INVALID, "skip mode must be 0-7");
+        g_tune_skip_mode = value;
+        return GXY_OK;
+    }
     return set_error(GXY_ERR_INVALID, "unknown tuning knob");
 }
 
@@ -2470,6 +2549,8 @@ int gxy_gpu_get_tuning(int knob, int *value) {
     else if (knob == GXY_TUNE_TRAV_STEPS) *value = g_tune_trav_steps;
     else if (knob == GXY_TUNE_CAMERA_PACKET) *value = g_tune_cam_packet;
     else if (knob == GXY_TUNE_MARCH_STEPS) *value = g_tune_march_steps;
+    else if (knob == GXY_TUNE_SKIP_CLEAR) *value = g_tune_skip_clear;
+    else if (knob == GXY_TUNE_SKIP_MODE) *value = g_tune_skip_mode;
     else return set_error(GXY_ERR_INVALID, "unknown tuning knob");
     return GXY_OK;
 }
@@ -2757,11 +2838,11 @@ static int batch_enqueue(Batch *b, const DevScene &Su, bool uniform, const Frame
                 if (mb3) {
                     if (lines) k_cam_query<true, 4, true><<<query_grid(), kThreads, 0, st>>>(Su, a);
                     else k_cam_query<true, 4, false><<<query_grid(), kThreads, 0, st>>>(Su, a);
-                    k_prim_march<true, 3><<<march_grid(3), kThreads, 0, st>>>(Su, a);
+                    launch_prim_march<true, 3>(march_grid(3), st, Su, a);
                 } else {
                     if (lines) k_cam_query<true, 2, true><<<march_grid(2), kThreads, 0, st>>>(Su, a);
                     else k_cam_query<true, 2, false><<<march_grid(2), kThreads, 0, st>>>(Su, a);
-                    k_prim_march<true, 2><<<march_grid(2), kThreads, 0, st>>>(Su, a);
+                    launch_prim_march<true, 2>(march_grid(2), st, Su, a);
                 }
             } else {
                 CK(cudaEventRecord(b->fork[g], st));
@@ -2772,11 +2853,11 @@ static int batch_enqueue(Batch *b, const DevScene &Su, bool uniform, const Frame
                 if (mb3) {
                     if (lines) k_sec_query<true, 4, true><<<query_grid(), kThreads, 0, st>>>(Su, a);
                     else k_sec_query<true, 4, false><<<query_grid(), kThreads, 0, st>>>(Su, a);
-                    k_sec_march<true, 4><<<query_grid(), kThreads, 0, st>>>(Su, a);
+                    launch_sec_march<true, 4>(query_grid(), st, Su, a);
                 } else {
                     if (lines) k_sec_query<true, 2, true><<<march_grid(2), kThreads, 0, st>>>(Su, a);
                     else k_sec_query<true, 2, false><<<march_grid(2), kThreads, 0, st>>>(Su, a);
-                    k_sec_march<true, 2><<<march_grid(2), kThreads, 0, st>>>(Su, a);
+                    launch_sec_march<true, 2>(march_grid(2), st, Su, a);
                 }
                 CK(cudaStreamWaitEvent(st, b->join[g], 0));
             }
@@ -2819,8 +2900,8 @@ static int batch_enqueue(Batch *b, const DevScene &Su, bool uniform, const Frame
             else GXY_GEN_LAUNCH(2);
 #undef GXY_GEN_LAUNCH
             if (a.split) {
-                if (g_tune_minb == 3) k_sec_march<true, 4><<<query_grid(), kThreads, 0, st>>>(Su, a);
-                else k_sec_march<true, 2><<<march_grid(2), kThreads, 0, st>>>(Su, a);
+                if (g_tune_minb == 3) launch_sec_march<true, 4>(query_grid(), st, Su, a);
+                else launch_sec_march<true, 2>(march_grid(2), st, Su, a);
             }
             CK(cudaGetLastError());
         }
@@ -2956,6 +3037,7 @@ int gxy_gpu_batch_submit(gxy_batch batch, const gxy_job *jobs, int n_jobs, int f
     A.n_jobs = n_jobs;
     A.trav_steps = g_tune_trav_steps;
     A.march_steps = g_tune_march_steps;
+    A.skip_mode = g_tune_skip_mode;
     A.total_pix = pix;
     A.job0 = b->h_jobs[0];
     for (int k = 0; k < NQ; k++) A.qcap[k] = (unsigned)b->qcap[k];
@@ -3064,6 +3146,7 @@ int gxy_gpu_batch_counters(gxy_batch batch, gxy_counters *out) {
     out->nodes = (int64_t)c.nodes;
     out->prim_tests = (int64_t)(c.tri_tests + c.sph_tests);
     out->overflow = c.overflow;
+    out->samples_skipped = (int64_t)c.skipped;
     return GXY_OK;
 }
 

@@ -34,6 +34,7 @@ struct TraceOut {
 
 struct RayStats {
     unsigned samples = 0, nodes = 0, tris = 0, sphs = 0;
+    unsigned skipped = 0;            // march positions whose sample was never read (clear bricks)
     int ovf = 0;
 };
 
@@ -506,8 +507,17 @@ struct SecMarch {
     float tEntry, tExitVolume, tTimeout, tTerm, tThis, tLast, sLast;
     float cr, cg, cb, ca;
     bool surface, opaque, done;
+    bool bclear;                     // the brick `bid` is clear
+    bool prev_clear;                 // the previous position lay in a clear brick
+    bool lazy;                       // sLast not read yet (its interval composited nothing)
+    int bid;
     CellCache cc;
 };
+
+// Sample position of march distance t; one expression at every use (device
+// code is built without multiply-add contraction), so a sample read late
+// (SecMarch::lazy) equals the one its own step would have read.
+__device__ __forceinline__ V3 march_point(const SecMarch &M, float t) { return M.org + t * M.dir; }
 
 __device__ __forceinline__ void sec_march_init(const DevScene &S, const TraceIn &R, float t_term, bool surface,
                                                SecMarch &M) {
@@ -523,47 +533,185 @@ __device__ __forceinline__ void sec_march_init(const DevScene &S, const TraceIn 
     M.tThis = M.tEntry;
     M.sLast = 0.0f;
     M.cc.ix = -1; M.cc.iy = -1; M.cc.iz = -1;
+    M.bid = -1;
+    M.bclear = false;
+    M.prev_clear = false;
+    M.lazy = false;
     M.done = !(M.tThis <= M.tTerm && !M.opaque);
 }
 
-// Up to `steps` iterations of the march loop (TraceRays.ispc:470-556 for a
-// shadow/AO ray: compositing `color *= 1 - (dt/step) * clamp(alpha/rate)`).
-__device__ __forceinline__ void sec_march_steps(const DevScene &S, const DevTF &tf, SecMarch &M, int steps,
-                                                RayStats &st) {
+// Up to `steps` iterations of the march loop (TraceRays.ispc:470-556), as a
+// resumable state.  PRIMARY composites front to back with the primary-ray
+// weight `color += (1 - color.a) * clamp(alpha/rate) * [rgb, 1]`; otherwise
+// the shadow/AO attenuation `color *= 1 - (dt/step) * clamp(alpha/rate)`.
+//
+// Empty-space skipping with unchanged results: an interval between two
+// positions that both lie in clear bricks has zero opacity (tf_clear_below),
+// so its compositing is a no-op and neither sample is needed for it.  The
+// step then reads no voxels; the position still counts as a sample and the
+// distance sequence (tThis, tLast, tTerm) advances exactly as Galaxy's.  A
+// sample skipped this way is read later, from the same position, only if
+// the next interval does composite.
+// Distances t >= t0 along the ray over which every sample position lies in
+// the brick of g, as vol_pos computes positions: the ray's span inside the
+// brick's box shrunk by m = 1/64 voxel per side.  Per axis, to first order,
+// the computed grid coordinate of org + t*dir differs from the exact one by
+// at most u (|inv| (3|t d| + 2|o| + |vo|) + |g|), and the exact coordinate at
+// a computed slab distance (B - g0) * rcp(d * inv) from the slab B by at most
+// u (2 |inv| (|o| + |vo|) + 4 |inv| |t d|), u = 2^-24.  Their sum stays below
+// u K with K = 7 |inv| (T |d| + |o| + |vo|) + 2 (hi + 1) (T the largest |t|,
+// hi the box's upper grid coordinate, which also covers the rounding of the
+// shrunk bounds); K < 2^17 keeps it under m / 2.  False when that bound
+// fails on some axis or the span is empty.  A zero direction component
+// leaves its coordinate exactly constant (o + t*0 == o).
+__device__ __forceinline__ bool brick_axis(float o, float d, float vo, float inv, int b, float t0, float &lo_t,
+                                           float &hi_t) {
+    constexpr float m = 1.0f / 64.0f;
+    if (d == 0.0f) {
+        lo_t = -INFINITY;
+        hi_t = INFINITY;
+        return true;
+    }
+    const float lo = (float)(kBrick * b) + m, hi = (float)(kBrick * b + kBrick) - m;
+    const float g0 = (o - vo) * inv, dg = d * inv;
+    if (dg == 0.0f) return false;
+    const float r = __frcp_rn(dg);
+    const float ta = (lo - g0) * r, tb = (hi - g0) * r;
+    lo_t = fminf(ta, tb);
+    hi_t = fmaxf(ta, tb);
+    const float T = fmaxf(fabsf(t0), fabsf(hi_t));
+    return 7.0f * fabsf(inv) * (T * fabsf(d) + fabsf(o) + fabsf(vo)) + 2.0f * (hi + 1.0f) < 131072.0f;
+}
+
+__device__ __forceinline__ bool brick_span(const DevVolume &v, V3 org, V3 dir, const VolPos &g, float t0,
+                                           float &t_in, float &t_out) {
+    float lx, hx, ly, hy, lz, hz;
+    if (!brick_axis(org.x, dir.x, v.ox, v.ix, g.ix >> 2, t0, lx, hx)) return false;
+    if (!brick_axis(org.y, dir.y, v.oy, v.iy, g.iy >> 2, t0, ly, hy)) return false;
+    if (!brick_axis(org.z, dir.z, v.oz, v.iz, g.iz >> 2, t0, lz, hz)) return false;
+    t_in = fmaxf(fmaxf(lx, ly), lz);
+    t_out = fminf(fminf(hx, hy), hz);
+    return t_in <= t_out;
+}
+
+// Positions one fast run may pass over (a brick holds at most about
+// 4 sqrt(3) * sampling_rate of them; the cap only bounds the loop).
+constexpr int kMaxRun = 64;
+
+// Composite the interval ending at tThis whose sample value is sv.
+template <bool PRIMARY>
+__device__ __forceinline__ void march_composite(const DevScene &S, const DevTF &tf, SecMarch &M, float sv,
+                                                float tThis) {
+    V3 sc;
+    float so = tf_lookup(tf, sv, PRIMARY, sc);
+    if (so > 0.0f) {
+        float wo = S.rate_pow2 ? so * S.inv_rate : so / S.rate;
+        if (wo > 1.0f) wo = 1.0f;
+        if (wo < 0.0f) wo = 0.0f;
+        if (PRIMARY) {
+            float f = 1.0f - M.ca;
+            M.cr = M.cr + f * (wo * sc.x);
+            M.cg = M.cg + f * (wo * sc.y);
+            M.cb = M.cb + f * (wo * sc.z);
+            M.ca = M.ca + f * wo;
+        } else {
+            float w = ((tThis - M.tLast) / S.step) * wo;
+            float f = 1.0f - w;
+            M.cr = M.cr * f;
+            M.cg = M.cg * f;
+            M.cb = M.cb * f;
+            M.ca = M.ca * f;
+        }
+        // only a composited interval changes the colour, so only here can
+        // the ray become opaque (it was not before)
+        M.opaque = (fmin_(fmin_(M.cr, M.cg), M.cb) >= 1.0f || M.ca > S.opaque_alpha);
+        if (M.opaque) M.tTerm = tThis;
+    }
+}
+
+// Next march distance after tThis (TraceRays.ispc:548-553).
+__device__ __forceinline__ float march_next(float t, float tEntry, float epsilon, float step, float tTerm) {
+    return (t == tEntry) ? (tEntry + epsilon) : (((t + step) > tTerm) && (t < tTerm)) ? tTerm : t + step;
+}
+
+// SKIP: the scene carries clear-brick flags and this pass uses them (the
+// variant without them keeps the smaller march state).  runs: fast runs.
+template <bool PRIMARY, bool SKIP>
+__device__ __forceinline__ void march_steps(const DevScene &S, const DevTF &tf, SecMarch &M, int steps, int runs,
+                                            RayStats &st) {
     const DevVolume &vv = S.vol[0];
-    const float step = S.step, epsilon = S.march_eps, oa = S.opaque_alpha;
+    const float step = S.step, epsilon = S.march_eps;
+    if (!SKIP) {
+        for (int it = 0; it < steps && !M.done; it++) {
+            float tThis = M.tThis;
+            float sThis = vol_sample_at(vv, vol_pos(vv, march_point(M, tThis)), M.cc);
+            st.samples++;
+            if (tThis > M.tEntry && M.tLast >= epsilon && vv.volume_render)
+                march_composite<PRIMARY>(S, tf, M, (M.sLast + sThis) / 2.0f, tThis);
+            M.sLast = sThis;
+            M.tLast = tThis;
+            M.tThis = march_next(tThis, M.tEntry, epsilon, step, M.tTerm);
+            M.done = !(M.tThis <= M.tTerm && !M.opaque);
+        }
+        return;
+    }
     for (int it = 0; it < steps && !M.done; it++) {
         float tThis = M.tThis;
-        V3 coord = M.org + tThis * M.dir;
-        float sThis = vol_sample_cached(vv, coord, M.cc);
+        VolPos g = vol_pos(vv, march_point(M, tThis));
+        int bid = brick_of(vv, g);
+        if (bid != M.bid) {
+            M.bid = bid;
+            M.bclear = __ldg(vv.clear + bid) != 0;
+        }
         st.samples++;
-        if (tThis > M.tEntry && M.tLast >= epsilon) {
-            if (vv.volume_render) {
-                float sv = (M.sLast + sThis) / 2.0f;
-                V3 unused;
-                float so = tf_lookup(tf, sv, false, unused);
-                if (so > 0.0f) {
-                    float wo = S.rate_pow2 ? so * S.inv_rate : so / S.rate;
-                    if (wo > 1.0f) wo = 1.0f;
-                    if (wo < 0.0f) wo = 0.0f;
-                    float w = ((tThis - M.tLast) / step) * wo;
-                    float f = 1.0f - w;
-                    M.cr = M.cr * f;
-                    M.cg = M.cg * f;
-                    M.cb = M.cb * f;
-                    M.ca = M.ca * f;
-                }
+        if (tThis > M.tEntry && M.tLast >= epsilon && vv.volume_render && !(M.bclear && M.prev_clear)) {
+            if (M.lazy) {
+                M.sLast = vol_sample_at(vv, vol_pos(vv, march_point(M, M.tLast)), M.cc);
+                st.skipped--;
+            }
+            float sThis = vol_sample_at(vv, g, M.cc);
+            march_composite<PRIMARY>(S, tf, M, (M.sLast + sThis) / 2.0f, tThis);
+            M.sLast = sThis;
+            M.lazy = false;
+        } else {
+            M.lazy = true;
+            st.skipped++;
+        }
+        M.prev_clear = M.bclear;
+        M.tLast = tThis;
+        M.tThis = march_next(tThis, M.tEntry, epsilon, step, M.tTerm);
+        M.done = !(M.tThis <= M.tTerm && !M.opaque);
+        // Fast run through the rest of a clear brick: the positions that
+        // provably stay in it (brick_span) have clear intervals on both
+        // sides, so only the distance sequence advances.  The colour, and
+        // with it `opaque` (false here), does not change.
+        float t_in, t_out;
+        if (runs && !M.done && M.bclear && brick_span(vv, M.org, M.dir, g, tThis, t_in, t_out) &&
+            M.tThis >= t_in) {
+            float t = M.tThis, tl = M.tLast;
+            const float tTerm = M.tTerm, tEntry = M.tEntry;
+            int k = 0;
+            while (k < kMaxRun && t <= t_out && t <= tTerm) {   // t <= tTerm: not done (never opaque here)
+                tl = t;
+                t = march_next(t, tEntry, epsilon, step, tTerm);
+                k++;
+            }
+            if (k) {
+                M.tThis = t;
+                M.tLast = tl;
+                M.lazy = true;
+                M.done = !(t <= tTerm);
+                st.samples += k;
+                st.skipped += k;
             }
         }
-        M.sLast = sThis;
-        M.opaque = (fmin_(fmin_(M.cr, M.cg), M.cb) >= 1.0f || M.ca > oa);
-        if (M.opaque) M.tTerm = tThis;
-        M.tLast = tThis;
-        M.tThis = (tThis == M.tEntry) ? (M.tEntry + epsilon)
-                  : (((tThis + step) > M.tTerm) && (tThis < M.tTerm)) ? M.tTerm
-                                                                      : tThis + step;
-        M.done = !(M.tThis <= M.tTerm && !M.opaque);
     }
+}
+
+template <bool SKIP>
+__device__ __forceinline__ void sec_march_steps(const DevScene &S, const DevTF &tf, SecMarch &M, int steps,
+                                                int runs, RayStats &st) {
+    march_steps<false, SKIP>(S, tf, M, steps, runs, st);
 }
 
 // Termination flags of a finished march (TraceRays.ispc:574-617, shadow/AO).
@@ -613,42 +761,11 @@ __device__ __forceinline__ void cam_slices(const DevScene &S, const DevTF *tfs, 
 }
 
 // Compositing march of a primary ray (TraceRays.ispc:470-556 with the
-// primary-ray weight `color += (1 - color.a) * clamp(alpha/rate) * [rgb, 1]`).
+// primary-ray weight).
+template <bool SKIP>
 __device__ __forceinline__ void prim_march_steps(const DevScene &S, const DevTF &tf, SecMarch &M, int steps,
-                                                 RayStats &st) {
-    const DevVolume &vv = S.vol[0];
-    const float step = S.step, epsilon = S.march_eps, oa = S.opaque_alpha;
-    for (int it = 0; it < steps && !M.done; it++) {
-        float tThis = M.tThis;
-        V3 coord = M.org + tThis * M.dir;
-        float sThis = vol_sample_cached(vv, coord, M.cc);
-        st.samples++;
-        if (tThis > M.tEntry && M.tLast >= epsilon) {
-            if (vv.volume_render) {
-                float sv = (M.sLast + sThis) / 2.0f;
-                V3 sc;
-                float so = tf_lookup(tf, sv, true, sc);
-                if (so > 0.0f) {
-                    float wo = S.rate_pow2 ? so * S.inv_rate : so / S.rate;
-                    if (wo > 1.0f) wo = 1.0f;
-                    if (wo < 0.0f) wo = 0.0f;
-                    float f = 1.0f - M.ca;
-                    M.cr = M.cr + f * (wo * sc.x);
-                    M.cg = M.cg + f * (wo * sc.y);
-                    M.cb = M.cb + f * (wo * sc.z);
-                    M.ca = M.ca + f * wo;
-                }
-            }
-        }
-        M.sLast = sThis;
-        M.opaque = (fmin_(fmin_(M.cr, M.cg), M.cb) >= 1.0f || M.ca > oa);
-        if (M.opaque) M.tTerm = tThis;
-        M.tLast = tThis;
-        M.tThis = (tThis == M.tEntry) ? (M.tEntry + epsilon)
-                  : (((tThis + step) > M.tTerm) && (tThis < M.tTerm)) ? M.tTerm
-                                                                      : tThis + step;
-        M.done = !(M.tThis <= M.tTerm && !M.opaque);
-    }
+                                                 int runs, RayStats &st) {
+    march_steps<true, SKIP>(S, tf, M, steps, runs, st);
 }
 
 // Termination flags of a finished primary march: a surface found with

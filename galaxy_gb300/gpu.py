@@ -114,6 +114,8 @@ TUNE_LEAF_MAX = 6
 TUNE_TRAV_STEPS = 7
 TUNE_MARCH_STEPS = 8
 TUNE_CAMERA_PACKET = 9
+TUNE_SKIP_CLEAR = 10
+TUNE_SKIP_MODE = 11
 
 
 def set_tuning(knob, value):

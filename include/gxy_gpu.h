@@ -216,11 +216,14 @@ typedef struct gxy_counters {
     int64_t dropped;          /* DROP_ON_FLOOR                        */
     int64_t kept;             /* KEEP_HERE re-traces                  */
     int64_t bounces;          /* queue generations processed          */
-    int64_t samples;          /* volume samples taken                 */
+    int64_t samples;          /* volume samples taken (march positions) */
     int64_t nodes;            /* BVH8 node lines visited              */
     int64_t prim_tests;       /* primitive intersection tests         */
     int32_t overflow;         /* non-zero if a queue overflowed       */
     int32_t pad;
+    int64_t samples_skipped;  /* of `samples`: positions whose voxels were
+                                 never read (both ends of their interval in
+                                 bricks below the zero-opacity threshold) */
 } gxy_counters;
 
 typedef struct gxy_scene_s *gxy_scene;
@@ -278,6 +281,7 @@ typedef struct gxy_generation_stats {
     int64_t rays_in;       /* queue records read (0 for the camera generation) */
     int64_t enqueued;      /* queue records written                         */
     int64_t segments, samples, nodes, tri_tests, sph_tests, terminated;
+    int64_t samples_skipped;
 } gxy_generation_stats;
 int gxy_gpu_set_profiling(gxy_scene scene, int on);
 
@@ -304,6 +308,20 @@ int gxy_gpu_set_profiling(gxy_scene scene, int on);
 #define GXY_TUNE_CAMERA_PACKET   9   /* 1 (default): camera rays of a frame queried by
                                         warps over 8x4 pixel tiles with one shared BVH8
                                         traversal; 0: per-lane refill traversal */
+#define GXY_TUNE_SKIP_CLEAR     10   /* read at scene commit.  1 (default): flag the volume
+                                        bricks whose samples all lie below the transfer
+                                        function's zero-opacity threshold; the march
+                                        passes then read no voxels for intervals between
+                                        two such positions (same images and counters);
+                                        0: no flags, every sample read */
+#define GXY_TUNE_SKIP_MODE      11   /* clear-brick skipping per march pass, bits:
+                                        1 (default): the camera-ray march also advances
+                                        through the rest of a flagged brick in one run of
+                                        distance updates (it always skips per position);
+                                        2: the shadow/AO march skips per position;
+                                        4: with 2, the shadow/AO march runs likewise
+                                        (incoherent rays: a warp then waits for its
+                                        longest run) */
 int gxy_gpu_set_tuning(int knob, int value);
 int gxy_gpu_get_tuning(int knob, int *value);
 int gxy_gpu_query_generations(gxy_scene scene, gxy_generation_stats *out, int max, int32_t *n);
