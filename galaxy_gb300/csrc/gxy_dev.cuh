@@ -52,7 +52,14 @@ struct DevVolume {
     // transfer function's zero-opacity threshold (tf_clear_below), so an
     // interval between two such samples composites nothing.
     const unsigned char *clear;
+    // Per superbrick of kSuper^3 bricks (32^3 cells): 1 when every brick
+    // within one brick of it is clear, so a position whose computed cell is
+    // within a brick (4 voxels) of the superbrick lies in a clear brick.
+    const unsigned char *sclear;
+    int nsx, nsy, nsz;
 };
+constexpr int kSuper = 8;            // bricks per superbrick side
+constexpr int kSuperCells = kSuper * kBrick;
 
 struct DevPartition {
     float lo[3], hi[3];
@@ -312,6 +319,11 @@ __device__ __forceinline__ VolPos vol_pos(const DevVolume &v, V3 p) {
 // Linear index of the brick holding the cell of g.
 __device__ __forceinline__ int brick_of(const DevVolume &v, const VolPos &g) {
     return ((g.iz >> 2) * v.nby + (g.iy >> 2)) * v.nbx + (g.ix >> 2);
+}
+
+// Linear index of the superbrick holding the cell of g.
+__device__ __forceinline__ int super_of(const DevVolume &v, const VolPos &g) {
+    return ((g.iz >> 5) * v.nsy + (g.iy >> 5)) * v.nsx + (g.ix >> 5);
 }
 
 __device__ __forceinline__ float vol_sample_at(const DevVolume &v, const VolPos &g, CellCache &cc) {

@@ -424,6 +424,24 @@ __global__ void k_brick_clear(const float *bricked, int64_t n_bricks, float belo
 // and opac[i + 1].  With opac[0 .. z-1] zero, every v below
 // r0 + (z - 1) / k interpolates two zeros; the bound is pulled in by 1e-4
 // relative to cover the rounding of (v - r0) * k.  -inf when opac[0] > 0.
+// Per superbrick: the AND of the clear flags of its bricks and of the bricks
+// one brick around it (clamped to the grid).  One thread per superbrick.
+__global__ void k_superbrick_clear(const unsigned char *clear, int nbx, int nby, int nbz, int nsx, int nsy, int nsz,
+                                   unsigned char *sclear) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nsx * nsy * nsz) return;
+    const int sx = s % nsx, sy = (s / nsx) % nsy, sz = s / (nsx * nsy);
+    unsigned char all = 1;
+    for (int bz = max(sz * kSuper - 1, 0); bz <= min(sz * kSuper + kSuper, nbz - 1) && all; bz++)
+        for (int by = max(sy * kSuper - 1, 0); by <= min(sy * kSuper + kSuper, nby - 1) && all; by++)
+            for (int bx = max(sx * kSuper - 1, 0); bx <= min(sx * kSuper + kSuper, nbx - 1); bx++)
+                if (!clear[((int64_t)bz * nby + by) * nbx + bx]) {
+                    all = 0;
+                    break;
+                }
+    sclear[s] = all;
+}
+
 static float tf_clear_below(const DevTF &t) {
     int z = 0;
     while (z < GXY_TF_SIZE && t.opac[z] == 0.0f) z++;
@@ -515,6 +533,17 @@ static int commit(const gxy_scene_desc *d, Scene *sc) {
             CK(cudaGetLastError());
             CK(cudaDeviceSynchronize());
             V.clear = clear;
+            V.nsx = (V.nbx + kSuper - 1) / kSuper;
+            V.nsy = (V.nby + kSuper - 1) / kSuper;
+            V.nsz = (nbz + kSuper - 1) / kSuper;
+            const int ns = V.nsx * V.nsy * V.nsz;
+            unsigned char *sclear;
+            if ((rc = arena().alloc((void **)&sclear, (size_t)ns))) return rc;
+            sc->owned.push_back(sclear);
+            k_superbrick_clear<<<(ns + 127) / 128, 128>>>(clear, V.nbx, V.nby, nbz, V.nsx, V.nsy, V.nsz, sclear);
+            CK(cudaGetLastError());
+            CK(cudaDeviceSynchronize());
+            V.sclear = sclear;
         }
         V.n_slices = v.n_slices;
         for (int k = 0; k < v.n_slices; k++)
@@ -1581,7 +1610,7 @@ __global__ void __launch_bounds__(kThreads, MINB) k_cam_packet(DevScene S, Frame
 // March pass of split primary tracing with per-lane refill: composite the
 // volume up to the query pass's stop distance, then shade (ambient, AO spawn,
 // diffuse, shadow spawn), classify, route and accumulate as primary_ray does.
-template <bool BATCH, int MINB, bool SKIP>
+template <bool BATCH, int MINB, int SKIP>
 __global__ void __launch_bounds__(kThreads, MINB) k_prim_march(DevScene S, FrameArgs A) {
     __shared__ DevTF tfs[kMaxVol];
     load_tfs(S, tfs);
@@ -1651,7 +1680,7 @@ __global__ void __launch_bounds__(kThreads, MINB) k_prim_march(DevScene S, Frame
 // lanes keep marching, so warps stay full across rays of different march
 // lengths.  Each record carries the query pass's stop distance and surface
 // flag.  USCENE / batch as for the other frame kernels (uniform scene only).
-template <bool BATCH, int MINB, bool SKIP>
+template <bool BATCH, int MINB, int SKIP>
 __global__ void __launch_bounds__(kThreads, MINB) k_sec_march(DevScene S, FrameArgs A) {
     __shared__ DevTF tfs[kMaxVol];
     load_tfs(S, tfs);
@@ -1686,7 +1715,7 @@ __global__ void __launch_bounds__(kThreads, MINB) k_sec_march(DevScene S, FrameA
             }
         }
         if (!__any_sync(0xffffffffu, have)) break;
-        if (have && !M.done) sec_march_steps<SKIP>(S, tfs[0], M, max(A.march_steps, 1), A.skip_mode & 4, st);
+        if (have && !M.done) sec_march_steps<SKIP>(S, tfs[0], M, max(A.march_steps, 1), 1, st);
         bool fin = have && M.done;
         int dest = GXY_DROP_ON_FLOOR;
         TraceOut T;
@@ -1928,23 +1957,25 @@ static unsigned grid_for(int64_t n) {
 static unsigned march_grid(int minb) {
     int sms = 152, per = 1;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, g_device);
-    if (minb == 3) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_sec_march<false, 3, false>, kThreads, 0);
-    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_sec_march<false, 2, false>, kThreads, 0);
+    if (minb == 3) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_sec_march<false, 3, 0>, kThreads, 0);
+    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_sec_march<false, 2, 0>, kThreads, 0);
     return (unsigned)(sms * (per < 1 ? 1 : per));
 }
 
-// The march passes with or without clear-brick skipping: the camera-ray
-// march skips whenever the scene has the flags, the shadow/AO march when
-// GXY_TUNE_SKIP_MODE bit 1 also asks for it.
+// The march passes with or without clear-brick skipping (march_steps'
+// SKIP levels): the camera-ray march skips per position whenever the scene
+// has the flags; the shadow/AO march takes the lean superbrick jumps with
+// GXY_TUNE_SKIP_MODE bit 1 and per-position skipping with bit 2.
 template <bool BATCH, int MINB>
 static void launch_prim_march(unsigned grid, cudaStream_t st, const DevScene &S, const FrameArgs &A) {
-    if (S.vol[0].clear) k_prim_march<BATCH, MINB, true><<<grid, kThreads, 0, st>>>(S, A);
-    else k_prim_march<BATCH, MINB, false><<<grid, kThreads, 0, st>>>(S, A);
+    if (S.vol[0].clear) k_prim_march<BATCH, MINB, 2><<<grid, kThreads, 0, st>>>(S, A);
+    else k_prim_march<BATCH, MINB, 0><<<grid, kThreads, 0, st>>>(S, A);
 }
 template <bool BATCH, int MINB>
 static void launch_sec_march(unsigned grid, cudaStream_t st, const DevScene &S, const FrameArgs &A) {
-    if (S.vol[0].clear && (A.skip_mode & 2)) k_sec_march<BATCH, MINB, true><<<grid, kThreads, 0, st>>>(S, A);
-    else k_sec_march<BATCH, MINB, false><<<grid, kThreads, 0, st>>>(S, A);
+    if (S.vol[0].clear && (A.skip_mode & 4)) k_sec_march<BATCH, MINB, 2><<<grid, kThreads, 0, st>>>(S, A);
+    else if (S.vol[0].clear && (A.skip_mode & 2)) k_sec_march<BATCH, MINB, 1><<<grid, kThreads, 0, st>>>(S, A);
+    else k_sec_march<BATCH, MINB, 0><<<grid, kThreads, 0, st>>>(S, A);
 }
 
 // The refill query passes and the shadow/AO march run at 4 resident blocks

@@ -511,6 +511,8 @@ struct SecMarch {
     bool prev_clear;                 // the previous position lay in a clear brick
     bool lazy;                       // sLast not read yet (its interval composited nothing)
     int bid;
+    int sbid;                        // superbrick whose clear run was last looked up
+    float tRun;                      // positions t < tRun lie in a run of clear superbricks
     CellCache cc;
 };
 
@@ -534,6 +536,8 @@ __device__ __forceinline__ void sec_march_init(const DevScene &S, const TraceIn 
     M.sLast = 0.0f;
     M.cc.ix = -1; M.cc.iy = -1; M.cc.iz = -1;
     M.bid = -1;
+    M.sbid = -1;
+    M.tRun = -INFINITY;
     M.bclear = false;
     M.prev_clear = false;
     M.lazy = false;
@@ -594,9 +598,73 @@ __device__ __forceinline__ bool brick_span(const DevVolume &v, V3 org, V3 dir, c
     return t_in <= t_out;
 }
 
+// End of the run of clear superbricks that holds the cell of g at distance
+// t0: the distance at which the ray enters a superbrick that is not clear,
+// +inf when it enters none before tEnd.  A 3-D DDA over the superbrick grid
+// along G(t) = (org - origin) * inv + t * dir * inv; a position the march
+// computes at t < the result lies, up to rounding far below a voxel (K <
+// 2^20 per axis: under 1/16 voxel), in or next to a visited superbrick, so
+// in a brick their dilated flags cover.  Positions outside the grid clamp
+// to its edge cells, so an axis that leaves the grid stays on its edge
+// superbrick.  At most 64 superbricks per call.
+// One axis of the DDA: the distance of the next superbrick boundary and
+// the distance between boundaries; false when the rounding bound fails.
+__device__ __forceinline__ bool dda_axis(float o, float d, float vo, float inv, int c, float T, int &sgn, float &tn,
+                                         float &dt) {
+    if (!(fabsf(inv) * (T * fabsf(d) + fabsf(o) + fabsf(vo)) < 1048576.0f)) return false;
+    const float g0 = (o - vo) * inv, dg = d * inv;
+    if (dg > 0.0f) {
+        sgn = 1;
+        tn = ((float)((c + 1) * kSuperCells) - g0) / dg;
+        dt = (float)kSuperCells / dg;
+    } else if (dg < 0.0f) {
+        sgn = -1;
+        tn = ((float)(c * kSuperCells) - g0) / dg;
+        dt = -(float)kSuperCells / dg;
+    } else {
+        sgn = 0;
+        tn = INFINITY;
+        dt = 0.0f;
+    }
+    return true;
+}
+
+// Step one axis of the DDA; an axis that leaves the grid stays on its edge
+// superbrick (positions outside the grid clamp to its edge cells).
+__device__ __forceinline__ void dda_step(int &c, int sgn, int n, float &tn, float dt) {
+    c += sgn;
+    tn += dt;
+    if (c < 0 || c >= n) {
+        c = c < 0 ? 0 : n - 1;
+        tn = INFINITY;
+    }
+}
+
+__device__ __forceinline__ float clear_run_end(const DevVolume &v, V3 org, V3 dir, const VolPos &g, float t0,
+                                               float tEnd) {
+    const float T = fmaxf(fabsf(t0), fabsf(tEnd));
+    int cx = g.ix >> 5, cy = g.iy >> 5, cz = g.iz >> 5, sx, sy, sz;
+    float tx, ty, tz, dx, dy, dz;
+    if (!dda_axis(org.x, dir.x, v.ox, v.ix, cx, T, sx, tx, dx) || !dda_axis(org.y, dir.y, v.oy, v.iy, cy, T, sy, ty, dy) ||
+        !dda_axis(org.z, dir.z, v.oz, v.iz, cz, T, sz, tz, dz))
+        return t0;
+    float t = fminf(fminf(tx, ty), tz);
+    for (int k = 0; k < 64; k++) {
+        if (!(t <= tEnd)) return INFINITY;
+        if (t == tx) dda_step(cx, sx, v.nsx, tx, dx);
+        else if (t == ty) dda_step(cy, sy, v.nsy, ty, dy);
+        else dda_step(cz, sz, v.nsz, tz, dz);
+        if (!__ldg(v.sclear + (cz * v.nsy + cy) * v.nsx + cx)) return t;
+        t = fminf(fminf(tx, ty), tz);
+    }
+    return t;
+}
+
 // Positions one fast run may pass over (a brick holds at most about
-// 4 sqrt(3) * sampling_rate of them; the cap only bounds the loop).
+// 4 sqrt(3) * sampling_rate of them; the cap only bounds the loop), and one
+// pass of a superbrick run.
 constexpr int kMaxRun = 64;
+constexpr int kMaxCount = 4096;
 
 // Composite the interval ending at tThis whose sample value is sv.
 template <bool PRIMARY>
@@ -634,14 +702,86 @@ __device__ __forceinline__ float march_next(float t, float tEntry, float epsilon
     return (t == tEntry) ? (tEntry + epsilon) : (((t + step) > tTerm) && (t < tTerm)) ? tTerm : t + step;
 }
 
-// SKIP: the scene carries clear-brick flags and this pass uses them (the
-// variant without them keeps the smaller march state).  runs: fast runs.
-template <bool PRIMARY, bool SKIP>
+// Pass over the positions t of the distance sequence with t < tr and
+// t <= tTerm, exactly as repeated march_next would, counting them (at most
+// cap); t becomes the first position not passed over, tl the last one
+// passed over.  Inside one binade [2^(e-1), 2^e) of positive floats, with
+// t away from tEntry, fl(t + step) = t + D ulps for a fixed D: the floats of
+// the binade are the integers of their bit patterns, t is on that grid, and
+// the rounding of t + step to it does not depend on t except on an exact
+// tie (step / ulp = n + 1/2, left to single steps).  So a chunk of positions
+// is an arithmetic progression in the bit pattern, taken while every
+// position stays below tr and every successor stays at or below tTerm (no
+// clamp) and at least one ulp below the binade's end (t + step then rounds
+// inside the binade).  Other positions take single march_next steps.
+__device__ __forceinline__ int advance_clear(float &t, float &tl, float tr, float tTerm, float tEntry, float epsilon,
+                                             float step, int cap) {
+    int k = 0;
+    while (k < cap && t < tr && t <= tTerm) {
+        const int tb = __float_as_int(t);
+        const int E = (tb >> 23) & 0xff;
+        if (t > 0.0f && t != tEntry && E >= 24 && E < 254) {
+            const int bend = (tb & 0x7f800000) + 0x00800000;
+            const float tn = t + step;
+            const int D = __float_as_int(tn) - tb;
+            const float r = step * __int_as_float((277 - E) << 23);   // step / ulp(t), exact
+            if (D >= 1 && __float_as_int(tn) < bend && r - floorf(r) != 0.5f) {
+                const int A = min(__float_as_int(tTerm), bend - 1) - tb;
+                const int B = tr < INFINITY ? __float_as_int(tr) - tb : 0x7fffffff;
+                int m = min(A / D, (B - 1) / D + 1);
+                m = min(m, cap - k);
+                if (m >= 1) {
+                    tl = __int_as_float(tb + (m - 1) * D);
+                    t = __int_as_float(tb + m * D);
+                    k += m;
+                    continue;
+                }
+            }
+        }
+        tl = t;
+        t = march_next(t, tEntry, epsilon, step, tTerm);
+        k++;
+    }
+    return k;
+}
+
+// Lean skipping: if the position at tp (already marched, or the first
+// position tEntry) lies in a clear superbrick, pass over the following
+// positions of the clear superbrick run ahead (their predecessors are all
+// clear), then read the sample of the last one passed over, so the plain
+// march resumes with a valid sLast.
+__device__ __forceinline__ void lean_run(const DevVolume &vv, SecMarch &M, float tp, float epsilon, float step,
+                                         RayStats &st) {
+    const VolPos g = vol_pos(vv, march_point(M, tp));
+    if (!__ldg(vv.sclear + super_of(vv, g))) return;
+    const float tr = clear_run_end(vv, M.org, M.dir, g, tp, M.tTerm);
+    float t = M.tThis, tl = M.tLast;
+    const int k = advance_clear(t, tl, tr, M.tTerm, M.tEntry, epsilon, step, kMaxCount);
+    if (k) {
+        M.tThis = t;
+        M.tLast = tl;
+        M.done = !(t <= M.tTerm);
+        st.samples += k;
+        st.skipped += k;
+        if (!M.done) {
+            M.sLast = vol_sample_at(vv, vol_pos(vv, march_point(M, tl)), M.cc);
+            st.skipped--;
+        }
+    }
+}
+
+// SKIP 0: every position sampled.  SKIP 1 (lean): as 0, plus, at the
+// first position and after each refill round, a jump over the run of clear
+// superbricks ahead (lean_run); no extra march state.  SKIP 2: per-position
+// clear-brick skipping with lazy samples, superbrick runs and (runs) brick
+// runs.  The scene must carry the clear flags for 1 and 2.
+template <bool PRIMARY, int SKIP>
 __device__ __forceinline__ void march_steps(const DevScene &S, const DevTF &tf, SecMarch &M, int steps, int runs,
                                             RayStats &st) {
     const DevVolume &vv = S.vol[0];
     const float step = S.step, epsilon = S.march_eps;
-    if (!SKIP) {
+    if (SKIP < 2) {
+        if (SKIP == 1 && M.tThis == M.tEntry) lean_run(vv, M, M.tEntry, epsilon, step, st);
         for (int it = 0; it < steps && !M.done; it++) {
             float tThis = M.tThis;
             float sThis = vol_sample_at(vv, vol_pos(vv, march_point(M, tThis)), M.cc);
@@ -653,9 +793,25 @@ __device__ __forceinline__ void march_steps(const DevScene &S, const DevTF &tf, 
             M.tThis = march_next(tThis, M.tEntry, epsilon, step, M.tTerm);
             M.done = !(M.tThis <= M.tTerm && !M.opaque);
         }
+        if (SKIP == 1 && !M.done) lean_run(vv, M, M.tLast, epsilon, step, st);
         return;
     }
     for (int it = 0; it < steps && !M.done; it++) {
+        if (M.tThis < M.tRun) {
+            // inside a run of clear superbricks whose previous position is
+            // clear too: only the distance sequence advances
+            float t = M.tThis, tl = M.tLast;
+            const float tTerm = M.tTerm;
+            const int k = advance_clear(t, tl, M.tRun, tTerm, M.tEntry, epsilon, step, kMaxCount);
+            M.tThis = t;
+            M.tLast = tl;
+            M.lazy = true;
+            M.prev_clear = true;
+            M.done = !(t <= tTerm);
+            st.samples += k;
+            st.skipped += k;
+            continue;
+        }
         float tThis = M.tThis;
         VolPos g = vol_pos(vv, march_point(M, tThis));
         int bid = brick_of(vv, g);
@@ -681,6 +837,18 @@ __device__ __forceinline__ void march_steps(const DevScene &S, const DevTF &tf, 
         M.tLast = tThis;
         M.tThis = march_next(tThis, M.tEntry, epsilon, step, M.tTerm);
         M.done = !(M.tThis <= M.tTerm && !M.opaque);
+        // A clear brick in a superbrick not looked up yet: find the run of
+        // clear superbricks ahead (the next iterations count through it).
+        if (M.bclear && !M.done) {
+            const int sb = super_of(vv, g);
+            if (sb != M.sbid) {
+                M.sbid = sb;
+                if (__ldg(vv.sclear + sb)) {
+                    M.tRun = clear_run_end(vv, M.org, M.dir, g, tThis, M.tTerm);
+                    if (M.tThis < M.tRun) continue;
+                }
+            }
+        }
         // Fast run through the rest of a clear brick: the positions that
         // provably stay in it (brick_span) have clear intervals on both
         // sides, so only the distance sequence advances.  The colour, and
@@ -689,13 +857,9 @@ __device__ __forceinline__ void march_steps(const DevScene &S, const DevTF &tf, 
         if (runs && !M.done && M.bclear && brick_span(vv, M.org, M.dir, g, tThis, t_in, t_out) &&
             M.tThis >= t_in) {
             float t = M.tThis, tl = M.tLast;
-            const float tTerm = M.tTerm, tEntry = M.tEntry;
-            int k = 0;
-            while (k < kMaxRun && t <= t_out && t <= tTerm) {   // t <= tTerm: not done (never opaque here)
-                tl = t;
-                t = march_next(t, tEntry, epsilon, step, tTerm);
-                k++;
-            }
+            const float tTerm = M.tTerm;
+            // positions t <= t_out: below the next float up from t_out
+            const int k = advance_clear(t, tl, nextafterf(t_out, INFINITY), tTerm, M.tEntry, epsilon, step, kMaxRun);
             if (k) {
                 M.tThis = t;
                 M.tLast = tl;
@@ -708,7 +872,7 @@ __device__ __forceinline__ void march_steps(const DevScene &S, const DevTF &tf, 
     }
 }
 
-template <bool SKIP>
+template <int SKIP>
 __device__ __forceinline__ void sec_march_steps(const DevScene &S, const DevTF &tf, SecMarch &M, int steps,
                                                 int runs, RayStats &st) {
     march_steps<false, SKIP>(S, tf, M, steps, runs, st);
@@ -762,7 +926,7 @@ __device__ __forceinline__ void cam_slices(const DevScene &S, const DevTF *tfs, 
 
 // Compositing march of a primary ray (TraceRays.ispc:470-556 with the
 // primary-ray weight).
-template <bool SKIP>
+template <int SKIP>
 __device__ __forceinline__ void prim_march_steps(const DevScene &S, const DevTF &tf, SecMarch &M, int steps,
                                                  int runs, RayStats &st) {
     march_steps<true, SKIP>(S, tf, M, steps, runs, st);

@@ -317,11 +317,14 @@ int gxy_gpu_set_profiling(gxy_scene scene, int on);
 #define GXY_TUNE_SKIP_MODE      11   /* clear-brick skipping per march pass, bits:
                                         1 (default): the camera-ray march also advances
                                         through the rest of a flagged brick in one run of
-                                        distance updates (it always skips per position);
-                                        2: the shadow/AO march skips per position;
-                                        4: with 2, the shadow/AO march runs likewise
-                                        (incoherent rays: a warp then waits for its
-                                        longest run) */
+                                        distance updates (it always skips per position
+                                        and jumps runs of clear 32^3 superbricks);
+                                        2: the shadow/AO march jumps runs of clear
+                                        superbricks at its first position and after each
+                                        refill round, sampling every other position;
+                                        4: the shadow/AO march skips as the camera-ray
+                                        march does (incoherent rays: a warp runs both
+                                        paths when its lanes differ) */
 int gxy_gpu_set_tuning(int knob, int value);
 int gxy_gpu_get_tuning(int knob, int *value);
 int gxy_gpu_query_generations(gxy_scene scene, gxy_generation_stats *out, int max, int32_t *n);

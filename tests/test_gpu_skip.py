@@ -36,8 +36,9 @@ def commit(gpu, vis, skip):
 
 
 def render_pair(gpu, cam, vis, level):
-    """Level 1: clear flags, both march passes skip one position per step;
-    level 2: flags and fast runs in both passes.  Against the scene without
+    """Level 1: clear flags, per-position skipping in the camera-ray march
+    and superbrick jumps in the shadow/AO march; level 2: per-position
+    skipping and brick runs in both passes.  Against the scene without
     flags."""
     L = S.resolve_lights(vis.lighting, cam)
     on, off = commit(gpu, vis, 1), commit(gpu, vis, 0)
@@ -161,5 +162,37 @@ def test_checkerboard_brick_boundaries(gpu, eye, block, level):
     a, b, ca, cb, L = render_pair(gpu, cam, vis, level)
     same_frames(a, b, ca, cb)
     assert ca["samples_skipped"] > 0.02 * ca["samples"]
+    ref, cnt = O.OracleScene(vis).render(cam, L, nthreads=8)
+    image_close(a, ref)
+
+
+@pytest.mark.parametrize("level", [1, 2])
+@pytest.mark.parametrize("eye", [(2.2, 1.6, 2.9), (0.5, 0.5, 2.5), (-1.3, 0.9, 0.2)])
+def test_superbrick_runs(gpu, eye, level):
+    """A 160^3 volume, clear except for a dense ball and a dense slab: most
+    rays cross runs of clear 32^3 superbricks (the DDA path) before, between
+    and after the dense parts, at oblique and axis-aligned angles, with
+    shadows and AO so both march passes run."""
+    n = 160
+    g = np.random.default_rng(11)
+    z, y, x = np.meshgrid(np.arange(n), np.arange(n), np.arange(n), indexing="ij")
+    ball = ((x - 80) ** 2 + (y - 70) ** 2 + (z - 90) ** 2) < 22 ** 2
+    slab = (x > 120) & (x < 131) & (y < 60)
+    f = np.where(ball | slab, 0.35 + 0.6 * g.random((n, n, n), dtype=np.float32),
+                 0.25 * g.random((n, n, n), dtype=np.float32)).astype(np.float32)
+    vol = S.Volume(f, origin=(0.0, 0.0, 0.0), deltas=(1.0 / (n - 1),) * 3)
+    vv = S.VolumeVis(vol, volume_rendering=True, colormap=scenes.COOLWARM,
+                     opacitymap=[(0.0, 0.0), (0.3, 0.0), (1.0, 0.4)])
+    parts = S.Particles(g.uniform(0.05, 0.95, size=(400, 3)).astype(np.float32), np.zeros(400, np.float32))
+    L = S.Lighting()
+    L.lights, L.types = [(-0.577, -0.577, -0.577)], [0]
+    L.shadows, L.n_ao, L.ao_radius, L.Ka, L.Kd = True, 2, 0.3, 0.5, 0.5
+    vis = S.Visualization([vv, S.ParticlesVis(parts, radius0=0.02, radius1=0.02)], L, partitions=(2, 1, 1),
+                          sampling_rate=2.0, opaque_alpha=0.99)
+    d = tuple(0.5 - e for e in eye)
+    cam = S.Camera(eye, d, (0, 1, 0), 40.0, 96, 96)
+    a, b, ca, cb, L = render_pair(gpu, cam, vis, level)
+    same_frames(a, b, ca, cb)
+    assert ca["samples_skipped"] > 0.5 * ca["samples"]
     ref, cnt = O.OracleScene(vis).render(cam, L, nthreads=8)
     image_close(a, ref)
