@@ -521,8 +521,7 @@ __device__ __forceinline__ void node_children(float4 n0, float4 n1, const uint4 
     const uint64_t Ax = f2dup(scx * idx), Bx = f2dup((n0.x - org.x) * idx);
     const uint64_t Ay = f2dup(scy * idy), By = f2dup((n0.y - org.y) * idy);
     const uint64_t Az = f2dup(scz * idz), Bz = f2dup((n0.z - org.z) * idz);
-    leafhits = 0;
-    n_inner = 0;
+    uint32_t hitm = 0;
 #pragma unroll
     for (int k = 0; k < 4; k++) {
         const uint32_t lx = W[k], ly = W[4 + k], lz = W[8 + k], hx = W[12 + k], hy = W[16 + k], hz = W[20 + k];
@@ -532,16 +531,25 @@ __device__ __forceinline__ void node_children(float4 n0, float4 n1, const uint4 
 #pragma unroll
         for (int h = 0; h < 2; h++) {
             const int i = 2 * k + h;
-            const uint32_t mb = (i < 4 ? meta_lo >> (8 * i) : meta_hi >> (8 * (i - 4))) & 0xffu;
             float tn = fmaxf(max3f(f2get(txa, h), f2get(tya, h), f2get(tza, h)), t0);
             float tf = fminf(min3f(f2get(txb, h), f2get(tyb, h), f2get(tzb, h)), tmax);
-            bool hit = mb != 0xffu && tn <= tf * 1.00000048f + 1e-30f;
-            bool inner = hit && ((imask >> i) & 1u);
-            key[i] = inner ? ((__float_as_uint(tn) & ~7u) | (uint32_t)i) : 0xffffffffu;
-            n_inner += inner ? 1 : 0;
-            if (hit && !((imask >> i) & 1u)) leafhits |= 1u << i;
+            if (tn <= tf * 1.00000048f + 1e-30f) hitm |= 1u << i;
+            key[i] = (__float_as_uint(tn) & ~7u) | (uint32_t)i;
         }
     }
+    // Empty slots carry meta 0xff; every filled slot's meta byte is below
+    // 0x80 (inner: rank < 8; leaf: (count - 1) << 5 | offset < 128), so the
+    // bytes' high bits are the empty mask: gather bits 7, 15, 23, 31 to
+    // bits 21-24 with one multiply (the partial products do not overlap).
+    const uint32_t elo = ((((meta_lo >> 7) & 0x01010101u) * 0x00204081u) >> 21) & 0xfu;
+    const uint32_t ehi = ((((meta_hi >> 7) & 0x01010101u) * 0x00204081u) >> 21) & 0xfu;
+    hitm &= ~(elo | (ehi << 4));
+    const uint32_t inner = hitm & imask;
+    leafhits = hitm & ~imask;
+    n_inner = __popc(inner);
+#pragma unroll
+    for (int i = 0; i < 8; i++)
+        if (!((inner >> i) & 1u)) key[i] = 0xffffffffu;
 }
 
 // 32-bit compare-exchange for the sorting network below.
