@@ -349,6 +349,17 @@ __global__ void k_collapse(DevScene S, const float *sph_radius, int n, const int
     } else {
         ch[nc++] = ref;   // whole (small) tree as one leaf: only for a small root
     }
+    // inner children first (stable), so an inner child's rank among the
+    // node's inner children is its slot: the traversal finds it at
+    // child_base + slot without reading the meta byte
+    {
+        int tmp[8], m = 0;
+        for (int k = 0; k < nc; k++)
+            if (ch[k] >= 0 && size_of(ch[k]) > kLeafMax) tmp[m++] = ch[k];
+        for (int k = 0; k < nc; k++)
+            if (!(ch[k] >= 0 && size_of(ch[k]) > kLeafMax)) tmp[m++] = ch[k];
+        for (int k = 0; k < nc; k++) ch[k] = tmp[k];
+    }
     int n_int = 0, n_prims = 0;
     for (int k = 0; k < nc; k++) {
         if (ch[k] >= 0 && size_of(ch[k]) > kLeafMax) n_int++;

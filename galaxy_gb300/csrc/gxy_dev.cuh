@@ -640,13 +640,13 @@ __device__ __noinline__ bool bvh_closest(const DevScene &S, V3 org, V3 dir, floa
                 for (int j = 7; j >= 1; j--) {
                     if (j < n_inner) {
                         uint32_t slot = key[j] & 7u;
-                        uint32_t mb = (slot < 4 ? meta_lo >> (8 * slot) : meta_hi >> (8 * (slot - 4))) & 0xffu;
+                        const uint32_t mb = slot;   // inner children sit in the first slots, in rank order
                         if (sp < 64) stack[sp++] = make_uint2(child_base + mb, key[j] & ~7u);
                         else ovf = 1;   // reported as GXY_ERR_OVERFLOW by the host
                     }
                 }
                 uint32_t slot = key[0] & 7u;
-                uint32_t mb = (slot < 4 ? meta_lo >> (8 * slot) : meta_hi >> (8 * (slot - 4))) & 0xffu;
+                const uint32_t mb = slot;   // inner children sit in the first slots, in rank order
                 cur = child_base + mb;
                 cur_tn = __uint_as_float(key[0] & ~7u);
                 continue;
@@ -769,13 +769,13 @@ __device__ __forceinline__ bool trav_step(const DevScene &S, TravState &T, STACK
         for (int j = 7; j >= 1; j--) {
             if (j < n_inner) {
                 uint32_t slot = key[j] & 7u;
-                uint32_t mb = (slot < 4 ? meta_lo >> (8 * slot) : meta_hi >> (8 * (slot - 4))) & 0xffu;
+                const uint32_t mb = slot;   // inner children sit in the first slots, in rank order
                 if (T.sp < 64) stack.set(T.sp++, make_uint2(child_base + mb, key[j] & ~7u));
                 else ovf = 1;
             }
         }
         uint32_t slot = key[0] & 7u;
-        uint32_t mb = (slot < 4 ? meta_lo >> (8 * slot) : meta_hi >> (8 * (slot - 4))) & 0xffu;
+        const uint32_t mb = slot;   // inner children sit in the first slots, in rank order
         T.cur = child_base + mb;
         T.cur_tn = __uint_as_float(key[0] & ~7u);
         return false;
@@ -887,7 +887,7 @@ __device__ __forceinline__ bool packet_closest(const DevScene &S, V3 org, V3 dir
                 for (int j = 7; j >= 1; j--) {
                     if (j < cnt && lane == j) {
                         uint32_t slot = m[j] & 7u;
-                        uint32_t mb = (slot < 4 ? meta_lo >> (8 * slot) : meta_hi >> (8 * (slot - 4))) & 0xffu;
+                        const uint32_t mb = slot;   // inner children sit in the first slots, in rank order
                         wstack[sp + (cnt - 1 - j)] = make_uint2(child_base + mb, m[j] & ~7u);
                     }
                 }
@@ -895,7 +895,7 @@ __device__ __forceinline__ bool packet_closest(const DevScene &S, V3 org, V3 dir
             }
             __syncwarp();
             uint32_t slot = m[0] & 7u;
-            uint32_t mb = (slot < 4 ? meta_lo >> (8 * slot) : meta_hi >> (8 * (slot - 4))) & 0xffu;
+            const uint32_t mb = slot;   // inner children sit in the first slots, in rank order
             cur = child_base + mb;
             continue;
         }
