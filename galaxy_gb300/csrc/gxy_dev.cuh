@@ -863,40 +863,34 @@ __device__ __forceinline__ bool packet_closest(const DevScene &S, V3 org, V3 dir
                 }
             }
         }
-        // children entered by any lane, keyed by the nearest entry over the lanes
+        // children entered by any lane, keyed by the nearest entry over the
+        // lanes; lane j < 8 holds slot j's key and its rank among the 8 (the
+        // keys of entered children are distinct -- the slot is in the low
+        // bits -- and 0xffffffff marks the others, which rank last)
         uint32_t m[8];
-        int cnt = 0;
 #pragma unroll
-        for (int i = 0; i < 8; i++) {
-            m[i] = __reduce_min_sync(FULL, key[i]);
-            cnt += m[i] != 0xffffffffu ? 1 : 0;
-        }
+        for (int i = 0; i < 8; i++) m[i] = __reduce_min_sync(FULL, key[i]);
+        uint32_t mine = m[0];
+#pragma unroll
+        for (int i = 1; i < 8; i++)
+            if (lane == i) mine = m[i];
+        const bool entered = lane < 8 && mine != 0xffffffffu;
+        const int cnt = __popc(__ballot_sync(FULL, entered));
         if (cnt) {
-            cas(m[0], m[1]); cas(m[2], m[3]); cas(m[4], m[5]); cas(m[6], m[7]);
-            cas(m[0], m[2]); cas(m[1], m[3]); cas(m[4], m[6]); cas(m[5], m[7]);
-            cas(m[1], m[2]); cas(m[5], m[6]); cas(m[0], m[4]); cas(m[3], m[7]);
-            cas(m[1], m[5]); cas(m[2], m[6]);
-            cas(m[1], m[4]); cas(m[3], m[6]);
-            cas(m[2], m[4]); cas(m[3], m[5]);
-            cas(m[3], m[4]);
-            // far-to-near onto the stack: m[cnt-1] deepest ... m[1] on top
+            int rank = 0;
+#pragma unroll
+            for (int i = 0; i < 8; i++) rank += m[i] < mine ? 1 : 0;
+            // far-to-near onto the stack: rank cnt-1 deepest ... rank 1 on
+            // top; inner children sit in the first slots, in rank order, so
+            // slot j's node is child_base + j
             if (sp + cnt - 1 > 64) {
                 ovf = 1;
             } else {
-#pragma unroll
-                for (int j = 7; j >= 1; j--) {
-                    if (j < cnt && lane == j) {
-                        uint32_t slot = m[j] & 7u;
-                        const uint32_t mb = slot;   // inner children sit in the first slots, in rank order
-                        wstack[sp + (cnt - 1 - j)] = make_uint2(child_base + mb, m[j] & ~7u);
-                    }
-                }
+                if (entered && rank >= 1) wstack[sp + (cnt - 1 - rank)] = make_uint2(child_base + (mine & 7u), mine & ~7u);
                 sp += cnt - 1;
             }
             __syncwarp();
-            uint32_t slot = m[0] & 7u;
-            const uint32_t mb = slot;   // inner children sit in the first slots, in rank order
-            cur = child_base + mb;
+            cur = child_base + (__reduce_min_sync(FULL, entered ? mine : 0xffffffffu) & 7u);
             continue;
         }
         // pop the nearest stacked node some lane may still need
