@@ -16,7 +16,8 @@ repeated while a pass still changes something):
   * queue chunk of the refill queries: BVH8 node visits per refill round;
   * march tiling: volume samples per refill round of the march passes;
   * clear-brick skipping: fast runs in the camera-ray march, skipping (and
-    fast runs) in the shadow/AO march.
+    fast runs) in the shadow/AO march, the occlusion shortcut of the
+    shadow/AO query.
 
 tune_bvh() picks the scene-level BVH builder (radix tree, or a binned-SAH
 top over radix-tree clusters) by committing the scene with each.
@@ -38,7 +39,7 @@ KNOBS = (
     ("camera_packet", gpu.TUNE_CAMERA_PACKET, (0, 1)),
     ("trav_steps", gpu.TUNE_TRAV_STEPS, (4, 8, 16)),
     ("march_steps", gpu.TUNE_MARCH_STEPS, (8, 16, 32, 64)),
-    ("skip_mode", gpu.TUNE_SKIP_MODE, (0, 1, 3, 7)),
+    ("skip_mode", gpu.TUNE_SKIP_MODE, (0, 1, 3, 7, 9, 11)),
 )
 
 

@@ -703,9 +703,11 @@ struct LocalStack {
 };
 // LINES: the scene has path-line segments (their test is compiled in only
 // then, so the register budget of the common case is unchanged).
+// stop_below: the query may end at the first accepted hit nearer than this
+// (the caller needs no more than "some hit before stop_below" then).
 template <bool LINES, class STACK>
 __device__ __forceinline__ bool trav_step(const DevScene &S, TravState &T, STACK &stack, unsigned &nodes,
-                                          unsigned &tris, unsigned &sphs, int &ovf) {
+                                          unsigned &tris, unsigned &sphs, int &ovf, float stop_below = -INFINITY) {
     while (!(T.cur_tn <= T.h.t)) {
         if (T.sp == 0) return true;
         uint2 e = stack.get(--T.sp);
@@ -757,6 +759,7 @@ __device__ __forceinline__ bool trav_step(const DevScene &S, TravState &T, STACK
             }
         }
     }
+    if (T.found && T.h.t < stop_below) return true;
     if (n_inner) {
         cas(key[0], key[1]); cas(key[2], key[3]); cas(key[4], key[5]); cas(key[6], key[7]);
         cas(key[0], key[2]); cas(key[1], key[3]); cas(key[4], key[6]); cas(key[5], key[7]);

@@ -1305,6 +1305,7 @@ __global__ void __launch_bounds__(kThreads, MINB) k_sec_query(DevScene S, FrameA
     LocalStack stack{stack_mem};
     unsigned src = 0;   // the lane's input record (shadow, then AO index space)
     float ray_t = 0.0f;
+    float stop_below = -INFINITY;   // clear segment: any hit before this ends the ray here
     bool have = false, done = false, surface = false, slice_ahead = false, zero = false;
     for (;;) {
         bool need = !have;
@@ -1344,8 +1345,21 @@ __global__ void __launch_bounds__(kThreads, MINB) k_sec_query(DevScene S, FrameA
                     }
                 }
                 zero = in.r == 0.0f && in.g == 0.0f && in.b == 0.0f && in.o == 0.0f;
+                // Occlusion shortcut (GXY_TUNE_SKIP_MODE bit 3): when every
+                // march position of this partition, tEntry .. ray_t, lies in
+                // clear superbricks, the march would leave the payload as it
+                // is, so a surface anywhere before ray_t ends the ray here
+                // with the payload unchanged -- the nearest surface is not
+                // needed and the query stops at the first hit before ray_t.
+                stop_below = -INFINITY;
+                if ((A.skip_mode & 8) && S.vol[0].sclear && !zero) {
+                    const DevVolume &vv = S.vol[0];
+                    const VolPos g = vol_pos(vv, in.org + tEntry * dir);
+                    if (__ldg(vv.sclear + super_of(vv, g)) && clear_run_end(vv, in.org, dir, g, tEntry, ray_t) > ray_t)
+                        stop_below = ray_t;
+                }
                 // a zero payload is culled whatever the query finds: no traversal
-                done = zero || trav_init(S, T, in.org, dir, ray_t0, in.tmax);
+                done = zero || (surface && stop_below > -INFINITY) || trav_init(S, T, in.org, dir, ray_t0, in.tmax);
                 have = true;
             }
         }
@@ -1353,9 +1367,28 @@ __global__ void __launch_bounds__(kThreads, MINB) k_sec_query(DevScene S, FrameA
         // one copy of the step body: unrolled copies overflow the instruction cache
 #pragma unroll 1
         for (int k = 0; k < max(A.trav_steps, 1) && have && !done; k++)
-            done = trav_step<LINES>(S, T, stack, st.nodes, st.tris, st.sphs, st.ovf);
+            done = trav_step<LINES>(S, T, stack, st.nodes, st.tris, st.sphs, st.ovf, stop_below);
         bool fin = have && done;
         bool to_march = false;
+        if (fin && stop_below > -INFINITY && (surface || (T.found && T.h.t < stop_below))) {
+            // ends at a surface inside its clear segment: terminate as the
+            // march pass would (payload unchanged, SURFACE)
+            TraceIn in;
+            int x, y, job;
+            load_ray(src < ns ? A.qin[Q_SHADOW] : A.qin[Q_AO], src < ns ? src : src - ns, in, x, y, job);
+            const bool op = fmin_(fmin_(in.r, in.g), in.b) >= 1.0f || in.o > S.opaque_alpha;
+            const int cls = classify_ray(in.type, (op ? GXY_RAY_OPAQUE : 0) | GXY_RAY_SURFACE);
+            const int dest = assign_destination(S, in.part, in.type, cls, in.org, in.dir);
+            const DevJob &J = BATCH ? A.jobs[job] : A.job0;
+            if (dest == GXY_TERMINATED) {
+                c.term++;
+                add_pixel(J.fb, J.cam.width, x, y, in.r, in.g, in.b, in.o);
+            } else {
+                c.drop++;
+            }
+            fin = false;
+            have = false;
+        }
         if (fin) {
             bool h = !zero && T.found;
             if (h && T.h.t < ray_t) {
@@ -1933,7 +1966,7 @@ int sah_cluster_size() { return g_tune_sah == 1 ? 256 : g_tune_sah; }
 static int g_tune_leaf = 1;         // primitives per BVH8 leaf (at most)
 static int g_tune_trav_steps = 8;   // node visits per refill round of the query passes
 static int g_tune_march_steps = 16; // samples per refill round of the march passes
-static int g_tune_skip_mode = 1;    // clear-brick skipping per march pass (GXY_TUNE_SKIP_MODE bits)
+static int g_tune_skip_mode = 9;    // clear-brick skipping per pass (GXY_TUNE_SKIP_MODE bits)
 static int g_tune_cam_packet = 1;   // single-frame camera query: warp-cooperative (1) or per-lane refill (0)
 int leaf_max() { return g_tune_leaf; }
 
@@ -2562,7 +2595,7 @@ int gxy_gpu_set_tuning(int knob, int value) {
         return GXY_OK;
     }
     if (knob == GXY_TUNE_SKIP_MODE) {
-        if (value < 0 || value > 7) return set_error(GXY_ERR_INVALID, "skip mode must be 0-7");
+        if (value < 0 || value > 15) return set_error(GXY_ERR_INVALID, "skip mode must be 0-15");
         g_tune_skip_mode = value;
         return GXY_OK;
     }

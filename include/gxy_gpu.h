@@ -314,8 +314,8 @@ int gxy_gpu_set_profiling(gxy_scene scene, int on);
                                         passes then read no voxels for intervals between
                                         two such positions (same images and counters);
                                         0: no flags, every sample read */
-#define GXY_TUNE_SKIP_MODE      11   /* clear-brick skipping per march pass, bits:
-                                        1 (default): the camera-ray march also advances
+#define GXY_TUNE_SKIP_MODE      11   /* clear-brick skipping per pass, bits (default 9):
+                                        1: the camera-ray march also advances
                                         through the rest of a flagged brick in one run of
                                         distance updates (it always skips per position
                                         and jumps runs of clear 32^3 superbricks);
@@ -324,7 +324,13 @@ int gxy_gpu_set_profiling(gxy_scene scene, int on);
                                         refill round, sampling every other position;
                                         4: the shadow/AO march skips as the camera-ray
                                         march does (incoherent rays: a warp runs both
-                                        paths when its lanes differ) */
+                                        paths when its lanes differ);
+                                        8 (default): occlusion shortcut -- a shadow/AO ray whose
+                                        march positions in its partition all lie in clear
+                                        superbricks ends at the first surface the query
+                                        finds before the partition exit, unmarched (same
+                                        frames; fewer samples, node visits and primitive
+                                        tests counted) */
 int gxy_gpu_set_tuning(int knob, int value);
 int gxy_gpu_get_tuning(int knob, int *value);
 int gxy_gpu_query_generations(gxy_scene scene, gxy_generation_stats *out, int max, int32_t *n);
