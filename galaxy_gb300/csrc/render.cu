@@ -197,6 +197,7 @@ struct Scene {
     static constexpr int kMaxLaunch = 256;   // counter slots per frame
     DevScene *d_scene = nullptr;             // device copy of S (batches)
     DRay *qmarch = nullptr;                  // split-path march queue
+    float *qmarch_hit = nullptr;             // per march record: the query's closest hit (0: none)
     size_t qmarch_cap = 0;
     DRay *pmarch = nullptr;                  // split primary march queue
     float4 *pmarch_hit = nullptr;
@@ -222,6 +223,7 @@ struct Scene {
         for (int b = 0; b < 2; b++)
             for (int k = 0; k < 3; k++) arena().free(q[b][k]);
         arena().free(qmarch);
+        arena().free(qmarch_hit);
         arena().free(pmarch);
         arena().free(pmarch_hit);
         arena().free(qcount);
@@ -775,12 +777,12 @@ __device__ __forceinline__ unsigned warp_excl_scan(unsigned v, unsigned &tot) {
 }
 
 __device__ __forceinline__ void put_ray(DRay *q, unsigned idx, V3 o, float t, V3 d, float tmax, float r, float g,
-                                        float b, float a, int x, int y, int meta) {
+                                        float b, float a, int x, int y, int meta, int spare = 0) {
     DRay *p = q + idx;
     p->o = make_float4(o.x, o.y, o.z, t);
     p->d = make_float4(d.x, d.y, d.z, tmax);
     p->c = make_float4(r, g, b, a);
-    p->m = make_int4(x, y, meta, 0);
+    p->m = make_int4(x, y, meta, spare);
 }
 
 enum { Q_PRIM = 0, Q_SHADOW = 1, Q_AO = 2, NQ = 3 };
@@ -811,6 +813,10 @@ struct FrameArgs {
     // split shadow/AO tracing (volume scenes): query pass -> march queue -> march pass
     int split;
     DRay *qmarch;
+    // Frame path: the query pass's closest hit per march record, handed on
+    // in the spare word of a shadow/AO record that moves to the next
+    // partition, where the query then reuses it (null: no hand-on).
+    float *qmarch_hit;
     unsigned *qmarch_count;            // [0] records, [1] fetch cursor of the march pass
     unsigned qmarch_cap;
     // split primary tracing: camera query pass -> primary march queue -> march pass
@@ -1047,16 +1053,18 @@ __device__ __forceinline__ int secondary_ray(const DevScene &S, const DevTF *tfs
 
 // Warp-collective: hand shadow/AO rays to their neighbour brick's queue.
 __device__ __forceinline__ void emit_secondary(bool act, int dest, int q, int job, const TraceIn &in, int x, int y,
-                                               const TraceOut &T, const FrameArgs &A, LocalCounters &c) {
+                                               const TraceOut &T, const FrameArgs &A, LocalCounters &c,
+                                               float carry = 0.0f) {
     unsigned cs = (act && dest >= 0 && q == Q_SHADOW) ? 1u : 0u;
     unsigned ca = (act && dest >= 0 && q == Q_AO) ? 1u : 0u;
     unsigned is = warp_reserve(cs, A.qout_count + Q_SHADOW, A.qcap[Q_SHADOW], c.ovf);
     unsigned ia = warp_reserve(ca, A.qout_count + Q_AO, A.qcap[Q_AO], c.ovf);
     if (cs && is != 0xffffffffu)
         put_ray(A.qout[Q_SHADOW], is, in.org, T.t, in.dir, in.tmax, T.r, T.g, T.b, T.o, x, y,
-                make_meta(in.type, dest, job));
+                make_meta(in.type, dest, job), __float_as_int(carry));
     if (ca && ia != 0xffffffffu)
-        put_ray(A.qout[Q_AO], ia, in.org, T.t, in.dir, in.tmax, T.r, T.g, T.b, T.o, x, y, make_meta(in.type, dest, job));
+        put_ray(A.qout[Q_AO], ia, in.org, T.t, in.dir, in.tmax, T.r, T.g, T.b, T.o, x, y, make_meta(in.type, dest, job),
+                __float_as_int(carry));
     c.enq += cs + ca;
 }
 
@@ -1306,6 +1314,7 @@ __global__ void __launch_bounds__(kThreads, MINB) k_sec_query(DevScene S, FrameA
     unsigned src = 0;   // the lane's input record (shadow, then AO index space)
     float ray_t = 0.0f;
     float stop_below = -INFINITY;   // clear segment: any hit before this ends the ray here
+    float carry_out = 0.0f;         // closest hit handed on with the march record (0: none)
     bool have = false, done = false, surface = false, slice_ahead = false, zero = false;
     for (;;) {
         bool need = !have;
@@ -1358,8 +1367,24 @@ __global__ void __launch_bounds__(kThreads, MINB) k_sec_query(DevScene S, FrameA
                     if (__ldg(vv.sclear + super_of(vv, g)) && clear_run_end(vv, in.org, dir, g, tEntry, ray_t) > ray_t)
                         stop_below = ray_t;
                 }
+                // A ray handed on from the previous partition carries the
+                // closest hit its query found over its whole extent (the
+                // spare word of the record); it is this query's answer as
+                // well, so there is no traversal.
+                const float carried =
+                    A.qmarch_hit ? __int_as_float(__ldg(reinterpret_cast<const int *>(
+                                                      (idx < ns ? A.qin[Q_SHADOW] + idx : A.qin[Q_AO] + (idx - ns))) + 15))
+                                 : 0.0f;
                 // a zero payload is culled whatever the query finds: no traversal
-                done = zero || (surface && stop_below > -INFINITY) || trav_init(S, T, in.org, dir, ray_t0, in.tmax);
+                if (zero || (surface && stop_below > -INFINITY)) {
+                    done = true;
+                } else if (carried > 0.0f) {
+                    T.found = true;
+                    T.h.t = carried;
+                    done = true;
+                } else {
+                    done = trav_init(S, T, in.org, dir, ray_t0, in.tmax);
+                }
                 have = true;
             }
         }
@@ -1391,6 +1416,7 @@ __global__ void __launch_bounds__(kThreads, MINB) k_sec_query(DevScene S, FrameA
         }
         if (fin) {
             bool h = !zero && T.found;
+            carry_out = h ? T.h.t : 0.0f;
             if (h && T.h.t < ray_t) {
                 ray_t = T.h.t;
                 surface = true;
@@ -1414,6 +1440,7 @@ __global__ void __launch_bounds__(kThreads, MINB) k_sec_query(DevScene S, FrameA
                 p->d = __ldg(q + 1);
                 p->c = __ldg(q + 2);
                 p->m = make_int4(m.x, m.y, m.z | (surface ? 8 : 0), __float_as_int(ray_t));
+                if (A.qmarch_hit) A.qmarch_hit[idx] = carry_out;
             }
         }
         if (fin) have = false;
@@ -1725,6 +1752,7 @@ __global__ void __launch_bounds__(kThreads, MINB) k_sec_march(DevScene S, FrameA
     SecMarch M;
     TraceIn in;
     int x = 0, y = 0, job = 0, q = Q_SHADOW;
+    float carry = 0.0f;   // the query's closest hit, handed on if the ray changes partition
     bool have = false;
     for (;;) {
         bool need = !have;
@@ -1739,6 +1767,7 @@ __global__ void __launch_bounds__(kThreads, MINB) k_sec_march(DevScene S, FrameA
             if (idx < n) {
                 load_ray(A.qmarch, idx, in, x, y, job);
                 int4 m = __ldg(reinterpret_cast<const int4 *>(A.qmarch + idx) + 3);
+                carry = A.qmarch_hit ? __ldg(A.qmarch_hit + idx) : 0.0f;
                 bool surface = (in.type & 8) != 0;
                 in.type &= 7;
                 q = in.type == GXY_RAY_SHADOW ? Q_SHADOW : Q_AO;
@@ -1768,7 +1797,7 @@ __global__ void __launch_bounds__(kThreads, MINB) k_sec_march(DevScene S, FrameA
                 c.hand++;
             }
         }
-        if (__any_sync(0xffffffffu, fin && dest >= 0)) emit_secondary(fin, dest, q, job, in, x, y, T, A, c);
+        if (__any_sync(0xffffffffu, fin && dest >= 0)) emit_secondary(fin, dest, q, job, in, x, y, T, A, c, carry);
         if (fin) have = false;
     }
     flush_counters(A.ctr, c, st);
@@ -1967,6 +1996,7 @@ static int g_tune_leaf = 1;         // primitives per BVH8 leaf (at most)
 static int g_tune_trav_steps = 8;   // node visits per refill round of the query passes
 static int g_tune_march_steps = 16; // samples per refill round of the march passes
 static int g_tune_skip_mode = 9;    // clear-brick skipping per pass (GXY_TUNE_SKIP_MODE bits)
+static int g_tune_carry_hits = 1;   // hand the closest hit on with shadow/AO rays that change partition
 static int g_tune_cam_packet = 1;   // single-frame camera query: warp-cooperative (1) or per-lane refill (0)
 int leaf_max() { return g_tune_leaf; }
 
@@ -2039,10 +2069,13 @@ static int ensure_queues(Scene *sc, const size_t need[3]) {
     size_t mneed = need[1] + need[2];
     if (sc->qmarch_cap < mneed) {
         arena().free(sc->qmarch);
+        arena().free(sc->qmarch_hit);
         sc->qmarch = nullptr;
+        sc->qmarch_hit = nullptr;
         sc->qmarch_cap = 0;
         int rc = arena().alloc((void **)&sc->qmarch, mneed * sizeof(DRay));
         if (rc) return rc;
+        if ((rc = arena().alloc((void **)&sc->qmarch_hit, mneed * sizeof(float)))) return rc;
         sc->qmarch_cap = mneed;
     }
     for (int k = 0; k < 3; k++) {
@@ -2104,6 +2137,7 @@ static int render(Scene *sc, const gxy_camera &cam, const gxy_lighting &lt, floa
     A.total_pix = npix;
     A.split = split_eligible(S) ? 1 : 0;
     A.qmarch = sc->qmarch;
+    A.qmarch_hit = g_tune_carry_hits ? sc->qmarch_hit : nullptr;
     A.qmarch_count = sc->qcount + 12;   // [0] records, [1] march cursor, [2] query cursor
     A.qmarch_cap = (unsigned)sc->qmarch_cap;
     A.split_prim = (split_eligible(S) && g_tune_split_prim) ? 1 : 0;
@@ -2594,6 +2628,10 @@ int gxy_gpu_set_tuning(int knob, int value) {
         g_tune_skip_clear = value ? 1 : 0;
         return GXY_OK;
     }
+    if (knob == GXY_TUNE_CARRY_HITS) {
+        g_tune_carry_hits = value ? 1 : 0;
+        return GXY_OK;
+    }
     if (knob == GXY_TUNE_SKIP_MODE) {
         if (value < 0 || value > 15) return set_error(GXY_ERR_INVALID, "skip mode must be 0-15");
         g_tune_skip_mode = value;
@@ -2615,6 +2653,7 @@ int gxy_gpu_get_tuning(int knob, int *value) {
     else if (knob == GXY_TUNE_MARCH_STEPS) *value = g_tune_march_steps;
     else if (knob == GXY_TUNE_SKIP_CLEAR) *value = g_tune_skip_clear;
     else if (knob == GXY_TUNE_SKIP_MODE) *value = g_tune_skip_mode;
+    else if (knob == GXY_TUNE_CARRY_HITS) *value = g_tune_carry_hits;
     else return set_error(GXY_ERR_INVALID, "unknown tuning knob");
     return GXY_OK;
 }

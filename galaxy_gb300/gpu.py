@@ -116,6 +116,7 @@ TUNE_MARCH_STEPS = 8
 TUNE_CAMERA_PACKET = 9
 TUNE_SKIP_CLEAR = 10
 TUNE_SKIP_MODE = 11
+TUNE_CARRY_HITS = 13
 
 
 def set_tuning(knob, value):

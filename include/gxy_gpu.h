@@ -331,6 +331,12 @@ int gxy_gpu_set_profiling(gxy_scene scene, int on);
                                         finds before the partition exit, unmarched (same
                                         frames; fewer samples, node visits and primitive
                                         tests counted) */
+#define GXY_TUNE_CARRY_HITS     13   /* 1 (default): a shadow/AO ray that moves to the next
+                                        partition carries the closest hit its query found
+                                        over its whole extent, and the next partition's
+                                        query reuses it instead of traversing again (the
+                                        same hit, except for a surface within float
+                                        rounding of the shared face); 0: query again */
 int gxy_gpu_set_tuning(int knob, int value);
 int gxy_gpu_get_tuning(int knob, int *value);
 int gxy_gpu_query_generations(gxy_scene scene, gxy_generation_stats *out, int max, int32_t *n);

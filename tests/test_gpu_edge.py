@@ -138,3 +138,28 @@ def test_autotuner_coordinate_descent(gpu):
         close(img, ref)
     finally:
         autotune.apply(before)
+
+
+def test_carried_hits_same_frames(gpu):
+    """Shadow/AO rays that move to the next partition carry their query's
+    closest hit (GXY_TUNE_CARRY_HITS): the frames and ray counters equal
+    those with a fresh query in every partition; only node visits and
+    primitive tests drop."""
+    cam, vis = scenes.mixed_scene(n=64, n_spheres=20000, width=128, height=128, partitions=(2, 2, 2), n_ao=4)
+    L = S.resolve_lights(vis.lighting, cam)
+    sc = gpu.Scene(vis)
+    before = gpu.get_tuning(gpu.TUNE_CARRY_HITS)
+    try:
+        gpu.set_tuning(gpu.TUNE_CARRY_HITS, 1)
+        a = sc.render_host(cam, L)
+        ca = sc.counters()
+        gpu.set_tuning(gpu.TUNE_CARRY_HITS, 0)
+        b = sc.render_host(cam, L)
+        cb = sc.counters()
+    finally:
+        gpu.set_tuning(gpu.TUNE_CARRY_HITS, before)
+    assert float(np.abs(a - b).max()) <= 1e-6
+    for k in ca:
+        if k not in ("nodes", "prim_tests", "sph_tests", "tri_tests"):
+            assert ca[k] == cb[k], k
+    assert ca["handoffs"] > 0 and ca["nodes"] < cb["nodes"]
