@@ -441,7 +441,7 @@ def main():
         gpu.set_tuning(gpu.TUNE_SPLIT_SECONDARY, vals[2])
         gpu.set_tuning(gpu.TUNE_SPLIT_PRIMARY, vals[3])
     elif args.autotune:
-        tuning = autotune.tune(sc, cam_c, L, frames=2)
+        tuning = autotune.tune(sc, cam_c, L, frames=4)
     sc.set_profiling(True)
     for _ in range(args.warmup):
         frame()
