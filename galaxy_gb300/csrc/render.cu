@@ -1981,7 +1981,7 @@ __global__ void k_rl_camera_write(DevScene S, DevCamera C, int part, const int *
     O.i[I_X][k] = x; O.i[I_Y][k] = y; O.i[I_TYPE][k] = GXY_RAY_PRIMARY; O.i[I_TERM][k] = 0;
 }
 
-// ============================================================ frame driver
+// ============================================================ frame loop
 // Run-time tuning knobs (gxy_gpu_set_tuning): resident blocks per SM the
 // kernels are compiled for (register budget 2 -> 128, 3 -> 80 registers per
 // thread) and the grid-stride grid size in blocks per SM.
