@@ -2658,6 +2658,14 @@ int gxy_gpu_get_tuning(int knob, int *value) {
     return GXY_OK;
 }
 
+int gxy_tf_clear_below(const gxy_tf *tf, float *threshold) {
+    if (!tf || !threshold) return set_error(GXY_ERR_INVALID, "null argument");
+    DevTF t;
+    tf_to_dev(*tf, t);
+    *threshold = tf_clear_below(t);
+    return GXY_OK;
+}
+
 int gxy_gpu_set_profiling(gxy_scene scene, int on) {
     if (!scene) return set_error(GXY_ERR_INVALID, "null scene");
     reinterpret_cast<Scene *>(scene)->profile = on ? 1 : 0;

@@ -782,7 +782,7 @@ __device__ __forceinline__ void march_steps(const DevScene &S, const DevTF &tf, 
                                             RayStats &st) {
     const DevVolume &vv = S.vol[0];
     const float step = S.step, epsilon = S.march_eps;
-    if (SKIP < 2) {
+    if constexpr (SKIP < 2) {
         if (SKIP == 1 && M.tThis == M.tEntry) lean_run(vv, M, M.tEntry, epsilon, step, st);
         for (int it = 0; it < steps && !M.done; it++) {
             float tThis = M.tThis;
@@ -796,79 +796,79 @@ __device__ __forceinline__ void march_steps(const DevScene &S, const DevTF &tf, 
             M.done = !(M.tThis <= M.tTerm && !M.opaque);
         }
         if (SKIP == 1 && !M.done) lean_run(vv, M, M.tLast, epsilon, step, st);
-        return;
-    }
-    for (int it = 0; it < steps && !M.done; it++) {
-        if (M.tThis < M.tRun) {
-            // inside a run of clear superbricks whose previous position is
-            // clear too: only the distance sequence advances
-            float t = M.tThis, tl = M.tLast;
-            const float tTerm = M.tTerm;
-            const int k = advance_clear(t, tl, M.tRun, tTerm, M.tEntry, epsilon, step, kMaxCount);
-            M.tThis = t;
-            M.tLast = tl;
-            M.lazy = true;
-            M.prev_clear = true;
-            M.done = !(t <= tTerm);
-            st.samples += k;
-            st.skipped += k;
-            continue;
-        }
-        float tThis = M.tThis;
-        VolPos g = vol_pos(vv, march_point(M, tThis));
-        int bid = brick_of(vv, g);
-        if (bid != M.bid) {
-            M.bid = bid;
-            M.bclear = __ldg(vv.clear + bid) != 0;
-        }
-        st.samples++;
-        if (tThis > M.tEntry && M.tLast >= epsilon && vv.volume_render && !(M.bclear && M.prev_clear)) {
-            if (M.lazy) {
-                M.sLast = vol_sample_at(vv, vol_pos(vv, march_point(M, M.tLast)), M.cc);
-                st.skipped--;
-            }
-            float sThis = vol_sample_at(vv, g, M.cc);
-            march_composite<PRIMARY>(S, tf, M, (M.sLast + sThis) / 2.0f, tThis);
-            M.sLast = sThis;
-            M.lazy = false;
-        } else {
-            M.lazy = true;
-            st.skipped++;
-        }
-        M.prev_clear = M.bclear;
-        M.tLast = tThis;
-        M.tThis = march_next(tThis, M.tEntry, epsilon, step, M.tTerm);
-        M.done = !(M.tThis <= M.tTerm && !M.opaque);
-        // A clear brick in a superbrick not looked up yet: find the run of
-        // clear superbricks ahead (the next iterations count through it).
-        if (M.bclear && !M.done) {
-            const int sb = super_of(vv, g);
-            if (sb != M.sbid) {
-                M.sbid = sb;
-                if (__ldg(vv.sclear + sb)) {
-                    M.tRun = clear_run_end(vv, M.org, M.dir, g, tThis, M.tTerm);
-                    if (M.tThis < M.tRun) continue;
-                }
-            }
-        }
-        // Fast run through the rest of a clear brick: the positions that
-        // provably stay in it (brick_span) have clear intervals on both
-        // sides, so only the distance sequence advances.  The colour, and
-        // with it `opaque` (false here), does not change.
-        float t_in, t_out;
-        if (runs && !M.done && M.bclear && brick_span(vv, M.org, M.dir, g, tThis, t_in, t_out) &&
-            M.tThis >= t_in) {
-            float t = M.tThis, tl = M.tLast;
-            const float tTerm = M.tTerm;
-            // positions t <= t_out: below the next float up from t_out
-            const int k = advance_clear(t, tl, nextafterf(t_out, INFINITY), tTerm, M.tEntry, epsilon, step, kMaxRun);
-            if (k) {
+    } else {
+        for (int it = 0; it < steps && !M.done; it++) {
+            if (M.tThis < M.tRun) {
+                // inside a run of clear superbricks whose previous position is
+                // clear too: only the distance sequence advances
+                float t = M.tThis, tl = M.tLast;
+                const float tTerm = M.tTerm;
+                const int k = advance_clear(t, tl, M.tRun, tTerm, M.tEntry, epsilon, step, kMaxCount);
                 M.tThis = t;
                 M.tLast = tl;
                 M.lazy = true;
+                M.prev_clear = true;
                 M.done = !(t <= tTerm);
                 st.samples += k;
                 st.skipped += k;
+                continue;
+            }
+            float tThis = M.tThis;
+            VolPos g = vol_pos(vv, march_point(M, tThis));
+            int bid = brick_of(vv, g);
+            if (bid != M.bid) {
+                M.bid = bid;
+                M.bclear = __ldg(vv.clear + bid) != 0;
+            }
+            st.samples++;
+            if (tThis > M.tEntry && M.tLast >= epsilon && vv.volume_render && !(M.bclear && M.prev_clear)) {
+                if (M.lazy) {
+                    M.sLast = vol_sample_at(vv, vol_pos(vv, march_point(M, M.tLast)), M.cc);
+                    st.skipped--;
+                }
+                float sThis = vol_sample_at(vv, g, M.cc);
+                march_composite<PRIMARY>(S, tf, M, (M.sLast + sThis) / 2.0f, tThis);
+                M.sLast = sThis;
+                M.lazy = false;
+            } else {
+                M.lazy = true;
+                st.skipped++;
+            }
+            M.prev_clear = M.bclear;
+            M.tLast = tThis;
+            M.tThis = march_next(tThis, M.tEntry, epsilon, step, M.tTerm);
+            M.done = !(M.tThis <= M.tTerm && !M.opaque);
+            // A clear brick in a superbrick not looked up yet: find the run of
+            // clear superbricks ahead (the next iterations count through it).
+            if (M.bclear && !M.done) {
+                const int sb = super_of(vv, g);
+                if (sb != M.sbid) {
+                    M.sbid = sb;
+                    if (__ldg(vv.sclear + sb)) {
+                        M.tRun = clear_run_end(vv, M.org, M.dir, g, tThis, M.tTerm);
+                        if (M.tThis < M.tRun) continue;
+                    }
+                }
+            }
+            // Fast run through the rest of a clear brick: the positions that
+            // provably stay in it (brick_span) have clear intervals on both
+            // sides, so only the distance sequence advances.  The colour, and
+            // with it `opaque` (false here), does not change.
+            float t_in, t_out;
+            if (runs && !M.done && M.bclear && brick_span(vv, M.org, M.dir, g, tThis, t_in, t_out) &&
+                M.tThis >= t_in) {
+                float t = M.tThis, tl = M.tLast;
+                const float tTerm = M.tTerm;
+                // positions t <= t_out: below the next float up from t_out
+                const int k = advance_clear(t, tl, nextafterf(t_out, INFINITY), tTerm, M.tEntry, epsilon, step, kMaxRun);
+                if (k) {
+                    M.tThis = t;
+                    M.tLast = tl;
+                    M.lazy = true;
+                    M.done = !(t <= tTerm);
+                    st.samples += k;
+                    st.skipped += k;
+                }
             }
         }
     }

@@ -61,6 +61,7 @@ def lib():
         "gxy_gpu_batch_counters": [vp, C.POINTER(A.gxy_counters)],
         "gxy_gpu_batch_stream": [vp, C.POINTER(vp)],
         "gxy_gpu_set_tuning": [C.c_int, C.c_int],
+        "gxy_tf_clear_below": [C.POINTER(A.gxy_tf), C.POINTER(C.c_float)],
         "gxy_gpu_get_tuning": [C.c_int, C.POINTER(C.c_int)],
         "gxy_gpu_classify": [C.POINTER(A.gxy_raylist)],
         "gxy_gpu_assign_destinations": [vp, C.c_int, C.POINTER(A.gxy_raylist)],
@@ -121,6 +122,13 @@ TUNE_CARRY_HITS = 13
 
 def set_tuning(knob, value):
     check(lib().gxy_gpu_set_tuning(int(knob), int(value)))
+
+
+def tf_clear_below(tf):
+    """Zero-opacity threshold of a gxy_tf (host only; see gxy_gpu.h)."""
+    t = C.c_float()
+    check(lib().gxy_tf_clear_below(C.byref(tf), C.byref(t)))
+    return t.value
 
 
 def get_tuning(knob):

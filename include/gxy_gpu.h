@@ -337,6 +337,12 @@ int gxy_gpu_set_profiling(gxy_scene scene, int on);
                                         query reuses it instead of traversing again (the
                                         same hit, except for a surface within float
                                         rounding of the shared face); 0: query again */
+/* The threshold the empty-space skipping uses (no counterpart in the
+ * reference): the largest T such that every data value below T, and NaN,
+ * has opacity exactly 0 in the transfer-function lookup; -inf when the
+ * lowest entry's opacity is positive, +inf when every entry's is zero.
+ * Host only: needs neither a device nor gxy_gpu_init. */
+int gxy_tf_clear_below(const gxy_tf *tf, float *threshold);
 int gxy_gpu_set_tuning(int knob, int value);
 int gxy_gpu_get_tuning(int knob, int *value);
 int gxy_gpu_query_generations(gxy_scene scene, gxy_generation_stats *out, int max, int32_t *n);

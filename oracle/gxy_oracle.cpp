@@ -1504,6 +1504,10 @@ int oracle_tf_resample(const float *cmap, int ncm, const float *omap, int nom, i
     return 0;
 }
 
+// The transfer function's opacity of one value, in single precision (the
+// lookup the march composites with).
+float oracle_tf_opacity(const gxy_tf *tf, float v) { return tf_opacity<float>(*tf, v); }
+
 int oracle_ao_tables(float *u, float *v) {
     const AOTables &t = ao_tables();
     memcpy(u, t.u, sizeof t.u);

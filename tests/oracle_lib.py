@@ -41,6 +41,8 @@ def lib():
         L.oracle_tf_resample.argtypes = [A.f32p, C.c_int, A.f32p, C.c_int, C.c_int, C.c_float, C.c_float,
                                          C.POINTER(A.gxy_tf)]
         L.oracle_ao_tables.argtypes = [A.f32p, A.f32p]
+        L.oracle_tf_opacity.restype = C.c_float
+        L.oracle_tf_opacity.argtypes = [C.POINTER(A.gxy_tf), C.c_float]
         L.oracle_quantize.argtypes = [A.f32p, C.c_int, C.c_int, C.POINTER(C.c_uint8)]
         _lib = L
     return _lib
