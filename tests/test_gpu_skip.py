@@ -206,3 +206,38 @@ def test_superbrick_runs(gpu, eye, level):
         assert ca["samples"] < cb["samples"] and ca["nodes"] < cb["nodes"]
     ref, cnt = O.OracleScene(vis).render(cam, L, nthreads=8)
     image_close(a, ref)
+
+
+@pytest.mark.parametrize("level", [1, 2, 3])
+def test_offset_anisotropic_volume(gpu, level):
+    """A volume away from the origin, with a different spacing on each axis
+    and counts that are multiples of neither the brick (4 cells) nor the
+    superbrick (32 cells): partial bricks and superbricks at the far faces,
+    rays crossing them obliquely, shadows and AO across two partitions."""
+    nx, ny, nz = 70, 83, 45
+    org, dl = (-1.3, 0.4, 2.0), (0.02, 0.015, 0.03)
+    g = np.random.default_rng(17)
+    z, y, x = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
+    f = 0.2 * g.random((nz, ny, nx), dtype=np.float32)
+    for cx, cy, cz, r in ((20, 30, 12, 9.0), (55, 70, 35, 7.0), (66, 10, 40, 6.0)):
+        f += np.exp(-((x - cx) ** 2 + (y - cy) ** 2 + (z - cz) ** 2) / (2 * r * r)).astype(np.float32)
+    vol = S.Volume(f.astype(np.float32), origin=org, deltas=dl)
+    lo = np.array(org, np.float32)
+    hi = lo + np.array(dl, np.float32) * (np.array((nx, ny, nz), np.float32) - 1)
+    vv = S.VolumeVis(vol, volume_rendering=True, colormap=scenes.COOLWARM,
+                     opacitymap=[(0.0, 0.0), (0.3, 0.0), (1.2, 0.6)])
+    pts = (lo + (hi - lo) * g.uniform(0.05, 0.95, size=(300, 3))).astype(np.float32)
+    parts = S.Particles(pts, np.zeros(300, np.float32))
+    L = S.Lighting()
+    L.lights, L.types = [(-0.577, -0.577, -0.577)], [0]
+    L.shadows, L.n_ao, L.ao_radius, L.Ka, L.Kd = True, 2, 0.2, 0.5, 0.5
+    vis = S.Visualization([vv, S.ParticlesVis(parts, radius0=0.03, radius1=0.03)], L, partitions=(2, 1, 1),
+                          sampling_rate=2.0, opaque_alpha=0.99)
+    c = (lo + hi) / 2
+    eye = tuple(float(v) for v in c + np.array([1.6, 0.9, 2.3], np.float32))
+    cam = S.Camera(eye, tuple(float(v) for v in c - np.array(eye, np.float32)), (0, 1, 0), 40.0, 80, 80)
+    a, b, ca, cb, L = render_pair(gpu, cam, vis, level)
+    same_frames(a, b, ca, cb, level)
+    assert ca["samples_skipped"] > 0.1 * ca["samples"]
+    ref, cnt = O.OracleScene(vis).render(cam, L, nthreads=8)
+    image_close(a, ref)
