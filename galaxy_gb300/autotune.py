@@ -53,18 +53,50 @@ def apply(setting):
             gpu.set_tuning(knob, int(setting[name]))
 
 
+def descend(measure, start, knobs=KNOBS, passes=2):
+    """Coordinate descent: from the setting `start` (knob name -> value),
+    try every other value of one knob at a time, keep a change when
+    measure(setting) -- a time, lower is better -- improves, and repeat the
+    sweep while a pass still changes something (at most `passes` sweeps).
+    Each distinct setting is measured once.  Returns (best setting, its
+    time, [setting with ms_per_frame, ...] in measurement order)."""
+    measured = {}
+    results = []
+
+    def cost(setting):
+        key = tuple(sorted(setting.items()))
+        if key not in measured:
+            measured[key] = measure(setting)
+            results.append(dict(setting, ms_per_frame=measured[key]))
+        return measured[key]
+
+    best = dict(start)
+    best_ms = cost(best)
+    for _ in range(passes):
+        changed = False
+        for name, _, values in knobs:
+            for v in values:
+                if v == best[name]:
+                    continue
+                cand = dict(best, **{name: v})
+                ms = cost(cand)
+                if ms < best_ms:
+                    best, best_ms, changed = cand, ms, True
+        if not changed:
+            break
+    return best, best_ms, results
+
+
 def tune(scene, camera, lighting, frames=3, passes=2, knobs=KNOBS, verbose=False):
+    """descend() over real frames of the caller's scene, timed with CUDA
+    events on the render stream after one warm-up frame per setting; leaves
+    the library set to the best setting."""
     import torch
     stream = torch.cuda.current_stream()
     cam = camera.c() if hasattr(camera, "c") else camera
     fb = torch.zeros((cam.height, cam.width, 4), dtype=torch.float32, device="cuda")
-    measured = {}
-    results = []
 
     def measure(setting):
-        key = tuple(sorted(setting.items()))
-        if key in measured:
-            return measured[key]
         apply(setting)
         fb.zero_()
         scene.render(cam, lighting, fb.data_ptr(), stream.cuda_stream)
@@ -77,26 +109,11 @@ def tune(scene, camera, lighting, frames=3, passes=2, knobs=KNOBS, verbose=False
         e1.record(stream)
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1) / frames
-        measured[key] = ms
-        results.append(dict(setting, ms_per_frame=ms))
         if verbose:
-            print("autotune", results[-1], flush=True)
+            print("autotune", dict(setting, ms_per_frame=ms), flush=True)
         return ms
 
-    best = current()
-    best_ms = measure(best)
-    for _ in range(passes):
-        changed = False
-        for name, _, values in knobs:
-            for v in values:
-                if v == best[name]:
-                    continue
-                cand = dict(best, **{name: v})
-                ms = measure(cand)
-                if ms < best_ms:
-                    best, best_ms, changed = cand, ms, True
-        if not changed:
-            break
+    best, best_ms, results = descend(measure, current(), knobs, passes)
     apply(best)
     return {"best": dict(best, ms_per_frame=best_ms), "candidates": results}
 

@@ -104,3 +104,32 @@ def test_tf_resample_edges():
     op = np.ctypeslib.as_array(tf.opacities)
     assert op[0] == 0.0 and op[-1] == 0.0 and abs(op[127] - 0.996) < 0.01
     assert list(tf.range) == [0.0, 1.0]
+
+
+def test_autotune_descent_finds_the_separable_optimum():
+    """The autotuner's search (autotune.descend) on a synthetic cost with a
+    known optimum: a sum of one term per knob reaches it in one sweep plus
+    a confirming one, measures each setting once, and reports the best."""
+    from galaxy_gb300 import autotune
+    knobs = (("a", 1, (1, 2, 3)), ("b", 2, (8, 16, 32)), ("c", 3, (0, 1)))
+    target = {"a": 3, "b": 8, "c": 1}
+    calls = []
+
+    def measure(s):
+        calls.append(dict(s))
+        return sum(abs(knobs[i][2].index(s[n]) - knobs[i][2].index(target[n])) + 1.0
+                   for i, (n, _, _) in enumerate(knobs))
+
+    best, ms, results = autotune.descend(measure, {"a": 1, "b": 16, "c": 0}, knobs, passes=3)
+    assert best == target and ms == 3.0
+    keys = [tuple(sorted(c.items())) for c in calls]
+    assert len(keys) == len(set(keys)) == len(results)
+    assert min(r["ms_per_frame"] for r in results) == ms
+
+
+def test_autotune_descent_keeps_start_when_nothing_is_faster():
+    from galaxy_gb300 import autotune
+    knobs = (("a", 1, (1, 2)), ("b", 2, (4, 8)))
+    best, ms, results = autotune.descend(lambda s: 5.0 if s == {"a": 2, "b": 8} else 9.0,
+                                         {"a": 2, "b": 8}, knobs)
+    assert best == {"a": 2, "b": 8} and ms == 5.0 and len(results) == 3
