@@ -133,3 +133,35 @@ def test_autotune_descent_keeps_start_when_nothing_is_faster():
     best, ms, results = autotune.descend(lambda s: 5.0 if s == {"a": 2, "b": 8} else 9.0,
                                          {"a": 2, "b": 8}, knobs)
     assert best == {"a": 2, "b": 8} and ms == 5.0 and len(results) == 3
+
+
+def test_poisson_requests_are_seeded_and_shaped():
+    """Serving arrivals: Poisson at the given rate (mean gap 1/rate),
+    image sides log-uniform within the range, deterministic per seed."""
+    from galaxy_gb300 import serve
+
+    def make(rng, rid, t, key, side):
+        return (rid, t, key, side)
+
+    a = serve.poisson_requests(200.0, 4000, ["x", "y"], make, seed=3, side_range=(256, 4096))
+    b = serve.poisson_requests(200.0, 4000, ["x", "y"], make, seed=3, side_range=(256, 4096))
+    assert a == b
+    t = np.array([r[1] for r in a])
+    assert np.all(np.diff(t) > 0)
+    assert abs(np.mean(np.diff(t)) - 1 / 200.0) < 0.1 / 200.0
+    sides = np.array([r[3] for r in a])
+    assert sides.min() >= 256 and sides.max() <= 4096
+    # log-uniform: about half the sides below the geometric mean 1024
+    assert 0.45 < np.mean(sides < 1024) < 0.55
+    assert {r[2] for r in a} == {"x", "y"}
+
+
+def test_serving_summary():
+    from types import SimpleNamespace as R
+    from galaxy_gb300 import serve
+    reqs = [R(arrival=0.0, t_done=0.010 * (i + 1), rays=100, refused=False) for i in range(100)]
+    reqs.append(R(arrival=0.0, t_done=None, rays=0, refused=True))
+    s = serve.summarize(reqs, makespan=2.0)
+    assert s["requests"] == 101 and s["completed"] == 100 and s["refused"] == 1
+    assert s["rays"] == 10000 and s["rays_per_s"] == 5000.0
+    assert abs(s["p50_ms"] - 505.0) < 1e-6 and abs(s["p99_ms"] - 990.1) < 1e-6
