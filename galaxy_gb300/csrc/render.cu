@@ -1375,7 +1375,9 @@ __global__ void __launch_bounds__(kThreads, MINB) k_sec_query(DevScene S, FrameA
                     A.qmarch_hit ? __int_as_float(__ldg(reinterpret_cast<const int *>(
                                                       (idx < ns ? A.qin[Q_SHADOW] + idx : A.qin[Q_AO] + (idx - ns))) + 15))
                                  : 0.0f;
-                // a zero payload is culled whatever the query finds: no traversal
+                // no traversal for a zero payload (culled whatever the query
+                // finds) or a slice surface inside a clear segment (the ray
+                // ends there, see the shortcut above)
                 if (zero || (surface && stop_below > -INFINITY)) {
                     done = true;
                 } else if (carried > 0.0f) {
