@@ -165,3 +165,21 @@ def test_serving_summary():
     assert s["requests"] == 101 and s["completed"] == 100 and s["refused"] == 1
     assert s["rays"] == 10000 and s["rays_per_s"] == 5000.0
     assert abs(s["p50_ms"] - 505.0) < 1e-6 and abs(s["p99_ms"] - 990.1) < 1e-6
+
+
+def test_algorithmic_bytes_of_a_generation():
+    """The roofline's per-launch byte model: 64 B per record read and
+    written, 128 B per node line, 48 B per triangle and 16 B per sphere
+    tested, 4 B per sample read (positions in clear bricks read nothing),
+    32 B per framebuffer contribution."""
+    import importlib.util
+    import os
+    spec = importlib.util.spec_from_file_location(
+        "bench_mod", os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "bench.py"))
+    bench = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(bench)
+    g = {"rays_in": 10, "enqueued": 3, "nodes": 7, "tri_tests": 2, "sph_tests": 5, "samples": 100,
+         "samples_skipped": 60, "terminated": 4}
+    assert bench.algorithmic_bytes(g) == 64 * 13 + 128 * 7 + 48 * 2 + 16 * 5 + 4 * 40 + 32 * 4
+    g.pop("samples_skipped")
+    assert bench.algorithmic_bytes(g) == 64 * 13 + 128 * 7 + 48 * 2 + 16 * 5 + 4 * 100 + 32 * 4
