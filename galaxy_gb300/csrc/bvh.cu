@@ -412,6 +412,8 @@ __global__ void k_collapse(DevScene S, const float *sph_radius, int n, const int
         } else {
             int f = r >= 0 ? first[r] : ~r;
             int cnt = size_of(r);
+            // (cnt <= 4 and poff < 32 keep a filled slot's byte below 0x80;
+            // the traversal reads bit 7 of the meta bytes as "empty slot")
             nd.meta[k] = (uint8_t)(((cnt - 1) << 5) | poff);
             for (int j = 0; j < cnt; j++) write_slot(S, sph_radius, ids[f + j], slots, pbase + poff + j);
             poff += cnt;
