@@ -116,9 +116,11 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def cpu_baseline(cam, vis, target_s=15.0, threads=None):
-    """The oracle (CPU restatement of Galaxy's path) on a band of image rows
-    around the middle of the image, sized to about target_s seconds."""
+def cpu_baseline(cam, vis, target_s=10.0, threads=None):
+    """The oracle (CPU restatement of Galaxy's path) on the host cores:
+    whole frames of the workload, repeated until about target_s seconds of
+    CPU work.  Returns the baseline record, the oracle scene, the resolved
+    lighting and the first frame (the parity reference of the GPU frame)."""
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     import oracle_lib as O
     from galaxy_gb300 import scene as S
@@ -127,22 +129,39 @@ def cpu_baseline(cam, vis, target_s=15.0, threads=None):
     t0 = time.time()
     osc = O.OracleScene(vis)
     setup = time.time() - t0
-    mid = cam.height // 2
-    rows = max(4, threads)
-    # probe band, then size the sample to target_s
-    r0 = mid - rows // 2
-    t0 = time.time()
-    _, c = osc.render(cam, L, nthreads=threads, rows=(r0, r0 + rows))
-    dt = max(time.time() - t0, 1e-3)
-    rows2 = int(min(cam.height, max(rows, rows * target_s / dt)))
-    r0 = max(0, mid - rows2 // 2)
-    t0 = time.time()
-    _, c = osc.render(cam, L, nthreads=threads, rows=(r0, r0 + rows2))
-    dt = time.time() - t0
-    rays = c["primary"] + c["shadow"] + c["ao"]
+    frames, rays, dt, first, counts = 0, 0, 0.0, None, None
+    while frames == 0 or (dt < target_s and frames < 50):
+        t0 = time.time()
+        fb, c = osc.render(cam, L, nthreads=threads)
+        dt += time.time() - t0
+        if first is None:
+            first, counts = fb, c
+        frames += 1
+        rays += c["primary"] + c["shadow"] + c["ao"]
     return {"value": rays / dt, "unit": "rays/s", "cores": threads, "kind": "port",
-            "sample": "rows %d-%d of %dx%d (%d rays, %.1f s; scene set-up %.1f s excluded)" % (
-                r0, r0 + rows2, cam.width, cam.height, rays, dt, setup), "seconds": dt}, osc, L
+            "sample": "%d whole %dx%d frame(s), %d rays, %.1f s (scene set-up %.1f s excluded)" % (
+                frames, cam.width, cam.height, rays, dt, setup), "seconds": dt / frames,
+            "frames": frames}, osc, L, first, counts
+
+
+PARITY_RMSE = 1e-3      # image RMSE bound of the workloads (RGB, fp32 framebuffer)
+PARITY_CH = 2.0 / 255   # per-channel bound, met by 99.9 % of channels
+
+
+def parity(img, ref, gpu_counts, ref_counts):
+    """GPU frame against the oracle frame of the same camera and lighting."""
+    d = np.abs(img[..., :3].astype(np.float64) - ref[..., :3].astype(np.float64))
+    rmse = float(np.sqrt(np.mean(d ** 2)))
+    within = float(np.mean(d <= PARITY_CH))
+    q = lambda a: (np.trunc(255.0 * a.astype(np.float32)).astype(np.int64) & 0xff)   # ColorImageWriter bytes
+    dq = np.abs(q(img[..., :3]) - q(ref[..., :3]))
+    rays = {"gpu": {k: int(gpu_counts[k + "_rays"]) for k in ("primary", "shadow", "ao")},
+            "oracle": {k: int(ref_counts[k]) for k in ("primary", "shadow", "ao")}}
+    return {"against": "oracle frame of the same camera and lighting (whole image)",
+            "rmse": rmse, "max_abs": float(d.max()), "frac_within_2_255": within,
+            "png_bytes_equal": float(np.mean(dq == 0)), "png_max_byte_diff": int(dq.max()),
+            "rays": rays, "tolerance": {"rmse": PARITY_RMSE, "channel": PARITY_CH, "channel_frac": 0.999},
+            "pass": bool(rmse <= PARITY_RMSE and within >= 0.999)}
 
 
 def dist_setup(n_gpus):
@@ -177,54 +196,72 @@ def run_reference(args):
     if rank != 0:
         return
     cam, vis, cfg = make_workload(args.workload)
+    if args.image:
+        cam.width = cam.height = args.image
+        cfg = dict(cfg, image=[args.image, args.image], workload=cfg["workload"] + " (image %d^2)" % args.image)
     threads = os.cpu_count() or 1
-    per_step = max(2.0, 90.0 / max(1, args.steps + args.warmup))
-    # the first call sizes the row band; every step then renders that band
-    base, osc, L = cpu_baseline(cam, vis, target_s=per_step, threads=threads)
-    band = [int(x) for x in base["sample"].split()[1].split("-")]
+    # every step renders the whole frame of the workload on all host cores
+    base, osc, L, _, _ = cpu_baseline(cam, vis, target_s=0.0, threads=threads)
     vals, secs = [], []
     for i in range(args.warmup + args.steps):
         t0 = time.time()
-        _, c = osc.render(cam, L, nthreads=threads, rows=(band[0], band[1]))
+        _, c = osc.render(cam, L, nthreads=threads)
         dt = time.time() - t0
         if i >= args.warmup:
             vals.append((c["primary"] + c["shadow"] + c["ao"]) / dt)
             secs.append(dt)
     v = float(np.median(vals))
-    base["seconds"] = float(np.median(secs))
+    sample = "whole %dx%d frame per step (%d steps, median)" % (cam.width, cam.height, args.steps)
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "rays/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": base["seconds"] * 1e3,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": float(np.median(secs)) * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic", "config": cfg,
-            "cpu_baseline": {"value": v, "unit": "rays/s", "cores": threads, "kind": "port",
-                             "sample": base["sample"]},
+            "cpu_baseline": {"value": v, "unit": "rays/s", "cores": threads, "kind": "port", "sample": sample},
             "e2e": {"value": v, "unit": "rays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
 
-def run_serve(args):
-    """Serving workload: Poisson arrivals over two resident scenes (the
-    partitioned mixed scene and a 10M-triangle displaced-sphere mesh); each
-    request a random camera on a sphere around the scene and a random light
-    direction, image side log-uniform in [256, 4096].  The requests are
-    served by the continuous-batching loop and, separately, one at a time
-    through the plain path; both report rays/s and p50/p95/p99 latency."""
-    import copy
-    import torch
-    from galaxy_gb300 import gpu, scenes, serve
+def serve_table(vis_m=None, sc_m=None):
+    """The serving workload's resident scenes: the partitioned mixed scene
+    (committed here unless given) and a 10M-triangle displaced-sphere mesh;
+    returns (scene table, visualizations, commit seconds)."""
+    from galaxy_gb300 import gpu, scenes
     from galaxy_gb300 import scene as S
-    torch.cuda.set_device(0)
-    gpu.init(0)
-    cam_m, vis_m = scenes.mixed_scene()
+    t0 = time.time()
+    if vis_m is None:
+        vis_m = scenes.mixed_scene()[1]
     mesh = scenes.displaced_sphere_mesh(10_000_000)
     L = S.Lighting()
     L.lights, L.types, L.shadows, L.n_ao, L.ao_radius = [(-0.577, -0.577, -0.577)], [0], True, 2, 0.05
     vis_t = S.Visualization([S.TrianglesVis(mesh, colormap=scenes.COOLWARM)], L, box=(0, 0, 0, 1, 1, 1))
-    t0 = time.time()
-    table = {"mixed": gpu.Scene(vis_m), "mesh": gpu.Scene(vis_t)}
-    commit_s = time.time() - t0
-    viss = {"mixed": vis_m, "mesh": vis_t}
-    lo, hi = args.side_min, args.side_max
+    table = {"mixed": sc_m if sc_m is not None else gpu.Scene(vis_m), "mesh": gpu.Scene(vis_t)}
+    return table, {"mixed": vis_m, "mesh": vis_t}, time.time() - t0
+
+
+def serve_compare(table, viss, rate, n_requests, side_min=256, side_max=4096, slots=3, coop=False,
+                  time_limit=120.0, check=6):
+    """Poisson arrivals at `rate` over the resident scenes; each request a
+    random camera on a sphere around the scene plus, with probability 1/3
+    each, a random transfer-function change or a random light direction;
+    image side log-uniform in [side_min, side_max].  The requests are served
+    by the continuous-batching loop and, separately, one at a time through
+    the plain path; both report rays/s and p50/p95/p99 latency, and the
+    images of `check` requests are compared between the two paths."""
+    import copy
+    import torch
+    from galaxy_gb300 import gpu, scenes, serve
+    from galaxy_gb300 import scene as S
+
+    def random_tf(rng, key):
+        if key == "mixed":
+            op = copy.copy(viss[key].operators[0])
+            a = float(rng.uniform(0.1, 0.5))
+            op.opacitymap = [(0.0, 0.0), (a, 0.0), (1.0, float(rng.uniform(0.4, 1.0)))]
+            op.colormap = [tuple([c[0]] + list(np.roll(c[1:], int(rng.integers(0, 3))))) for c in op.colormap]
+            return [(gpu.VIS_VOLUME, 0, op.tf())]
+        op = copy.copy(viss[key].operators[0])
+        op.colormap = [(c[0],) + tuple(float(x) for x in rng.uniform(0, 1, 3)) for c in op.colormap]
+        return [(gpu.VIS_TRIANGLES, 0, op.tf())]
 
     def make(rng, rid, arrival, key, side):
         th, ph = rng.uniform(0.2, 1.3), rng.uniform(0, 2 * np.pi)
@@ -232,50 +269,73 @@ def run_serve(args):
         eye = (0.5 + dist * np.sin(th) * np.cos(ph), 0.5 + dist * np.cos(th), 0.5 + dist * np.sin(th) * np.sin(ph))
         cam = S.Camera(eye, (0.5 - eye[0], 0.5 - eye[1], 0.5 - eye[2]), (0, 1, 0), 35.0, side, side)
         lit = copy.copy(viss[key].lighting)
-        d = rng.normal(size=3)
-        d = -np.abs(d) / np.linalg.norm(d)
-        lit.lights, lit.types = [tuple(float(x) for x in d)], [0]
-        return serve.Request(rid, arrival, key, cam, S.resolve_lights(lit, cam).c())
+        change = int(rng.integers(0, 3))      # 0 camera only, 1 + transfer function, 2 + light
+        tf = random_tf(rng, key) if change == 1 else None
+        if change == 2:
+            d = rng.normal(size=3)
+            d = -np.abs(d) / np.linalg.norm(d)
+            lit.lights, lit.types = [tuple(float(x) for x in d)], [0]
+        return serve.Request(rid, arrival, key, cam, S.resolve_lights(lit, cam).c(), tf=tf)
 
-    reqs = serve.poisson_requests(args.rate, args.requests, ["mixed", "mesh"], make, side_range=(lo, hi))
-    # warm-up (not timed): one small request of each scene on both paths
-    warm = [make(np.random.default_rng(1), i, 0.0, k, 256) for i, k in enumerate(["mixed", "mesh"])]
-    serve.serve_plain(table, [copy.copy(w) for w in warm])
-    slot_pixels = hi * hi
-    srv = serve.Server(table, n_slots=args.slots, slot_pixels=slot_pixels, max_jobs=64, max_shadow=1, max_ao=4,
-                       fb_budget=16 << 30, use_graph=True, cooperative=args.coop)
+    defaults = {"mixed": [(gpu.VIS_VOLUME, 0, viss["mixed"].operators[0].tf()),
+                          (gpu.VIS_PARTICLES, 0, viss["mixed"].operators[1].tf())],
+                "mesh": [(gpu.VIS_TRIANGLES, 0, viss["mesh"].operators[0].tf())]}
+    keys = sorted(table)
+    reqs = serve.poisson_requests(rate, n_requests, keys, make, side_range=(side_min, side_max))
+    # warm-up (not timed): small requests of each scene on both paths, with and without a TF change
+    wr = np.random.Generator(np.random.Philox(1))
+    warm = [make(wr, 10_000 + i, 0.0, k, 256) for i, k in enumerate(keys * 3)]
+    serve.serve_plain(table, [copy.copy(w) for w in warm], default_tfs=defaults)
+    slot_pixels = side_max * side_max
+    srv = serve.Server(table, n_slots=slots, slot_pixels=slot_pixels, max_jobs=64, max_shadow=1, max_ao=4,
+                       fb_budget=16 << 30, use_graph=True, cooperative=coop)
     srv.run([copy.copy(w) for w in warm])
+    keep = {r.id for r in reqs if r.camera.width <= 2048}
+    keep = set(sorted(keep)[:check])
     served_reqs = [copy.copy(r) for r in reqs]
     plain_reqs = [copy.copy(r) for r in reqs]
-    served = srv.run(served_reqs, time_limit=args.time_limit)
+    served = srv.run(served_reqs, time_limit=time_limit, keep=keep)
     srv.release()
     torch.cuda.synchronize()
-    plain = serve.serve_plain(table, plain_reqs, time_limit=args.time_limit)
-    # served vs plain images on a sample of the requests (same camera/light)
-    rmse = 0.0
-    chk = gpu.Batch(slot_pixels, 8, 1, 4)
-    for r in reqs[: min(6, len(reqs))]:
-        fa = torch.zeros((r.camera.height, r.camera.width, 4), device="cuda")
-        fb_ = torch.zeros_like(fa)
-        torch.cuda.synchronize()
-        chk.submit([(table[r.scene], r.camera, r.lighting, fa.data_ptr())], use_graph=True, cooperative=args.coop)
-        chk.wait(120000)
-        table[r.scene].render(r.camera, r.lighting, fb_.data_ptr(), torch.cuda.current_stream().cuda_stream)
-        torch.cuda.synchronize()
-        rmse = max(rmse, float(torch.sqrt(torch.mean((fa[..., :3] - fb_[..., :3]) ** 2)).item()))
-    chk.release()
+    plain = serve.serve_plain(table, plain_reqs, time_limit=time_limit, keep=keep, default_tfs=defaults)
+    rmse, max_abs, checked = 0.0, 0.0, 0
+    for a, b in zip(served_reqs, plain_reqs):
+        if a.id in keep and a.fb is not None and b.fb is not None:
+            d = np.abs(a.fb[..., :3] - b.fb[..., :3])
+            rmse = max(rmse, float(np.sqrt(np.mean(d ** 2))))
+            max_abs = max(max_abs, float(d.max()))
+            checked += 1
+    kinds = {"camera": sum(1 for r in reqs if r.tf is None), "transfer_function": sum(1 for r in reqs if r.tf)}
+    return {"rate": rate, "requests": n_requests, "slots": slots, "slot_pixels": slot_pixels,
+            "side_range": [side_min, side_max], "request_kinds": kinds,
+            "served": served, "plain": plain,
+            "served_over_plain_rays_per_s": served["rays_per_s"] / max(1e-9, plain["rays_per_s"]),
+            "latency_ms": {"served": {k: served.get(k + "_ms") for k in ("p50", "p95", "p99")},
+                           "plain": {k: plain.get(k + "_ms") for k in ("p50", "p95", "p99")}},
+            "images_served_vs_plain": {"requests": checked, "max_rmse": rmse, "max_abs": max_abs,
+                                       "pass": bool(checked > 0 and rmse <= PARITY_RMSE)}}
+
+
+def run_serve(args):
+    """Serving workload (--mode serve): Poisson arrivals over the partitioned
+    mixed scene and a 10M-triangle mesh, served by the continuous-batching
+    loop and one at a time through the plain path."""
+    import torch
+    from galaxy_gb300 import gpu
+    torch.cuda.set_device(0)
+    gpu.init(0)
+    table, viss, commit_s = serve_table()
+    res = serve_compare(table, viss, args.rate, args.requests, args.side_min, args.side_max, args.slots,
+                        args.coop, args.time_limit)
+    served = res["served"]
     out = {"metric": METRIC, "value": served["rays_per_s"], "unit": "rays/s", "n_gpus": 1,
-           "steps": args.requests, "warmup": len(warm), "higher_is_better": True, "scaling": "weak",
+           "steps": args.requests, "warmup": 6, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
            "config": {"workload": "serving: Poisson %.0f req/s over the partitioned mixed scene and a 10M-triangle "
-                                  "mesh, random camera + light per request, image side log-uniform %d..%d"
-                                  % (args.rate, lo, hi), "rate": args.rate, "requests": args.requests,
-                      "slots": args.slots, "slot_pixels": slot_pixels},
-           "served": served, "plain": plain,
-           "served_over_plain_rays_per_s": served["rays_per_s"] / max(1e-9, plain["rays_per_s"]),
-           "latency_ms": {k: served.get(k + "_ms") for k in ("p50", "p95", "p99")},
-           "rmse_served_vs_plain": rmse,
-           "scene_commit_s": commit_s}
+                                  "mesh, random camera + transfer-function or light change per request, image side "
+                                  "log-uniform %d..%d" % (args.rate, args.side_min, args.side_max),
+                      "rate": args.rate, "requests": args.requests, "slots": args.slots},
+           "served_vs_plain": res, "scene_commit_s": commit_s}
     print(json.dumps(out), flush=True)
 
 
@@ -352,7 +412,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="mixed", choices=["mixed", "volume", "triangles"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--image", type=int, default=0, help="override the image side (smaller profiling cases)")
     ap.add_argument("--mode", default="frame", choices=["frame", "serve", "batch"])
     ap.add_argument("--jobs", type=int, default=64, help="batch mode: number of render jobs")
@@ -363,6 +423,10 @@ def main():
     ap.add_argument("--side-max", type=int, default=4096)
     ap.add_argument("--time-limit", type=float, default=120.0)
     ap.add_argument("--coop", action="store_true", help="serve with cooperative single-launch batches")
+    ap.add_argument("--serve-rate", type=float, default=800.0,
+                    help="frame mode: arrival rate of the bounded served-vs-plain comparison")
+    ap.add_argument("--serve-requests", type=int, default=60,
+                    help="frame mode: requests of the served-vs-plain comparison (0: skip it)")
     ap.add_argument("--no-autotune", dest="autotune", action="store_false",
                     help="skip the autotuner (occupancy, grid size, split tracing) before timing")
     ap.add_argument("--tune", default="", help="fixed tuning 'blocks_per_sm,grid_per_sm,split' (implies --no-autotune)")
@@ -534,12 +598,25 @@ def main():
            "scene_commit_s": commit_s, "bvh": sc.bvh_info(),
            "gpu_launches": launches, "roofline": roof, "e2e": e2e, "clocks": clk,
            "tuning": dict(tuning if tuning else {"best": autotune.current()}, bvh=bvh_tuning)}
+    # ---- the metric's served-vs-plain comparison (bounded serving run over
+    # this scene and a 10M-triangle mesh)
+    if rank == 0 and args.workload == "mixed" and args.serve_requests > 0 and not args.image:
+        table, viss, _ = serve_table(vis_m=vis, sc_m=sc)
+        out["served_vs_plain"] = serve_compare(table, viss, args.serve_rate, args.serve_requests)
+        table["mesh"].release()
+        del table
+    parity_ok = True
     if rank == 0 and not args.no_cpu_baseline:
-        base, _, _ = cpu_baseline(cam, vis, target_s=args.cpu_seconds)
+        base, _, _, ref_img, ref_counts = cpu_baseline(cam, vis, target_s=args.cpu_seconds)
         base.pop("seconds", None)
         out["cpu_baseline"] = base
+        # the last end-to-end frame (host framebuffer) against the oracle's
+        out["parity"] = parity(host_fb, ref_img, c, ref_counts)
+        parity_ok = out["parity"]["pass"]
     if rank == 0:
         print(json.dumps(out), flush=True)
+    if not parity_ok:
+        sys.exit("parity failed: GPU frame differs from the oracle frame beyond the stated tolerance")
 
 
 def ctypes_size(t):

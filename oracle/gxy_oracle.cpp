@@ -1073,8 +1073,35 @@ static void trace_one(const Scene &S, int part, Rays &R, int i, Stats *st, doubl
 }
 
 // TraceRays::Trace (TraceRays.cpp:68-146) with GXY_REVERSE_LIGHTING.
+// Worker threads of the RayList entry points (oracle_set_threads); the
+// per-ray trace has no shared state, so rays are split into chunks.
+static int g_threads = 1;
+template <class F> static void parallel_rays(int n, F f) {
+    const int nt = std::max(1, std::min(g_threads, n / 256 + 1));
+    if (nt == 1) {
+        for (int i = 0; i < n; i++) f(i);
+        return;
+    }
+    std::atomic<int> next{0};
+    std::vector<std::thread> th;
+    for (int t = 0; t < nt; t++)
+        th.emplace_back([&]() {
+            for (;;) {
+                const int a = next.fetch_add(1024);
+                if (a >= n) break;
+                const int b = std::min(n, a + 1024);
+                for (int i = a; i < b; i++) f(i);
+            }
+        });
+    for (auto &t : th) t.join();
+}
+
 static void trace_list(const Scene &S, int part, const gxy_lighting &L, Rays &in, Rays &out, Stats *st) {
-    for (int i = 0; i < in.n; i++) trace_one<float>(S, part, in, i, st);
+    if (st) {
+        for (int i = 0; i < in.n; i++) trace_one<float>(S, part, in, i, st);
+    } else {
+        parallel_rays(in.n, [&](int i) { trace_one<float>(S, part, in, i, nullptr); });
+    }
     const float eps = S.desc.epsilon;
     int n = in.n;
     std::vector<int> ao_off(n), sh_off(n, -1);
@@ -1408,9 +1435,12 @@ int oracle_trace_f64(void *sp, int part, gxy_raylist *in, double *rgba64) {
     Scene *s = (Scene *)sp;
     Rays R;
     rays_from_c(*in, R);
-    for (int i = 0; i < R.n; i++) trace_one<double>(*s, part, R, i, nullptr, rgba64 + 4 * i);
+    parallel_rays(R.n, [&](int i) { trace_one<double>(*s, part, R, i, nullptr, rgba64 + 4 * i); });
     return 0;
 }
+
+// Threads used by oracle_trace_raylist and oracle_trace_f64 (default 1).
+void oracle_set_threads(int n) { g_threads = n < 1 ? 1 : n; }
 
 int oracle_classify(gxy_raylist *rl) {
     Rays R;

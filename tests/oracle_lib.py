@@ -44,6 +44,8 @@ def lib():
         L.oracle_tf_opacity.restype = C.c_float
         L.oracle_tf_opacity.argtypes = [C.POINTER(A.gxy_tf), C.c_float]
         L.oracle_quantize.argtypes = [A.f32p, C.c_int, C.c_int, C.POINTER(C.c_uint8)]
+        L.oracle_set_threads.argtypes = [C.c_int]
+        L.oracle_set_threads(os.cpu_count() or 1)
         _lib = L
     return _lib
 
