@@ -3272,7 +3272,9 @@ int gxy_gpu_batch_counters(gxy_batch batch, gxy_counters *out) {
 // memory.  Its scratch -- one flag and one output offset per pixel plus the
 // scan's temporary storage -- is the fixed array below, part of this
 // library's device image: every GPU that loads the library holds it until the
-// process exits, and every call on that GPU shares it.
+// process exits, and every call on that GPU shares it.  All of a call's work
+// goes to the calling thread's per-thread default stream, which the call
+// synchronises before it returns.
 namespace gxy {
 
 constexpr int64_t kNoAllocMaxPixels = int64_t(1) << 20;   // 1024 x 1024 camera pixels
@@ -3290,12 +3292,24 @@ static unsigned char *g_noalloc_addr[kNoAllocMaxDevices];
 // Device address of g_noalloc_scratch on the current device.  In host code
 // the symbol names a host-side stand-in, not device memory, so the address is
 // looked up with cudaGetSymbolAddress, once per device with that device
-// current, on the first call there.
+// current, on the first call there (which also loads this library's device
+// code on that device, the array included, under lazy module loading).  A
+// cached address is re-validated on every call: after a cudaDeviceReset the
+// module is loaded afresh and the old address no longer names device memory
+// of this device, so it is looked up again.
 static int noalloc_scratch(unsigned char **out) {
     int dev = -1;
     CK(cudaGetDevice(&dev));
     if (dev < 0 || dev >= kNoAllocMaxDevices) return set_error(GXY_ERR_INVALID, "device ordinal out of range");
     std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (g_noalloc_addr[dev]) {
+        cudaPointerAttributes a;
+        if (cudaPointerGetAttributes(&a, g_noalloc_addr[dev]) != cudaSuccess || a.type != cudaMemoryTypeDevice ||
+            a.device != dev) {
+            cudaGetLastError();
+            g_noalloc_addr[dev] = nullptr;
+        }
+    }
     if (!g_noalloc_addr[dev]) {
         void *p = nullptr;
         CK(cudaGetSymbolAddress(&p, g_noalloc_scratch));
@@ -3320,6 +3334,57 @@ static bool gpu_addressable(const void *p, int dev) {
     return false;
 }
 
+// True if the `bytes` bytes from `p` are GPU-addressable from device `dev`:
+// both ends pass gpu_addressable and, for device and managed memory, the
+// range lies inside the one allocation that holds `p` (cuMemGetAddressRange,
+// taken through the runtime's driver entry points, so no driver library is
+// linked).
+static bool gpu_range_ok(const void *p, size_t bytes, int dev) {
+    if (!gpu_addressable(p, dev)) return false;
+    if (bytes == 0) return true;
+    const char *last = static_cast<const char *>(p) + (bytes - 1);
+    if (!gpu_addressable(last, dev)) return false;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    if (a.type == cudaMemoryTypeHost) return true;
+    typedef int (*range_fn)(unsigned long long *, size_t *, unsigned long long);
+    static range_fn fn = nullptr;
+    static bool looked = false;
+    {
+        std::lock_guard<std::mutex> lock(g_noalloc_mu);
+        if (!looked) {
+            void *f = nullptr;
+            cudaDriverEntryPointQueryResult q;
+            if (cudaGetDriverEntryPointByVersion("cuMemGetAddressRange", &f, 3020, cudaEnableDefault, &q) ==
+                    cudaSuccess &&
+                q == cudaDriverEntryPointSuccess)
+                fn = reinterpret_cast<range_fn>(f);
+            else
+                cudaGetLastError();
+            looked = true;
+        }
+    }
+    if (!fn) return true;   // both ends checked above
+    unsigned long long base = 0;
+    size_t size = 0;
+    if (fn(&base, &size, (unsigned long long)(uintptr_t)p) != 0) return false;
+    const unsigned long long lo = (unsigned long long)(uintptr_t)p;
+    return lo >= base && lo - base + bytes <= size;
+}
+
+// Zero the 25 arrays of the first n records (fields the camera pass leaves
+// unset read as zero, as in gxy_gpu_generate_initial_rays); a kernel rather
+// than cudaMemset, so it serves every GPU-addressable memory kind alike.
+__global__ void k_rl_zero(RLDev O, int n) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    for (int k = 0; k < 20; k++) O.f[k][i] = 0.0f;
+    for (int k = 0; k < 5; k++) O.i[k][i] = 0;
+}
+
 }  // namespace gxy
 
 extern "C" int gxy_gpu_generate_initial_rays_noalloc(gxy_scene scene, int partition, const gxy_camera *camera,
@@ -3341,14 +3406,16 @@ extern "C" int gxy_gpu_generate_initial_rays_noalloc(gxy_scene scene, int partit
     int32_t *oi[5];
     host_f(*out, of);
     host_i(*out, oi);
+    // every array must hold out->n records in memory the GPU can write
+    const size_t cap = (size_t)out->n;
     for (int k = 0; k < 20; k++)
-        if (!of[k] || !gpu_addressable(of[k], dev))
+        if (!of[k] || !gpu_range_ok(of[k], cap * sizeof(float), dev))
             return set_error(GXY_ERR_INVALID, "output RayList float array " + std::to_string(k) +
-                                                  " is not memory the GPU can address");
+                                                  " is not memory the GPU can address for its capacity");
     for (int k = 0; k < 5; k++)
-        if (!oi[k] || !gpu_addressable(oi[k], dev))
+        if (!oi[k] || !gpu_range_ok(oi[k], cap * sizeof(int32_t), dev))
             return set_error(GXY_ERR_INVALID, "output RayList int array " + std::to_string(k) +
-                                                  " is not memory the GPU can address");
+                                                  " is not memory the GPU can address for its capacity");
     unsigned char *scratch = nullptr;
     int rc = noalloc_scratch(&scratch);
     if (rc) return rc;
@@ -3356,34 +3423,35 @@ extern "C" int gxy_gpu_generate_initial_rays_noalloc(gxy_scene scene, int partit
     int *pos = reinterpret_cast<int *>(scratch + kNoAllocPosOffset);
     void *scan_tmp = scratch + kNoAllocScanOffset;
     size_t scan_bytes = 0;
-    CK(cub::DeviceScan::ExclusiveSum(nullptr, scan_bytes, flag, pos, (int)n));
+    CK(cub::DeviceScan::ExclusiveSum(nullptr, scan_bytes, flag, pos, (int)n, cudaStreamPerThread));
     if (scan_bytes > kNoAllocScanBytes)
         return set_error(GXY_ERR_OVERFLOW, "scan temporary storage does not fit the fixed scratch");
     // The flag pass writes flag[0, n), the scan writes pos[0, n) and sets up
     // its own temporary storage, so nothing left by an earlier call is read.
+    const cudaStream_t st = cudaStreamPerThread;
     DevCamera C = setup_camera(*camera);
     unsigned g = (unsigned)((n + 255) / 256);
-    k_rl_camera_flags<<<g, 256>>>(sc->S, C, partition, flag);
+    k_rl_camera_flags<<<g, 256, 0, st>>>(sc->S, C, partition, flag);
     CK(cudaGetLastError());
-    CK(cub::DeviceScan::ExclusiveSum(scan_tmp, scan_bytes, flag, pos, (int)n));
-    int last_pos = 0, last_flag = 0;
-    CK(cudaMemcpy(&last_pos, pos + n - 1, sizeof(int), cudaMemcpyDeviceToHost));
-    CK(cudaMemcpy(&last_flag, flag + n - 1, sizeof(int), cudaMemcpyDeviceToHost));
-    int total = last_pos + last_flag;
+    CK(cub::DeviceScan::ExclusiveSum(scan_tmp, scan_bytes, flag, pos, (int)n, st));
+    int last[2] = {0, 0};
+    CK(cudaMemcpyAsync(&last[0], pos + n - 1, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(&last[1], flag + n - 1, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    int total = last[0] + last[1];
     *n_out = total;
     if (total > out->n) return set_error(GXY_ERR_OVERFLOW, "output RayList too small");
     if (total) {
-        // fields the camera pass leaves unset read as zero, as in gxy_gpu_generate_initial_rays
-        for (int k = 0; k < 20; k++) CK(cudaMemset(of[k], 0, (size_t)total * sizeof(float)));
-        for (int k = 0; k < 5; k++) CK(cudaMemset(oi[k], 0, (size_t)total * sizeof(int32_t)));
         RLDev O{};
         for (int k = 0; k < 20; k++) O.f[k] = of[k];
         for (int k = 0; k < 5; k++) O.i[k] = oi[k];
         O.n = total;
-        k_rl_camera_write<<<g, 256>>>(sc->S, C, partition, flag, pos, O);
+        k_rl_zero<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(O, total);
+        CK(cudaGetLastError());
+        k_rl_camera_write<<<g, 256, 0, st>>>(sc->S, C, partition, flag, pos, O);
         CK(cudaGetLastError());
     }
-    CK(cudaStreamSynchronize(0));
+    CK(cudaStreamSynchronize(st));
     return GXY_OK;
     GUARD_END
 }

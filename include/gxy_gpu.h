@@ -449,15 +449,25 @@ int gxy_gpu_accumulate_terminated(const gxy_raylist *rays, float *fb_rgba, int w
  * allocator holds the GPU's memory, where a cudaFree would synchronise the
  * whole device and stall the simulation's streams.  The caller passes the
  * output RayList in memory the GPU can address (device memory of the current
- * device, managed memory, or mapped pinned host memory; all 25 arrays,
- * capacity out->n); the result equals gxy_gpu_generate_initial_rays's.
+ * device, managed memory, or mapped pinned host memory); each of the 25
+ * arrays must hold out->n records -- the whole range is checked before
+ * anything is written (for device and managed memory it must lie inside one
+ * allocation), and a shorter or unaddressable array is refused with
+ * GXY_ERR_INVALID.  The result equals gxy_gpu_generate_initial_rays's.
  * Scratch is a fixed 8.25 MiB array in this library's device image, held on
  * every GPU that loads the library until the process exits.  Images above
- * 1048576 pixels (1024 x 1024) are refused with GXY_ERR_INVALID.  The first
- * call on each device looks up the array's device address (with that device
- * current); make that first call before any stream capture.  All calls on a
- * device share the array, so calls that overlap on the GPU (from several
- * host threads) race: serialise them.  Returns after the rays are written. */
+ * 1048576 pixels (1024 x 1024) are refused with GXY_ERR_INVALID.
+ * The first call on each device looks up the array's device address (with
+ * that device current).  Under CUDA's default lazy module loading that first
+ * call also loads the library's device code there, and with it the 8.25 MiB
+ * array: make the first call (or set CUDA_MODULE_LOADING=EAGER) before the
+ * simulation's allocator reserves the device memory, and before any stream
+ * capture.  Later calls re-check the cached address and look it up again
+ * after a cudaDeviceReset.  All calls on a device share the array, so calls
+ * that overlap on the GPU (from several host threads) race: serialise them.
+ * The work runs on the calling thread's per-thread default stream
+ * (cudaStreamPerThread), so it waits for no other stream except the legacy
+ * default stream, and the call returns after the rays are written. */
 int gxy_gpu_generate_initial_rays_noalloc(gxy_scene scene, int partition, const gxy_camera *camera,
                                           gxy_raylist *out, int32_t *n_out);
 

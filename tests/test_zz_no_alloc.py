@@ -3,11 +3,13 @@
 Some callers may not allocate device memory: a visualization step run in situ
 inside a simulation whose own allocator holds the GPU's memory, where a
 cudaFree would synchronise the whole device and stall the simulation's
-streams.  They pass an output RayList they already hold in device memory, and
-the entry point keeps its scratch in a fixed array inside the library.  These
+streams.  They pass an output RayList they already hold in memory the GPU can
+address (device memory, managed memory or mapped pinned host memory), and the
+entry point keeps its scratch in a fixed array inside the library.  These
 tests call it through the C ABI and compare its rays with those of
 gxy_gpu_generate_initial_rays, bit for bit (the parity tests hold camera rays
-to exact equality), on two calls in a row that share the fixed scratch.
+to exact equality), on two calls in a row that share the fixed scratch, for
+each of the three memory kinds; and check what it refuses.
 
 The file is named to be collected last, so a run that stops at the first
 failure has run every other test before this one.
@@ -52,6 +54,50 @@ def device_raylist(torch, cap):
     return arrs, rl
 
 
+def cudart():
+    """The CUDA runtime the library links (same instance, so its managed and
+    mapped pinned allocations are the ones the library's checks see)."""
+    rt = C.CDLL("libcudart.so.13")
+    rt.cudaMallocManaged.argtypes = [C.POINTER(C.c_void_p), C.c_size_t, C.c_uint]
+    rt.cudaHostAlloc.argtypes = [C.POINTER(C.c_void_p), C.c_size_t, C.c_uint]
+    rt.cudaFree.argtypes = [C.c_void_p]
+    rt.cudaFreeHost.argtypes = [C.c_void_p]
+    rt.cudaDeviceSynchronize.argtypes = []
+    return rt
+
+
+class HostVisibleRayList:
+    """25 arrays of `cap` records in managed memory (kind "managed") or in
+    mapped pinned host memory (kind "pinned"), filled with a sentinel."""
+
+    def __init__(self, kind, cap):
+        self.rt = cudart()
+        self.kind = kind
+        self.ptrs = []
+        self.arrs = {}
+        rl = A.gxy_raylist()
+        for k in A.RAY_FLOAT_FIELDS + A.RAY_INT_FIELDS:
+            p = C.c_void_p()
+            if kind == "managed":
+                assert self.rt.cudaMallocManaged(C.byref(p), cap * 4, 1) == 0   # cudaMemAttachGlobal
+            else:
+                assert self.rt.cudaHostAlloc(C.byref(p), cap * 4, 2) == 0       # cudaHostAllocMapped
+            self.ptrs.append(p.value)
+            isf = k in A.RAY_FLOAT_FIELDS
+            a = np.ctypeslib.as_array(C.cast(p, A.f32p if isf else A.i32p), (cap,))
+            a[:] = np.nan if isf else -7
+            self.arrs[k] = a
+            setattr(rl, k, C.cast(p, A.f32p if isf else A.i32p))
+        rl.n = cap
+        self.rl = rl
+
+    def free(self):
+        self.rt.cudaDeviceSynchronize()
+        for p in self.ptrs:
+            (self.rt.cudaFree if self.kind == "managed" else self.rt.cudaFreeHost)(C.c_void_p(p))
+        self.ptrs = []
+
+
 def call_noalloc(gpu, f, scene, part, cam, rl):
     n = C.c_int32(-1)
     rc = f(scene.h, part, C.byref(cam), C.byref(rl), C.byref(n))
@@ -61,7 +107,8 @@ def call_noalloc(gpu, f, scene, part, cam, rl):
 def assert_same_rays(arrs, ref, n):
     assert ref.n == n
     for k in A.RAY_FLOAT_FIELDS + A.RAY_INT_FIELDS:
-        got = arrs[k][:n].cpu().numpy()
+        got = arrs[k][:n]
+        got = got.cpu().numpy() if hasattr(got, "cpu") else np.array(got)
         want = getattr(ref, k)
         assert got.dtype == want.dtype, k
         assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), k
@@ -123,4 +170,64 @@ def test_noalloc_refuses_what_it_cannot_do(env):
     rc, n = call_noalloc(gpu, f, scene, 0, cam.c(), rl)
     assert rc == A.GXY_OK
     assert_same_rays(arrs, ref, n)
+    del scene
+
+
+@pytest.mark.parametrize("kind", ["managed", "pinned"])
+def test_noalloc_host_visible_memory_twice(env, kind):
+    """The two other memory kinds the entry point accepts: managed memory
+    and mapped pinned host memory, two calls in a row, bit for bit."""
+    torch, gpu, f = env
+    cam_a, vis = scenes.mixed_scene(n=64, n_spheres=4000, width=128, height=96, partitions=(2, 1, 1))
+    cam_b = scenes.mixed_scene(n=64, n_spheres=4000, width=80, height=64, partitions=(2, 1, 1))[0]
+    scene = gpu.Scene(vis)
+    out = HostVisibleRayList(kind, 128 * 96)
+    try:
+        for part, cam in ((0, cam_a.c()), (1, cam_b.c())):
+            ref = scene.generate_initial_rays(part, cam)
+            assert ref.n > 0
+            rc, n = call_noalloc(gpu, f, scene, part, cam, out.rl)
+            assert rc == A.GXY_OK, rc
+            assert_same_rays(out.arrs, ref, n)
+    finally:
+        out.free()
+    del scene
+
+
+def test_noalloc_refuses_capacity_beyond_the_arrays(env):
+    """A capacity larger than the caller's arrays is refused before anything
+    is written: the whole range must lie inside one allocation (arrays of
+    their own cudaMalloc here; a caching allocator's tensors lie inside its
+    larger segments, which is all the check can see)."""
+    torch, gpu, f = env
+    cam, vis = scenes.mixed_scene(n=32, n_spheres=500, width=64, height=48, partitions=(1, 1, 1))
+    scene = gpu.Scene(vis)
+    rt = cudart()
+    rt.cudaMalloc.argtypes = [C.POINTER(C.c_void_p), C.c_size_t]
+    rt.cudaMemcpy.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t, C.c_int]
+    cap = 64
+    sentinel = np.full(cap, np.nan, np.float32)
+    ptrs = []
+    rl = A.gxy_raylist()
+    try:
+        for k in A.RAY_FLOAT_FIELDS + A.RAY_INT_FIELDS:
+            p = C.c_void_p()
+            assert rt.cudaMalloc(C.byref(p), cap * 4) == 0
+            assert rt.cudaMemcpy(p, sentinel.ctypes.data, cap * 4, 1) == 0   # host to device
+            ptrs.append(p)
+            setattr(rl, k, C.cast(p, A.f32p if k in A.RAY_FLOAT_FIELDS else A.i32p))
+        rl.n = 64 * 48
+        rc, _ = call_noalloc(gpu, f, scene, 0, cam.c(), rl)
+        assert rc == A.GXY_ERR_INVALID
+        back = np.zeros(cap, np.float32)
+        assert rt.cudaMemcpy(back.ctypes.data, ptrs[0], cap * 4, 2) == 0     # device to host
+        assert np.isnan(back).all()
+        # the same arrays with their true capacity are accepted
+        rl.n = cap
+        rc, n = call_noalloc(gpu, f, scene, 0, cam.c(), rl)
+        assert rc in (A.GXY_OK, A.GXY_ERR_OVERFLOW)
+    finally:
+        rt.cudaDeviceSynchronize()
+        for p in ptrs:
+            rt.cudaFree(p)
     del scene
