@@ -18,6 +18,7 @@ GXY_ERR_OVERFLOW = -4
 GXY_ERR_TIMEOUT = -5
 GXY_ERR_ADMISSION = -6
 GXY_ERR_NOT_INIT = -7
+GXY_ERR_CANCELLED = -8
 
 RAY_PRIMARY, RAY_SHADOW, RAY_AO, RAY_EMPTY = 0x1, 0x2, 0x4, 0x8
 RAY_SURFACE, RAY_OPAQUE, RAY_BOUNDARY, RAY_TIMEOUT = 0x1, 0x2, 0x4, 0x8
@@ -116,7 +117,7 @@ class gxy_counters(C.Structure):
     _fields_ = [(n, C.c_int64) for n in (
         "primary_rays", "secondary_rays", "shadow_rays", "ao_rays", "segments",
         "handoffs", "terminated", "dropped", "kept", "bounces", "samples", "nodes",
-        "prim_tests")] + [("overflow", C.c_int32), ("pad", C.c_int32), ("samples_skipped", C.c_int64)]
+        "prim_tests")] + [("overflow", C.c_int32), ("bands", C.c_int32), ("samples_skipped", C.c_int64)]
 
 
 def fptr(a):

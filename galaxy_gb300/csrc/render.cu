@@ -189,10 +189,24 @@ static void ao_tables(float4 *out) {
 }
 
 // ================================================================ scene
+// Device buffers of the datasets and the BVH, shared by a committed scene and
+// the views made from it (gxy_gpu_scene_view); freed with the last of them.
+struct SharedBuffers {
+    std::vector<void *> ptrs;
+    ~SharedBuffers() {
+        for (void *p : ptrs) arena().free(p);
+    }
+};
+
 struct Scene {
     DevScene S;
     gxy_partition_info pinfo;
-    std::vector<void *> owned;
+    std::shared_ptr<SharedBuffers> heavy = std::make_shared<SharedBuffers>();
+    std::vector<void *> light;               // this handle's own buffers (TF table, flags, device copy)
+    std::vector<DevTF> tf_host;              // host copy of the TF table S.tfs
+    float *bmax[kMaxVol] = {};               // per volume brick: largest voxel + margin (shared)
+    int64_t n_bricks[kMaxVol] = {};
+    int nbz[kMaxVol] = {};
     BVHInfo bvh;
     static constexpr int kMaxLaunch = 256;   // counter slots per frame
     DevScene *d_scene = nullptr;             // device copy of S (batches)
@@ -203,11 +217,14 @@ struct Scene {
     float4 *pmarch_hit = nullptr;
     size_t pmarch_cap = 0;
     DRay *q[2][3] = {{nullptr, nullptr, nullptr}, {nullptr, nullptr, nullptr}};   // ping-pong x (primary, shadow, AO)
-    size_t qcap[3] = {0, 0, 0};
+    size_t qcap[2][3] = {{0, 0, 0}, {0, 0, 0}};
+    unsigned *rowx = nullptr;           // per image row: camera rays emitted beyond one per pixel
+    size_t rowx_cap = 0;
     unsigned int *qcount = nullptr;     // 2 x 3 queue counters
     DevCounters *ctr = nullptr;         // kMaxLaunch slots, one per launch
     DevCounters last{};
     int64_t bounces = 0;
+    int bands = 1;                      // image-row bands of the last frame
     float *fbtmp = nullptr;
     size_t fbtmp_elems = 0;
     int profile = 0;
@@ -219,7 +236,7 @@ struct Scene {
     cudaEvent_t fork = nullptr, join = nullptr;
     std::mutex mu;                      // one render at a time per scene
     ~Scene() {
-        for (void *p : owned) arena().free(p);
+        for (void *p : light) arena().free(p);
         for (int b = 0; b < 2; b++)
             for (int k = 0; k < 3; k++) arena().free(q[b][k]);
         arena().free(qmarch);
@@ -229,17 +246,30 @@ struct Scene {
         arena().free(qcount);
         arena().free(ctr);
         arena().free(fbtmp);
+        arena().free(rowx);
         for (cudaEvent_t e : events) cudaEventDestroy(e);
         if (fork) cudaEventDestroy(fork);
         if (join) cudaEventDestroy(join);
         if (side) cudaStreamDestroy(side);
-        if (bvh.nodes_ptr) arena().free(bvh.nodes_ptr);
-        if (bvh.slots_ptr) arena().free(bvh.slots_ptr);
     }
+    // dataset buffers (shared with views)
     int upload(const void *src, size_t bytes, void **dst) {
         int rc = arena().alloc(dst, bytes ? bytes : 16);
         if (rc) return rc;
-        owned.push_back(*dst);
+        heavy->ptrs.push_back(*dst);
+        if (bytes) CK(cudaMemcpy(*dst, src, bytes, cudaMemcpyHostToDevice));
+        return GXY_OK;
+    }
+    // this handle's own buffers
+    int alloc_light(void **dst, size_t bytes) {
+        int rc = arena().alloc(dst, bytes ? bytes : 16);
+        if (rc) return rc;
+        light.push_back(*dst);
+        return GXY_OK;
+    }
+    int upload_light(const void *src, size_t bytes, void **dst) {
+        int rc = alloc_light(dst, bytes);
+        if (rc) return rc;
         if (bytes) CK(cudaMemcpy(*dst, src, bytes, cudaMemcpyHostToDevice));
         return GXY_OK;
     }
@@ -404,12 +434,13 @@ __global__ void k_brick_volume(const float *lin, int nx, int ny, int nz, int nbx
     out[e] = lin[((int64_t)z * ny + y) * nx + x];
 }
 
-// Per brick of a bricked volume: 1 when no trilinear sample inside it can
-// reach `below`.  A sample is a convex combination of the brick's voxels, so
-// it exceeds their maximum by at most a few ulps of rounding in the weights
+// Per brick of a bricked volume: an upper bound of every trilinear sample
+// inside it.  A sample is a convex combination of the brick's voxels, so it
+// exceeds their maximum by at most a few ulps of rounding in the weights
 // (margin 1e-5 relative); NaN voxels are left out of the maximum because a
-// sample touching one is NaN, whose opacity is zero.  One warp per brick.
-__global__ void k_brick_clear(const float *bricked, int64_t n_bricks, float below, unsigned char *clear) {
+// sample touching one is NaN, whose opacity is zero.  -inf for a brick of
+// NaN voxels only.  One warp per brick; computed once at commit.
+__global__ void k_brick_max(const float *bricked, int64_t n_bricks, float *bmax) {
     const int64_t b = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (b >= n_bricks) return;       // uniform per warp: blockDim is a multiple of 32
@@ -417,7 +448,16 @@ __global__ void k_brick_clear(const float *bricked, int64_t n_bricks, float belo
     float m = -INFINITY;
     for (int o = lane; o < kBrickSide * kBrickSide * kBrickSide; o += 32) m = fmaxf(m, p[o]);
     for (int s = 16; s > 0; s >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, s));
-    if (lane == 0) clear[b] = (m == -INFINITY) ? (below > -INFINITY) : (m + fabsf(m) * 1e-5f < below);
+    if (lane == 0) bmax[b] = (m == -INFINITY) ? m : m + fabsf(m) * 1e-5f;
+}
+
+// Per brick: 1 when no sample inside it can reach `below` (the transfer
+// function's zero-opacity threshold), i.e. its bound lies below it; a brick
+// of NaN voxels is clear whenever the threshold is above -inf.  Recomputed
+// whenever the volume's transfer function changes.
+__global__ void k_brick_flags(const float *bmax, int64_t n_bricks, float below, unsigned char *clear) {
+    const int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (b < n_bricks) clear[b] = bmax[b] < below;
 }
 
 // Threshold T of a transfer function such that tf_lookup gives opacity
@@ -457,6 +497,18 @@ static float tf_clear_below(const DevTF &t) {
         if (f > T) T = f;
     }
     return T;
+}
+
+// Clear-brick and superbrick flags of volume V for zero-opacity threshold
+// `below`, from the per-brick bounds, on stream st.
+static int volume_flags(const DevVolume &V, const float *bm, int64_t nb, int nbz, float below, cudaStream_t st) {
+    k_brick_flags<<<(unsigned)((nb + 255) / 256), 256, 0, st>>>(bm, nb, below, const_cast<unsigned char *>(V.clear));
+    CK(cudaGetLastError());
+    const int ns = V.nsx * V.nsy * V.nsz;
+    k_superbrick_clear<<<(ns + 127) / 128, 128, 0, st>>>(V.clear, V.nbx, V.nby, nbz, V.nsx, V.nsy, V.nsz,
+                                                         const_cast<unsigned char *>(V.sclear));
+    CK(cudaGetLastError());
+    return GXY_OK;
 }
 
 // Commit-time knob GXY_TUNE_SKIP_CLEAR: build the per-brick clear flags
@@ -507,7 +559,7 @@ static int commit(const gxy_scene_desc *d, Scene *sc) {
             CK(cudaMemcpy(lin, v.samples, nvox * sizeof(float), cudaMemcpyHostToDevice));
             float *bricked;
             if ((rc = arena().alloc((void **)&bricked, (size_t)n_out * sizeof(float)))) return rc;
-            sc->owned.push_back(bricked);
+            sc->heavy->ptrs.push_back(bricked);
             k_brick_volume<<<(unsigned)((n_out + 255) / 256), 256>>>(lin, V.nx, V.ny, V.nz, V.nbx, V.nby, n_out,
                                                                      bricked);
             CK(cudaGetLastError());
@@ -528,24 +580,24 @@ static int commit(const gxy_scene_desc *d, Scene *sc) {
         tfs.push_back(t);
         if (g_tune_skip_clear) {
             const int64_t nb = n_out / kBrickFloats;
-            unsigned char *clear;
-            if ((rc = arena().alloc((void **)&clear, (size_t)nb))) return rc;
-            sc->owned.push_back(clear);
-            k_brick_clear<<<(unsigned)((nb * 32 + 255) / 256), 256>>>(V.data, nb, tf_clear_below(t), clear);
+            float *bm;
+            if ((rc = arena().alloc((void **)&bm, (size_t)nb * sizeof(float)))) return rc;
+            sc->heavy->ptrs.push_back(bm);
+            k_brick_max<<<(unsigned)((nb * 32 + 255) / 256), 256>>>(V.data, nb, bm);
             CK(cudaGetLastError());
-            CK(cudaDeviceSynchronize());
-            V.clear = clear;
+            sc->bmax[m] = bm;
+            sc->n_bricks[m] = nb;
+            sc->nbz[m] = nbz;
             V.nsx = (V.nbx + kSuper - 1) / kSuper;
             V.nsy = (V.nby + kSuper - 1) / kSuper;
             V.nsz = (nbz + kSuper - 1) / kSuper;
-            const int ns = V.nsx * V.nsy * V.nsz;
-            unsigned char *sclear;
-            if ((rc = arena().alloc((void **)&sclear, (size_t)ns))) return rc;
-            sc->owned.push_back(sclear);
-            k_superbrick_clear<<<(ns + 127) / 128, 128>>>(clear, V.nbx, V.nby, nbz, V.nsx, V.nsy, V.nsz, sclear);
-            CK(cudaGetLastError());
-            CK(cudaDeviceSynchronize());
+            unsigned char *clear, *sclear;
+            if ((rc = sc->alloc_light((void **)&clear, (size_t)nb))) return rc;
+            if ((rc = sc->alloc_light((void **)&sclear, (size_t)V.nsx * V.nsy * V.nsz))) return rc;
+            V.clear = clear;
             V.sclear = sclear;
+            if ((rc = volume_flags(V, bm, nb, nbz, tf_clear_below(t), 0))) return rc;
+            CK(cudaDeviceSynchronize());
         }
         V.n_slices = v.n_slices;
         for (int k = 0; k < v.n_slices; k++)
@@ -674,8 +726,9 @@ static int commit(const gxy_scene_desc *d, Scene *sc) {
     make_partitions(*d, gbox, S);
     void *p;
     if (tfs.empty()) tfs.resize(1);
-    if ((rc = sc->upload(tfs.data(), tfs.size() * sizeof(DevTF), &p))) return rc;
+    if ((rc = sc->upload_light(tfs.data(), tfs.size() * sizeof(DevTF), &p))) return rc;
     S.tfs = (const DevTF *)p;
+    sc->tf_host = tfs;
     float4 ao[256];
     ao_tables(ao);
     if ((rc = sc->upload(ao, sizeof ao, &p))) return rc;
@@ -686,11 +739,87 @@ static int commit(const gxy_scene_desc *d, Scene *sc) {
         drad = (float *)p;
     }
     if ((rc = build_bvh8(S, drad, arena(), 0, sc->bvh))) return rc;
+    if (sc->bvh.nodes_ptr) sc->heavy->ptrs.push_back(sc->bvh.nodes_ptr);
+    if (sc->bvh.slots_ptr) sc->heavy->ptrs.push_back(sc->bvh.slots_ptr);
+    sc->bvh.nodes_ptr = sc->bvh.slots_ptr = nullptr;
     CK(cudaDeviceSynchronize());
-    if ((rc = sc->upload(&S, sizeof S, &p))) return rc;
+    if ((rc = sc->upload_light(&S, sizeof S, &p))) return rc;
     sc->d_scene = (DevScene *)p;
     if ((rc = arena().alloc((void **)&sc->qcount, 16 * sizeof(unsigned int)))) return rc;
     if ((rc = arena().alloc((void **)&sc->ctr, Scene::kMaxLaunch * sizeof(DevCounters)))) return rc;
+    return GXY_OK;
+}
+
+// ------------------------------------------------ transfer functions, views
+// MappedVis_set_transferFunction (MappedVis.ispc:35) on a committed scene:
+// the operator's 4 KB table entry is replaced in device memory; for a volume
+// the clear-brick and superbrick flags are recomputed from the per-brick
+// bounds (no BVH rebuild, no re-bricking).  The device pointers in DevScene
+// do not change, so launches that take the scene by value and batches that
+// read its device copy both see the new table.
+static int scene_set_tf(Scene *sc, int kind, int index, const gxy_tf &tf, cudaStream_t st) {
+    DevScene &S = sc->S;
+    int slot = -1, vol = -1;
+    if (kind == GXY_VIS_VOLUME && index >= 0 && index < S.n_vol) {
+        slot = S.vol[index].tf;
+        vol = index;
+    } else if (kind == GXY_VIS_TRIANGLES && index >= 0 && index < S.n_tri_sets) {
+        slot = S.tri_sets[index].tf;
+    } else if (kind == GXY_VIS_PARTICLES && index >= 0 && index < S.n_sph_sets) {
+        slot = S.sph_sets[index].tf;
+    } else if (kind == GXY_VIS_PATHLINES && index >= 0 && index < S.n_line_sets) {
+        slot = S.line_sets[index].tf;
+    }
+    if (slot < 0 || slot >= (int)sc->tf_host.size())
+        return set_error(GXY_ERR_INVALID, "no such operator for a transfer function");
+    tf_to_dev(tf, sc->tf_host[slot]);
+    CK(cudaMemcpyAsync(const_cast<DevTF *>(S.tfs) + slot, &sc->tf_host[slot], sizeof(DevTF),
+                       cudaMemcpyHostToDevice, st));
+    if (vol >= 0 && S.vol[vol].clear) {
+        int rc = volume_flags(S.vol[vol], sc->bmax[vol], sc->n_bricks[vol], sc->nbz[vol],
+                              tf_clear_below(sc->tf_host[slot]), st);
+        if (rc) return rc;
+    }
+    CK(cudaStreamSynchronize(st));
+    return GXY_OK;
+}
+
+// A second handle on a committed scene: the datasets and the BVH are shared,
+// the transfer-function table, the clear flags and the device copy of the
+// scene are its own (copies of the base's current ones), so set_tf on the
+// view leaves the base -- and frames in flight on it -- untouched.
+static int scene_view(Scene *base, Scene *v) {
+    v->S = base->S;
+    v->pinfo = base->pinfo;
+    v->heavy = base->heavy;
+    v->bvh = base->bvh;
+    v->tf_host = base->tf_host;
+    for (int m = 0; m < kMaxVol; m++) {
+        v->bmax[m] = base->bmax[m];
+        v->n_bricks[m] = base->n_bricks[m];
+        v->nbz[m] = base->nbz[m];
+    }
+    DevScene &S = v->S;
+    void *p;
+    int rc;
+    if ((rc = v->upload_light(v->tf_host.data(), v->tf_host.size() * sizeof(DevTF), &p))) return rc;
+    S.tfs = (const DevTF *)p;
+    for (int m = 0; m < S.n_vol; m++) {
+        DevVolume &V = S.vol[m];
+        if (!V.clear) continue;
+        const size_t ns = (size_t)V.nsx * V.nsy * V.nsz;
+        unsigned char *clear, *sclear;
+        if ((rc = v->alloc_light((void **)&clear, (size_t)v->n_bricks[m]))) return rc;
+        if ((rc = v->alloc_light((void **)&sclear, ns))) return rc;
+        CK(cudaMemcpy(clear, base->S.vol[m].clear, (size_t)v->n_bricks[m], cudaMemcpyDeviceToDevice));
+        CK(cudaMemcpy(sclear, base->S.vol[m].sclear, ns, cudaMemcpyDeviceToDevice));
+        V.clear = clear;
+        V.sclear = sclear;
+    }
+    if ((rc = v->upload_light(&S, sizeof S, &p))) return rc;
+    v->d_scene = (DevScene *)p;
+    if ((rc = arena().alloc((void **)&v->qcount, 16 * sizeof(unsigned int)))) return rc;
+    if ((rc = arena().alloc((void **)&v->ctr, Scene::kMaxLaunch * sizeof(DevCounters)))) return rc;
     return GXY_OK;
 }
 
@@ -803,6 +932,10 @@ struct FrameArgs {
     const DevJob *jobs;                // batch launches
     int n_jobs;
     long long total_pix;
+    // single-frame camera passes: the band of image rows [band_y0,
+    // band_y0 + band_rows) this launch generates (the whole image unless the
+    // frame is split into bands to fit its queues)
+    int band_y0, band_rows;
     const DRay *qin[NQ];
     unsigned nin[NQ];
     const unsigned *nin_dev;           // batch split passes: input queue counts in device memory
@@ -1103,7 +1236,7 @@ __device__ __forceinline__ void camera_pass(const DevScene &Sp, const DevTF *tfs
             int w = J->cam.width;
             int64_t li = i - (BATCH ? J->pix0 : 0);
             x = (int)(li % w);
-            y = (int)(li / w);
+            y = (int)(li / w) + (BATCH ? 0 : A.band_y0);
             pending = camera_ray(S, J->cam, x, y, in.org, in.dir);
             in.t = 0.0f;
             in.tmax = FLT_MAX;
@@ -1188,7 +1321,7 @@ __global__ void __launch_bounds__(kThreads, MINB) k_primary(DevScene S, FrameArg
     LocalCounters c;
     const int64_t start = (int64_t)blockIdx.x * blockDim.x, stride = (int64_t)gridDim.x * blockDim.x;
     if (KIND == K_CAMERA) {
-        camera_pass<false, true>(S, tfs, A, nullptr, (int64_t)A.job0.cam.width * A.job0.cam.height, start, stride, st,
+        camera_pass<false, true>(S, tfs, A, nullptr, (int64_t)A.job0.cam.width * A.band_rows, start, stride, st,
                                  c);
     } else {
         unsigned n[NQ] = {A.nin[Q_PRIM], 0u, 0u};
@@ -1471,7 +1604,7 @@ __global__ void __launch_bounds__(kThreads, MINB) k_cam_query(DevScene S, FrameA
     LocalCounters c;
     const int lane = threadIdx.x & 31;
     const unsigned npix =
-        BATCH ? (unsigned)A.total_pix : (unsigned)A.job0.cam.width * (unsigned)A.job0.cam.height;
+        BATCH ? (unsigned)A.total_pix : (unsigned)A.job0.cam.width * (unsigned)A.band_rows;
     unsigned *cursor = A.pmarch_count + 2;
     TravState T;
     uint2 stack_mem[64];
@@ -1508,7 +1641,7 @@ __global__ void __launch_bounds__(kThreads, MINB) k_cam_query(DevScene S, FrameA
                 }
                 const DevCamera &cam = BATCH ? A.jobs[job].cam : A.job0.cam;
                 x = (int)(li % (unsigned)cam.width);
-                y = (int)(li / (unsigned)cam.width);
+                y = (int)(li / (unsigned)cam.width) + (BATCH ? 0 : A.band_y0);
                 pending = camera_ray(S, cam, x, y, org, dir0);
                 fresh = true;
                 first = true;
@@ -1597,7 +1730,7 @@ __global__ void __launch_bounds__(kThreads, MINB) k_cam_packet(DevScene S, Frame
     const int lane = threadIdx.x & 31;
     uint2 *wstack = wstacks[threadIdx.x >> 5];
     const DevCamera &cam = A.job0.cam;
-    const int w = cam.width, hgt = cam.height;
+    const int w = cam.width, y0 = A.band_y0, hgt = A.band_rows;   // rows [y0, y0 + hgt) of the image
     const unsigned npix = (unsigned)w * (unsigned)hgt;
     const unsigned tiles_x = (unsigned)(w + 7) / 8, ntiles = tiles_x * (unsigned)((hgt + 3) / 4);
     unsigned *cursor = A.pmarch_count + 2;
@@ -1607,9 +1740,10 @@ __global__ void __launch_bounds__(kThreads, MINB) k_cam_packet(DevScene S, Frame
         if (lane == 0) tile = atomicAdd(cursor, 1u);
         tile = __shfl_sync(FULL, tile, 0);
         if (tile >= ntiles) break;
-        const int x = (int)(tile % tiles_x) * 8 + (lane & 7), y = (int)(tile / tiles_x) * 4 + (lane >> 3);
-        const bool valid = x < w && y < hgt;
-        const unsigned pix = valid ? (unsigned)y * (unsigned)w + (unsigned)x : 0u;
+        const int x = (int)(tile % tiles_x) * 8 + (lane & 7), yb = (int)(tile / tiles_x) * 4 + (lane >> 3);
+        const int y = y0 + yb;
+        const bool valid = x < w && yb < hgt;
+        const unsigned pix = valid ? (unsigned)yb * (unsigned)w + (unsigned)x : 0u;   // slot within the band
         V3 org = v3(0, 0, 0), dir0 = v3(1, 1, 1);
         uint64_t pending = 0;
         if (valid) {
@@ -2054,46 +2188,107 @@ static unsigned query_grid() {
     return (unsigned)(sms * (per < 1 ? 1 : per));
 }
 
-static int ensure_queues(Scene *sc, const size_t need[3]) {
-    size_t pneed = need[0];
-    if (sc->pmarch_cap < pneed) {
-        arena().free(sc->pmarch);
-        arena().free(sc->pmarch_hit);
-        sc->pmarch = nullptr;
-        sc->pmarch_hit = nullptr;
-        sc->pmarch_cap = 0;
-        int rc = arena().alloc((void **)&sc->pmarch, pneed * sizeof(DRay));
-        if (rc) return rc;
-        rc = arena().alloc((void **)&sc->pmarch_hit, 2 * pneed * sizeof(float4));
-        if (rc) return rc;
-        sc->pmarch_cap = pneed;
-    }
-    size_t mneed = need[1] + need[2];
-    if (sc->qmarch_cap < mneed) {
-        arena().free(sc->qmarch);
-        arena().free(sc->qmarch_hit);
-        sc->qmarch = nullptr;
-        sc->qmarch_hit = nullptr;
-        sc->qmarch_cap = 0;
-        int rc = arena().alloc((void **)&sc->qmarch, mneed * sizeof(DRay));
-        if (rc) return rc;
-        if ((rc = arena().alloc((void **)&sc->qmarch_hit, mneed * sizeof(float)))) return rc;
-        sc->qmarch_cap = mneed;
-    }
+// Queue memory of the frame path.  Every buffer grows to the exact worst
+// case of what the next launch can write, computed from counts the host
+// knows, so no ray is ever dropped for want of room: Galaxy never loses a
+// ray either -- it splits an over-large list and enqueues every part
+// (Renderer.cpp:674-690).  Where the worst case does not fit the HBM budget
+// (or GXY_TUNE_QUEUE_LIMIT), the frame is split into bands of image rows,
+// each a complete wavefront, as Galaxy splits lists.
+static int g_tune_queue_limit = 0;   // records per queue buffer; 0 = none
+
+// Grow *buf (capacity *cap records of `rec` bytes, plus `side` bytes per
+// record in *aux when aux is given) to at least n records.  A buffer only
+// grows; headroom of 1/8 keeps repeated frames from regrowing it.  If the
+// larger buffer cannot be had, the old capacity is taken back when possible
+// and GXY_ERR_OOM is returned.
+static int grow(void **buf, void **aux, size_t *cap, size_t n, size_t rec, size_t side) {
+    if (*cap >= n) return GXY_OK;
+    if (g_tune_queue_limit && n > (size_t)g_tune_queue_limit)
+        return set_error(GXY_ERR_OOM, "queue of " + std::to_string(n) + " records exceeds GXY_TUNE_QUEUE_LIMIT");
+    const size_t old = *cap;
+    auto release = [&]() {
+        arena().free(*buf);
+        *buf = nullptr;
+        if (aux) {
+            arena().free(*aux);
+            *aux = nullptr;
+        }
+        *cap = 0;
+    };
+    auto take = [&](size_t want) -> bool {
+        if (!want) return false;
+        if (arena().alloc(buf, want * rec) != GXY_OK) return false;
+        if (aux && side && arena().alloc(aux, want * side) != GXY_OK) {
+            arena().free(*buf);
+            *buf = nullptr;
+            return false;
+        }
+        *cap = want;
+        return true;
+    };
+    release();
+    size_t want = n + n / 8 + 1024;
+    if (g_tune_queue_limit && want > (size_t)g_tune_queue_limit) want = (size_t)g_tune_queue_limit;
+    if (want > 0xffffffffull) want = n;
+    if (n > 0xffffffffull) return set_error(GXY_ERR_INVALID, "queue too large");
+    if (take(want) || take(n)) return GXY_OK;
+    cudaGetLastError();
+    take(old);
+    return set_error(GXY_ERR_OOM, "no room for a queue of " + std::to_string(n) + " records");
+}
+
+static int grow_set(Scene *sc, int set, const size_t need[3]) {
     for (int k = 0; k < 3; k++) {
-        if (sc->qcap[k] >= need[k]) continue;
-        for (int b = 0; b < 2; b++) {
-            arena().free(sc->q[b][k]);
-            sc->q[b][k] = nullptr;
-        }
-        sc->qcap[k] = 0;
-        for (int b = 0; b < 2; b++) {
-            int rc = arena().alloc((void **)&sc->q[b][k], need[k] * sizeof(DRay));
-            if (rc) return rc;
-        }
-        sc->qcap[k] = need[k];
+        int rc = grow((void **)&sc->q[set][k], nullptr, &sc->qcap[set][k], need[k] ? need[k] : 1, sizeof(DRay), 0);
+        if (rc) return rc;
     }
     return GXY_OK;
+}
+
+// Room for a band of P pixels emitting E camera rays (per partition,
+// Camera.cpp:431-441).  Its camera generation writes at most E continuing
+// primaries, nl*E shadow and na*E AO rays (queue set 0) and, split, P slots
+// plus one record per further partition (march records); the first hand-off
+// generation at most E, 2*nl*E and 2*na*E (set 1) and (nl+na)*E march
+// records.  Set 0 and the camera march records are allocated here; set 1
+// and the march records only have to fit the budget (and the queue limit),
+// since they grow to the counts actually queued.
+static int fit_band(Scene *sc, size_t P, size_t E, int nl, int na, bool split_prim, bool split) {
+    const size_t set0[3] = {E, E * (size_t)nl, E * (size_t)na};
+    const size_t set1[3] = {E, 2 * E * (size_t)nl, 2 * E * (size_t)na};
+    const size_t pm = P + (E > P ? E - P : 0) + 32, qm = split ? E * (size_t)(nl + na) + 32 : 0;
+    if (g_tune_queue_limit) {
+        const size_t lim = (size_t)g_tune_queue_limit;
+        for (int k = 0; k < 3; k++)
+            if (set0[k] > lim || set1[k] > lim)
+                return set_error(GXY_ERR_OOM, "band exceeds GXY_TUNE_QUEUE_LIMIT");
+        if ((split_prim && pm > lim) || qm > lim) return set_error(GXY_ERR_OOM, "band exceeds GXY_TUNE_QUEUE_LIMIT");
+    }
+    size_t extra = 0;   // bytes beyond what is allocated now
+    for (int k = 0; k < 3; k++) {
+        if (set0[k] > sc->qcap[0][k]) extra += (set0[k] - sc->qcap[0][k]) * sizeof(DRay);
+        if (set1[k] > sc->qcap[1][k]) extra += (set1[k] - sc->qcap[1][k]) * sizeof(DRay);
+    }
+    if (split_prim && pm > sc->pmarch_cap) extra += (pm - sc->pmarch_cap) * (sizeof(DRay) + 2 * sizeof(float4));
+    if (qm > sc->qmarch_cap) extra += (qm - sc->qmarch_cap) * (sizeof(DRay) + sizeof(float));
+    if (!arena().would_fit(extra)) return set_error(GXY_ERR_OOM, "band's queues exceed the HBM budget");
+    int rc = grow_set(sc, 0, set0);
+    if (rc == GXY_OK && split_prim)
+        rc = grow((void **)&sc->pmarch, (void **)&sc->pmarch_hit, &sc->pmarch_cap, pm, sizeof(DRay),
+                  2 * sizeof(float4));
+    return rc;
+}
+
+// Per image row: camera rays emitted beyond one per pixel (a ray whose entry
+// point lies on a face shared by bricks is emitted by each, Camera.cpp:440-441).
+__global__ void k_row_extra(DevScene S, DevCamera C, unsigned *rowx) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= (int64_t)C.width * C.height) return;
+    V3 o, d;
+    const int x = (int)(i % C.width), y = (int)(i / C.width);
+    const int k = __popcll(camera_ray(S, C, x, y, o, d));
+    if (k > 1) atomicAdd(rowx + y, (unsigned)(k - 1));
 }
 
 static void add_counters(DevCounters &a, const DevCounters &b) {
@@ -2106,8 +2301,11 @@ static void add_counters(DevCounters &a, const DevCounters &b) {
 // One frame: generation 0 from the camera, then generations of the primary
 // queue and the shadow+AO queues until every queue is empty.  The host reads
 // the three queue counts (12 bytes) after each generation to size the next
-// launches; each launch adds into its own counter slot, and when profiling
-// is on a pair of events brackets each launch, so profiling adds no syncs.
+// launches and to grow their output queues to the worst case beforehand;
+// each launch adds into its own counter slot, and when profiling is on a
+// pair of events brackets each launch, so profiling adds no syncs.  When the
+// camera generation's queues do not fit, the image is rendered in bands of
+// rows, each band a complete wavefront into the same framebuffer.
 static int render(Scene *sc, const gxy_camera &cam, const gxy_lighting &lt, float *fb, cudaStream_t st) {
     if (cam.width <= 0 || cam.height <= 0) return set_error(GXY_ERR_INVALID, "bad image size");
     DevScene &S = sc->S;
@@ -2117,14 +2315,10 @@ static int render(Scene *sc, const gxy_camera &cam, const gxy_lighting &lt, floa
     int rc = setup_lights(lt, A.job0.L);
     if (rc) return rc;
     if (A.job0.L.n == 0) return set_error(GXY_ERR_INVALID, "lighting needs at least one light");
-    int64_t npix = (int64_t)cam.width * cam.height;
-    size_t slack = (size_t)npix / 8 + 4096;
-    size_t need[3] = {(size_t)npix + slack, (size_t)npix * (A.job0.L.shadows ? A.job0.L.n : 0) + slack,
-                      (size_t)npix * A.job0.L.n_ao + slack};
-    if ((rc = ensure_queues(sc, need))) return rc;
+    const int W = cam.width, H = cam.height;
+    const int nl = A.job0.L.shadows ? A.job0.L.n : 0, na = A.job0.L.n_ao;
+    const bool split = split_eligible(S), split_prim = split && g_tune_split_prim;
     const int maxl = Scene::kMaxLaunch;
-    CK(cudaMemsetAsync(sc->ctr, 0, maxl * sizeof(DevCounters), st));
-    CK(cudaMemsetAsync(sc->qcount, 0, 16 * sizeof(unsigned), st));
     if (sc->profile && (int)sc->events.size() < 2 * maxl) {
         for (int k = (int)sc->events.size(); k < 2 * maxl; k++) {
             cudaEvent_t e;
@@ -2132,39 +2326,69 @@ static int render(Scene *sc, const gxy_camera &cam, const gxy_lighting &lt, floa
             sc->events.push_back(e);
         }
     }
-    A.job0.fb = fb;
-    A.job0.scene = sc->d_scene;
-    A.job0.pix0 = 0;
-    A.n_jobs = 1;
-    A.total_pix = npix;
-    A.split = split_eligible(S) ? 1 : 0;
-    A.qmarch = sc->qmarch;
-    A.qmarch_hit = g_tune_carry_hits ? sc->qmarch_hit : nullptr;
-    A.qmarch_count = sc->qcount + 12;   // [0] records, [1] march cursor, [2] query cursor
-    A.qmarch_cap = (unsigned)sc->qmarch_cap;
-    A.split_prim = (split_eligible(S) && g_tune_split_prim) ? 1 : 0;
-    A.trav_steps = g_tune_trav_steps;
-    A.march_steps = g_tune_march_steps;
-    A.skip_mode = g_tune_skip_mode;
-    A.pmarch = sc->pmarch;
-    A.pmarch_hit = sc->pmarch_hit;
-    A.pmarch_count = sc->qcount + 8;    // [0] records, [1] march cursor, [2] camera query cursor, [3] extra slots
-    A.pmarch_cap = (unsigned)sc->pmarch_cap;
-    for (int k = 0; k < 3; k++) A.qcap[k] = (unsigned)sc->qcap[k];
-    struct LaunchRec { int gen, kind; unsigned rays_in; };
-    std::vector<LaunchRec> recs;
-    int nl = 0;
     if (!sc->side) {
         CK(cudaStreamCreateWithFlags(&sc->side, cudaStreamNonBlocking));
         CK(cudaEventCreateWithFlags(&sc->fork, cudaEventDisableTiming));
         CK(cudaEventCreateWithFlags(&sc->join, cudaEventDisableTiming));
     }
+    // camera rays per row: one per pixel, plus the rays a pixel emits into a
+    // further partition (counted on the device when there are several)
+    std::vector<unsigned> rowx(H, 0u);
+    if (S.np > 1) {
+        if (sc->rowx_cap < (size_t)H) {
+            arena().free(sc->rowx);
+            sc->rowx = nullptr;
+            sc->rowx_cap = 0;
+            if ((rc = arena().alloc((void **)&sc->rowx, (size_t)H * sizeof(unsigned)))) return rc;
+            sc->rowx_cap = H;
+        }
+        CK(cudaMemsetAsync(sc->rowx, 0, (size_t)H * sizeof(unsigned), st));
+        const int64_t npix = (int64_t)W * H;
+        k_row_extra<<<(unsigned)((npix + 255) / 256), 256, 0, st>>>(S, A.job0.cam, sc->rowx);
+        CK(cudaGetLastError());
+        CK(cudaMemcpyAsync(rowx.data(), sc->rowx, (size_t)H * sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+    }
+    // bands: the whole image if its camera generation fits, else halve
+    auto band_max = [&](int rows, size_t &P, size_t &E) {
+        P = (size_t)W * rows;
+        E = 0;
+        for (int y0 = 0; y0 < H; y0 += rows) {
+            size_t e = 0;
+            for (int y = y0; y < std::min(H, y0 + rows); y++) e += (size_t)W + rowx[y];
+            E = std::max(E, e);
+        }
+    };
+    int rows = H;
+    for (;;) {
+        size_t P, E;
+        band_max(rows, P, E);
+        rc = fit_band(sc, P, E, nl, na, split_prim, split);
+        if (rc == GXY_OK) break;
+        if (rows == 1) return set_error(GXY_ERR_OOM, "not even one image row's camera rays fit: " + last_error());
+        rows = (rows + 1) / 2;
+    }
+    A.job0.fb = fb;
+    A.job0.scene = sc->d_scene;
+    A.job0.pix0 = 0;
+    A.n_jobs = 1;
+    A.trav_steps = g_tune_trav_steps;
+    A.march_steps = g_tune_march_steps;
+    A.skip_mode = g_tune_skip_mode;
+    A.qmarch_count = sc->qcount + 12;   // [0] records, [1] march cursor, [2] query cursor
+    A.pmarch_count = sc->qcount + 8;    // [0] records, [1] march cursor, [2] camera query cursor, [3] extra slots
+    struct LaunchRec { int gen, kind; unsigned rays_in; };
+    std::vector<LaunchRec> recs;
+    int nl_launch = 0;
     const bool lines = S.n_seg > 0;
+    sc->last = DevCounters{};
+    sc->gens.clear();
+    int64_t gens_total = 0;
     auto launch = [&](int kind, int gen, unsigned rays_in, int64_t items, cudaStream_t st) -> int {
-        if (nl >= maxl) return set_error(GXY_ERR_TIMEOUT, "too many launches in one frame");
-        A.ctr = sc->ctr + nl;
+        if (nl_launch >= maxl) return set_error(GXY_ERR_TIMEOUT, "too many launches in one frame");
+        A.ctr = sc->ctr + nl_launch;
         unsigned g = grid_for(items);
-        if (sc->profile) CK(cudaEventRecord(sc->events[2 * nl], st));
+        if (sc->profile) CK(cudaEventRecord(sc->events[2 * nl_launch], st));
         if (kind == K_SECONDARY && A.split) CK(cudaMemsetAsync(A.qmarch_count, 0, 3 * sizeof(unsigned), st));
         if (kind == K_CAMERA && A.split_prim) CK(cudaMemsetAsync(A.pmarch_count, 0, 4 * sizeof(unsigned), st));
         if (g_tune_minb == 3) {
@@ -2197,82 +2421,127 @@ static int render(Scene *sc, const gxy_camera &cam, const gxy_lighting &lt, floa
             else launch_sec_march<false, 2>(march_grid(2), st, S, A);
         }
         CK(cudaGetLastError());
-        if (sc->profile) CK(cudaEventRecord(sc->events[2 * nl + 1], st));
+        if (sc->profile) CK(cudaEventRecord(sc->events[2 * nl_launch + 1], st));
         recs.push_back({gen, kind, rays_in});
-        nl++;
+        nl_launch++;
         return GXY_OK;
     };
-    int cur = 0;   // queue set written by the last generation
-    for (int k = 0; k < 3; k++) A.qout[k] = sc->q[cur][k];
-    A.qout_count = sc->qcount + 3 * cur;
-    if ((rc = launch(K_CAMERA, 0, 0, npix, st))) return rc;
-    if (A.split_prim && (rc = launch(K_PMARCH, 0, 0, 1 << 30, st))) return rc;
-    A.split_prim = 0;   // later generations trace handed-off primaries in one pass
-    int gen = 1;
-    for (;;) {
-        unsigned n[3];
-        CK(cudaMemcpyAsync(n, sc->qcount + 3 * cur, sizeof n, cudaMemcpyDeviceToHost, st));
+    // counter slots and per-launch statistics of the launches so far
+    auto collect = [&]() -> int {
+        if (!nl_launch) return GXY_OK;
+        std::vector<DevCounters> slots(nl_launch);
+        CK(cudaMemcpyAsync(slots.data(), sc->ctr, nl_launch * sizeof(DevCounters), cudaMemcpyDeviceToHost, st));
         CK(cudaStreamSynchronize(st));
-        for (int k = 0; k < 3; k++)
-            if (n[k] > sc->qcap[k]) n[k] = (unsigned)sc->qcap[k];   // overflow already flagged
-        if (n[0] + n[1] + n[2] == 0) break;
-        int nxt = cur ^ 1;
-        CK(cudaMemsetAsync(sc->qcount + 3 * nxt, 0, 3 * sizeof(unsigned), st));
+        for (int k = 0; k < nl_launch; k++) add_counters(sc->last, slots[k]);
+        if (sc->profile) {
+            for (int k = 0; k < nl_launch; k++) {
+                gxy_generation_stats g{};
+                float ms = 0;
+                CK(cudaEventElapsedTime(&ms, sc->events[2 * k], sc->events[2 * k + 1]));
+                g.ms = ms;
+                g.generation = recs[k].gen;
+                g.kind = recs[k].kind;
+                g.rays_in = recs[k].kind == K_CAMERA ? 0
+                            : (recs[k].kind == K_MARCH || recs[k].kind == K_PMARCH) ? (int64_t)slots[k].marched
+                                                                                      : recs[k].rays_in;
+                const DevCounters &c = slots[k];
+                g.enqueued = (int64_t)c.enqueued;
+                g.segments = (int64_t)c.segments;
+                g.samples = (int64_t)c.samples;
+                g.samples_skipped = (int64_t)c.skipped;
+                g.nodes = (int64_t)c.nodes;
+                g.tri_tests = (int64_t)c.tri_tests;
+                g.sph_tests = (int64_t)c.sph_tests;
+                g.terminated = (int64_t)c.terminated;
+                sc->gens.push_back(g);
+            }
+        }
+        recs.clear();
+        nl_launch = 0;
+        return GXY_OK;
+    };
+    for (int y0 = 0; y0 < H; y0 += rows) {
+        A.band_y0 = y0;
+        A.band_rows = std::min(rows, H - y0);
+        A.total_pix = (long long)W * A.band_rows;
+        A.split = split ? 1 : 0;
+        A.split_prim = split_prim ? 1 : 0;
+        A.qmarch = sc->qmarch;
+        A.qmarch_hit = g_tune_carry_hits ? sc->qmarch_hit : nullptr;
+        A.qmarch_cap = (unsigned)sc->qmarch_cap;
+        A.pmarch = sc->pmarch;
+        A.pmarch_hit = sc->pmarch_hit;
+        A.pmarch_cap = (unsigned)sc->pmarch_cap;
+        // counter slots: a band ends its launches' records before the next
+        if (nl_launch > maxl - 64 && (rc = collect())) return rc;
+        CK(cudaMemsetAsync(sc->ctr + nl_launch, 0, (maxl - nl_launch) * sizeof(DevCounters), st));
+        CK(cudaMemsetAsync(sc->qcount, 0, 16 * sizeof(unsigned), st));
+        int cur = 0;   // queue set written by the last generation
         for (int k = 0; k < 3; k++) {
-            A.qin[k] = sc->q[cur][k];
-            A.nin[k] = n[k];
-            A.qout[k] = sc->q[nxt][k];
+            A.qout[k] = sc->q[cur][k];
+            A.qcap[k] = (unsigned)sc->qcap[cur][k];
         }
-        A.qout_count = sc->qcount + 3 * nxt;
-        // Continuing primaries and shadow/AO rays of one generation are
-        // independent (both only append to the next generation's queues), so
-        // the primaries, whose launch is bound by its longest march, run on
-        // the side stream beside the shadow/AO passes.
-        const bool sec = n[Q_SHADOW] + n[Q_AO] != 0;
-        const bool overlap = n[Q_PRIM] && sec;
-        if (overlap) {
-            CK(cudaEventRecord(sc->fork, st));
-            CK(cudaStreamWaitEvent(sc->side, sc->fork, 0));
+        A.qout_count = sc->qcount + 3 * cur;
+        if ((rc = launch(K_CAMERA, 0, 0, A.total_pix, st))) return rc;
+        if (A.split_prim && (rc = launch(K_PMARCH, 0, 0, 1 << 30, st))) return rc;
+        A.split_prim = 0;   // later generations trace handed-off primaries in one pass
+        int gen = 1;
+        for (;;) {
+            unsigned n[3];
+            CK(cudaMemcpyAsync(n, sc->qcount + 3 * cur, sizeof n, cudaMemcpyDeviceToHost, st));
+            CK(cudaStreamSynchronize(st));
+            for (int k = 0; k < 3; k++)
+                if (n[k] > sc->qcap[cur][k]) n[k] = (unsigned)sc->qcap[cur][k];   // overflow already flagged
+            if (n[0] + n[1] + n[2] == 0) break;
+            int nxt = cur ^ 1;
+            // worst case of this generation's output: a primary continues
+            // at most once and spawns nl shadow and na AO rays; a shadow/AO
+            // ray moves on at most once
+            const size_t need[3] = {(size_t)n[Q_PRIM], (size_t)n[Q_SHADOW] + (size_t)nl * n[Q_PRIM],
+                                    (size_t)n[Q_AO] + (size_t)na * n[Q_PRIM]};
+            int grc = grow_set(sc, nxt, need);
+            if (grc == GXY_OK && A.split)
+                grc = grow((void **)&sc->qmarch, (void **)&sc->qmarch_hit, &sc->qmarch_cap,
+                           (size_t)n[Q_SHADOW] + n[Q_AO] + 32, sizeof(DRay), sizeof(float));
+            // a queue that cannot grow keeps its room; a generation that then
+            // runs out of it reports GXY_ERR_OVERFLOW
+            if (grc) cudaGetLastError();
+            A.qmarch = sc->qmarch;
+            A.qmarch_hit = g_tune_carry_hits ? sc->qmarch_hit : nullptr;
+            A.qmarch_cap = (unsigned)sc->qmarch_cap;
+            CK(cudaMemsetAsync(sc->qcount + 3 * nxt, 0, 3 * sizeof(unsigned), st));
+            for (int k = 0; k < 3; k++) {
+                A.qin[k] = sc->q[cur][k];
+                A.nin[k] = n[k];
+                A.qout[k] = sc->q[nxt][k];
+                A.qcap[k] = (unsigned)sc->qcap[nxt][k];
+            }
+            A.qout_count = sc->qcount + 3 * nxt;
+            // Continuing primaries and shadow/AO rays of one generation are
+            // independent (both only append to the next generation's queues), so
+            // the primaries, whose launch is bound by its longest march, run on
+            // the side stream beside the shadow/AO passes.
+            const bool sec = n[Q_SHADOW] + n[Q_AO] != 0;
+            const bool overlap = n[Q_PRIM] && sec;
+            if (nl_launch + 3 > maxl && (rc = collect())) return rc;
+            if (overlap) {
+                CK(cudaEventRecord(sc->fork, st));
+                CK(cudaStreamWaitEvent(sc->side, sc->fork, 0));
+            }
+            if (n[Q_PRIM] && (rc = launch(K_PRIMARY, gen, n[Q_PRIM], n[Q_PRIM], overlap ? sc->side : st))) return rc;
+            if (overlap) CK(cudaEventRecord(sc->join, sc->side));
+            if (sec && (rc = launch(K_SECONDARY, gen, n[Q_SHADOW] + n[Q_AO], (int64_t)n[Q_SHADOW] + n[Q_AO], st)))
+                return rc;
+            if (sec && A.split && (rc = launch(K_MARCH, gen, 0, 1 << 30, st))) return rc;
+            if (overlap) CK(cudaStreamWaitEvent(st, sc->join, 0));
+            cur = nxt;
+            gen++;
         }
-        if (n[Q_PRIM] && (rc = launch(K_PRIMARY, gen, n[Q_PRIM], n[Q_PRIM], overlap ? sc->side : st))) return rc;
-        if (overlap) CK(cudaEventRecord(sc->join, sc->side));
-        if (sec && (rc = launch(K_SECONDARY, gen, n[Q_SHADOW] + n[Q_AO], (int64_t)n[Q_SHADOW] + n[Q_AO], st)))
-            return rc;
-        if (sec && A.split && (rc = launch(K_MARCH, gen, 0, 1 << 30, st))) return rc;
-        if (overlap) CK(cudaStreamWaitEvent(st, sc->join, 0));
-        cur = nxt;
-        gen++;
+        gens_total = std::max<int64_t>(gens_total, gen);
     }
-    std::vector<DevCounters> slots(nl);
-    CK(cudaMemcpyAsync(slots.data(), sc->ctr, nl * sizeof(DevCounters), cudaMemcpyDeviceToHost, st));
-    CK(cudaStreamSynchronize(st));
-    sc->last = DevCounters{};
-    for (int k = 0; k < nl; k++) add_counters(sc->last, slots[k]);
-    sc->bounces = gen;
-    sc->gens.clear();
-    if (sc->profile) {
-        for (int k = 0; k < nl; k++) {
-            gxy_generation_stats g{};
-            float ms = 0;
-            CK(cudaEventElapsedTime(&ms, sc->events[2 * k], sc->events[2 * k + 1]));
-            g.ms = ms;
-            g.generation = recs[k].gen;
-            g.kind = recs[k].kind;
-            g.rays_in = recs[k].kind == K_CAMERA ? 0
-                        : (recs[k].kind == K_MARCH || recs[k].kind == K_PMARCH) ? (int64_t)slots[k].marched
-                                                                                  : recs[k].rays_in;
-            const DevCounters &c = slots[k];
-            g.enqueued = (int64_t)c.enqueued;
-            g.segments = (int64_t)c.segments;
-            g.samples = (int64_t)c.samples;
-            g.samples_skipped = (int64_t)c.skipped;
-            g.nodes = (int64_t)c.nodes;
-            g.tri_tests = (int64_t)c.tri_tests;
-            g.sph_tests = (int64_t)c.sph_tests;
-            g.terminated = (int64_t)c.terminated;
-            sc->gens.push_back(g);
-        }
-    }
+    if ((rc = collect())) return rc;
+    sc->bounces = gens_total;
+    sc->bands = (H + rows - 1) / rows;
     if (sc->last.overflow) return set_error(GXY_ERR_OVERFLOW, "a ray queue or traversal stack overflowed");
     return GXY_OK;
 }
@@ -2405,6 +2674,30 @@ int gxy_gpu_scene_release(gxy_scene scene) {
     if (!scene) return set_error(GXY_ERR_INVALID, "null scene");
     cudaDeviceSynchronize();
     delete reinterpret_cast<Scene *>(scene);
+    return GXY_OK;
+    GUARD_END
+}
+
+int gxy_gpu_scene_set_tf(gxy_scene scene, int vis_kind, int index, const gxy_tf *tf, void *stream) {
+    GUARD_BEGIN
+    if (!scene || !tf) return set_error(GXY_ERR_INVALID, "null argument");
+    Scene *sc = reinterpret_cast<Scene *>(scene);
+    std::lock_guard<std::mutex> lk(sc->mu);
+    return scene_set_tf(sc, vis_kind, index, *tf, (cudaStream_t)stream);
+    GUARD_END
+}
+
+int gxy_gpu_scene_view(gxy_scene scene, gxy_scene *out) {
+    GUARD_BEGIN
+    if (!scene || !out) return set_error(GXY_ERR_INVALID, "null argument");
+    Scene *base = reinterpret_cast<Scene *>(scene);
+    std::unique_ptr<Scene> v(new Scene());
+    {
+        std::lock_guard<std::mutex> lk(base->mu);
+        int rc = scene_view(base, v.get());
+        if (rc) return rc;
+    }
+    *out = reinterpret_cast<gxy_scene>(v.release());
     return GXY_OK;
     GUARD_END
 }
@@ -2570,6 +2863,7 @@ int gxy_gpu_query_counters(gxy_scene scene, gxy_counters *out) {
     out->prim_tests = (int64_t)(c.tri_tests + c.sph_tests);
     out->overflow = c.overflow;
     out->samples_skipped = (int64_t)c.skipped;
+    out->bands = sc->bands;
     return GXY_OK;
 }
 
@@ -2639,6 +2933,11 @@ int gxy_gpu_set_tuning(int knob, int value) {
         g_tune_skip_mode = value;
         return GXY_OK;
     }
+    if (knob == GXY_TUNE_QUEUE_LIMIT) {
+        if (value < 0) return set_error(GXY_ERR_INVALID, "queue limit must be >= 0");
+        g_tune_queue_limit = value;
+        return GXY_OK;
+    }
     return set_error(GXY_ERR_INVALID, "unknown tuning knob");
 }
 
@@ -2656,6 +2955,7 @@ int gxy_gpu_get_tuning(int knob, int *value) {
     else if (knob == GXY_TUNE_SKIP_CLEAR) *value = g_tune_skip_clear;
     else if (knob == GXY_TUNE_SKIP_MODE) *value = g_tune_skip_mode;
     else if (knob == GXY_TUNE_CARRY_HITS) *value = g_tune_carry_hits;
+    else if (knob == GXY_TUNE_QUEUE_LIMIT) *value = g_tune_queue_limit;
     else return set_error(GXY_ERR_INVALID, "unknown tuning knob");
     return GXY_OK;
 }
@@ -2865,6 +3165,15 @@ struct Batch {
     bool pending = false;
     int cooperative = 0;
     int last_rc = GXY_OK;
+    // the last submission, kept for continuations: a submission that leaves
+    // rays after its kBatchGens generations is continued from its queues
+    FrameArgs lastA{};
+    WaveArgs lastW{};
+    DevScene lastS{};
+    bool last_uniform = true;
+    int last_jobs = 0;
+    int swap = 0;                      // queue sets exchanged by an odd number of continuations
+    int continuations = 0;
     std::vector<void *> dev;
     ~Batch() {
         if (stream) cudaStreamSynchronize(stream);
@@ -2915,20 +3224,30 @@ static int batch_grid(bool uniform) {
 }
 
 // Enqueue one submission on the batch stream (captured into a graph or not).
-static int batch_enqueue(Batch *b, const DevScene &Su, bool uniform, const FrameArgs &A, const WaveArgs &W,
-                         int n_jobs, int cooperative) {
+// cont: a continuation of the last submission -- no camera generation; the
+// queue counts the last generation left (copied aside into d_status[2..4])
+// become generation 0's, and the queue sets are exchanged so that
+// generation 1 reads the set the last generation wrote.  Counters add up.
+static int batch_enqueue(Batch *b, const DevScene &Su, bool uniform, const FrameArgs &A, const WaveArgs &W0,
+                         int n_jobs, int cooperative, bool cont = false) {
     cudaStream_t st = b->stream;
-    CK(cudaMemcpyAsync(b->d_jobs, b->h_jobs, n_jobs * sizeof(DevJob), cudaMemcpyHostToDevice, st));
+    WaveArgs W = W0;
+    if (b->swap)
+        for (int k = 0; k < NQ; k++) std::swap(W.q[0][k], W.q[1][k]);
+    if (!cont) CK(cudaMemcpyAsync(b->d_jobs, b->h_jobs, n_jobs * sizeof(DevJob), cudaMemcpyHostToDevice, st));
     CK(cudaMemsetAsync(b->counts, 0, (kBatchGens + 1) * NQ * sizeof(unsigned), st));
     CK(cudaMemsetAsync(b->mcounts, 0, (kBatchGens + 1) * 4 * sizeof(unsigned), st));
-    CK(cudaMemsetAsync(b->ctr, 0, sizeof(DevCounters), st));
+    if (!cont) CK(cudaMemsetAsync(b->ctr, 0, sizeof(DevCounters), st));
+    if (cont)
+        CK(cudaMemcpyAsync(b->counts, b->d_status + 2, NQ * sizeof(unsigned), cudaMemcpyDeviceToDevice, st));
+    const int g_first = cont ? 1 : 0;
     if (!cooperative && uniform && split_eligible(Su) && g_tune_split_prim) {
         // Split passes as in a single frame: camera query + primary march,
         // then per generation the continuing primaries (side stream) beside
         // the shadow/AO query and march; counts are read on the device.
         const int grid = gen_grid(true);
         const bool lines = Su.n_seg > 0;
-        for (int g = 0; g < kBatchGens; g++) {
+        for (int g = g_first; g < kBatchGens; g++) {
             FrameArgs a = A;
             for (int k = 0; k < NQ; k++) {
                 a.qin[k] = W.q[(g + 1) & 1][k];
@@ -2987,7 +3306,7 @@ static int batch_enqueue(Batch *b, const DevScene &Su, bool uniform, const Frame
         const bool split = uniform && split_eligible(Su);
         // generation g reads counts[g-1], writes counts[g] and queue set g&1
         int grid = gen_grid(uniform);
-        for (int g = 0; g < kBatchGens; g++) {
+        for (int g = g_first; g < kBatchGens; g++) {
             FrameArgs a = A;
             for (int k = 0; k < NQ; k++) {
                 a.qin[k] = W.q[(g + 1) & 1][k];
@@ -3162,6 +3481,13 @@ int gxy_gpu_batch_submit(gxy_batch batch, const gxy_job *jobs, int n_jobs, int f
     W.max_gen = 64;
     W.status = b->d_status;
     const DevScene &Su = first->S;
+    b->swap = 0;
+    b->continuations = 0;
+    b->lastA = A;
+    b->lastW = W;
+    b->lastS = Su;
+    b->last_uniform = uniform;
+    b->last_jobs = n_jobs;
     if (use_graph) {
         cudaGraph_t g;
         CK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
@@ -3196,9 +3522,27 @@ int gxy_gpu_batch_submit(gxy_batch batch, const gxy_job *jobs, int n_jobs, int f
     GUARD_END
 }
 
-static int batch_finish(Batch *b) {
-    b->pending = false;
+// A finished submission: its status, or -- when rays are left after its
+// generations and nothing overflowed -- a continuation from its queues
+// (*continued, the batch stays pending).  Up to kMaxContinuations.
+constexpr int kMaxContinuations = 64;
+static int batch_finish(Batch *b, bool *continued) {
+    *continued = false;
     int left = b->cooperative ? b->h_status[1] : (b->h_status[2] + b->h_status[3] + b->h_status[4]);
+    if (left > 0 && !b->cooperative && !b->h_ctr->overflow && b->continuations < kMaxContinuations) {
+        b->swap ^= 1;
+        b->continuations++;
+        int rc = batch_enqueue(b, b->lastS, b->last_uniform, b->lastA, b->lastW, b->last_jobs, 0, true);
+        if (rc == GXY_OK && cudaEventRecord(b->done, b->stream) != cudaSuccess)
+            rc = set_error(GXY_ERR_CUDA, "event record failed");
+        if (rc) {
+            b->pending = false;
+            return b->last_rc = rc;
+        }
+        *continued = true;
+        return GXY_OK;
+    }
+    b->pending = false;
     if (left > 0) return b->last_rc = set_error(GXY_ERR_OVERFLOW, "rays left after the generation limit");
     if (b->h_ctr->overflow) return b->last_rc = set_error(GXY_ERR_OVERFLOW, "a batch queue overflowed");
     return b->last_rc = GXY_OK;
@@ -3218,8 +3562,10 @@ int gxy_gpu_batch_poll(gxy_batch batch, int *done) {
         return GXY_OK;
     }
     if (e != cudaSuccess) return set_error(GXY_ERR_CUDA, cudaGetErrorString(e));
-    *done = 1;
-    return batch_finish(b);
+    bool cont = false;
+    int rc = batch_finish(b, &cont);
+    *done = cont ? 0 : 1;
+    return rc;
     GUARD_END
 }
 
@@ -3231,7 +3577,12 @@ int gxy_gpu_batch_wait(gxy_batch batch, int timeout_ms) {
     auto t0 = std::chrono::steady_clock::now();
     for (;;) {
         cudaError_t e = cudaEventQuery(b->done);
-        if (e == cudaSuccess) return batch_finish(b);
+        if (e == cudaSuccess) {
+            bool cont = false;
+            int rc = batch_finish(b, &cont);
+            if (!cont) return rc;
+            continue;
+        }
         if (e != cudaErrorNotReady) return set_error(GXY_ERR_CUDA, cudaGetErrorString(e));
         double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
         if (timeout_ms >= 0 && ms > timeout_ms) return set_error(GXY_ERR_TIMEOUT, "batch did not finish in time");
@@ -3254,7 +3605,8 @@ int gxy_gpu_batch_counters(gxy_batch batch, gxy_counters *out) {
     out->terminated = (int64_t)c.terminated;
     out->dropped = (int64_t)c.dropped;
     out->kept = (int64_t)c.kept;
-    out->bounces = b->cooperative ? b->h_status[0] : kBatchGens;
+    out->bounces = b->cooperative ? b->h_status[0] : kBatchGens + (int64_t)b->continuations * (kBatchGens - 1);
+    out->bands = 1;
     out->samples = (int64_t)c.samples;
     out->nodes = (int64_t)c.nodes;
     out->prim_tests = (int64_t)(c.tri_tests + c.sph_tests);

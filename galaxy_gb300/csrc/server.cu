@@ -48,6 +48,7 @@ struct SReq {
     size_t fb_bytes = 0;
     int64_t rays = 0;
     int state = R_WAITING;
+    bool cancel = false;                // cancelled while running: the result is discarded
     int error = GXY_OK;
     std::string message;
 };
@@ -96,8 +97,9 @@ void Server::finish(Slot &s) {
         SReq &r = reqs[id];
         r.t_done = t;
         r.rays = tot ? (int64_t)((double)rays * r.pixels / tot) : 0;
-        r.state = rc == GXY_OK ? R_DONE : R_FAILED;
-        r.error = rc;
+        r.state = (rc == GXY_OK && !r.cancel) ? R_DONE : R_FAILED;
+        r.error = r.cancel ? GXY_ERR_CANCELLED : rc;
+        if (r.cancel) r.message = "cancelled";
         pending--;
     }
     s.ids.clear();
@@ -285,6 +287,28 @@ int gxy_server_poll(gxy_server server, int64_t id, int *done) {
     auto it = s->reqs.find(id);
     if (it == s->reqs.end()) return set_error(GXY_ERR_INVALID, "unknown request");
     *done = it->second.state >= R_DONE ? 1 : 0;
+    return GXY_OK;
+}
+
+int gxy_server_cancel(gxy_server server, int64_t id, int *was_running) {
+    if (!server) return set_error(GXY_ERR_INVALID, "null server");
+    Server *s = reinterpret_cast<Server *>(server);
+    std::lock_guard<std::mutex> lock(s->mu);
+    auto it = s->reqs.find(id);
+    if (it == s->reqs.end()) return set_error(GXY_ERR_INVALID, "unknown request");
+    SReq &r = it->second;
+    if (was_running) *was_running = r.state == R_RUNNING;
+    if (r.state == R_WAITING) {
+        s->waiting.erase(std::find(s->waiting.begin(), s->waiting.end(), id));
+        r.state = R_FAILED;
+        r.error = GXY_ERR_CANCELLED;
+        r.message = "cancelled";
+        r.t_done = s->now();
+        s->pending--;
+        s->cv.notify_all();
+    } else if (r.state == R_RUNNING) {
+        r.cancel = true;   // its batch runs to the end; the image is discarded
+    }
     return GXY_OK;
 }
 

@@ -39,6 +39,8 @@ def lib():
         "gxy_gpu_hbm_in_use": [C.POINTER(C.c_size_t)],
         "gxy_gpu_scene_commit": [C.POINTER(A.gxy_scene_desc), C.POINTER(vp)],
         "gxy_gpu_scene_release": [vp],
+        "gxy_gpu_scene_set_tf": [vp, C.c_int, C.c_int, C.POINTER(A.gxy_tf), vp],
+        "gxy_gpu_scene_view": [vp, C.POINTER(vp)],
         "gxy_gpu_scene_partition_info": [vp, C.c_int, C.POINTER(A.gxy_partition_info)],
         "gxy_gpu_scene_bvh_info": [vp, C.POINTER(i64), C.POINTER(i64), C.POINTER(C.c_double)],
         "gxy_scene_partition_layout": [C.POINTER(A.gxy_scene_desc), C.c_int, C.POINTER(A.gxy_partition_info)],
@@ -71,6 +73,7 @@ def lib():
         "gxy_server_submit": [vp, vp, C.POINTER(A.gxy_camera), C.POINTER(A.gxy_lighting), C.POINTER(i64)],
         "gxy_server_poll": [vp, i64, C.POINTER(C.c_int)],
         "gxy_server_drain": [vp, C.c_int],
+        "gxy_server_cancel": [vp, i64, C.POINTER(C.c_int)],
         "gxy_server_take": [vp, i64, A.f32p, C.POINTER(C.c_double), C.POINTER(i64)],
     }
     for name, args in sig.items():
@@ -118,6 +121,7 @@ TUNE_CAMERA_PACKET = 9
 TUNE_SKIP_CLEAR = 10
 TUNE_SKIP_MODE = 11
 TUNE_CARRY_HITS = 13
+TUNE_QUEUE_LIMIT = 14
 
 
 def set_tuning(knob, value):
@@ -154,15 +158,36 @@ def resolve_lights(lighting, camera):
     return out
 
 
-class Scene:
-    """A committed Visualization on the device (gxy_gpu_scene_commit)."""
+VIS_VOLUME, VIS_TRIANGLES, VIS_PARTICLES, VIS_PATHLINES = 0, 1, 2, 3
 
-    def __init__(self, vis):
+
+class Scene:
+    """A committed Visualization on the device (gxy_gpu_scene_commit), or a
+    view of one (Scene.view())."""
+
+    def __init__(self, vis=None, _handle=None, _base=None):
         ensure_init()
+        if _handle is not None:
+            self.desc = _base.desc
+            self.h = _handle
+            return
         self.desc = vis.desc()
         h = C.c_void_p()
         check(lib().gxy_gpu_scene_commit(C.byref(self.desc), C.byref(h)))
         self.h = h
+
+    def view(self):
+        """A second handle sharing this scene's datasets and BVH, with its own
+        transfer functions (gxy_gpu_scene_view)."""
+        h = C.c_void_p()
+        check(lib().gxy_gpu_scene_view(self.h, C.byref(h)))
+        return Scene(_handle=h, _base=self)
+
+    def set_tf(self, kind, index, tf, stream=None):
+        """Replace the transfer function (a gxy_tf, or a MappedVis whose tf()
+        gives one) of operator `index` of `kind` (VIS_VOLUME ...)."""
+        t = tf.tf() if hasattr(tf, "tf") else tf
+        check(lib().gxy_gpu_scene_set_tf(self.h, int(kind), int(index), C.byref(t), C.c_void_p(stream or 0)))
 
     def release(self):
         if getattr(self, "h", None) and self.h.value:
@@ -204,7 +229,7 @@ class Scene:
     def counters(self):
         c = A.gxy_counters()
         check(lib().gxy_gpu_query_counters(self.h, C.byref(c)))
-        d = {f: getattr(c, f) for f, _ in A.gxy_counters._fields_ if f != "pad"}
+        d = {f: getattr(c, f) for f, _ in A.gxy_counters._fields_}
         t, s, e = C.c_int64(), C.c_int64(), C.c_int64()
         check(lib().gxy_gpu_query_counters_ex(self.h, C.byref(t), C.byref(s), C.byref(e)))
         d.update(tri_tests=t.value, sph_tests=s.value, enqueued=e.value)
@@ -319,7 +344,7 @@ class Batch:
     def counters(self):
         c = A.gxy_counters()
         check(lib().gxy_gpu_batch_counters(self.h, C.byref(c)))
-        return {f: getattr(c, f) for f, _ in A.gxy_counters._fields_ if f != "pad"}
+        return {f: getattr(c, f) for f, _ in A.gxy_counters._fields_}
 
 
 class NativeServer:
@@ -364,6 +389,12 @@ class NativeServer:
         d = C.c_int(0)
         check(lib().gxy_server_poll(self.h, int(rid), C.byref(d)))
         return bool(d.value)
+
+    def cancel(self, rid):
+        """Cancel a request; returns True if it was already running."""
+        w = C.c_int(0)
+        check(lib().gxy_server_cancel(self.h, int(rid), C.byref(w)))
+        return bool(w.value)
 
     def drain(self, timeout_ms=600000):
         check(lib().gxy_server_drain(self.h, int(timeout_ms)))

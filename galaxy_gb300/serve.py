@@ -5,8 +5,9 @@ This plays the role of Galaxy's serving front ends -- ViewerClientServer's
 returned per ServerRendering::AddLocalPixels, ServerRendering.cpp:45-66) and
 GuiClientServer's `gui::render` (src/guiserver/GuiClientServer.cpp:375-407)
 -- without their socket transport: a request names a resident scene and
-carries a camera, a light change and an image size.  The loop itself is the
-library's C++ worker (gxy_server_*, src csrc/server.cu); it
+carries a camera, a light change or a transfer-function change, and an
+image size.  The loop itself is the library's C++ worker (gxy_server_*,
+csrc/server.cu); it
 
   * admits waiting requests whenever a batch slot is free and the
     framebuffers fit the HBM budget (admission control; a request too large
@@ -17,8 +18,16 @@ library's C++ worker (gxy_server_*, src csrc/server.cu); it
   * polls the slots and records each request's latency (arrival ->
     framebuffer complete on the device); the client takes the image.
 
+A request that changes a transfer function renders through a view of its
+scene (gxy_gpu_scene_view: the datasets and BVH shared, the transfer
+functions its own) taken from a small pool per scene, so requests with
+different transfer functions are on the GPU at once while the resident
+scene keeps its own.
+
 serve_plain() serves the same requests one at a time through the plain
-single-frame path (gxy_gpu_render) for comparison.  CommandSession reads a
+single-frame path (gxy_gpu_render) for comparison, changing the resident
+scene's transfer functions in place (gxy_gpu_scene_set_tf) as a viewer's
+json command does.  CommandSession reads a
 viewer client's command lines (json / window / render / renderMany ...) and
 streams each frame's pixels back as AddLocalPixels messages.
 """
@@ -34,14 +43,15 @@ from . import scene as S
 
 class Request:
     __slots__ = ("id", "arrival", "scene", "camera", "lighting", "pixels", "fb", "t_submit", "t_done", "rays",
-                 "refused")
+                 "refused", "tf")
 
-    def __init__(self, rid, arrival, scene, camera, lighting):
+    def __init__(self, rid, arrival, scene, camera, lighting, tf=None):
         self.id = rid
         self.arrival = arrival
         self.scene = scene          # key into the scene table
         self.camera = camera        # scene.Camera
         self.lighting = lighting    # gxy_lighting (resolved)
+        self.tf = tf                # None, or [(vis kind, operator index, gxy_tf), ...]
         self.pixels = camera.width * camera.height
         self.fb = None
         self.t_submit = None
@@ -63,20 +73,40 @@ class Server:
 
     def __init__(self, scenes, n_slots=4, slot_pixels=8 << 20, max_jobs=64, max_shadow=1, max_ao=4,
                  fb_budget=8 << 30, use_graph=True, keep_results=False, cooperative=False,
-                 small_pixels=1 << 20, small_batch_pixels=4 << 20, big_wait_s=0.05):
+                 small_pixels=1 << 20, small_batch_pixels=4 << 20, big_wait_s=0.05, max_views=16):
         self.scenes = scenes
         self.keep_results = keep_results
         self.slot_pixels = slot_pixels
+        self.max_views = max_views
+        self.views = {}             # scene key -> [[view, id of its last request], ...]
         self.native = gpu.NativeServer(n_slots, slot_pixels, max_jobs, max_shadow, max_ao, fb_budget,
                                        small_pixels, small_batch_pixels, big_wait_s, use_graph, cooperative)
 
     def release(self):
         self.native.release()
+        for pool in self.views.values():
+            for v in pool:
+                v[0].release()
+        self.views = {}
 
-    def run(self, requests, time_limit=120.0):
+    def _view(self, key):
+        """A view of scene `key` whose last request has finished (a new one
+        while the pool is below max_views)."""
+        pool = self.views.setdefault(key, [])
+        while True:
+            for v in pool:
+                if v[1] is None or self.native.poll(v[1]):
+                    return v
+            if len(pool) < self.max_views:
+                pool.append([self.scenes[key].view(), None])
+                return pool[-1]
+            time.sleep(50e-6)
+
+    def run(self, requests, time_limit=120.0, keep=None):
         """Submit `requests` (sorted by arrival, seconds from start) in real
         time, wait for all, and return the statistics dict; with
-        keep_results each request's image is left in r.fb (host array)."""
+        keep_results (or r.id in `keep`) each request's image is left in
+        r.fb (host array)."""
         t0 = time.perf_counter()
         submitted = []
         for r in requests:
@@ -85,23 +115,34 @@ class Server:
                 break
             if r.arrival > now:
                 time.sleep(r.arrival - now)
+            sc, view = self.scenes[r.scene], None
+            if r.tf:
+                view = self._view(r.scene)
+                for kind, index, tf in r.tf:
+                    view[0].set_tf(kind, index, tf)
+                sc = view[0]
             try:
-                rid = self.native.submit(self.scenes[r.scene], r.camera, r.lighting)
+                rid = self.native.submit(sc, r.camera, r.lighting)
             except gpu.GxyError as e:
                 if e.code != A.GXY_ERR_ADMISSION:
                     raise
                 r.refused = True
                 continue
+            if view is not None:
+                view[1] = rid
             r.t_submit = time.perf_counter() - t0
             submitted.append((r, rid))
         left = max(1.0, time_limit - (time.perf_counter() - t0))
         self.native.drain(int(left * 1000))
         makespan = time.perf_counter() - t0
         for r, rid in submitted:
-            img, lat, rays = self.native.take(rid, image=self.keep_results)
+            img, lat, rays = self.native.take(rid, image=self.keep_results or (keep is not None and r.id in keep))
             r.t_done = r.t_submit + lat
             r.rays = rays
             r.fb = img
+        for pool in self.views.values():
+            for v in pool:
+                v[1] = None
         return summarize(requests, makespan)
 
 
@@ -117,27 +158,46 @@ def summarize(requests, makespan):
     return out
 
 
-def serve_plain(scenes, requests, time_limit=120.0):
+def serve_plain(scenes, requests, time_limit=120.0, keep=None, default_tfs=None):
     """The same requests, one at a time through the plain single-frame path
-    (gxy_gpu_render on the default stream), in arrival order."""
+    (gxy_gpu_render on torch's current stream), in arrival order.  A request
+    with transfer functions sets them on the resident scene first
+    (gxy_gpu_scene_set_tf); the next request without any restores
+    default_tfs[key] (the committed ones).  Images of requests whose id is in
+    `keep` are left in r.fb (host array)."""
     import torch
     t0 = time.perf_counter()
     stream = torch.cuda.current_stream()
+    changed = {}
     for r in requests:
         now = time.perf_counter() - t0
         if now > time_limit:
             break
         if r.arrival > now:
             time.sleep(r.arrival - now)
-        fb = torch.zeros((r.camera.height, r.camera.width, 4), dtype=torch.float32, device="cuda")
         sc = scenes[r.scene]
         r.t_submit = time.perf_counter() - t0
+        if r.tf:
+            for kind, index, tf in r.tf:
+                sc.set_tf(kind, index, tf, stream.cuda_stream)
+            changed[r.scene] = True
+        elif changed.get(r.scene):
+            for kind, index, tf in (default_tfs or {}).get(r.scene, []):
+                sc.set_tf(kind, index, tf, stream.cuda_stream)
+            changed[r.scene] = False
+        fb = torch.zeros((r.camera.height, r.camera.width, 4), dtype=torch.float32, device="cuda")
         sc.render(r.camera, r.lighting, fb.data_ptr(), stream.cuda_stream)
         stream.synchronize()
         r.t_done = time.perf_counter() - t0
         c = sc.counters()
         r.rays = c["primary_rays"] + c["shadow_rays"] + c["ao_rays"]
+        if keep is not None and r.id in keep:
+            r.fb = fb.cpu().numpy()
         del fb
+    for key, ch in changed.items():
+        if ch:
+            for kind, index, tf in (default_tfs or {}).get(key, []):
+                scenes[key].set_tf(kind, index, tf, stream.cuda_stream)
     return summarize(requests, time.perf_counter() - t0)
 
 

@@ -48,6 +48,7 @@ extern "C" {
 #define GXY_ERR_TIMEOUT    -5   /* a bounded device or host wait ran out      */
 #define GXY_ERR_ADMISSION  -6   /* request refused by the HBM budget          */
 #define GXY_ERR_NOT_INIT   -7   /* gxy_gpu_init has not been called           */
+#define GXY_ERR_CANCELLED  -8   /* the request was cancelled                   */
 
 /* ---- ray flags: src/renderer/RayFlags.h:28-36 -------------------------- */
 #define GXY_RAY_PRIMARY    0x001
@@ -220,7 +221,8 @@ typedef struct gxy_counters {
     int64_t nodes;            /* BVH8 node lines visited              */
     int64_t prim_tests;       /* primitive intersection tests         */
     int32_t overflow;         /* non-zero if a queue overflowed       */
-    int32_t pad;
+    int32_t bands;            /* bands of image rows the frame was rendered in
+                                 (1 unless its queues did not fit at once) */
     int64_t samples_skipped;  /* of `samples`: positions whose voxels were
                                  never read (both ends of their interval in
                                  bricks below the zero-opacity threshold) */
@@ -239,7 +241,36 @@ int gxy_gpu_last_error(char *buf, int buflen);
 int gxy_gpu_hbm_in_use(size_t *bytes);
 
 int gxy_gpu_scene_commit(const gxy_scene_desc *desc, gxy_scene *out);
+/* Releases one handle (a committed scene or a view); the datasets and the
+ * BVH are freed with the last handle that shares them. */
 int gxy_gpu_scene_release(gxy_scene scene);
+
+/* Operator kinds of a scene, in gxy_scene_desc order. */
+#define GXY_VIS_VOLUME     0
+#define GXY_VIS_TRIANGLES  1
+#define GXY_VIS_PARTICLES  2
+#define GXY_VIS_PATHLINES  3
+/* MappedVis_set_transferFunction (src/renderer/MappedVis.ispc:35) after
+ * MappedVis::local_commit (MappedVis.cpp:277-338) on a committed scene:
+ * replaces the transfer function of operator `index` of kind `vis_kind`.  For
+ * a volume the clear-brick flags of the empty-space skipping are recomputed
+ * on the device from per-brick bounds kept since the commit; nothing else is
+ * rebuilt (no BVH build, no re-bricking).  The work is queued on `stream`
+ * (cudaStream_t, NULL = legacy default) and the call returns once it is done,
+ * so later frames on any stream see the new function.  Frames of this scene
+ * still running on other streams must finish first (the caller orders them;
+ * a view, below, avoids the wait).  Frames equal those of a fresh commit with
+ * the new function. */
+int gxy_gpu_scene_set_tf(gxy_scene scene, int vis_kind, int index, const gxy_tf *tf, void *stream);
+/* A new handle on a committed scene, as a second Visualization over the same
+ * Datasets (Visualization.cpp:293-340 binds operators to datasets by name):
+ * the volumes, geometry and BVH are shared, the transfer functions and the
+ * clear-brick flags are the view's own (copies of the scene's current ones).
+ * gxy_gpu_scene_set_tf on a view changes only the view, so requests with
+ * different transfer functions render concurrently.  Costs the view's
+ * transfer-function table, flags and queue counters (a few MiB), no dataset
+ * copy.  Release it with gxy_gpu_scene_release. */
+int gxy_gpu_scene_view(gxy_scene scene, gxy_scene *out);
 int gxy_gpu_scene_partition_info(gxy_scene scene, int partition, gxy_partition_info *out);
 /* Host-only: the brick boxes and neighbours a commit of desc would use. */
 int gxy_scene_partition_layout(const gxy_scene_desc *desc, int partition, gxy_partition_info *out);
@@ -331,6 +362,12 @@ int gxy_gpu_set_profiling(gxy_scene scene, int on);
                                         finds before the partition exit, unmarched (same
                                         frames; fewer samples, node visits and primitive
                                         tests counted) */
+#define GXY_TUNE_QUEUE_LIMIT    14   /* largest ray-queue buffer of the frame path, in records
+                                        (0, default: none but the HBM budget).  Queues grow to
+                                        the worst case of the next launch; a frame whose camera
+                                        rays do not fit is rendered in bands of image rows; a
+                                        later generation that still runs out of room reports
+                                        GXY_ERR_OVERFLOW */
 #define GXY_TUNE_CARRY_HITS     13   /* 1 (default): a shadow/AO ray that moves to the next
                                         partition carries the closest hit its query found
                                         over its whole extent, and the next partition's
@@ -418,6 +455,12 @@ int gxy_server_release(gxy_server server);
 int gxy_server_submit(gxy_server server, gxy_scene scene, const gxy_camera *camera,
                       const gxy_lighting *lighting, int64_t *id);
 int gxy_server_poll(gxy_server server, int64_t id, int *done);
+/* Cancel a request (no counterpart in Galaxy, whose servers render each
+ * request to the end): a waiting request is removed at once; a running one
+ * finishes its batch (the other requests in it are unaffected) and its image
+ * is discarded.  gxy_server_take then returns GXY_ERR_CANCELLED for it.
+ * *was_running (may be NULL) tells which case applied. */
+int gxy_server_cancel(gxy_server server, int64_t id, int *was_running);
 /* Bounded host wait until every submitted request has finished. */
 int gxy_server_drain(gxy_server server, int timeout_ms);
 /* Copy a finished request's image to host rgba (height*width*4 fp32, or
