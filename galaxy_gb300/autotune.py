@@ -13,7 +13,10 @@ repeated while a pass still changes something):
   * split camera-ray tracing, likewise;
   * camera-ray traversal per thread (per-lane refill) or per warp (one
     shared traversal for an 8x4 pixel tile);
-  * queue chunk of the refill queries: BVH8 node visits per refill round;
+  * traversal round of the refill queries: BVH8 node visits per refill
+    round;
+  * queue chunk of the shadow/AO query: records a block takes from the ray
+    queue at once (1k-64k; as needed when 0);
   * march tiling: volume samples per refill round of the march passes;
   * clear-brick skipping: fast runs in the camera-ray march, skipping (and
     fast runs) in the shadow/AO march, the occlusion shortcut of the
@@ -38,6 +41,7 @@ KNOBS = (
     ("split_primary", gpu.TUNE_SPLIT_PRIMARY, (0, 1)),
     ("camera_packet", gpu.TUNE_CAMERA_PACKET, (0, 1)),
     ("trav_steps", gpu.TUNE_TRAV_STEPS, (4, 8, 16)),
+    ("queue_chunk", gpu.TUNE_QUEUE_CHUNK, (0, 1024, 4096, 16384, 65536)),
     ("march_steps", gpu.TUNE_MARCH_STEPS, (8, 16, 32, 64)),
     ("skip_mode", gpu.TUNE_SKIP_MODE, (0, 1, 3, 7, 9, 11)),
 )

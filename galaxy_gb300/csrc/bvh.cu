@@ -226,9 +226,8 @@ __global__ void k_refit(int n, const uint32_t *ids, const float4 *plo, const flo
 // Binned-SAH refinement of the top of the radix tree.  The radix tree is cut
 // into clusters -- maximal subtrees of at most C primitives -- and the tree
 // above them is rebuilt top down by binned SAH over the clusters' boxes
-// (build_top_sah on the host: a few thousand to a hundred thousand
-// clusters), so the levels that every ray visits get surface-area splits
-// while the bottom keeps the Morton structure.
+// (k_sah_level, on the device), so the levels that every ray visits get
+// surface-area splits while the bottom keeps the Morton structure.
 __global__ void k_clusters(int n, int C, const int *parent, const int *leaf_parent, const int *first, const int *last,
                            int *refs, unsigned int *count) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -426,130 +425,229 @@ static inline unsigned blocks_for(int64_t n, int b) { return (unsigned)((n + b -
 
 // Build the BVH8 for the geometry described by S (S.nodes/S.slots are set
 // on success).  sph_radius: per-sphere radius (device).
-// Host binned-SAH build over the clusters (box lo/hi, primitive count in
-// lo.w): 32 centroid bins on each axis, cost area(L)*prims(L) +
-// area(R)*prims(R), split at the cheapest bin boundary (by index when every
-// centroid coincides).  Node t of the result is binary node base + t; a
-// child is a cluster ref (refs[k]) or another top node.  A top node's size
-// is stated as at least 5 primitives so that the collapse, which decides
-// leaves by size (at most 4 primitives per leaf), always opens it.
-static inline int __float_as_int_host(float f) {
-    int i;
-    memcpy(&i, &f, sizeof i);
-    return i;
-}
-struct TopNode {
-    int left, right;
-    float lo[3], hi[3];
-    int count;
+// Binned-SAH build over the clusters on the device (box lo/hi, primitive
+// count in lo.w): top down, one level of split tasks per launch, one block
+// per task.  Per task: the box and the centroid bounds of its clusters; 32
+// centroid bins on each axis; cost area(L)*prims(L) + area(R)*prims(R) at
+// every bin boundary, the cheapest kept (the first of equals, axes x, y, z);
+// a stable partition at that boundary (by position when every centroid
+// coincides).  A segment of one cluster becomes a child ref (refs[k]); a
+// longer one a new top node (binary node base + id) and a task of the next
+// level.  A top node's size is stated as at least 5 primitives so that the
+// collapse, which decides leaves by size (at most 4 primitives per leaf),
+// always opens it.
+struct SahTask {
+    int node, begin, end;
 };
-static void build_top_sah(const std::vector<float4> &clo, const std::vector<float4> &chi, const std::vector<int> &refs,
-                          int base, std::vector<TopNode> &out) {
-    const int m = (int)refs.size();
-    std::vector<int> idx(m);
-    for (int k = 0; k < m; k++) idx[k] = k;
-    auto cen = [&](int k, int a) {
-        const float *l = &clo[k].x, *h = &chi[k].x;
-        return 0.5f * (l[a] + h[a]);
-    };
-    auto area = [](const float *lo, const float *hi) {
-        float x = hi[0] - lo[0], y = hi[1] - lo[1], z = hi[2] - lo[2];
-        return x * y + y * z + z * x;
-    };
-    struct Task {
-        int node, begin, end;
-    };
-    out.clear();
-    out.reserve(m > 1 ? m - 1 : 1);
-    out.push_back(TopNode{});
-    std::vector<Task> todo{{0, 0, m}};
-    constexpr int NB = 32;
-    while (!todo.empty()) {
-        Task t = todo.back();
-        todo.pop_back();
-        TopNode &nd = out[t.node];
-        float cmin[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, cmax[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
-        for (int a = 0; a < 3; a++) { nd.lo[a] = FLT_MAX; nd.hi[a] = -FLT_MAX; }
-        int count = 0;
-        for (int i = t.begin; i < t.end; i++) {
-            int k = idx[i];
-            const float *l = &clo[k].x, *h = &chi[k].x;
+constexpr int kSahBins = 32;
+
+__device__ __forceinline__ float sah_area(float lx, float ly, float lz, float hx, float hy, float hz) {
+    float x = hx - lx, y = hy - ly, z = hz - lz;
+    return x * y + y * z + z * x;
+}
+__device__ __forceinline__ float sah_cen(const float4 &lo, const float4 &hi, int a) {
+    const float l = a == 0 ? lo.x : a == 1 ? lo.y : lo.z, h = a == 0 ? hi.x : a == 1 ? hi.y : hi.z;
+    return 0.5f * (l + h);
+}
+__device__ __forceinline__ int sah_bin(float c, float cmin, float ext) {
+    return min(kSahBins - 1, (int)((c - cmin) / ext * kSahBins));
+}
+
+__global__ void __launch_bounds__(256) k_sah_level(const float4 *clo, const float4 *chi, const int *refs,
+                                                   const int *idx_in, int *idx_out, const SahTask *tin,
+                                                   const unsigned *n_in, SahTask *tout, unsigned *n_out,
+                                                   unsigned *node_ctr, int base, int *left, int *right, int *first,
+                                                   int *last, float4 *nlo, float4 *nhi) {
+    __shared__ unsigned s_lo[3], s_hi[3], s_cmin[3], s_cmax[3];
+    __shared__ int s_count;
+    __shared__ unsigned s_blo[3][kSahBins][3], s_bhi[3][kSahBins][3];
+    __shared__ int s_bn[3][kSahBins], s_bc[3][kSahBins];
+    __shared__ int s_axis, s_bin, s_nleft, s_warp[8];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const unsigned ntask = *n_in;
+    for (unsigned t = blockIdx.x; t < ntask; t += gridDim.x) {
+        const SahTask T = tin[t];
+        // 1. node box, centroid bounds, primitive count
+        if (tid < 3) {
+            s_lo[tid] = s_cmin[tid] = 0xffffffffu;
+            s_hi[tid] = s_cmax[tid] = 0u;
+        }
+        if (tid == 0) s_count = 0;
+        for (int i = tid; i < 3 * kSahBins * 3; i += blockDim.x) {
+            (&s_blo[0][0][0])[i] = 0xffffffffu;
+            (&s_bhi[0][0][0])[i] = 0u;
+        }
+        for (int i = tid; i < 3 * kSahBins; i += blockDim.x) {
+            (&s_bn[0][0])[i] = 0;
+            (&s_bc[0][0])[i] = 0;
+        }
+        __syncthreads();
+        for (int i0 = T.begin; i0 < T.end; i0 += blockDim.x) {
+            const int i = i0 + tid;
+            const bool ok = i < T.end;
+            float4 lo = make_float4(0, 0, 0, 0), hi = lo;
+            if (ok) {
+                const int k = idx_in[i];
+                lo = clo[k];
+                hi = chi[k];
+            }
+            const float l3[3] = {lo.x, lo.y, lo.z}, h3[3] = {hi.x, hi.y, hi.z};
+#pragma unroll
             for (int a = 0; a < 3; a++) {
-                nd.lo[a] = std::min(nd.lo[a], l[a]);
-                nd.hi[a] = std::max(nd.hi[a], h[a]);
-                cmin[a] = std::min(cmin[a], cen(k, a));
-                cmax[a] = std::max(cmax[a], cen(k, a));
+                const float c = 0.5f * (l3[a] + h3[a]);
+                const unsigned vl = __reduce_min_sync(0xffffffffu, ok ? f2o(l3[a]) : 0xffffffffu);
+                const unsigned vh = __reduce_max_sync(0xffffffffu, ok ? f2o(h3[a]) : 0u);
+                const unsigned cl = __reduce_min_sync(0xffffffffu, ok ? f2o(c) : 0xffffffffu);
+                const unsigned ch = __reduce_max_sync(0xffffffffu, ok ? f2o(c) : 0u);
+                if (lane == 0) {
+                    atomicMin(&s_lo[a], vl);
+                    atomicMax(&s_hi[a], vh);
+                    atomicMin(&s_cmin[a], cl);
+                    atomicMax(&s_cmax[a], ch);
+                }
             }
-            count += __float_as_int_host(clo[k].w);
+            const int cnt = __reduce_add_sync(0xffffffffu, ok ? __float_as_int(lo.w) : 0);
+            if (lane == 0) atomicAdd(&s_count, cnt);
         }
-        nd.count = count;
-        // best bin boundary over the three axes
-        float best = FLT_MAX;
-        int best_axis = -1, best_bin = 0;
+        __syncthreads();
+        float cmin[3], ext[3];
+#pragma unroll
         for (int a = 0; a < 3; a++) {
-            float ext = cmax[a] - cmin[a];
-            if (!(ext > 0.f)) continue;
-            float blo[NB][3], bhi[NB][3];
-            int bn[NB] = {0}, bc[NB] = {0};
-            for (int b = 0; b < NB; b++)
-                for (int q = 0; q < 3; q++) { blo[b][q] = FLT_MAX; bhi[b][q] = -FLT_MAX; }
-            for (int i = t.begin; i < t.end; i++) {
-                int k = idx[i];
-                int b = std::min(NB - 1, (int)((cen(k, a) - cmin[a]) / ext * NB));
-                const float *l = &clo[k].x, *h = &chi[k].x;
-                for (int q = 0; q < 3; q++) { blo[b][q] = std::min(blo[b][q], l[q]); bhi[b][q] = std::max(bhi[b][q], h[q]); }
-                bn[b] += __float_as_int_host(clo[k].w);
-                bc[b]++;
-            }
-            float llo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, lhi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
-            float lcost[NB];
-            int ln = 0, lc = 0;
-            int litems[NB];
-            for (int b = 0; b < NB; b++) {
-                for (int q = 0; q < 3; q++) { llo[q] = std::min(llo[q], blo[b][q]); lhi[q] = std::max(lhi[q], bhi[b][q]); }
-                ln += bn[b];
-                lc += bc[b];
-                litems[b] = lc;
-                lcost[b] = lc ? area(llo, lhi) * ln : 0.f;
-            }
-            float rlo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, rhi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
-            int rn = 0;
-            for (int b = NB - 1; b >= 1; b--) {
-                for (int q = 0; q < 3; q++) { rlo[q] = std::min(rlo[q], blo[b][q]); rhi[q] = std::max(rhi[q], bhi[b][q]); }
-                rn += bn[b];
-                int left_items = litems[b - 1];
-                if (left_items == 0 || left_items == t.end - t.begin) continue;
-                float cost = lcost[b - 1] + area(rlo, rhi) * rn;
-                if (cost < best) { best = cost; best_axis = a; best_bin = b - 1; }
+            cmin[a] = o2f(s_cmin[a]);
+            ext[a] = o2f(s_cmax[a]) - cmin[a];
+        }
+        // 2. bins on every axis with a centroid extent
+        for (int i = T.begin + tid; i < T.end; i += blockDim.x) {
+            const int k = idx_in[i];
+            const float4 lo = clo[k], hi = chi[k];
+            const float l3[3] = {lo.x, lo.y, lo.z}, h3[3] = {hi.x, hi.y, hi.z};
+#pragma unroll
+            for (int a = 0; a < 3; a++) {
+                if (!(ext[a] > 0.f)) continue;
+                const int b = sah_bin(sah_cen(lo, hi, a), cmin[a], ext[a]);
+#pragma unroll
+                for (int q = 0; q < 3; q++) {
+                    atomicMin(&s_blo[a][b][q], f2o(l3[q]));
+                    atomicMax(&s_bhi[a][b][q], f2o(h3[q]));
+                }
+                atomicAdd(&s_bn[a][b], __float_as_int(lo.w));
+                atomicAdd(&s_bc[a][b], 1);
             }
         }
-        int mid;
-        if (best_axis < 0) {
-            mid = (t.begin + t.end) / 2;
-        } else {
-            const int a = best_axis;
-            const float ext = cmax[a] - cmin[a];
-            auto it = std::partition(idx.begin() + t.begin, idx.begin() + t.end, [&](int k) {
-                return std::min(NB - 1, (int)((cen(k, a) - cmin[a]) / ext * NB)) <= best_bin;
-            });
-            mid = (int)(it - idx.begin());
-            if (mid == t.begin || mid == t.end) mid = (t.begin + t.end) / 2;
-        }
-        int child[2];
-        const int rb[2] = {t.begin, mid}, re[2] = {mid, t.end};
-        for (int c = 0; c < 2; c++) {
-            if (re[c] - rb[c] == 1) {
-                child[c] = refs[idx[rb[c]]];
-            } else {
-                int id = (int)out.size();
-                out.push_back(TopNode{});
-                todo.push_back({id, rb[c], re[c]});
-                child[c] = base + id;
+        __syncthreads();
+        // 3. the cheapest bin boundary (as the sweep from both ends)
+        if (tid == 0) {
+            float best = FLT_MAX;
+            int best_axis = -1, best_bin = 0, best_left = 0;
+            for (int a = 0; a < 3; a++) {
+                if (!(ext[a] > 0.f)) continue;
+                float lcost[kSahBins];
+                int litems[kSahBins];
+                float llo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, lhi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+                int ln = 0, lc = 0;
+                for (int b = 0; b < kSahBins; b++) {
+                    for (int q = 0; q < 3; q++) {
+                        if (s_bc[a][b]) {
+                            llo[q] = fminf(llo[q], o2f(s_blo[a][b][q]));
+                            lhi[q] = fmaxf(lhi[q], o2f(s_bhi[a][b][q]));
+                        }
+                    }
+                    ln += s_bn[a][b];
+                    lc += s_bc[a][b];
+                    litems[b] = lc;
+                    lcost[b] = lc ? sah_area(llo[0], llo[1], llo[2], lhi[0], lhi[1], lhi[2]) * ln : 0.f;
+                }
+                float rlo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, rhi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+                int rn = 0;
+                for (int b = kSahBins - 1; b >= 1; b--) {
+                    for (int q = 0; q < 3; q++) {
+                        if (s_bc[a][b]) {
+                            rlo[q] = fminf(rlo[q], o2f(s_blo[a][b][q]));
+                            rhi[q] = fmaxf(rhi[q], o2f(s_bhi[a][b][q]));
+                        }
+                    }
+                    rn += s_bn[a][b];
+                    const int left_items = litems[b - 1];
+                    if (left_items == 0 || left_items == T.end - T.begin) continue;
+                    const float cost = lcost[b - 1] + sah_area(rlo[0], rlo[1], rlo[2], rhi[0], rhi[1], rhi[2]) * rn;
+                    if (cost < best) {
+                        best = cost;
+                        best_axis = a;
+                        best_bin = b - 1;
+                        best_left = left_items;
+                    }
+                }
             }
+            s_axis = best_axis;
+            s_bin = best_bin;
+            s_nleft = best_axis < 0 ? (T.end - T.begin) / 2 : best_left;
         }
-        out[t.node].left = child[0];
-        out[t.node].right = child[1];
+        __syncthreads();
+        const int axis = s_axis, bbin = s_bin, nleft = s_nleft;
+        // 4. stable partition into idx_out (order kept on each side)
+        int lbase = 0, rbase = 0;
+        for (int i0 = T.begin; i0 < T.end; i0 += blockDim.x) {
+            const int i = i0 + tid;
+            const bool ok = i < T.end;
+            int k = 0;
+            bool is_left = false;
+            if (ok) {
+                k = idx_in[i];
+                is_left = axis < 0 ? (i - T.begin) < nleft
+                                   : sah_bin(sah_cen(clo[k], chi[k], axis), cmin[axis], ext[axis]) <= bbin;
+            }
+            const unsigned bl = __ballot_sync(0xffffffffu, ok && is_left);
+            const unsigned br = __ballot_sync(0xffffffffu, ok && !is_left);
+            if (lane == 0) s_warp[warp] = (int)(__popc(bl) | (__popc(br) << 16));
+            __syncthreads();
+            int lo_l = 0, lo_r = 0, tot_l = 0, tot_r = 0;
+            for (int w = 0; w < (int)(blockDim.x >> 5); w++) {
+                const int v = s_warp[w];
+                if (w < warp) {
+                    lo_l += v & 0xffff;
+                    lo_r += v >> 16;
+                }
+                tot_l += v & 0xffff;
+                tot_r += v >> 16;
+            }
+            const unsigned lt = (1u << lane) - 1u;
+            if (ok) {
+                const int pos = is_left ? T.begin + lbase + lo_l + __popc(bl & lt)
+                                        : T.begin + nleft + rbase + lo_r + __popc(br & lt);
+                idx_out[pos] = k;
+            }
+            lbase += tot_l;
+            rbase += tot_r;
+            __syncthreads();
+        }
+        // 5. the node and its children
+        if (tid == 0) {
+            const int node = base + T.node;
+            nlo[node] = make_float4(o2f(s_lo[0]), o2f(s_lo[1]), o2f(s_lo[2]), 0.f);
+            nhi[node] = make_float4(o2f(s_hi[0]), o2f(s_hi[1]), o2f(s_hi[2]), 0.f);
+            first[node] = 0;
+            last[node] = max(s_count, 5) - 1;   // stated size >= 5: never a leaf
+            const int rb[2] = {T.begin, T.begin + nleft}, re[2] = {T.begin + nleft, T.end};
+            int child[2];
+            for (int c = 0; c < 2; c++) {
+                if (re[c] - rb[c] == 1) {
+                    child[c] = refs[idx_out[rb[c]]];
+                } else {
+                    const int id = (int)atomicAdd(node_ctr, 1u);
+                    tout[atomicAdd(n_out, 1u)] = SahTask{id, rb[c], re[c]};
+                    child[c] = base + id;
+                }
+            }
+            left[node] = child[0];
+            right[node] = child[1];
+        }
+        __syncthreads();
     }
+}
+
+__global__ void k_iota(int m, int *idx) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < m) idx[i] = i;
 }
 
 int build_bvh8(DevScene &S, const float *sph_radius, DeviceArena &arena, cudaStream_t st, BVHInfo &info) {
@@ -619,33 +717,35 @@ int build_bvh8(DevScene &S, const float *sph_radius, DeviceArena &arena, cudaStr
             k_cluster_info<<<blocks_for(m, 256), 256, 0, st>>>((int)m, refs, B.ids2, B.plo, B.phi, B.first, B.last,
                                                                B.nlo, B.nhi, clo, chi);
             CK(cudaGetLastError());
-            std::vector<int> h_refs(m);
-            std::vector<float4> h_lo(m), h_hi(m);
-            CK(cudaMemcpyAsync(h_refs.data(), refs, m * sizeof(int), cudaMemcpyDeviceToHost, st));
-            CK(cudaMemcpyAsync(h_lo.data(), clo, m * sizeof(float4), cudaMemcpyDeviceToHost, st));
-            CK(cudaMemcpyAsync(h_hi.data(), chi, m * sizeof(float4), cudaMemcpyDeviceToHost, st));
-            CK(cudaStreamSynchronize(st));
-            std::vector<TopNode> top;
+            // the top tree on the device, level by level; the host reads the
+            // number of open tasks once per 16 levels
+            int *idxa, *idxb;
+            SahTask *ta, *tb;
+            unsigned *tctr;   // [0], [1] task counts (ping-pong), [2] top nodes
+            ALLOC(idxa, m); ALLOC(idxb, m); ALLOC(ta, m); ALLOC(tb, m); ALLOC(tctr, 4);
+            k_iota<<<blocks_for(m, 256), 256, 0, st>>>((int)m, idxa);
+            const SahTask root_task{0, 0, (int)m};
+            const unsigned c0[4] = {1u, 0u, 1u, 0u};
+            CK(cudaMemcpyAsync(ta, &root_task, sizeof root_task, cudaMemcpyHostToDevice, st));
+            CK(cudaMemcpyAsync(tctr, c0, sizeof c0, cudaMemcpyHostToDevice, st));
             const int base = ni;
-            build_top_sah(h_lo, h_hi, h_refs, base, top);
-            const int t = (int)top.size();
-            std::vector<int> L(t), R(t), F(t), Z(t);
-            std::vector<float4> LO(t), HI(t);
-            for (int k = 0; k < t; k++) {
-                L[k] = top[k].left;
-                R[k] = top[k].right;
-                F[k] = 0;
-                Z[k] = std::max(top[k].count, 5) - 1;   // stated size >= 5: never a leaf
-                LO[k] = make_float4(top[k].lo[0], top[k].lo[1], top[k].lo[2], 0.f);
-                HI[k] = make_float4(top[k].hi[0], top[k].hi[1], top[k].hi[2], 0.f);
+            int cur = 0;
+            for (int lvl = 0;; lvl += 16) {
+                for (int k = 0; k < 16; k++) {
+                    CK(cudaMemsetAsync(tctr + (cur ^ 1), 0, sizeof(unsigned), st));
+                    k_sah_level<<<1024, 256, 0, st>>>(clo, chi, refs, cur ? idxb : idxa, cur ? idxa : idxb,
+                                                      cur ? tb : ta, tctr + cur, cur ? ta : tb, tctr + (cur ^ 1),
+                                                      tctr + 2, base, B.left, B.right, B.first, B.last, B.nlo,
+                                                      B.nhi);
+                    cur ^= 1;
+                }
+                CK(cudaGetLastError());
+                unsigned open = 0;
+                CK(cudaMemcpyAsync(&open, tctr + cur, sizeof open, cudaMemcpyDeviceToHost, st));
+                CK(cudaStreamSynchronize(st));
+                if (!open) break;
+                if (lvl > (int)m) return set_error(GXY_ERR_INVALID, "SAH top build did not converge");
             }
-            CK(cudaMemcpyAsync(B.left + base, L.data(), t * sizeof(int), cudaMemcpyHostToDevice, st));
-            CK(cudaMemcpyAsync(B.right + base, R.data(), t * sizeof(int), cudaMemcpyHostToDevice, st));
-            CK(cudaMemcpyAsync(B.first + base, F.data(), t * sizeof(int), cudaMemcpyHostToDevice, st));
-            CK(cudaMemcpyAsync(B.last + base, Z.data(), t * sizeof(int), cudaMemcpyHostToDevice, st));
-            CK(cudaMemcpyAsync(B.nlo + base, LO.data(), t * sizeof(float4), cudaMemcpyHostToDevice, st));
-            CK(cudaMemcpyAsync(B.nhi + base, HI.data(), t * sizeof(float4), cudaMemcpyHostToDevice, st));
-            CK(cudaStreamSynchronize(st));   // the host vectors go out of scope
             root_ref = base;
             info.sah_levels = (int)m;   // clusters under the SAH top tree
         }

@@ -146,12 +146,14 @@ class Server:
         return summarize(requests, makespan)
 
 
-def summarize(requests, makespan):
+def summarize(requests, makespan, busy_s=None):
     lat = np.array([r.t_done - r.arrival for r in requests if r.t_done is not None])
     rays = sum(r.rays for r in requests if r.t_done is not None)
     out = {"requests": len(requests), "completed": int(len(lat)),
            "refused": int(sum(1 for r in requests if r.refused)), "makespan_s": makespan,
            "rays": float(rays), "rays_per_s": float(rays / makespan) if makespan > 0 else 0.0}
+    if busy_s is not None and makespan > 0:
+        out["gpu_busy_frac"] = float(busy_s / makespan)   # time with a request on the GPU
     if len(lat):
         out.update(p50_ms=float(np.percentile(lat, 50) * 1e3), p95_ms=float(np.percentile(lat, 95) * 1e3),
                    p99_ms=float(np.percentile(lat, 99) * 1e3), mean_ms=float(lat.mean() * 1e3))
@@ -198,7 +200,8 @@ def serve_plain(scenes, requests, time_limit=120.0, keep=None, default_tfs=None)
         if ch:
             for kind, index, tf in (default_tfs or {}).get(key, []):
                 scenes[key].set_tf(kind, index, tf, stream.cuda_stream)
-    return summarize(requests, time.perf_counter() - t0)
+    busy = sum(r.t_done - r.t_submit for r in requests if r.t_done is not None)
+    return summarize(requests, time.perf_counter() - t0, busy)
 
 
 def poisson_requests(rate, count, scene_keys, make_request, seed=7, side_range=(256, 4096)):

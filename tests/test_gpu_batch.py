@@ -1,6 +1,7 @@
 """Batched frames (one persistent wavefront launch for many jobs) and the
 continuous-batching serving loop: every job's image equals the same frame
-rendered alone through the plain path (within float-atomic ordering)."""
+rendered alone through the plain path (within float-atomic ordering), and
+served requests match the oracle's render of the same camera and lighting."""
 import numpy as np
 import pytest
 
@@ -105,6 +106,15 @@ def test_serving_results_match_alone(env):
         ref = alone(torch, table[r.scene], r.camera, r.lighting)
         assert np.abs(r.fb - ref).max() <= 1e-5
     srv.release()
+    # and against the oracle: a request served in the mix is the reference
+    # path's image of its camera and lighting
+    import oracle_lib as O
+    for r in reqs[:6]:
+        vis = sc[r.scene][2]
+        ref, cnt = O.OracleScene(vis).render(r.camera, S.resolve_lights(vis.lighting, r.camera))
+        d = np.abs(r.fb[..., :3] - ref[..., :3])
+        assert float(np.sqrt(np.mean(d ** 2))) <= 1e-3
+        assert float(np.mean(d <= 2.0 / 255)) >= 0.999
 
 
 def test_native_server_contract(env):
