@@ -915,7 +915,7 @@ __device__ __forceinline__ void put_ray(DRay *q, unsigned idx, V3 o, float t, V3
 }
 
 enum { Q_PRIM = 0, Q_SHADOW = 1, Q_AO = 2, NQ = 3 };
-enum { K_CAMERA = 0, K_PRIMARY = 1, K_SECONDARY = 2, K_MARCH = 3, K_PMARCH = 4 };
+enum { K_CAMERA = 0, K_PRIMARY = 1, K_SECONDARY = 2, K_MARCH = 3, K_PMARCH = 4, K_PQUERY = 5 };
 constexpr int kMaxJobs = 1024;
 
 // One render job (a camera x visualization of a RenderingSet).
@@ -954,6 +954,7 @@ struct FrameArgs {
     unsigned qmarch_cap;
     // split primary tracing: camera query pass -> primary march queue -> march pass
     int trav_steps;                    // refill query passes: BVH8 node visits per refill round
+    int queue_chunk;                   // shadow/AO query: records a warp takes from the queue at once (0: as needed)
     int march_steps;                   // refill march passes: samples per refill round
     int skip_mode;                     // GXY_TUNE_SKIP_MODE bits
     int split_prim;
@@ -1441,6 +1442,9 @@ __global__ void __launch_bounds__(kThreads, MINB) k_sec_query(DevScene S, FrameA
     const unsigned ns = BATCH ? min(__ldg(A.nin_dev + Q_SHADOW), A.qcap[Q_SHADOW]) : A.nin[Q_SHADOW];
     const unsigned n = ns + (BATCH ? min(__ldg(A.nin_dev + Q_AO), A.qcap[Q_AO]) : A.nin[Q_AO]);
     unsigned *cursor = A.qmarch_count + 2;
+    // records this warp has taken from the queue and not yet handed out:
+    // [wnext, wend), refilled queue_chunk records at a time (GXY_TUNE_QUEUE_CHUNK)
+    unsigned wnext = 0, wend = 0;
     TravState T;
     uint2 stack_mem[64];
     LocalStack stack{stack_mem};
@@ -1452,13 +1456,32 @@ __global__ void __launch_bounds__(kThreads, MINB) k_sec_query(DevScene S, FrameA
     for (;;) {
         bool need = !have;
         unsigned mask = __ballot_sync(0xffffffffu, need);
-        unsigned base = 0;
+        unsigned base = 0, split = 32, base2 = 0;   // ranks below `split` from base, the rest from base2
         if (mask) {
-            if (lane == 0) base = atomicAdd(cursor, (unsigned)__popc(mask));
-            base = __shfl_sync(0xffffffffu, base, 0);
+            const unsigned cnt = (unsigned)__popc(mask);
+            if (A.queue_chunk <= 0) {
+                if (lane == 0) base = atomicAdd(cursor, cnt);
+                base = __shfl_sync(0xffffffffu, base, 0);
+            } else {
+                const unsigned avail = wend - wnext;
+                base = wnext;
+                if (avail >= cnt) {
+                    wnext += cnt;
+                } else {
+                    const unsigned take = max((unsigned)A.queue_chunk, cnt - avail);
+                    unsigned nb = 0;
+                    if (lane == 0) nb = atomicAdd(cursor, take);
+                    nb = __shfl_sync(0xffffffffu, nb, 0);
+                    split = avail;
+                    base2 = nb;
+                    wnext = nb + (cnt - avail);
+                    wend = nb + take;
+                }
+            }
         }
         if (need) {
-            unsigned idx = base + __popc(mask & ((1u << lane) - 1u));
+            const unsigned r = __popc(mask & ((1u << lane) - 1u));
+            unsigned idx = r < split ? base + r : base2 + (r - split);
             if (idx < n) {
                 TraceIn in;
                 int x, y, job;
@@ -1703,6 +1726,87 @@ __global__ void __launch_bounds__(kThreads, MINB) k_cam_query(DevScene S, FrameA
                                    (zmask & 4) ? 0.f : T.dir.z, FLT_MAX);
                 r->c = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
                 r->m = make_int4(x, y, make_meta(GXY_RAY_PRIMARY | (surface ? 8 : 0), part, job), __float_as_int(ray_t));
+                A.pmarch_hit[2 * (size_t)idx] = make_float4(hit_n.x, hit_n.y, hit_n.z, hit_c.x);
+                A.pmarch_hit[2 * (size_t)idx + 1] = make_float4(hit_c.y, hit_c.z, 0.0f, 0.0f);
+            }
+        }
+        if (fin) have = false;
+    }
+    flush_counters(A.ctr, c, st);
+}
+
+// Query pass of split tracing for handed-off primaries (single-frame path,
+// generations after the camera's): the primary queue's rays, each carrying
+// its composited colour and distance, with per-lane refill as k_cam_query --
+// clip to the ray's brick, slices, resumable BVH8 traversal -- then a march
+// record (stop distance, surface flag, hit normal and colour beside it) for
+// k_prim_march, which composites with clear-brick skipping, shades, spawns,
+// classifies and routes exactly as for camera rays.
+template <int MINB, bool LINES>
+__global__ void __launch_bounds__(kThreads, MINB) k_prim_query(DevScene S, FrameArgs A) {
+    __shared__ DevTF tfs[kMaxVol];
+    load_tfs(S, tfs);
+    RayStats st;
+    LocalCounters c;
+    const int lane = threadIdx.x & 31;
+    const unsigned n = A.nin[Q_PRIM];
+    unsigned *cursor = A.pmarch_count + 2;
+    TravState T;
+    uint2 stack_mem[64];
+    LocalStack stack{stack_mem};
+    V3 hit_n = v3(0, 0, 0), hit_c = v3(0, 0, 0);
+    unsigned src = 0;
+    float ray_t = 0.0f;
+    bool have = false, done = false, surface = false;
+    for (;;) {
+        const bool need = !have;
+        const unsigned mask = __ballot_sync(0xffffffffu, need);
+        unsigned base = 0;
+        if (mask) {
+            if (lane == 0) base = atomicAdd(cursor, (unsigned)__popc(mask));
+            base = __shfl_sync(0xffffffffu, base, 0);
+        }
+        if (need) {
+            const unsigned idx = base + __popc(mask & ((1u << lane) - 1u));
+            if (idx < n) {
+                TraceIn in;
+                int x, y, job;
+                src = idx;
+                load_ray(A.qin[Q_PRIM], idx, in, x, y, job);
+                c.seg++;
+                V3 dir;
+                float ray_t0, tEntry, tExitVolume;
+                sec_clip(S, in, dir, ray_t0, ray_t, tEntry, tExitVolume);
+                surface = false;
+                hit_n = v3(0, 0, 0);
+                hit_c = v3(0, 0, 0);
+                cam_slices(S, tfs, in.org, dir, ray_t0, ray_t, surface, hit_n, hit_c);
+                done = trav_init(S, T, in.org, dir, ray_t0, ray_t);
+                have = true;
+            }
+        }
+        if (!__any_sync(0xffffffffu, have)) break;
+#pragma unroll 1
+        for (int k = 0; k < max(A.trav_steps, 1) && have && !done; k++)
+            done = trav_step<LINES>(S, T, stack, st.nodes, st.tris, st.sphs, st.ovf);
+        const bool fin = have && done;
+        if (fin && T.found) {
+            ray_t = T.h.t;
+            surface = true;
+            geometry_shade(S, T.h, T.org, T.dir, hit_n, hit_c);
+        }
+        if (__any_sync(0xffffffffu, fin)) {
+            const unsigned idx = warp_reserve(fin ? 1u : 0u, A.pmarch_count, A.pmarch_cap, c.ovf);
+            if (fin && idx != 0xffffffffu) {
+                // the input record with the stop distance and the surface
+                // flag; the hit beside it
+                const float4 *q = reinterpret_cast<const float4 *>(A.qin[Q_PRIM] + src);
+                const int4 m = __ldg(reinterpret_cast<const int4 *>(q + 3));
+                DRay *r = A.pmarch + idx;
+                r->o = __ldg(q);
+                r->d = __ldg(q + 1);
+                r->c = __ldg(q + 2);
+                r->m = make_int4(m.x, m.y, m.z | (surface ? 8 : 0), __float_as_int(ray_t));
                 A.pmarch_hit[2 * (size_t)idx] = make_float4(hit_n.x, hit_n.y, hit_n.z, hit_c.x);
                 A.pmarch_hit[2 * (size_t)idx + 1] = make_float4(hit_c.y, hit_c.z, 0.0f, 0.0f);
             }
@@ -2134,6 +2238,8 @@ static int g_tune_march_steps = 16; // samples per refill round of the march pas
 static int g_tune_skip_mode = 9;    // clear-brick skipping per pass (GXY_TUNE_SKIP_MODE bits)
 static int g_tune_carry_hits = 1;   // hand the closest hit on with shadow/AO rays that change partition
 static int g_tune_cam_packet = 1;   // single-frame camera query: warp-cooperative (1) or per-lane refill (0)
+static int g_tune_queue_chunk = 0;  // shadow/AO query: records per block taken from the queue at once (0: as needed)
+static int g_tune_split_handoff = 1; // handed-off primaries of volume scenes: query + skipping march (1) or one pass (0)
 int leaf_max() { return g_tune_leaf; }
 
 // The split path applies to volume-rendered scenes with one volume and no
@@ -2373,6 +2479,7 @@ static int render(Scene *sc, const gxy_camera &cam, const gxy_lighting &lt, floa
     A.job0.pix0 = 0;
     A.n_jobs = 1;
     A.trav_steps = g_tune_trav_steps;
+    A.queue_chunk = g_tune_queue_chunk / (kThreads / 32);
     A.march_steps = g_tune_march_steps;
     A.skip_mode = g_tune_skip_mode;
     A.qmarch_count = sc->qcount + 12;   // [0] records, [1] march cursor, [2] query cursor
@@ -2390,7 +2497,8 @@ static int render(Scene *sc, const gxy_camera &cam, const gxy_lighting &lt, floa
         unsigned g = grid_for(items);
         if (sc->profile) CK(cudaEventRecord(sc->events[2 * nl_launch], st));
         if (kind == K_SECONDARY && A.split) CK(cudaMemsetAsync(A.qmarch_count, 0, 3 * sizeof(unsigned), st));
-        if (kind == K_CAMERA && A.split_prim) CK(cudaMemsetAsync(A.pmarch_count, 0, 4 * sizeof(unsigned), st));
+        if ((kind == K_CAMERA && A.split_prim) || kind == K_PQUERY)
+            CK(cudaMemsetAsync(A.pmarch_count, 0, 4 * sizeof(unsigned), st));
         if (g_tune_minb == 3) {
             if (kind == K_CAMERA && A.split_prim && g_tune_cam_packet && lines)
                 k_cam_packet<4, true><<<query_grid(), kThreads, 0, st>>>(S, A);
@@ -2404,6 +2512,8 @@ static int render(Scene *sc, const gxy_camera &cam, const gxy_lighting &lt, floa
             else if (kind == K_SECONDARY && A.split) k_sec_query<false, 4, false><<<query_grid(), kThreads, 0, st>>>(S, A);
             else if (kind == K_SECONDARY) k_secondary<3><<<g, kThreads, 0, st>>>(S, A);
             else if (kind == K_PMARCH) launch_prim_march<false, 3>(march_grid(3), st, S, A);
+            else if (kind == K_PQUERY && lines) k_prim_query<4, true><<<query_grid(), kThreads, 0, st>>>(S, A);
+            else if (kind == K_PQUERY) k_prim_query<4, false><<<query_grid(), kThreads, 0, st>>>(S, A);
             else launch_sec_march<false, 4>(query_grid(), st, S, A);
         } else {
             if (kind == K_CAMERA && A.split_prim && g_tune_cam_packet && lines)
@@ -2418,6 +2528,8 @@ static int render(Scene *sc, const gxy_camera &cam, const gxy_lighting &lt, floa
             else if (kind == K_SECONDARY && A.split) k_sec_query<false, 2, false><<<march_grid(2), kThreads, 0, st>>>(S, A);
             else if (kind == K_SECONDARY) k_secondary<2><<<g, kThreads, 0, st>>>(S, A);
             else if (kind == K_PMARCH) launch_prim_march<false, 2>(march_grid(2), st, S, A);
+            else if (kind == K_PQUERY && lines) k_prim_query<2, true><<<march_grid(2), kThreads, 0, st>>>(S, A);
+            else if (kind == K_PQUERY) k_prim_query<2, false><<<march_grid(2), kThreads, 0, st>>>(S, A);
             else launch_sec_march<false, 2>(march_grid(2), st, S, A);
         }
         CK(cudaGetLastError());
@@ -2503,9 +2615,16 @@ static int render(Scene *sc, const gxy_camera &cam, const gxy_lighting &lt, floa
             if (grc == GXY_OK && A.split)
                 grc = grow((void **)&sc->qmarch, (void **)&sc->qmarch_hit, &sc->qmarch_cap,
                            (size_t)n[Q_SHADOW] + n[Q_AO] + 32, sizeof(DRay), sizeof(float));
+            const bool split_handoff = split_prim && g_tune_split_handoff && n[Q_PRIM];
+            if (grc == GXY_OK && split_handoff)
+                grc = grow((void **)&sc->pmarch, (void **)&sc->pmarch_hit, &sc->pmarch_cap, (size_t)n[Q_PRIM] + 32,
+                           sizeof(DRay), 2 * sizeof(float4));
             // a queue that cannot grow keeps its room; a generation that then
             // runs out of it reports GXY_ERR_OVERFLOW
             if (grc) cudaGetLastError();
+            A.pmarch = sc->pmarch;
+            A.pmarch_hit = sc->pmarch_hit;
+            A.pmarch_cap = (unsigned)sc->pmarch_cap;
             A.qmarch = sc->qmarch;
             A.qmarch_hit = g_tune_carry_hits ? sc->qmarch_hit : nullptr;
             A.qmarch_cap = (unsigned)sc->qmarch_cap;
@@ -2523,12 +2642,17 @@ static int render(Scene *sc, const gxy_camera &cam, const gxy_lighting &lt, floa
             // the side stream beside the shadow/AO passes.
             const bool sec = n[Q_SHADOW] + n[Q_AO] != 0;
             const bool overlap = n[Q_PRIM] && sec;
-            if (nl_launch + 3 > maxl && (rc = collect())) return rc;
+            if (nl_launch + 4 > maxl && (rc = collect())) return rc;
             if (overlap) {
                 CK(cudaEventRecord(sc->fork, st));
                 CK(cudaStreamWaitEvent(sc->side, sc->fork, 0));
             }
-            if (n[Q_PRIM] && (rc = launch(K_PRIMARY, gen, n[Q_PRIM], n[Q_PRIM], overlap ? sc->side : st))) return rc;
+            if (n[Q_PRIM] && split_handoff) {
+                if ((rc = launch(K_PQUERY, gen, n[Q_PRIM], n[Q_PRIM], overlap ? sc->side : st))) return rc;
+                if ((rc = launch(K_PMARCH, gen, 0, 1 << 30, overlap ? sc->side : st))) return rc;
+            } else if (n[Q_PRIM] && (rc = launch(K_PRIMARY, gen, n[Q_PRIM], n[Q_PRIM], overlap ? sc->side : st))) {
+                return rc;
+            }
             if (overlap) CK(cudaEventRecord(sc->join, sc->side));
             if (sec && (rc = launch(K_SECONDARY, gen, n[Q_SHADOW] + n[Q_AO], (int64_t)n[Q_SHADOW] + n[Q_AO], st)))
                 return rc;
@@ -2933,6 +3057,16 @@ int gxy_gpu_set_tuning(int knob, int value) {
         g_tune_skip_mode = value;
         return GXY_OK;
     }
+    if (knob == GXY_TUNE_SPLIT_HANDOFF) {
+        g_tune_split_handoff = value ? 1 : 0;
+        return GXY_OK;
+    }
+    if (knob == GXY_TUNE_QUEUE_CHUNK) {
+        if (value != 0 && (value < 256 || value > 65536))
+            return set_error(GXY_ERR_INVALID, "queue chunk must be 0 or 256-65536 records");
+        g_tune_queue_chunk = value;
+        return GXY_OK;
+    }
     if (knob == GXY_TUNE_QUEUE_LIMIT) {
         if (value < 0) return set_error(GXY_ERR_INVALID, "queue limit must be >= 0");
         g_tune_queue_limit = value;
@@ -2956,6 +3090,8 @@ int gxy_gpu_get_tuning(int knob, int *value) {
     else if (knob == GXY_TUNE_SKIP_MODE) *value = g_tune_skip_mode;
     else if (knob == GXY_TUNE_CARRY_HITS) *value = g_tune_carry_hits;
     else if (knob == GXY_TUNE_QUEUE_LIMIT) *value = g_tune_queue_limit;
+    else if (knob == GXY_TUNE_QUEUE_CHUNK) *value = g_tune_queue_chunk;
+    else if (knob == GXY_TUNE_SPLIT_HANDOFF) *value = g_tune_split_handoff;
     else return set_error(GXY_ERR_INVALID, "unknown tuning knob");
     return GXY_OK;
 }
@@ -3468,6 +3604,7 @@ int gxy_gpu_batch_submit(gxy_batch batch, const gxy_job *jobs, int n_jobs, int f
     A.jobs = b->d_jobs;
     A.n_jobs = n_jobs;
     A.trav_steps = g_tune_trav_steps;
+    A.queue_chunk = g_tune_queue_chunk / (kThreads / 32);
     A.march_steps = g_tune_march_steps;
     A.skip_mode = g_tune_skip_mode;
     A.total_pix = pix;

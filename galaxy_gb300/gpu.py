@@ -122,6 +122,8 @@ TUNE_SKIP_CLEAR = 10
 TUNE_SKIP_MODE = 11
 TUNE_CARRY_HITS = 13
 TUNE_QUEUE_LIMIT = 14
+TUNE_QUEUE_CHUNK = 15
+TUNE_SPLIT_HANDOFF = 16
 
 
 def set_tuning(knob, value):

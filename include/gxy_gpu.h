@@ -368,6 +368,15 @@ int gxy_gpu_set_profiling(gxy_scene scene, int on);
                                         rays do not fit is rendered in bands of image rows; a
                                         later generation that still runs out of room reports
                                         GXY_ERR_OVERFLOW */
+#define GXY_TUNE_SPLIT_HANDOFF  16   /* 1 (default): primaries handed to the next partition of a
+                                        volume scene are traced as camera rays are, a query pass
+                                        plus the camera-ray march with clear-brick skipping; 0: one
+                                        pass per ray (same frames) */
+#define GXY_TUNE_QUEUE_CHUNK    15   /* shadow/AO query: records per 256-thread block taken from
+                                        the ray queue at once, 256-65536; each of the block's 8
+                                        warps takes 1/8 of them as one consecutive run and hands
+                                        them to its idle lanes in queue order (0, default: a warp
+                                        takes exactly what its idle lanes need) */
 #define GXY_TUNE_CARRY_HITS     13   /* 1 (default): a shadow/AO ray that moves to the next
                                         partition carries the closest hit its query found
                                         over its whole extent, and the next partition's

@@ -241,3 +241,27 @@ def test_offset_anisotropic_volume(gpu, level):
     assert ca["samples_skipped"] > 0.1 * ca["samples"]
     ref, cnt = O.OracleScene(vis).render(cam, L, nthreads=8)
     image_close(a, ref)
+
+
+@pytest.mark.parametrize("parts", [(2, 2, 2), (4, 1, 1)])
+def test_handed_off_primaries_split_same_frames(gpu, parts):
+    """Primaries handed to the next brick traced as a query pass plus the
+    skipping camera-ray march (GXY_TUNE_SPLIT_HANDOFF 1) or in one pass per
+    ray (0): the same frames and ray counters, and the oracle's image."""
+    cam, vis = scenes.mixed_scene(n=96, n_spheres=20000, width=128, height=128, partitions=parts, n_ao=2)
+    L = S.resolve_lights(vis.lighting, cam)
+    sc = gpu.Scene(vis)
+    out = {}
+    try:
+        for v in (0, 1):
+            gpu.set_tuning(gpu.TUNE_SPLIT_HANDOFF, v)
+            out[v] = (sc.render_host(cam, L), sc.counters())
+    finally:
+        gpu.set_tuning(gpu.TUNE_SPLIT_HANDOFF, 1)
+    (a, ca), (b, cb) = out[1], out[0]
+    assert ca["handoffs"] > 0
+    assert float(np.abs(a - b).max()) <= ATOMIC_ORDER_TOL
+    for k in ("primary_rays", "shadow_rays", "ao_rays", "segments", "handoffs", "terminated", "dropped", "samples"):
+        assert ca[k] == cb[k], k
+    ref, cnt = O.OracleScene(vis).render(cam, L)
+    image_close(a, ref)
