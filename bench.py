@@ -382,9 +382,11 @@ def run_batch(args):
     jobs = [make(j) for j in range(args.jobs)]
     warm = [make(1000 + j, 256) for j in range(6)]
     slot_pixels = 2048 * 2048
-    n_slots = max(args.slots, 4)   # 4-8 slot streams measured alike (1.60-1.62x), 2 slower (1.52x)
-    srv = serve.Server(table, n_slots=n_slots, slot_pixels=slot_pixels, max_jobs=64, max_shadow=1, max_ao=4,
-                       fb_budget=16 << 30, use_graph=True, small_pixels=1 << 20, small_batch_pixels=4 << 20)
+    n_slots = args.batch_slots
+    small, small_batch = args.small_pixels, args.small_batch_pixels
+    srv = serve.Server(table, n_slots=n_slots, slot_pixels=max(slot_pixels, small_batch), max_jobs=64, max_shadow=1,
+                       max_ao=4, fb_budget=16 << 30, use_graph=True, small_pixels=small,
+                       small_batch_pixels=small_batch)
     serve.serve_plain(table, [copy.copy(w) for w in warm])
     srv.run([copy.copy(w) for w in warm])
     batched = srv.run([copy.copy(r) for r in jobs], time_limit=args.time_limit)
@@ -399,7 +401,8 @@ def run_batch(args):
            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
            "config": {"workload": "batching: %d jobs over the triangle, volume and mixed scenes, image side "
                                   "log-uniform 128..2048, 0-2 shadow/AO levels" % args.jobs,
-                      "slots": n_slots, "slot_pixels": slot_pixels, "pixels": int(sum(r.pixels for r in jobs))},
+                      "slots": n_slots, "slot_pixels": max(slot_pixels, small_batch), "small_pixels": small,
+                      "small_batch_pixels": small_batch, "pixels": int(sum(r.pixels for r in jobs))},
            "batched": batched, "single_launch": single, "plain": plain, "chosen": chosen,
            "batched_over_plain_rays_per_s": best["rays_per_s"] / max(1e-9, plain["rays_per_s"]),
            "latency_ms": {k: best.get(k + "_ms") for k in ("p50", "p95", "p99")},
@@ -450,6 +453,11 @@ def main():
     ap.add_argument("--image", type=int, default=0, help="override the image side (smaller profiling cases)")
     ap.add_argument("--mode", default="frame", choices=["frame", "serve", "batch"])
     ap.add_argument("--jobs", type=int, default=64, help="batch mode: number of render jobs")
+    ap.add_argument("--batch-slots", type=int, default=4, help="batch mode: slot streams")
+    ap.add_argument("--small-pixels", type=int, default=1 << 20,
+                    help="batch mode: jobs up to this many pixels are packed together")
+    ap.add_argument("--small-batch-pixels", type=int, default=4 << 20,
+                    help="batch mode: pixels per packed submission")
     ap.add_argument("--rate", type=float, default=50.0)
     ap.add_argument("--requests", type=int, default=200)
     ap.add_argument("--slots", type=int, default=3)

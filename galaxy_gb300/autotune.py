@@ -13,6 +13,8 @@ repeated while a pass still changes something):
   * split camera-ray tracing, likewise;
   * camera-ray traversal per thread (per-lane refill) or per warp (one
     shared traversal for an 8x4 pixel tile);
+  * shadow/AO traversal per thread (per-lane refill) or per warp (one
+    shared traversal for 32 consecutive queue records);
   * traversal round of the refill queries: BVH8 node visits per refill
     round;
   * queue chunk of the shadow/AO query: records a block takes from the ray
@@ -40,6 +42,7 @@ KNOBS = (
     ("split", gpu.TUNE_SPLIT_SECONDARY, (0, 1)),
     ("split_primary", gpu.TUNE_SPLIT_PRIMARY, (0, 1)),
     ("camera_packet", gpu.TUNE_CAMERA_PACKET, (0, 1)),
+    ("sec_packet", gpu.TUNE_SEC_PACKET, (0, 1)),
     ("trav_steps", gpu.TUNE_TRAV_STEPS, (4, 8, 16)),
     ("queue_chunk", gpu.TUNE_QUEUE_CHUNK, (0, 1024, 4096, 16384, 65536)),
     ("march_steps", gpu.TUNE_MARCH_STEPS, (8, 16, 32, 64)),

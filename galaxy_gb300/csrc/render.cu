@@ -1606,6 +1606,121 @@ __global__ void __launch_bounds__(kThreads, MINB) k_sec_query(DevScene S, FrameA
     flush_counters(A.ctr, c, st);
 }
 
+// Warp-per-packet form of k_sec_query (GXY_TUNE_SEC_PACKET): a warp takes 32
+// consecutive shadow/AO records, each lane clips its ray and tests the
+// slices as k_sec_query does, and the warp finds the 32 rays' closest hits
+// with one shared BVH8 traversal (packet_closest: each node line fetched
+// once per warp, every lane testing its own ray).  The occlusion shortcut,
+// carried hits, the cull and the march records are k_sec_query's, so the
+// frames are the same; only the node and test counters differ.
+template <int MINB, bool LINES>
+__global__ void __launch_bounds__(kThreads, MINB) k_sec_packet(DevScene S, FrameArgs A) {
+    __shared__ uint2 wstacks[kThreads / 32][64];
+    RayStats st;
+    LocalCounters c;
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    uint2 *wstack = wstacks[threadIdx.x >> 5];
+    const unsigned ns = A.nin[Q_SHADOW];
+    const unsigned n = ns + A.nin[Q_AO];
+    unsigned *cursor = A.qmarch_count + 2;
+    for (;;) {
+        unsigned base = 0;
+        if (lane == 0) base = atomicAdd(cursor, 32u);
+        base = __shfl_sync(FULL, base, 0);
+        if (base >= n) break;
+        const unsigned src = base + lane;
+        const bool valid = src < n;
+        TraceIn in;
+        in.org = v3(0, 0, 0);
+        in.dir = v3(1, 1, 1);
+        in.t = 0.f;
+        in.tmax = 0.f;
+        in.r = in.g = in.b = in.o = 0.f;
+        in.type = 0;
+        in.part = 0;
+        int x = 0, y = 0, job = 0;
+        V3 dir = v3(1, 1, 1);
+        float ray_t0 = 0.f, ray_t = 0.f, stop_below = -INFINITY, carried = 0.f;
+        bool surface = false, slice_ahead = false, zero = true;
+        const DRay *rec = valid ? (src < ns ? A.qin[Q_SHADOW] + src : A.qin[Q_AO] + (src - ns)) : nullptr;
+        if (valid) {
+            load_ray(src < ns ? A.qin[Q_SHADOW] : A.qin[Q_AO], src < ns ? src : src - ns, in, x, y, job);
+            c.seg++;
+            float tEntry, tExitVolume;
+            sec_clip(S, in, dir, ray_t0, ray_t, tEntry, tExitVolume);
+            for (int m = 0; m < S.n_vol; m++) {
+                const DevVolume &vv = S.vol[m];
+                for (int k = 0; k < vv.n_slices; k++) {
+                    const float4 pl = vv.slices[k];
+                    const V3 pn = v3(pl.x, pl.y, pl.z);
+                    const float denom = dot(dir, pn);
+                    if (fabsf(denom) > 0.0001f) {
+                        const float t = (pl.w - dot(in.org, pn)) / denom;
+                        if (t >= ray_t0 && t <= in.tmax) slice_ahead = true;
+                        if (t >= ray_t0 && t <= ray_t) {
+                            ray_t = t;
+                            surface = true;
+                        }
+                    }
+                }
+            }
+            zero = in.r == 0.0f && in.g == 0.0f && in.b == 0.0f && in.o == 0.0f;
+            if ((A.skip_mode & 8) && S.vol[0].sclear && !zero) {
+                const DevVolume &vv = S.vol[0];
+                const VolPos g = vol_pos(vv, in.org + tEntry * dir);
+                if (__ldg(vv.sclear + super_of(vv, g)) && clear_run_end(vv, in.org, dir, g, tEntry, ray_t) > ray_t)
+                    stop_below = ray_t;
+            }
+            carried = A.qmarch_hit ? __int_as_float(__ldg(reinterpret_cast<const int *>(rec) + 15)) : 0.0f;
+        }
+        const bool active = valid && !zero && !(surface && stop_below > -INFINITY) && !(carried > 0.0f);
+        GeoHit gh;
+        bool found = packet_closest<LINES>(S, in.org, dir, ray_t0, in.tmax, active, wstack, gh, st.nodes, st.tris,
+                                           st.sphs, st.ovf);
+        float hit_t = gh.t;
+        if (valid && carried > 0.0f) {
+            found = true;
+            hit_t = carried;
+        }
+        bool to_march = false;
+        float carry_out = 0.0f;
+        if (valid && stop_below > -INFINITY && (surface || (found && hit_t < stop_below))) {
+            // ends at a surface inside its clear segment, payload unchanged
+            const bool op = fmin_(fmin_(in.r, in.g), in.b) >= 1.0f || in.o > S.opaque_alpha;
+            const int cls = classify_ray(in.type, (op ? GXY_RAY_OPAQUE : 0) | GXY_RAY_SURFACE);
+            const int dest = assign_destination(S, in.part, in.type, cls, in.org, in.dir);
+            if (dest == GXY_TERMINATED) {
+                c.term++;
+                add_pixel(A.job0.fb, A.job0.cam.width, x, y, in.r, in.g, in.b, in.o);
+            } else {
+                c.drop++;
+            }
+        } else if (valid) {
+            const bool h = !zero && found;
+            carry_out = h ? hit_t : 0.0f;
+            if (h && hit_t < ray_t) {
+                ray_t = hit_t;
+                surface = true;
+            }
+            if (zero || (!h && !surface && !slice_ahead && !S.has_iso)) c.drop++;
+            else to_march = true;
+        }
+        const unsigned idx = warp_reserve(to_march ? 1u : 0u, A.qmarch_count, A.qmarch_cap, c.ovf);
+        if (to_march && idx != 0xffffffffu) {
+            const float4 *q = reinterpret_cast<const float4 *>(rec);
+            const int4 m = __ldg(reinterpret_cast<const int4 *>(q + 3));
+            DRay *p = A.qmarch + idx;
+            p->o = __ldg(q);
+            p->d = __ldg(q + 1);
+            p->c = __ldg(q + 2);
+            p->m = make_int4(m.x, m.y, m.z | (surface ? 8 : 0), __float_as_int(ray_t));
+            if (A.qmarch_hit) A.qmarch_hit[idx] = carry_out;
+        }
+    }
+    flush_counters(A.ctr, c, st);
+}
+
 // Query pass of split camera-ray tracing with per-lane refill: a lane takes
 // the next pixel (BATCH: of all jobs, job by binary search) from a device cursor, and for each brick
 // its camera ray enters first (Camera.cpp:431-441) clips to the brick, tests
@@ -2240,6 +2355,7 @@ static int g_tune_carry_hits = 1;   // hand the closest hit on with shadow/AO ra
 static int g_tune_cam_packet = 1;   // single-frame camera query: warp-cooperative (1) or per-lane refill (0)
 static int g_tune_queue_chunk = 0;  // shadow/AO query: records per block taken from the queue at once (0: as needed)
 static int g_tune_split_handoff = 1; // handed-off primaries of volume scenes: query + skipping march (1) or one pass (0)
+static int g_tune_sec_packet = 0;    // shadow/AO query of a frame: per-lane refill (0) or warp per 32-ray packet (1)
 int leaf_max() { return g_tune_leaf; }
 
 // The split path applies to volume-rendered scenes with one volume and no
@@ -2508,6 +2624,10 @@ static int render(Scene *sc, const gxy_camera &cam, const gxy_lighting &lt, floa
             else if (kind == K_CAMERA && A.split_prim) k_cam_query<false, 4, false><<<query_grid(), kThreads, 0, st>>>(S, A);
             else if (kind == K_CAMERA) k_primary<K_CAMERA, 3><<<g, kThreads, 0, st>>>(S, A);
             else if (kind == K_PRIMARY) k_primary<K_PRIMARY, 3><<<g, kThreads, 0, st>>>(S, A);
+            else if (kind == K_SECONDARY && A.split && g_tune_sec_packet && lines)
+                k_sec_packet<4, true><<<query_grid(), kThreads, 0, st>>>(S, A);
+            else if (kind == K_SECONDARY && A.split && g_tune_sec_packet)
+                k_sec_packet<4, false><<<query_grid(), kThreads, 0, st>>>(S, A);
             else if (kind == K_SECONDARY && A.split && lines) k_sec_query<false, 4, true><<<query_grid(), kThreads, 0, st>>>(S, A);
             else if (kind == K_SECONDARY && A.split) k_sec_query<false, 4, false><<<query_grid(), kThreads, 0, st>>>(S, A);
             else if (kind == K_SECONDARY) k_secondary<3><<<g, kThreads, 0, st>>>(S, A);
@@ -2524,6 +2644,10 @@ static int render(Scene *sc, const gxy_camera &cam, const gxy_lighting &lt, floa
             else if (kind == K_CAMERA && A.split_prim) k_cam_query<false, 2, false><<<march_grid(2), kThreads, 0, st>>>(S, A);
             else if (kind == K_CAMERA) k_primary<K_CAMERA, 2><<<g, kThreads, 0, st>>>(S, A);
             else if (kind == K_PRIMARY) k_primary<K_PRIMARY, 2><<<g, kThreads, 0, st>>>(S, A);
+            else if (kind == K_SECONDARY && A.split && g_tune_sec_packet && lines)
+                k_sec_packet<2, true><<<march_grid(2), kThreads, 0, st>>>(S, A);
+            else if (kind == K_SECONDARY && A.split && g_tune_sec_packet)
+                k_sec_packet<2, false><<<march_grid(2), kThreads, 0, st>>>(S, A);
             else if (kind == K_SECONDARY && A.split && lines) k_sec_query<false, 2, true><<<march_grid(2), kThreads, 0, st>>>(S, A);
             else if (kind == K_SECONDARY && A.split) k_sec_query<false, 2, false><<<march_grid(2), kThreads, 0, st>>>(S, A);
             else if (kind == K_SECONDARY) k_secondary<2><<<g, kThreads, 0, st>>>(S, A);
@@ -3057,6 +3181,10 @@ int gxy_gpu_set_tuning(int knob, int value) {
         g_tune_skip_mode = value;
         return GXY_OK;
     }
+    if (knob == GXY_TUNE_SEC_PACKET) {
+        g_tune_sec_packet = value ? 1 : 0;
+        return GXY_OK;
+    }
     if (knob == GXY_TUNE_SPLIT_HANDOFF) {
         g_tune_split_handoff = value ? 1 : 0;
         return GXY_OK;
@@ -3092,6 +3220,7 @@ int gxy_gpu_get_tuning(int knob, int *value) {
     else if (knob == GXY_TUNE_QUEUE_LIMIT) *value = g_tune_queue_limit;
     else if (knob == GXY_TUNE_QUEUE_CHUNK) *value = g_tune_queue_chunk;
     else if (knob == GXY_TUNE_SPLIT_HANDOFF) *value = g_tune_split_handoff;
+    else if (knob == GXY_TUNE_SEC_PACKET) *value = g_tune_sec_packet;
     else return set_error(GXY_ERR_INVALID, "unknown tuning knob");
     return GXY_OK;
 }

@@ -124,6 +124,7 @@ TUNE_CARRY_HITS = 13
 TUNE_QUEUE_LIMIT = 14
 TUNE_QUEUE_CHUNK = 15
 TUNE_SPLIT_HANDOFF = 16
+TUNE_SEC_PACKET = 17
 
 
 def set_tuning(knob, value):

@@ -368,6 +368,9 @@ int gxy_gpu_set_profiling(gxy_scene scene, int on);
                                         rays do not fit is rendered in bands of image rows; a
                                         later generation that still runs out of room reports
                                         GXY_ERR_OVERFLOW */
+#define GXY_TUNE_SEC_PACKET     17   /* shadow/AO query of a frame: 0 (default) one lane per ray
+                                        with refill; 1 one warp per 32 consecutive rays with a
+                                        shared BVH8 traversal (same frames) */
 #define GXY_TUNE_SPLIT_HANDOFF  16   /* 1 (default): primaries handed to the next partition of a
                                         volume scene are traced as camera rays are, a query pass
                                         plus the camera-ray march with clear-brick skipping; 0: one

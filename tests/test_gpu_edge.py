@@ -1,7 +1,7 @@
 """Edge cases of the device path against the oracle: an empty scene, tiny
 and odd image sizes, empty ray lists, degenerate path-line segments,
-invalid arguments, a 4096x4096 frame checked on a band of rows; and the
-autotuner's coordinate descent."""
+invalid arguments, a whole 4096x4096 frame; and the autotuner's
+coordinate descent."""
 import numpy as np
 import pytest
 
@@ -103,17 +103,19 @@ def test_invalid_arguments_are_refused(gpu):
     assert e.value.code == A.GXY_ERR_INVALID
 
 
-def test_largest_frame_band_matches_oracle(gpu):
-    """4096x4096 (16.8 M camera rays, the serving workload's largest image):
-    the whole frame on the GPU, a 16-row band through the centre in the
-    oracle."""
-    cam, vis = scenes.triangle_spheres_scene(width=4096, height=4096, n_seg=48)
+def test_largest_frame_matches_oracle(gpu):
+    """4096x4096 (16.8 M camera rays, the serving workload's largest image)
+    of the ~197k-triangle scene with hard shadows: the whole frame on the
+    GPU and in the oracle."""
+    cam, vis = scenes.triangle_spheres_scene(width=4096, height=4096)
     L = S.resolve_lights(vis.lighting, cam)
-    img = gpu.Scene(vis).render_host(cam, L)
-    r0, r1 = 2040, 2056
-    ref, _ = O.OracleScene(vis).render(cam, L, nthreads=16, rows=(r0, r1))
-    close(img[r0:r1], ref[r0:r1])
-    assert img[:r0].any() and img[r1:].any()
+    sc = gpu.Scene(vis)
+    img = sc.render_host(cam, L)
+    ref, cnt = O.OracleScene(vis).render(cam, L)
+    close(img, ref)
+    c = sc.counters()
+    assert c["primary_rays"] == cnt["primary"] == 4096 * 4096
+    assert c["shadow_rays"] == cnt["shadow"]
 
 
 def test_autotuner_coordinate_descent(gpu):

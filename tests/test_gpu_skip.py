@@ -265,3 +265,29 @@ def test_handed_off_primaries_split_same_frames(gpu, parts):
         assert ca[k] == cb[k], k
     ref, cnt = O.OracleScene(vis).render(cam, L)
     image_close(a, ref)
+
+
+@pytest.mark.parametrize("shortcut", [1, 9])
+def test_warp_packet_shadow_query_same_frames(gpu, shortcut):
+    """Shadow/AO rays queried one lane per ray (GXY_TUNE_SEC_PACKET 0) or one
+    warp per 32-ray packet (1), with and without the occlusion shortcut: the
+    same frames and ray counters, and the oracle's image."""
+    cam, vis = scenes.mixed_scene(n=96, n_spheres=20000, width=128, height=128, partitions=(2, 2, 2), n_ao=4)
+    L = S.resolve_lights(vis.lighting, cam)
+    sc = gpu.Scene(vis)
+    before = gpu.get_tuning(gpu.TUNE_SKIP_MODE)
+    out = {}
+    try:
+        gpu.set_tuning(gpu.TUNE_SKIP_MODE, shortcut)
+        for v in (0, 1):
+            gpu.set_tuning(gpu.TUNE_SEC_PACKET, v)
+            out[v] = (sc.render_host(cam, L), sc.counters())
+    finally:
+        gpu.set_tuning(gpu.TUNE_SEC_PACKET, 0)
+        gpu.set_tuning(gpu.TUNE_SKIP_MODE, before)
+    (a, ca), (b, cb) = out[1], out[0]
+    assert float(np.abs(a - b).max()) <= ATOMIC_ORDER_TOL
+    for k in ("primary_rays", "shadow_rays", "ao_rays", "segments", "handoffs", "terminated", "dropped", "samples"):
+        assert ca[k] == cb[k], k
+    ref, cnt = O.OracleScene(vis).render(cam, L)
+    image_close(a, ref)
