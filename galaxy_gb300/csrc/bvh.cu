@@ -308,12 +308,80 @@ __device__ void write_slot(const DevScene &S, const float *sph_radius, uint32_t 
     }
 }
 
+// Cost-optimal collapse (GXY_TUNE_BVH_COLLAPSE 1, single-primitive leaves):
+// choose which binary nodes become wide nodes so that the summed surface
+// area of the wide nodes -- proportional to the expected number of node
+// visits of a ray -- is smallest while no wide node has more than 8
+// children, by a dynamic programme over the binary tree, bottom up as the
+// refit runs.  For binary node n and j = 1..8 child slots of its parent:
+//   D(n, j) = min over k of C(left, k) + C(right, j - k)   (n spread over j slots)
+//   C(n, 1) = area(n) + D(n, 8)                            (n one slot: a wide node)
+//   C(n, j) = min(C(n, j - 1), D(n, j))                    (at most j slots)
+// with C = 0 for a primitive.  Per node: cost[8] = C(n, 1..8); choice[j-1]
+// = the slot count j' that attains C(n, j) (1: one slot), choice[8 + j-1] =
+// the split k of D(n, j).  The collapse then expands D(root, 8).
+__global__ void k_collapse_cost(int n, const int *left, const int *right, const int *parent,
+                                const int *leaf_parent, int *flags, const float4 *nlo, const float4 *nhi,
+                                float *cost, uint8_t *choice) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int node = leaf_parent[i];
+    while (node >= 0) {
+        __threadfence();
+        if (atomicAdd(&flags[node], 1) == 0) return;   // first arrival: sibling not ready
+        __threadfence();
+        float cl[8], cr[8];
+        const int l = left[node], r = right[node];
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            cl[j] = l >= 0 ? __ldcg(cost + 8 * (size_t)l + j) : 0.0f;
+            cr[j] = r >= 0 ? __ldcg(cost + 8 * (size_t)r + j) : 0.0f;
+        }
+        float d[9];
+        uint8_t dk[9];
+        d[1] = FLT_MAX;
+        dk[1] = 0;
+        for (int j = 2; j <= 8; j++) {
+            float best = FLT_MAX;
+            int bk = 1;
+            for (int k = 1; k < j; k++) {
+                const float v = cl[k - 1] + cr[j - k - 1];
+                if (v < best) {
+                    best = v;
+                    bk = k;
+                }
+            }
+            d[j] = best;
+            dk[j] = (uint8_t)bk;
+        }
+        float c[9];
+        uint8_t cj[9];
+        c[1] = half_area(nlo[node], nhi[node]) + d[8];
+        cj[1] = 1;
+        for (int j = 2; j <= 8; j++) {
+            c[j] = c[j - 1];
+            cj[j] = cj[j - 1];
+            if (d[j] < c[j]) {
+                c[j] = d[j];
+                cj[j] = (uint8_t)j;
+            }
+        }
+#pragma unroll
+        for (int j = 1; j <= 8; j++) {
+            __stcg(cost + 8 * (size_t)node + (j - 1), c[j]);
+            choice[16 * (size_t)node + (j - 1)] = cj[j];
+            choice[16 * (size_t)node + 8 + (j - 1)] = dk[j];
+        }
+        node = node == 0 ? -1 : parent[node];
+    }
+}
+
 // One level of the collapse.  Work item: (binary ref, wide node index).
 __global__ void k_collapse(DevScene S, const float *sph_radius, int n, const int2 *qin, int nq, int2 *qout,
                            unsigned int *ctr, const int *left, const int *right, const int *first, const int *last,
                            const uint32_t *ids, const float4 *plo, const float4 *phi, const float4 *nlo,
                            const float4 *nhi, BVH8Node *nodes, float4 *slots, int max_nodes, int max_slots,
-                           int kLeafMax) {
+                           int kLeafMax, const uint8_t *choice) {
     int w = blockIdx.x * blockDim.x + threadIdx.x;
     if (w >= nq) return;
     int2 item = qin[w];
@@ -326,7 +394,28 @@ __global__ void k_collapse(DevScene S, const float *sph_radius, int n, const int
         if (r >= 0) { lo = nlo[r]; hi = nhi[r]; }
         else { uint32_t p = ids[~r]; lo = plo[p]; hi = phi[p]; }
     };
-    if (ref >= 0 && size_of(ref) > kLeafMax) {
+    if (ref >= 0 && size_of(ref) > kLeafMax && choice) {
+        // cost-optimal children: expand D(ref, 8) by the stored choices
+        int2 stk[24];   // (binary ref, slots << 1 | spread-over-slots)
+        int sp = 0;
+        stk[sp++] = make_int2(ref, (8 << 1) | 1);
+        while (sp > 0 && nc < 8) {
+            const int2 e = stk[--sp];
+            const int m = e.x, j = e.y >> 1;
+            if (e.y & 1) {   // D(m, j): left gets k slots, right j - k
+                const int k = choice[16 * (size_t)m + 8 + (j - 1)];
+                if (sp + 2 > 24) break;
+                stk[sp++] = make_int2(right[m], (j - k) << 1);
+                stk[sp++] = make_int2(left[m], k << 1);
+            } else if (m < 0) {
+                ch[nc++] = m;                                       // a primitive
+            } else {
+                const int jj = choice[16 * (size_t)m + (j - 1)];
+                if (jj == 1) ch[nc++] = m;                          // a wide node of its own
+                else stk[sp++] = make_int2(m, (jj << 1) | 1);
+            }
+        }
+    } else if (ref >= 0 && size_of(ref) > kLeafMax) {
         ch[nc++] = left[ref];
         ch[nc++] = right[ref];
         while (nc < 8) {
@@ -750,6 +839,16 @@ int build_bvh8(DevScene &S, const float *sph_radius, DeviceArena &arena, cudaStr
             info.sah_levels = (int)m;   // clusters under the SAH top tree
         }
     }
+    uint8_t *choice = nullptr;   // cost-optimal collapse: per binary node, the programme's choices
+    if (collapse_cost() && leaf_max() == 1 && root_ref == 0 && n > 1) {
+        float *cost;
+        ALLOC(cost, 8 * (size_t)ni);
+        ALLOC(choice, 16 * (size_t)ni);
+        CK(cudaMemsetAsync(B.flags, 0, sizeof(int) * ni, st));
+        k_collapse_cost<<<blocks_for(n, 256), 256, 0, st>>>(n, B.left, B.right, B.parent, leaf_parent, B.flags,
+                                                            B.nlo, B.nhi, cost, choice);
+        CK(cudaGetLastError());
+    }
     BVH8Node *nodes;
     float4 *slots;
     rc = arena.alloc((void **)&nodes, sizeof(BVH8Node) * (size_t)max_nodes);
@@ -768,7 +867,7 @@ int build_bvh8(DevScene &S, const float *sph_radius, DeviceArena &arena, cudaStr
         CK(cudaMemsetAsync(B.ctr + 2, 0, sizeof(unsigned int), st));
         k_collapse<<<blocks_for(nq, 128), 128, 0, st>>>(S, sph_radius, n, B.qa, nq, B.qb, B.ctr, B.left, B.right,
                                                         B.first, B.last, B.ids2, B.plo, B.phi, B.nlo, B.nhi, nodes,
-                                                        slots, max_nodes, max_slots, leaf_max());
+                                                        slots, max_nodes, max_slots, leaf_max(), choice);
         CK(cudaGetLastError());
         unsigned int hc[4];
         CK(cudaMemcpyAsync(hc, B.ctr, sizeof hc, cudaMemcpyDeviceToHost, st));

@@ -75,5 +75,8 @@ bool sah_builder();
 int sah_cluster_size();
 // Largest subtree (primitives) stored as one leaf of a wide node, 1-4.
 int leaf_max();
+// Wide-node collapse by the surface-area cost programme (true) or by
+// opening the largest child (false).
+bool collapse_cost();
 
 }  // namespace gxy

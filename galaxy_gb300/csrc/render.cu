@@ -2357,6 +2357,8 @@ static int g_tune_queue_chunk = 0;  // shadow/AO query: records per block taken 
 static int g_tune_split_handoff = 1; // handed-off primaries of volume scenes: query + skipping march (1) or one pass (0)
 static int g_tune_sec_packet = 0;    // shadow/AO query of a frame: per-lane refill (0) or warp per 32-ray packet (1)
 int leaf_max() { return g_tune_leaf; }
+static int g_tune_collapse = 1;     // BVH8 collapse: surface-area cost programme (1) or largest child first (0)
+bool collapse_cost() { return g_tune_collapse != 0; }
 
 // The split path applies to volume-rendered scenes with one volume and no
 // isovalues (the march pass keeps one sample value per lane).
@@ -3181,6 +3183,10 @@ int gxy_gpu_set_tuning(int knob, int value) {
         g_tune_skip_mode = value;
         return GXY_OK;
     }
+    if (knob == GXY_TUNE_BVH_COLLAPSE) {
+        g_tune_collapse = value ? 1 : 0;
+        return GXY_OK;
+    }
     if (knob == GXY_TUNE_SEC_PACKET) {
         g_tune_sec_packet = value ? 1 : 0;
         return GXY_OK;
@@ -3221,6 +3227,7 @@ int gxy_gpu_get_tuning(int knob, int *value) {
     else if (knob == GXY_TUNE_QUEUE_CHUNK) *value = g_tune_queue_chunk;
     else if (knob == GXY_TUNE_SPLIT_HANDOFF) *value = g_tune_split_handoff;
     else if (knob == GXY_TUNE_SEC_PACKET) *value = g_tune_sec_packet;
+    else if (knob == GXY_TUNE_BVH_COLLAPSE) *value = g_tune_collapse;
     else return set_error(GXY_ERR_INVALID, "unknown tuning knob");
     return GXY_OK;
 }

@@ -368,6 +368,11 @@ int gxy_gpu_set_profiling(gxy_scene scene, int on);
                                         rays do not fit is rendered in bands of image rows; a
                                         later generation that still runs out of room reports
                                         GXY_ERR_OVERFLOW */
+#define GXY_TUNE_BVH_COLLAPSE   18   /* read at scene commit.  How binary BVH nodes are grouped
+                                        into 8-wide nodes: 1 (default) the grouping of least summed
+                                        wide-node surface area, by a dynamic programme over the
+                                        tree (single-primitive leaves, no SAH top); 0 the greedy
+                                        rule, opening the child of largest area first */
 #define GXY_TUNE_SEC_PACKET     17   /* shadow/AO query of a frame: 0 (default) one lane per ray
                                         with refill; 1 one warp per 32 consecutive rays with a
                                         shared BVH8 traversal (same frames) */

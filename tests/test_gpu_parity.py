@@ -301,3 +301,31 @@ def test_sah_top_bvh_matches_oracle(gpu, which):
     image_close(img, ref)
     c = sc.counters()
     assert c["primary_rays"] == cnt["primary"] and c["shadow_rays"] == cnt["shadow"]
+
+
+@pytest.mark.parametrize("which", ["triangles", "mixed"])
+def test_cost_collapse_same_frames_fewer_nodes(gpu, which):
+    """BVH8 nodes grouped by the surface-area cost programme
+    (GXY_TUNE_BVH_COLLAPSE 1) or greedily (0): the same frames and ray
+    counts (the closest hit does not depend on the tree), fewer wide nodes."""
+    if which == "triangles":
+        cam, vis = scenes.triangle_spheres_scene(width=128, height=128, n_seg=32)
+    else:
+        cam, vis = scenes.mixed_scene(n=64, n_spheres=20000, width=112, height=112, partitions=(2, 2, 1), n_ao=2)
+    L = S.resolve_lights(vis.lighting, cam)
+    out = {}
+    try:
+        for v in (0, 1):
+            gpu.set_tuning(gpu.TUNE_BVH_COLLAPSE, v)
+            sc = gpu.Scene(vis)
+            out[v] = (sc.render_host(cam, L), sc.counters(), sc.bvh_info())
+    finally:
+        gpu.set_tuning(gpu.TUNE_BVH_COLLAPSE, 1)
+    (a, ca, ia), (b, cb, ib) = out[1], out[0]
+    assert float(np.abs(a - b).max()) <= 1e-6
+    for k in ("primary_rays", "shadow_rays", "ao_rays", "terminated", "samples"):
+        assert ca[k] == cb[k], k
+    assert ia["prim_refs"] == ib["prim_refs"]
+    assert ia["nodes"] < ib["nodes"]
+    ref, cnt = O.OracleScene(vis).render(cam, L)
+    image_close(a, ref)
