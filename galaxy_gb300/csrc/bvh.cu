@@ -320,7 +320,7 @@ __device__ void write_slot(const DevScene &S, const float *sph_radius, uint32_t 
 // with C = 0 for a primitive.  Per node: cost[8] = C(n, 1..8); choice[j-1]
 // = the slot count j' that attains C(n, j) (1: one slot), choice[8 + j-1] =
 // the split k of D(n, j).  The collapse then expands D(root, 8).
-__global__ void k_collapse_cost(int n, const int *left, const int *right, const int *parent,
+__global__ void k_collapse_cost(int n, int root, const int *left, const int *right, const int *parent,
                                 const int *leaf_parent, int *flags, const float4 *nlo, const float4 *nhi,
                                 float *cost, uint8_t *choice) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -372,7 +372,7 @@ __global__ void k_collapse_cost(int n, const int *left, const int *right, const 
             choice[16 * (size_t)node + (j - 1)] = cj[j];
             choice[16 * (size_t)node + 8 + (j - 1)] = dk[j];
         }
-        node = node == 0 ? -1 : parent[node];
+        node = node == root ? -1 : parent[node];
     }
 }
 
@@ -734,6 +734,20 @@ __global__ void __launch_bounds__(256) k_sah_level(const float4 *clo, const floa
     }
 }
 
+// Parents of the binned-SAH top tree's children (top nodes base .. base +
+// ntop - 1), so that bottom-up passes climb from the clusters into it.
+__global__ void k_top_parents(int ntop, int base, const int *left, const int *right, int *parent,
+                              int *leaf_parent) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ntop) return;
+    const int node = base + t;
+    const int c[2] = {left[node], right[node]};
+    for (int k = 0; k < 2; k++) {
+        if (c[k] >= 0) parent[c[k]] = node;
+        else leaf_parent[~c[k]] = node;
+    }
+}
+
 __global__ void k_iota(int m, int *idx) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < m) idx[i] = i;
@@ -764,8 +778,8 @@ int build_bvh8(DevScene &S, const float *sph_radius, DeviceArena &arena, cudaStr
     int ni = n > 1 ? n - 1 : 1;
     const int C = sah_builder() ? sah_cluster_size() : 0;   // top-level SAH over clusters of <= C primitives
     const int ncap = (C > 1 && n > C) ? 2 * ni : ni;       // room for the top tree's nodes after the radix tree's
-    ALLOC(B.left, ncap); ALLOC(B.right, ncap); ALLOC(B.parent, ni); ALLOC(B.first, ncap); ALLOC(B.last, ncap);
-    ALLOC(B.flags, ni); ALLOC(B.nlo, ncap); ALLOC(B.nhi, ncap);
+    ALLOC(B.left, ncap); ALLOC(B.right, ncap); ALLOC(B.parent, ncap); ALLOC(B.first, ncap); ALLOC(B.last, ncap);
+    ALLOC(B.flags, ncap); ALLOC(B.nlo, ncap); ALLOC(B.nhi, ncap);
     int *leaf_parent;
     ALLOC(leaf_parent, n);
     ALLOC(B.ctr, 8);
@@ -837,16 +851,20 @@ int build_bvh8(DevScene &S, const float *sph_radius, DeviceArena &arena, cudaStr
             }
             root_ref = base;
             info.sah_levels = (int)m;   // clusters under the SAH top tree
+            // the top tree's m - 1 nodes as parents of their children
+            k_top_parents<<<blocks_for(m - 1, 256), 256, 0, st>>>((int)m - 1, base, B.left, B.right, B.parent,
+                                                                  leaf_parent);
+            CK(cudaGetLastError());
         }
     }
     uint8_t *choice = nullptr;   // cost-optimal collapse: per binary node, the programme's choices
-    if (collapse_cost() && leaf_max() == 1 && root_ref == 0 && n > 1) {
+    if (collapse_cost() && leaf_max() == 1 && root_ref >= 0 && n > 1) {
         float *cost;
-        ALLOC(cost, 8 * (size_t)ni);
-        ALLOC(choice, 16 * (size_t)ni);
-        CK(cudaMemsetAsync(B.flags, 0, sizeof(int) * ni, st));
-        k_collapse_cost<<<blocks_for(n, 256), 256, 0, st>>>(n, B.left, B.right, B.parent, leaf_parent, B.flags,
-                                                            B.nlo, B.nhi, cost, choice);
+        ALLOC(cost, 8 * (size_t)ncap);
+        ALLOC(choice, 16 * (size_t)ncap);
+        CK(cudaMemsetAsync(B.flags, 0, sizeof(int) * ncap, st));
+        k_collapse_cost<<<blocks_for(n, 256), 256, 0, st>>>(n, root_ref, B.left, B.right, B.parent, leaf_parent,
+                                                            B.flags, B.nlo, B.nhi, cost, choice);
         CK(cudaGetLastError());
     }
     BVH8Node *nodes;
