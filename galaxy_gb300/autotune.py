@@ -47,6 +47,7 @@ KNOBS = (
     ("queue_chunk", gpu.TUNE_QUEUE_CHUNK, (0, 1024, 4096, 16384, 65536)),
     ("march_steps", gpu.TUNE_MARCH_STEPS, (8, 16, 32, 64)),
     ("skip_mode", gpu.TUNE_SKIP_MODE, (0, 1, 3, 7, 9, 11)),
+    ("runahead", gpu.TUNE_RUNAHEAD, (1, 2, 4, 8)),
 )
 
 

@@ -220,7 +220,8 @@ struct Scene {
     size_t qcap[2][3] = {{0, 0, 0}, {0, 0, 0}};
     unsigned *rowx = nullptr;           // per image row: camera rays emitted beyond one per pixel
     size_t rowx_cap = 0;
-    unsigned int *qcount = nullptr;     // 2 x 3 queue counters
+    static constexpr int kRing = 64;    // generations of queue counts kept in device memory
+    unsigned int *qcount = nullptr;     // [8..15] split-pass cursors, then kRing x 3 per-generation queue counts
     DevCounters *ctr = nullptr;         // kMaxLaunch slots, one per launch
     DevCounters last{};
     int64_t bounces = 0;
@@ -745,7 +746,7 @@ static int commit(const gxy_scene_desc *d, Scene *sc) {
     CK(cudaDeviceSynchronize());
     if ((rc = sc->upload_light(&S, sizeof S, &p))) return rc;
     sc->d_scene = (DevScene *)p;
-    if ((rc = arena().alloc((void **)&sc->qcount, 16 * sizeof(unsigned int)))) return rc;
+    if ((rc = arena().alloc((void **)&sc->qcount, (16 + 3 * Scene::kRing) * sizeof(unsigned int)))) return rc;
     if ((rc = arena().alloc((void **)&sc->ctr, Scene::kMaxLaunch * sizeof(DevCounters)))) return rc;
     return GXY_OK;
 }
@@ -818,7 +819,7 @@ static int scene_view(Scene *base, Scene *v) {
     }
     if ((rc = v->upload_light(&S, sizeof S, &p))) return rc;
     v->d_scene = (DevScene *)p;
-    if ((rc = arena().alloc((void **)&v->qcount, 16 * sizeof(unsigned int)))) return rc;
+    if ((rc = arena().alloc((void **)&v->qcount, (16 + 3 * Scene::kRing) * sizeof(unsigned int)))) return rc;
     if ((rc = arena().alloc((void **)&v->ctr, Scene::kMaxLaunch * sizeof(DevCounters)))) return rc;
     return GXY_OK;
 }
@@ -963,6 +964,14 @@ struct FrameArgs {
     unsigned *pmarch_count;            // [0] records, [1] fetch cursor, [2] camera query cursor, [3] extras
     unsigned pmarch_cap;
 };
+
+// Input count of queue k for a single-frame launch: the host's count, or --
+// for generations launched ahead without a host read -- the count the
+// previous generation left in device memory, bounded by nin[k] (the input
+// queue's capacity then).
+__device__ __forceinline__ unsigned frame_nin(const FrameArgs &A, int k) {
+    return A.nin_dev ? min(__ldg(A.nin_dev + k), A.nin[k]) : A.nin[k];
+}
 
 // Reserve cnt consecutive queue records for this thread: one warp-wide scan
 // and one atomic per warp.  Returns the first index (or ~0u if the queue is
@@ -1325,7 +1334,7 @@ __global__ void __launch_bounds__(kThreads, MINB) k_primary(DevScene S, FrameArg
         camera_pass<false, true>(S, tfs, A, nullptr, (int64_t)A.job0.cam.width * A.band_rows, start, stride, st,
                                  c);
     } else {
-        unsigned n[NQ] = {A.nin[Q_PRIM], 0u, 0u};
+        unsigned n[NQ] = {frame_nin(A, Q_PRIM), 0u, 0u};
         queue_pass<false, true>(S, tfs, A, n, start, stride, st, c);
     }
     flush_counters(A.ctr, c, st);
@@ -1337,7 +1346,7 @@ __global__ void __launch_bounds__(kThreads, MINB) k_secondary(DevScene S, FrameA
     load_tfs(S, tfs);
     RayStats st;
     LocalCounters c;
-    unsigned n[NQ] = {0u, A.nin[Q_SHADOW], A.nin[Q_AO]};
+    unsigned n[NQ] = {0u, frame_nin(A, Q_SHADOW), frame_nin(A, Q_AO)};
     queue_pass<false, true>(S, tfs, A, n, (int64_t)blockIdx.x * blockDim.x, (int64_t)gridDim.x * blockDim.x, st, c);
     flush_counters(A.ctr, c, st);
 }
@@ -1439,8 +1448,8 @@ __global__ void __launch_bounds__(kThreads, MINB) k_sec_query(DevScene S, FrameA
     RayStats st;
     LocalCounters c;
     const int lane = threadIdx.x & 31;
-    const unsigned ns = BATCH ? min(__ldg(A.nin_dev + Q_SHADOW), A.qcap[Q_SHADOW]) : A.nin[Q_SHADOW];
-    const unsigned n = ns + (BATCH ? min(__ldg(A.nin_dev + Q_AO), A.qcap[Q_AO]) : A.nin[Q_AO]);
+    const unsigned ns = BATCH ? min(__ldg(A.nin_dev + Q_SHADOW), A.qcap[Q_SHADOW]) : frame_nin(A, Q_SHADOW);
+    const unsigned n = ns + (BATCH ? min(__ldg(A.nin_dev + Q_AO), A.qcap[Q_AO]) : frame_nin(A, Q_AO));
     unsigned *cursor = A.qmarch_count + 2;
     // records this warp has taken from the queue and not yet handed out:
     // [wnext, wend), refilled queue_chunk records at a time (GXY_TUNE_QUEUE_CHUNK)
@@ -1621,8 +1630,8 @@ __global__ void __launch_bounds__(kThreads, MINB) k_sec_packet(DevScene S, Frame
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     uint2 *wstack = wstacks[threadIdx.x >> 5];
-    const unsigned ns = A.nin[Q_SHADOW];
-    const unsigned n = ns + A.nin[Q_AO];
+    const unsigned ns = frame_nin(A, Q_SHADOW);
+    const unsigned n = ns + frame_nin(A, Q_AO);
     unsigned *cursor = A.qmarch_count + 2;
     for (;;) {
         unsigned base = 0;
@@ -1864,7 +1873,7 @@ __global__ void __launch_bounds__(kThreads, MINB) k_prim_query(DevScene S, Frame
     RayStats st;
     LocalCounters c;
     const int lane = threadIdx.x & 31;
-    const unsigned n = A.nin[Q_PRIM];
+    const unsigned n = frame_nin(A, Q_PRIM);
     unsigned *cursor = A.pmarch_count + 2;
     TravState T;
     uint2 stack_mem[64];
@@ -2356,6 +2365,7 @@ static int g_tune_cam_packet = 1;   // single-frame camera query: warp-cooperati
 static int g_tune_queue_chunk = 0;  // shadow/AO query: records per block taken from the queue at once (0: as needed)
 static int g_tune_split_handoff = 1; // handed-off primaries of volume scenes: query + skipping march (1) or one pass (0)
 static int g_tune_sec_packet = 0;    // shadow/AO query of a frame: per-lane refill (0) or warp per 32-ray packet (1)
+static int g_tune_runahead = 16;     // frame generations launched per host read of the queue counts, at most
 int leaf_max() { return g_tune_leaf; }
 static int g_tune_collapse = 1;     // BVH8 collapse: surface-area cost programme (1) or largest child first (0)
 bool collapse_cost() { return g_tune_collapse != 0; }
@@ -2523,13 +2533,16 @@ static void add_counters(DevCounters &a, const DevCounters &b) {
 }
 
 // One frame: generation 0 from the camera, then generations of the primary
-// queue and the shadow+AO queues until every queue is empty.  The host reads
-// the three queue counts (12 bytes) after each generation to size the next
-// launches and to grow their output queues to the worst case beforehand;
-// each launch adds into its own counter slot, and when profiling is on a
-// pair of events brackets each launch, so profiling adds no syncs.  When the
-// camera generation's queues do not fit, the image is rendered in bands of
-// rows, each band a complete wavefront into the same framebuffer.
+// queue and the shadow+AO queues until every queue is empty.  Each
+// generation counts its output into a ring slot in device memory.  The host
+// reads the counts after the camera generation and then once per block of
+// up to GXY_TUNE_RUNAHEAD generations: it grows the queues the block writes
+// to the block's worst case beforehand, and the block's later generations
+// take their input counts from the ring (the launch grids are sized to the
+// bounds).  Each launch adds into its own counter slot, and when profiling
+// is on a pair of events brackets each launch, so profiling adds no syncs.
+// When the camera generation's queues do not fit, the image is rendered in
+// bands of rows, each band a complete wavefront into the same framebuffer.
 static int render(Scene *sc, const gxy_camera &cam, const gxy_lighting &lt, float *fb, cudaStream_t st) {
     if (cam.width <= 0 || cam.height <= 0) return set_error(GXY_ERR_INVALID, "bad image size");
     DevScene &S = sc->S;
@@ -2541,6 +2554,11 @@ static int render(Scene *sc, const gxy_camera &cam, const gxy_lighting &lt, floa
     if (A.job0.L.n == 0) return set_error(GXY_ERR_INVALID, "lighting needs at least one light");
     const int W = cam.width, H = cam.height;
     const int nl = A.job0.L.shadows ? A.job0.L.n : 0, na = A.job0.L.n_ao;
+    // a primary spawns shadow/AO rays only at a surface: geometry, an
+    // isosurface or a slice plane
+    bool spawns = S.nodes != nullptr || S.has_iso;
+    for (int m = 0; m < S.n_vol; m++) spawns = spawns || S.vol[m].n_slices > 0;
+    const int snl = spawns ? nl : 0, sna = spawns ? na : 0;
     const bool split = split_eligible(S), split_prim = split && g_tune_split_prim;
     const int maxl = Scene::kMaxLaunch;
     if (sc->profile && (int)sc->events.size() < 2 * maxl) {
@@ -2602,7 +2620,9 @@ static int render(Scene *sc, const gxy_camera &cam, const gxy_lighting &lt, floa
     A.skip_mode = g_tune_skip_mode;
     A.qmarch_count = sc->qcount + 12;   // [0] records, [1] march cursor, [2] query cursor
     A.pmarch_count = sc->qcount + 8;    // [0] records, [1] march cursor, [2] camera query cursor, [3] extra slots
-    struct LaunchRec { int gen, kind; unsigned rays_in; };
+    // rays_in of a launch whose input count stayed in device memory is
+    // filled in from the count ring when the host reads it (slot >= 0)
+    struct LaunchRec { int gen, kind; unsigned rays_in; int slot; };
     std::vector<LaunchRec> recs;
     int nl_launch = 0;
     const bool lines = S.n_seg > 0;
@@ -2660,13 +2680,33 @@ static int render(Scene *sc, const gxy_camera &cam, const gxy_lighting &lt, floa
         }
         CK(cudaGetLastError());
         if (sc->profile) CK(cudaEventRecord(sc->events[2 * nl_launch + 1], st));
-        recs.push_back({gen, kind, rays_in});
+        recs.push_back({gen, kind, rays_in, -1});
         nl_launch++;
+        return GXY_OK;
+    };
+    // per-generation queue counts (generation g counts into slot g % kRing)
+    unsigned *ring = sc->qcount + 16;
+    auto slot = [&](int g) { return ring + 3 * (g % Scene::kRing); };
+    unsigned hring[3 * Scene::kRing];
+    auto read_ring = [&]() -> int {
+        CK(cudaMemcpyAsync(hring, ring, sizeof hring, cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        for (LaunchRec &r : recs) {
+            if (r.slot < 0) continue;
+            const unsigned *c = hring + 3 * r.slot;
+            r.rays_in = (r.kind == K_PRIMARY || r.kind == K_PQUERY) ? c[Q_PRIM] : c[Q_SHADOW] + c[Q_AO];
+            r.slot = -1;
+        }
         return GXY_OK;
     };
     // counter slots and per-launch statistics of the launches so far
     auto collect = [&]() -> int {
         if (!nl_launch) return GXY_OK;
+        for (const LaunchRec &r : recs)
+            if (r.slot >= 0) {
+                if (int rc2 = read_ring()) return rc2;
+                break;
+            }
         std::vector<DevCounters> slots(nl_launch);
         CK(cudaMemcpyAsync(slots.data(), sc->ctr, nl_launch * sizeof(DevCounters), cudaMemcpyDeviceToHost, st));
         CK(cudaStreamSynchronize(st));
@@ -2713,79 +2753,145 @@ static int render(Scene *sc, const gxy_camera &cam, const gxy_lighting &lt, floa
         // counter slots: a band ends its launches' records before the next
         if (nl_launch > maxl - 64 && (rc = collect())) return rc;
         CK(cudaMemsetAsync(sc->ctr + nl_launch, 0, (maxl - nl_launch) * sizeof(DevCounters), st));
-        CK(cudaMemsetAsync(sc->qcount, 0, 16 * sizeof(unsigned), st));
-        int cur = 0;   // queue set written by the last generation
+        CK(cudaMemsetAsync(sc->qcount, 0, (16 + 3 * Scene::kRing) * sizeof(unsigned), st));
+        // generation g appends to the queue set g & 1 and counts into ring
+        // slot g % kRing; the camera generation is g = 0
         for (int k = 0; k < 3; k++) {
-            A.qout[k] = sc->q[cur][k];
-            A.qcap[k] = (unsigned)sc->qcap[cur][k];
+            A.qout[k] = sc->q[0][k];
+            A.qcap[k] = (unsigned)sc->qcap[0][k];
         }
-        A.qout_count = sc->qcount + 3 * cur;
+        A.qout_count = slot(0);
+        A.nin_dev = nullptr;
         if ((rc = launch(K_CAMERA, 0, 0, A.total_pix, st))) return rc;
         if (A.split_prim && (rc = launch(K_PMARCH, 0, 0, 1 << 30, st))) return rc;
         A.split_prim = 0;   // later generations trace handed-off primaries in one pass
-        int gen = 1;
+        if ((rc = read_ring())) return rc;
+        int gen = 1, cur = 0;   // cur: the queue set the last generation wrote
+        unsigned n[3];
+        for (int k = 0; k < 3; k++) n[k] = hring[k];
         for (;;) {
-            unsigned n[3];
-            CK(cudaMemcpyAsync(n, sc->qcount + 3 * cur, sizeof n, cudaMemcpyDeviceToHost, st));
-            CK(cudaStreamSynchronize(st));
             for (int k = 0; k < 3; k++)
                 if (n[k] > sc->qcap[cur][k]) n[k] = (unsigned)sc->qcap[cur][k];   // overflow already flagged
             if (n[0] + n[1] + n[2] == 0) break;
-            int nxt = cur ^ 1;
-            // worst case of this generation's output: a primary continues
-            // at most once and spawns nl shadow and na AO rays; a shadow/AO
-            // ray moves on at most once
-            const size_t need[3] = {(size_t)n[Q_PRIM], (size_t)n[Q_SHADOW] + (size_t)nl * n[Q_PRIM],
-                                    (size_t)n[Q_AO] + (size_t)na * n[Q_PRIM]};
-            int grc = grow_set(sc, nxt, need);
-            if (grc == GXY_OK && A.split)
-                grc = grow((void **)&sc->qmarch, (void **)&sc->qmarch_hit, &sc->qmarch_cap,
-                           (size_t)n[Q_SHADOW] + n[Q_AO] + 32, sizeof(DRay), sizeof(float));
+            const int nxt = cur ^ 1;
+            // worst case of the j-th output from here: a primary continues
+            // at most once per generation and spawns nl shadow and na AO
+            // rays; a shadow/AO ray moves on at most once
+            auto need = [&](int j, size_t out[3]) {
+                out[Q_PRIM] = n[Q_PRIM];
+                out[Q_SHADOW] = (size_t)n[Q_SHADOW] + (size_t)j * snl * n[Q_PRIM];
+                out[Q_AO] = (size_t)n[Q_AO] + (size_t)j * sna * n[Q_PRIM];
+            };
+            auto fits = [&](int set, int j) {
+                size_t w[3];
+                need(j, w);
+                for (int k = 0; k < 3; k++)
+                    if (w[k] > sc->qcap[set][k]) return false;
+                return true;
+            };
+            const size_t sa = (size_t)n[Q_SHADOW] + n[Q_AO], fan = (size_t)(snl + sna) * n[Q_PRIM];
+            // A block runs to the generation count of the scene's previous
+            // frame (at most GXY_TUNE_RUNAHEAD generations), so a repeated
+            // view launches no generation without rays; a frame that outlasts
+            // it goes on one generation per read.  The block writes its odd
+            // outputs (1, 3, ...) to set nxt and its even ones to set cur.
+            // Set cur holds the rays the block starts from, so it cannot
+            // grow: the block ends before an even output that would not fit
+            // there.  Set nxt and the march queue then grow to the block's
+            // worst case; if they cannot, the block is one generation.
+            const int kcap = sc->bounces > gen ? (int)std::min<int64_t>(g_tune_runahead, sc->bounces - gen) : 1;
+            int K = 1;
+            while (K < kcap && (((K + 1) & 1) || fits(cur, K + 1))) K++;
+            size_t w[3];
+            need((K & 1) ? K : K - 1, w);
+            int grc = grow_set(sc, nxt, w);
+            if (grc && K > 1) {
+                cudaGetLastError();
+                K = 1;
+                need(1, w);
+                grc = grow_set(sc, nxt, w);
+            }
             const bool split_handoff = split_prim && g_tune_split_handoff && n[Q_PRIM];
+            if (grc == GXY_OK && A.split) {
+                grc = grow((void **)&sc->qmarch, (void **)&sc->qmarch_hit, &sc->qmarch_cap, sa + (K - 1) * fan + 32,
+                           sizeof(DRay), sizeof(float));
+                if (grc && K > 1) {
+                    cudaGetLastError();
+                    K = 1;
+                    grc = grow((void **)&sc->qmarch, (void **)&sc->qmarch_hit, &sc->qmarch_cap, sa + 32, sizeof(DRay),
+                               sizeof(float));
+                }
+            }
             if (grc == GXY_OK && split_handoff)
                 grc = grow((void **)&sc->pmarch, (void **)&sc->pmarch_hit, &sc->pmarch_cap, (size_t)n[Q_PRIM] + 32,
                            sizeof(DRay), 2 * sizeof(float4));
             // a queue that cannot grow keeps its room; a generation that then
             // runs out of it reports GXY_ERR_OVERFLOW
-            if (grc) cudaGetLastError();
+            if (grc) {
+                cudaGetLastError();
+                K = 1;
+            }
             A.pmarch = sc->pmarch;
             A.pmarch_hit = sc->pmarch_hit;
             A.pmarch_cap = (unsigned)sc->pmarch_cap;
             A.qmarch = sc->qmarch;
             A.qmarch_hit = g_tune_carry_hits ? sc->qmarch_hit : nullptr;
             A.qmarch_cap = (unsigned)sc->qmarch_cap;
-            CK(cudaMemsetAsync(sc->qcount + 3 * nxt, 0, 3 * sizeof(unsigned), st));
-            for (int k = 0; k < 3; k++) {
-                A.qin[k] = sc->q[cur][k];
-                A.nin[k] = n[k];
-                A.qout[k] = sc->q[nxt][k];
-                A.qcap[k] = (unsigned)sc->qcap[nxt][k];
+            for (int j = 0; j < K; j++) {
+                const int g = gen + j, in = (j & 1) ? nxt : cur, out = in ^ 1;
+                // upper bounds of this generation's inputs (exact for j = 0)
+                const unsigned np = n[Q_PRIM];
+                const size_t nsa = sa + (size_t)j * fan;
+                CK(cudaMemsetAsync(slot(g), 0, 3 * sizeof(unsigned), st));
+                for (int k = 0; k < 3; k++) {
+                    A.qin[k] = sc->q[in][k];
+                    A.nin[k] = j ? (unsigned)sc->qcap[in][k] : n[k];
+                    A.qout[k] = sc->q[out][k];
+                    A.qcap[k] = (unsigned)sc->qcap[out][k];
+                }
+                A.nin_dev = j ? slot(g - 1) : nullptr;
+                A.qout_count = slot(g);
+                // Continuing primaries and shadow/AO rays of one generation are
+                // independent (both only append to the next generation's queues), so
+                // the primaries, whose launch is bound by its longest march, run on
+                // the side stream beside the shadow/AO passes.
+                const bool sec = nsa != 0;
+                const bool overlap = np && sec;
+                if (nl_launch + 4 > maxl && (rc = collect())) return rc;
+                const int first = nl_launch;
+                if (overlap) {
+                    CK(cudaEventRecord(sc->fork, st));
+                    CK(cudaStreamWaitEvent(sc->side, sc->fork, 0));
+                }
+                if (np && split_handoff) {
+                    if ((rc = launch(K_PQUERY, g, np, np, overlap ? sc->side : st))) return rc;
+                    if ((rc = launch(K_PMARCH, g, 0, 1 << 30, overlap ? sc->side : st))) return rc;
+                } else if (np && (rc = launch(K_PRIMARY, g, np, np, overlap ? sc->side : st))) {
+                    return rc;
+                }
+                if (overlap) CK(cudaEventRecord(sc->join, sc->side));
+                if (sec && (rc = launch(K_SECONDARY, g, (unsigned)std::min<size_t>(nsa, 0xffffffffu), (int64_t)nsa, st)))
+                    return rc;
+                if (sec && A.split && (rc = launch(K_MARCH, g, 0, 1 << 30, st))) return rc;
+                if (overlap) CK(cudaStreamWaitEvent(st, sc->join, 0));
+                if (j)
+                    for (int k = first; k < nl_launch; k++)
+                        if (recs[k].kind != K_PMARCH && recs[k].kind != K_MARCH) recs[k].slot = (g - 1) % Scene::kRing;
             }
-            A.qout_count = sc->qcount + 3 * nxt;
-            // Continuing primaries and shadow/AO rays of one generation are
-            // independent (both only append to the next generation's queues), so
-            // the primaries, whose launch is bound by its longest march, run on
-            // the side stream beside the shadow/AO passes.
-            const bool sec = n[Q_SHADOW] + n[Q_AO] != 0;
-            const bool overlap = n[Q_PRIM] && sec;
-            if (nl_launch + 4 > maxl && (rc = collect())) return rc;
-            if (overlap) {
-                CK(cudaEventRecord(sc->fork, st));
-                CK(cudaStreamWaitEvent(sc->side, sc->fork, 0));
+            // one read of the counts per block
+            if ((rc = read_ring())) return rc;
+            int done = K;   // generations of the block that had input
+            for (int j = 0; j < K; j++) {
+                const unsigned *c = hring + 3 * ((gen + j) % Scene::kRing);
+                if (c[0] + c[1] + c[2] == 0) {
+                    done = j + 1;
+                    break;
+                }
             }
-            if (n[Q_PRIM] && split_handoff) {
-                if ((rc = launch(K_PQUERY, gen, n[Q_PRIM], n[Q_PRIM], overlap ? sc->side : st))) return rc;
-                if ((rc = launch(K_PMARCH, gen, 0, 1 << 30, overlap ? sc->side : st))) return rc;
-            } else if (n[Q_PRIM] && (rc = launch(K_PRIMARY, gen, n[Q_PRIM], n[Q_PRIM], overlap ? sc->side : st))) {
-                return rc;
-            }
-            if (overlap) CK(cudaEventRecord(sc->join, sc->side));
-            if (sec && (rc = launch(K_SECONDARY, gen, n[Q_SHADOW] + n[Q_AO], (int64_t)n[Q_SHADOW] + n[Q_AO], st)))
-                return rc;
-            if (sec && A.split && (rc = launch(K_MARCH, gen, 0, 1 << 30, st))) return rc;
-            if (overlap) CK(cudaStreamWaitEvent(st, sc->join, 0));
-            cur = nxt;
-            gen++;
+            const unsigned *c = hring + 3 * ((gen + done - 1) % Scene::kRing);
+            for (int k = 0; k < 3; k++) n[k] = c[k];
+            cur = (done & 1) ? nxt : cur;
+            gen += done;
         }
         gens_total = std::max<int64_t>(gens_total, gen);
     }
@@ -3191,6 +3297,11 @@ int gxy_gpu_set_tuning(int knob, int value) {
         g_tune_sec_packet = value ? 1 : 0;
         return GXY_OK;
     }
+    if (knob == GXY_TUNE_RUNAHEAD) {
+        if (value < 1 || value > 16) return set_error(GXY_ERR_INVALID, "run-ahead must be 1-16 generations");
+        g_tune_runahead = value;
+        return GXY_OK;
+    }
     if (knob == GXY_TUNE_SPLIT_HANDOFF) {
         g_tune_split_handoff = value ? 1 : 0;
         return GXY_OK;
@@ -3228,6 +3339,7 @@ int gxy_gpu_get_tuning(int knob, int *value) {
     else if (knob == GXY_TUNE_SPLIT_HANDOFF) *value = g_tune_split_handoff;
     else if (knob == GXY_TUNE_SEC_PACKET) *value = g_tune_sec_packet;
     else if (knob == GXY_TUNE_BVH_COLLAPSE) *value = g_tune_collapse;
+    else if (knob == GXY_TUNE_RUNAHEAD) *value = g_tune_runahead;
     else return set_error(GXY_ERR_INVALID, "unknown tuning knob");
     return GXY_OK;
 }

@@ -126,6 +126,7 @@ TUNE_QUEUE_CHUNK = 15
 TUNE_SPLIT_HANDOFF = 16
 TUNE_SEC_PACKET = 17
 TUNE_BVH_COLLAPSE = 18
+TUNE_RUNAHEAD = 19
 
 
 def set_tuning(knob, value):

@@ -368,6 +368,17 @@ int gxy_gpu_set_profiling(gxy_scene scene, int on);
                                         rays do not fit is rendered in bands of image rows; a
                                         later generation that still runs out of room reports
                                         GXY_ERR_OVERFLOW */
+#define GXY_TUNE_RUNAHEAD       19   /* frame path: most generations launched per host read of
+                                        the queue counts, 1-16 (default 16).  After the camera
+                                        generation the host reads the three counts once per
+                                        block; a block runs to the generation count of the
+                                        scene's previous frame, and its later generations take
+                                        their input counts from device memory.  Its queues are
+                                        grown to the worst case of the whole block beforehand;
+                                        the block is shortened where the queue set still being
+                                        read holds too little room.  A scene's first frame, and
+                                        a frame that outlasts the previous one, read after every
+                                        generation; 1: always so */
 #define GXY_TUNE_BVH_COLLAPSE   18   /* read at scene commit.  How binary BVH nodes are grouped
                                         into 8-wide nodes: 1 (default) the grouping of least summed
                                         wide-node surface area, by a dynamic programme over the

@@ -303,11 +303,13 @@ def test_sah_top_bvh_matches_oracle(gpu, which):
     assert c["primary_rays"] == cnt["primary"] and c["shadow_rays"] == cnt["shadow"]
 
 
+@pytest.mark.parametrize("sah", [0, 16])
 @pytest.mark.parametrize("which", ["triangles", "mixed"])
-def test_cost_collapse_same_frames_fewer_nodes(gpu, which):
+def test_cost_collapse_same_frames_fewer_nodes(gpu, which, sah):
     """BVH8 nodes grouped by the surface-area cost programme
-    (GXY_TUNE_BVH_COLLAPSE 1) or greedily (0): the same frames and ray
-    counts (the closest hit does not depend on the tree), fewer wide nodes."""
+    (GXY_TUNE_BVH_COLLAPSE 1) or greedily (0), under the radix tree alone and
+    under a binned-SAH top: the same frames and ray counts (the closest hit
+    does not depend on the tree), fewer wide nodes."""
     if which == "triangles":
         cam, vis = scenes.triangle_spheres_scene(width=128, height=128, n_seg=32)
     else:
@@ -315,12 +317,14 @@ def test_cost_collapse_same_frames_fewer_nodes(gpu, which):
     L = S.resolve_lights(vis.lighting, cam)
     out = {}
     try:
+        gpu.set_tuning(gpu.TUNE_BVH_SAH, sah)
         for v in (0, 1):
             gpu.set_tuning(gpu.TUNE_BVH_COLLAPSE, v)
             sc = gpu.Scene(vis)
             out[v] = (sc.render_host(cam, L), sc.counters(), sc.bvh_info())
     finally:
         gpu.set_tuning(gpu.TUNE_BVH_COLLAPSE, 1)
+        gpu.set_tuning(gpu.TUNE_BVH_SAH, 0)
     (a, ca, ia), (b, cb, ib) = out[1], out[0]
     assert float(np.abs(a - b).max()) <= 1e-6
     for k in ("primary_rays", "shadow_rays", "ao_rays", "terminated", "samples"):
