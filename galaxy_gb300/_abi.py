@@ -181,7 +181,7 @@ class RayListArrays:
 class gxy_generation_stats(C.Structure):
     _fields_ = [("ms", C.c_double), ("generation", C.c_int32), ("kind", C.c_int32)] + [(n, C.c_int64) for n in (
         "rays_in", "enqueued", "segments", "samples", "nodes", "tri_tests", "sph_tests", "terminated",
-        "samples_skipped")]
+        "samples_skipped")] + [("start_ms", C.c_double)]
 
 
 class gxy_job(C.Structure):

@@ -2561,8 +2561,9 @@ static int render(Scene *sc, const gxy_camera &cam, const gxy_lighting &lt, floa
     const int snl = spawns ? nl : 0, sna = spawns ? na : 0;
     const bool split = split_eligible(S), split_prim = split && g_tune_split_prim;
     const int maxl = Scene::kMaxLaunch;
-    if (sc->profile && (int)sc->events.size() < 2 * maxl) {
-        for (int k = (int)sc->events.size(); k < 2 * maxl; k++) {
+    // a pair of events per launch, and the frame's start (the last)
+    if (sc->profile && (int)sc->events.size() < 2 * maxl + 1) {
+        for (int k = (int)sc->events.size(); k < 2 * maxl + 1; k++) {
             cudaEvent_t e;
             CK(cudaEventCreate(&e));
             sc->events.push_back(e);
@@ -2628,6 +2629,7 @@ static int render(Scene *sc, const gxy_camera &cam, const gxy_lighting &lt, floa
     const bool lines = S.n_seg > 0;
     sc->last = DevCounters{};
     sc->gens.clear();
+    if (sc->profile) CK(cudaEventRecord(sc->events[2 * maxl], st));
     int64_t gens_total = 0;
     auto launch = [&](int kind, int gen, unsigned rays_in, int64_t items, cudaStream_t st) -> int {
         if (nl_launch >= maxl) return set_error(GXY_ERR_TIMEOUT, "too many launches in one frame");
@@ -2714,9 +2716,11 @@ static int render(Scene *sc, const gxy_camera &cam, const gxy_lighting &lt, floa
         if (sc->profile) {
             for (int k = 0; k < nl_launch; k++) {
                 gxy_generation_stats g{};
-                float ms = 0;
+                float ms = 0, t0 = 0;
                 CK(cudaEventElapsedTime(&ms, sc->events[2 * k], sc->events[2 * k + 1]));
+                CK(cudaEventElapsedTime(&t0, sc->events[2 * maxl], sc->events[2 * k]));
                 g.ms = ms;
+                g.start_ms = t0;
                 g.generation = recs[k].gen;
                 g.kind = recs[k].kind;
                 g.rays_in = recs[k].kind == K_CAMERA ? 0

@@ -313,6 +313,8 @@ typedef struct gxy_generation_stats {
     int64_t enqueued;      /* queue records written                         */
     int64_t segments, samples, nodes, tri_tests, sph_tests, terminated;
     int64_t samples_skipped;
+    double  start_ms;      /* start of the launch after the frame's first launch
+                              (launches on the side stream overlap the others) */
 } gxy_generation_stats;
 int gxy_gpu_set_profiling(gxy_scene scene, int on);
 
