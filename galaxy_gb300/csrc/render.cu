@@ -993,8 +993,10 @@ __device__ __forceinline__ unsigned warp_reserve(unsigned cnt, unsigned *counter
     return idx;
 }
 
+// Per-thread counts (32 bits: a thread handles far fewer than 2^32 rays in
+// one launch, and the warp sums in flush_counters are 64-bit).
 struct LocalCounters {
-    unsigned long long prim = 0, sh = 0, ao = 0, seg = 0, hand = 0, term = 0, drop = 0, keep = 0, enq = 0, march = 0;
+    unsigned prim = 0, sh = 0, ao = 0, seg = 0, hand = 0, term = 0, drop = 0, keep = 0, enq = 0, march = 0;
     int ovf = 0;
 };
 
