@@ -48,6 +48,8 @@ KNOBS = (
     ("march_steps", gpu.TUNE_MARCH_STEPS, (8, 16, 32, 64)),
     ("skip_mode", gpu.TUNE_SKIP_MODE, (0, 1, 3, 7, 9, 11)),
     ("runahead", gpu.TUNE_RUNAHEAD, (1, 2, 4, 8)),
+    ("query_blocks", gpu.TUNE_QUERY_BLOCKS, (3, 4)),
+    ("pmarch_blocks", gpu.TUNE_PMARCH_BLOCKS, (2, 3)),
 )
 
 

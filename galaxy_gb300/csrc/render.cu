@@ -2368,6 +2368,8 @@ static int g_tune_queue_chunk = 0;  // shadow/AO query: records per block taken 
 static int g_tune_split_handoff = 1; // handed-off primaries of volume scenes: query + skipping march (1) or one pass (0)
 static int g_tune_sec_packet = 0;    // shadow/AO query of a frame: per-lane refill (0) or warp per 32-ray packet (1)
 static int g_tune_runahead = 16;     // frame generations launched per host read of the queue counts, at most
+static int g_tune_query_blocks = 3;  // shadow/AO query at 3 (80 registers) or 4 (64) blocks per SM (blocks_per_sm 3)
+static int g_tune_pmarch_blocks = 2; // camera-ray march at 2 (128 registers) or 3 (80) blocks per SM (blocks_per_sm 3)
 int leaf_max() { return g_tune_leaf; }
 static int g_tune_collapse = 1;     // BVH8 collapse: surface-area cost programme (1) or largest child first (0)
 bool collapse_cost() { return g_tune_collapse != 0; }
@@ -2413,10 +2415,21 @@ static void launch_sec_march(unsigned grid, cudaStream_t st, const DevScene &S, 
     else k_sec_march<BATCH, MINB, 0><<<grid, kThreads, 0, st>>>(S, A);
 }
 
-// The refill query passes and the shadow/AO march run at 4 resident blocks
-// per SM when the tuning asks for 3 (64 registers: more warps to cover
-// node-fetch and voxel-gather latency; measured faster than 80 registers
-// with fewer spills; the camera-ray march measured slower and stays at 3).
+// The camera and handed-off primary queries and the shadow/AO march run at
+// 4 resident blocks per SM when the tuning asks for 3 (64 registers: more
+// warps to cover node-fetch and voxel-gather latency; measured faster than
+// 80 registers).  The shadow/AO query and the camera-ray march have their
+// own knobs (GXY_TUNE_QUERY_BLOCKS, GXY_TUNE_PMARCH_BLOCKS): with 64
+// registers the query spills, and 3 blocks of 80 registers measured faster
+// (4.77 -> 4.54 ms per mixed 2048^2 frame); the march is a little faster at
+// 2 blocks of 128 registers than at 3 of 80.
+template <class K>
+static unsigned resident_grid(K kernel) {
+    int sms = 152, per = 1;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, g_device);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, kThreads, 0);
+    return (unsigned)(sms * (per < 1 ? 1 : per));
+}
 static unsigned query_grid() {
     int sms = 152, per = 1;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, g_device);
@@ -2654,9 +2667,14 @@ static int render(Scene *sc, const gxy_camera &cam, const gxy_lighting &lt, floa
                 k_sec_packet<4, true><<<query_grid(), kThreads, 0, st>>>(S, A);
             else if (kind == K_SECONDARY && A.split && g_tune_sec_packet)
                 k_sec_packet<4, false><<<query_grid(), kThreads, 0, st>>>(S, A);
+            else if (kind == K_SECONDARY && A.split && g_tune_query_blocks == 3 && lines)
+                k_sec_query<false, 3, true><<<resident_grid(k_sec_query<false, 3, true>), kThreads, 0, st>>>(S, A);
+            else if (kind == K_SECONDARY && A.split && g_tune_query_blocks == 3)
+                k_sec_query<false, 3, false><<<resident_grid(k_sec_query<false, 3, false>), kThreads, 0, st>>>(S, A);
             else if (kind == K_SECONDARY && A.split && lines) k_sec_query<false, 4, true><<<query_grid(), kThreads, 0, st>>>(S, A);
             else if (kind == K_SECONDARY && A.split) k_sec_query<false, 4, false><<<query_grid(), kThreads, 0, st>>>(S, A);
             else if (kind == K_SECONDARY) k_secondary<3><<<g, kThreads, 0, st>>>(S, A);
+            else if (kind == K_PMARCH && g_tune_pmarch_blocks == 2) launch_prim_march<false, 2>(march_grid(2), st, S, A);
             else if (kind == K_PMARCH) launch_prim_march<false, 3>(march_grid(3), st, S, A);
             else if (kind == K_PQUERY && lines) k_prim_query<4, true><<<query_grid(), kThreads, 0, st>>>(S, A);
             else if (kind == K_PQUERY) k_prim_query<4, false><<<query_grid(), kThreads, 0, st>>>(S, A);
@@ -3312,6 +3330,16 @@ int gxy_gpu_set_tuning(int knob, int value) {
         g_tune_split_handoff = value ? 1 : 0;
         return GXY_OK;
     }
+    if (knob == GXY_TUNE_QUERY_BLOCKS) {
+        if (value != 3 && value != 4) return set_error(GXY_ERR_INVALID, "query blocks per SM must be 3 or 4");
+        g_tune_query_blocks = value;
+        return GXY_OK;
+    }
+    if (knob == GXY_TUNE_PMARCH_BLOCKS) {
+        if (value != 2 && value != 3) return set_error(GXY_ERR_INVALID, "march blocks per SM must be 2 or 3");
+        g_tune_pmarch_blocks = value;
+        return GXY_OK;
+    }
     if (knob == GXY_TUNE_QUEUE_CHUNK) {
         if (value != 0 && (value < 256 || value > 65536))
             return set_error(GXY_ERR_INVALID, "queue chunk must be 0 or 256-65536 records");
@@ -3346,6 +3374,8 @@ int gxy_gpu_get_tuning(int knob, int *value) {
     else if (knob == GXY_TUNE_SEC_PACKET) *value = g_tune_sec_packet;
     else if (knob == GXY_TUNE_BVH_COLLAPSE) *value = g_tune_collapse;
     else if (knob == GXY_TUNE_RUNAHEAD) *value = g_tune_runahead;
+    else if (knob == GXY_TUNE_QUERY_BLOCKS) *value = g_tune_query_blocks;
+    else if (knob == GXY_TUNE_PMARCH_BLOCKS) *value = g_tune_pmarch_blocks;
     else return set_error(GXY_ERR_INVALID, "unknown tuning knob");
     return GXY_OK;
 }
@@ -3660,7 +3690,8 @@ static int batch_enqueue(Batch *b, const DevScene &Su, bool uniform, const Frame
                 if (mb3) {
                     if (lines) k_cam_query<true, 4, true><<<query_grid(), kThreads, 0, st>>>(Su, a);
                     else k_cam_query<true, 4, false><<<query_grid(), kThreads, 0, st>>>(Su, a);
-                    launch_prim_march<true, 3>(march_grid(3), st, Su, a);
+                    if (g_tune_pmarch_blocks == 2) launch_prim_march<true, 2>(march_grid(2), st, Su, a);
+                    else launch_prim_march<true, 3>(march_grid(3), st, Su, a);
                 } else {
                     if (lines) k_cam_query<true, 2, true><<<march_grid(2), kThreads, 0, st>>>(Su, a);
                     else k_cam_query<true, 2, false><<<march_grid(2), kThreads, 0, st>>>(Su, a);
@@ -3672,7 +3703,11 @@ static int batch_enqueue(Batch *b, const DevScene &Su, bool uniform, const Frame
                 if (mb3) k_batch_gen<K_PRIMARY, true, 3><<<grid, kThreads, 0, b->side>>>(Su, a, cin);
                 else k_batch_gen<K_PRIMARY, true, 2><<<grid, kThreads, 0, b->side>>>(Su, a, cin);
                 CK(cudaEventRecord(b->join[g], b->side));
-                if (mb3) {
+                if (mb3 && g_tune_query_blocks == 3) {
+                    if (lines) k_sec_query<true, 3, true><<<resident_grid(k_sec_query<true, 3, true>), kThreads, 0, st>>>(Su, a);
+                    else k_sec_query<true, 3, false><<<resident_grid(k_sec_query<true, 3, false>), kThreads, 0, st>>>(Su, a);
+                    launch_sec_march<true, 4>(query_grid(), st, Su, a);
+                } else if (mb3) {
                     if (lines) k_sec_query<true, 4, true><<<query_grid(), kThreads, 0, st>>>(Su, a);
                     else k_sec_query<true, 4, false><<<query_grid(), kThreads, 0, st>>>(Su, a);
                     launch_sec_march<true, 4>(query_grid(), st, Su, a);

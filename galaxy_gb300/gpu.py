@@ -127,6 +127,8 @@ TUNE_SPLIT_HANDOFF = 16
 TUNE_SEC_PACKET = 17
 TUNE_BVH_COLLAPSE = 18
 TUNE_RUNAHEAD = 19
+TUNE_QUERY_BLOCKS = 20
+TUNE_PMARCH_BLOCKS = 21
 
 
 def set_tuning(knob, value):
