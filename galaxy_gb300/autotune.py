@@ -50,6 +50,7 @@ KNOBS = (
     ("runahead", gpu.TUNE_RUNAHEAD, (1, 2, 4, 8)),
     ("query_blocks", gpu.TUNE_QUERY_BLOCKS, (3, 4)),
     ("pmarch_blocks", gpu.TUNE_PMARCH_BLOCKS, (2, 3)),
+    ("pquery_blocks", gpu.TUNE_PQUERY_BLOCKS, (2, 4)),
 )
 
 

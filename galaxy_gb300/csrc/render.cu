@@ -2368,8 +2368,9 @@ static int g_tune_queue_chunk = 0;  // shadow/AO query: records per block taken 
 static int g_tune_split_handoff = 1; // handed-off primaries of volume scenes: query + skipping march (1) or one pass (0)
 static int g_tune_sec_packet = 0;    // shadow/AO query of a frame: per-lane refill (0) or warp per 32-ray packet (1)
 static int g_tune_runahead = 16;     // frame generations launched per host read of the queue counts, at most
-static int g_tune_query_blocks = 3;  // shadow/AO query at 3 (80 registers) or 4 (64) blocks per SM (blocks_per_sm 3)
+static int g_tune_query_blocks = 3;  // shadow/AO query at 2 (128 registers), 3 (80) or 4 (64) blocks per SM (blocks_per_sm 3)
 static int g_tune_pmarch_blocks = 2; // camera-ray march at 2 (128 registers) or 3 (80) blocks per SM (blocks_per_sm 3)
+static int g_tune_pquery_blocks = 2; // frame camera and handed-off primary queries at 2 (128 registers) or 4 (64)
 int leaf_max() { return g_tune_leaf; }
 static int g_tune_collapse = 1;     // BVH8 collapse: surface-area cost programme (1) or largest child first (0)
 bool collapse_cost() { return g_tune_collapse != 0; }
@@ -2415,14 +2416,16 @@ static void launch_sec_march(unsigned grid, cudaStream_t st, const DevScene &S, 
     else k_sec_march<BATCH, MINB, 0><<<grid, kThreads, 0, st>>>(S, A);
 }
 
-// The camera and handed-off primary queries and the shadow/AO march run at
-// 4 resident blocks per SM when the tuning asks for 3 (64 registers: more
-// warps to cover node-fetch and voxel-gather latency; measured faster than
-// 80 registers).  The shadow/AO query and the camera-ray march have their
-// own knobs (GXY_TUNE_QUERY_BLOCKS, GXY_TUNE_PMARCH_BLOCKS): with 64
-// registers the query spills, and 3 blocks of 80 registers measured faster
-// (4.77 -> 4.54 ms per mixed 2048^2 frame); the march is a little faster at
-// 2 blocks of 128 registers than at 3 of 80.
+// The shadow/AO march and the batches' camera query run at 4 resident
+// blocks per SM when the tuning asks for 3 (64 registers: more warps to
+// cover node-fetch and voxel-gather latency; measured faster than 80
+// registers).  The frame path's queries and camera-ray march have their own
+// knobs, measured on the mixed 2048^2 frame: the shadow/AO query spills at
+// 64 registers and is faster at 3 blocks of 80 (GXY_TUNE_QUERY_BLOCKS;
+// 4.77 -> 4.54 ms per frame), the camera and handed-off primary queries at
+// 2 blocks of 128 (GXY_TUNE_PQUERY_BLOCKS; 1.39 -> 1.33 and 0.78 -> 0.63
+// ms), and the camera-ray march at 2 blocks of 128 (GXY_TUNE_PMARCH_BLOCKS;
+// 1.40 -> 1.36 ms).
 template <class K>
 static unsigned resident_grid(K kernel) {
     int sms = 152, per = 1;
@@ -2655,7 +2658,12 @@ static int render(Scene *sc, const gxy_camera &cam, const gxy_lighting &lt, floa
         if ((kind == K_CAMERA && A.split_prim) || kind == K_PQUERY)
             CK(cudaMemsetAsync(A.pmarch_count, 0, 4 * sizeof(unsigned), st));
         if (g_tune_minb == 3) {
-            if (kind == K_CAMERA && A.split_prim && g_tune_cam_packet && lines)
+            const bool pq2 = g_tune_pquery_blocks == 2;
+            if (kind == K_CAMERA && A.split_prim && g_tune_cam_packet && pq2 && lines)
+                k_cam_packet<2, true><<<resident_grid(k_cam_packet<2, true>), kThreads, 0, st>>>(S, A);
+            else if (kind == K_CAMERA && A.split_prim && g_tune_cam_packet && pq2)
+                k_cam_packet<2, false><<<resident_grid(k_cam_packet<2, false>), kThreads, 0, st>>>(S, A);
+            else if (kind == K_CAMERA && A.split_prim && g_tune_cam_packet && lines)
                 k_cam_packet<4, true><<<query_grid(), kThreads, 0, st>>>(S, A);
             else if (kind == K_CAMERA && A.split_prim && g_tune_cam_packet)
                 k_cam_packet<4, false><<<query_grid(), kThreads, 0, st>>>(S, A);
@@ -2667,6 +2675,10 @@ static int render(Scene *sc, const gxy_camera &cam, const gxy_lighting &lt, floa
                 k_sec_packet<4, true><<<query_grid(), kThreads, 0, st>>>(S, A);
             else if (kind == K_SECONDARY && A.split && g_tune_sec_packet)
                 k_sec_packet<4, false><<<query_grid(), kThreads, 0, st>>>(S, A);
+            else if (kind == K_SECONDARY && A.split && g_tune_query_blocks == 2 && lines)
+                k_sec_query<false, 2, true><<<resident_grid(k_sec_query<false, 2, true>), kThreads, 0, st>>>(S, A);
+            else if (kind == K_SECONDARY && A.split && g_tune_query_blocks == 2)
+                k_sec_query<false, 2, false><<<resident_grid(k_sec_query<false, 2, false>), kThreads, 0, st>>>(S, A);
             else if (kind == K_SECONDARY && A.split && g_tune_query_blocks == 3 && lines)
                 k_sec_query<false, 3, true><<<resident_grid(k_sec_query<false, 3, true>), kThreads, 0, st>>>(S, A);
             else if (kind == K_SECONDARY && A.split && g_tune_query_blocks == 3)
@@ -2676,6 +2688,10 @@ static int render(Scene *sc, const gxy_camera &cam, const gxy_lighting &lt, floa
             else if (kind == K_SECONDARY) k_secondary<3><<<g, kThreads, 0, st>>>(S, A);
             else if (kind == K_PMARCH && g_tune_pmarch_blocks == 2) launch_prim_march<false, 2>(march_grid(2), st, S, A);
             else if (kind == K_PMARCH) launch_prim_march<false, 3>(march_grid(3), st, S, A);
+            else if (kind == K_PQUERY && pq2 && lines)
+                k_prim_query<2, true><<<resident_grid(k_prim_query<2, true>), kThreads, 0, st>>>(S, A);
+            else if (kind == K_PQUERY && pq2)
+                k_prim_query<2, false><<<resident_grid(k_prim_query<2, false>), kThreads, 0, st>>>(S, A);
             else if (kind == K_PQUERY && lines) k_prim_query<4, true><<<query_grid(), kThreads, 0, st>>>(S, A);
             else if (kind == K_PQUERY) k_prim_query<4, false><<<query_grid(), kThreads, 0, st>>>(S, A);
             else launch_sec_march<false, 4>(query_grid(), st, S, A);
@@ -3331,8 +3347,13 @@ int gxy_gpu_set_tuning(int knob, int value) {
         return GXY_OK;
     }
     if (knob == GXY_TUNE_QUERY_BLOCKS) {
-        if (value != 3 && value != 4) return set_error(GXY_ERR_INVALID, "query blocks per SM must be 3 or 4");
+        if (value < 2 || value > 4) return set_error(GXY_ERR_INVALID, "query blocks per SM must be 2, 3 or 4");
         g_tune_query_blocks = value;
+        return GXY_OK;
+    }
+    if (knob == GXY_TUNE_PQUERY_BLOCKS) {
+        if (value != 2 && value != 4) return set_error(GXY_ERR_INVALID, "primary query blocks per SM must be 2 or 4");
+        g_tune_pquery_blocks = value;
         return GXY_OK;
     }
     if (knob == GXY_TUNE_PMARCH_BLOCKS) {
@@ -3376,6 +3397,7 @@ int gxy_gpu_get_tuning(int knob, int *value) {
     else if (knob == GXY_TUNE_RUNAHEAD) *value = g_tune_runahead;
     else if (knob == GXY_TUNE_QUERY_BLOCKS) *value = g_tune_query_blocks;
     else if (knob == GXY_TUNE_PMARCH_BLOCKS) *value = g_tune_pmarch_blocks;
+    else if (knob == GXY_TUNE_PQUERY_BLOCKS) *value = g_tune_pquery_blocks;
     else return set_error(GXY_ERR_INVALID, "unknown tuning knob");
     return GXY_OK;
 }
@@ -3703,7 +3725,11 @@ static int batch_enqueue(Batch *b, const DevScene &Su, bool uniform, const Frame
                 if (mb3) k_batch_gen<K_PRIMARY, true, 3><<<grid, kThreads, 0, b->side>>>(Su, a, cin);
                 else k_batch_gen<K_PRIMARY, true, 2><<<grid, kThreads, 0, b->side>>>(Su, a, cin);
                 CK(cudaEventRecord(b->join[g], b->side));
-                if (mb3 && g_tune_query_blocks == 3) {
+                if (mb3 && g_tune_query_blocks == 2) {
+                    if (lines) k_sec_query<true, 2, true><<<resident_grid(k_sec_query<true, 2, true>), kThreads, 0, st>>>(Su, a);
+                    else k_sec_query<true, 2, false><<<resident_grid(k_sec_query<true, 2, false>), kThreads, 0, st>>>(Su, a);
+                    launch_sec_march<true, 4>(query_grid(), st, Su, a);
+                } else if (mb3 && g_tune_query_blocks == 3) {
                     if (lines) k_sec_query<true, 3, true><<<resident_grid(k_sec_query<true, 3, true>), kThreads, 0, st>>>(Su, a);
                     else k_sec_query<true, 3, false><<<resident_grid(k_sec_query<true, 3, false>), kThreads, 0, st>>>(Su, a);
                     launch_sec_march<true, 4>(query_grid(), st, Su, a);

@@ -129,6 +129,7 @@ TUNE_BVH_COLLAPSE = 18
 TUNE_RUNAHEAD = 19
 TUNE_QUERY_BLOCKS = 20
 TUNE_PMARCH_BLOCKS = 21
+TUNE_PQUERY_BLOCKS = 22
 
 
 def set_tuning(knob, value):

@@ -399,11 +399,15 @@ int gxy_gpu_set_profiling(gxy_scene scene, int on);
                                         them to its idle lanes in queue order (0, default: a warp
                                         takes exactly what its idle lanes need) */
 #define GXY_TUNE_QUERY_BLOCKS   20   /* with GXY_TUNE_BLOCKS_PER_SM 3: resident blocks per SM of the
-                                        shadow/AO query, 3 (default: 80 registers per thread) or 4
-                                        (64 registers); the other refill queries run at 4 */
+                                        shadow/AO query, 2 (128 registers per thread), 3 (default:
+                                        80 registers) or 4 (64 registers); the other refill
+                                        queries run at 4 */
 #define GXY_TUNE_PMARCH_BLOCKS  21   /* with GXY_TUNE_BLOCKS_PER_SM 3: resident blocks per SM of the
                                         camera-ray march (and of handed-off primaries), 2 (default:
                                         128 registers per thread) or 3 (80 registers) */
+#define GXY_TUNE_PQUERY_BLOCKS  22   /* with GXY_TUNE_BLOCKS_PER_SM 3: resident blocks per SM of a
+                                        frame's warp-cooperative camera query and handed-off primary
+                                        query, 2 (default: 128 registers per thread) or 4 (64) */
 #define GXY_TUNE_CARRY_HITS     13   /* 1 (default): a shadow/AO ray that moves to the next
                                         partition carries the closest hit its query found
                                         over its whole extent, and the next partition's

@@ -94,22 +94,25 @@ def test_mixed_partitioned_scene(gpu, split):
 
 
 def test_query_and_march_register_budgets_same_frames(gpu):
-    """The shadow/AO query at 3 or 4 resident blocks per SM
-    (GXY_TUNE_QUERY_BLOCKS) and the camera-ray march at 2 or 3
-    (GXY_TUNE_PMARCH_BLOCKS): the same frames and counters, equal to the
-    oracle."""
+    """The shadow/AO query at 2, 3 or 4 resident blocks per SM
+    (GXY_TUNE_QUERY_BLOCKS), the camera-ray march at 2 or 3
+    (GXY_TUNE_PMARCH_BLOCKS) and the camera and handed-off primary queries
+    at 2 or 4 (GXY_TUNE_PQUERY_BLOCKS): the same frames and counters, equal
+    to the oracle."""
     cam, vis = scenes.mixed_scene(n=64, n_spheres=20000, width=128, height=128, partitions=(2, 2, 2), n_ao=4)
     L = S.resolve_lights(vis.lighting, cam)
     sc = gpu.Scene(vis)
     out = []
     try:
-        for qb, pb in ((3, 2), (4, 3), (3, 3), (4, 2)):
+        for qb, pb, cb in ((3, 2, 2), (4, 3, 4), (3, 3, 2), (4, 2, 4), (2, 2, 2)):
             gpu.set_tuning(gpu.TUNE_QUERY_BLOCKS, qb)
             gpu.set_tuning(gpu.TUNE_PMARCH_BLOCKS, pb)
+            gpu.set_tuning(gpu.TUNE_PQUERY_BLOCKS, cb)
             out.append((sc.render_host(cam, L), sc.counters()))
     finally:
         gpu.set_tuning(gpu.TUNE_QUERY_BLOCKS, 3)
         gpu.set_tuning(gpu.TUNE_PMARCH_BLOCKS, 2)
+        gpu.set_tuning(gpu.TUNE_PQUERY_BLOCKS, 2)
     for img, c in out[1:]:
         assert float(np.abs(img - out[0][0]).max()) <= 1e-6
         for k in ("primary_rays", "shadow_rays", "ao_rays", "terminated", "samples", "nodes"):
@@ -117,9 +120,11 @@ def test_query_and_march_register_budgets_same_frames(gpu):
     ref, cnt = O.OracleScene(vis).render(cam, L)
     image_close(out[0][0], ref)
     with pytest.raises(gpu.GxyError):
-        gpu.set_tuning(gpu.TUNE_QUERY_BLOCKS, 2)
+        gpu.set_tuning(gpu.TUNE_QUERY_BLOCKS, 5)
     with pytest.raises(gpu.GxyError):
         gpu.set_tuning(gpu.TUNE_PMARCH_BLOCKS, 4)
+    with pytest.raises(gpu.GxyError):
+        gpu.set_tuning(gpu.TUNE_PQUERY_BLOCKS, 3)
 
 
 @pytest.mark.parametrize("split_primary", [0, 1])
