@@ -549,22 +549,22 @@ def main():
         gpu.set_tuning(gpu.TUNE_SPLIT_PRIMARY, vals[3])
     elif args.autotune:
         tuning = autotune.tune(sc, cam_c, L, frames=4)
-    sc.set_profiling(True)
+    sc.set_profiling(False)
     for _ in range(args.warmup):
         frame()
     torch.cuda.synchronize()
     c = sc.counters()
     rays_per_frame = c["primary_rays"] + c["shadow_rays"] + c["ao_rays"]
 
-    # ---- timed region: K frames, per-frame events, clocks sampled
+    # ---- timed region: K frames, per-frame events, clocks sampled; the
+    # per-launch statistics are off here (their event records and reads
+    # would be timed too) and are taken over K more frames below
     clocks = ClockSampler(local)
     barrier(world)
     torch.cuda.synchronize()
     clocks.start()
     time.sleep(0.3)
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    gen_ms, gen_bytes = {}, {}
-    launches = 0
     t_start = torch.cuda.Event(enable_timing=True)
     t_end = torch.cuda.Event(enable_timing=True)
     t_start.record(stream)
@@ -572,6 +572,21 @@ def main():
         ev[k][0].record(stream)
         frame()
         ev[k][1].record(stream)
+    t_end.record(stream)
+    torch.cuda.synchronize()
+    barrier(world)
+    clk = clocks.stop()
+    total_ms = t_start.elapsed_time(t_end)
+
+    # ---- per-launch device time and counters of K profiled frames (events
+    # around every launch on its stream): the roofline's kernel time
+    sc.set_profiling(True)
+    frame()
+    torch.cuda.synchronize()
+    gen_ms, gen_bytes = {}, {}
+    launches = 0
+    for k in range(args.steps):
+        frame()
         gens = sc.generations()
         launches += len(gens)
         for g in gens:
@@ -582,12 +597,9 @@ def main():
                 continue
             gen_ms.setdefault(g["kind"], []).append(g["ms"])
             gen_bytes.setdefault(g["kind"], []).append(algorithmic_bytes(g))
-    t_end.record(stream)
     torch.cuda.synchronize()
-    barrier(world)
-    clk = clocks.stop()
     sc_last_gens = sc.generations()
-    total_ms = t_start.elapsed_time(t_end)
+    sc.set_profiling(False)
     frame_ms = [a.elapsed_time(b) for a, b in ev]
     total_ms = allreduce_max(total_ms, world)
     value = rays_per_frame * args.steps * world / (total_ms / 1e3)

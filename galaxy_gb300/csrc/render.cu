@@ -2404,10 +2404,22 @@ static unsigned march_grid(int minb) {
 // SKIP levels): the camera-ray march skips per position whenever the scene
 // has the flags; the shadow/AO march takes the lean superbrick jumps with
 // GXY_TUNE_SKIP_MODE bit 1 and per-position skipping with bit 2.
+// Grid of a refill kernel (it loops over its queue until the queue is
+// empty): one wave of the blocks that fit on the SMs at its own register
+// budget.
+template <class K>
+static unsigned one_wave(K kernel) {
+    int sms = 152, per = 1;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, g_device);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, kThreads, 0);
+    return (unsigned)(sms * (per < 1 ? 1 : per));
+}
 template <bool BATCH, int MINB>
-static void launch_prim_march(unsigned grid, cudaStream_t st, const DevScene &S, const FrameArgs &A) {
-    if (S.vol[0].clear) k_prim_march<BATCH, MINB, 2><<<grid, kThreads, 0, st>>>(S, A);
-    else k_prim_march<BATCH, MINB, 0><<<grid, kThreads, 0, st>>>(S, A);
+static void launch_prim_march(cudaStream_t st, const DevScene &S, const FrameArgs &A) {
+    if (S.vol[0].clear)
+        k_prim_march<BATCH, MINB, 2><<<one_wave(k_prim_march<BATCH, MINB, 2>), kThreads, 0, st>>>(S, A);
+    else
+        k_prim_march<BATCH, MINB, 0><<<one_wave(k_prim_march<BATCH, MINB, 0>), kThreads, 0, st>>>(S, A);
 }
 template <bool BATCH, int MINB>
 static void launch_sec_march(unsigned grid, cudaStream_t st, const DevScene &S, const FrameArgs &A) {
@@ -2426,13 +2438,6 @@ static void launch_sec_march(unsigned grid, cudaStream_t st, const DevScene &S, 
 // 2 blocks of 128 (GXY_TUNE_PQUERY_BLOCKS; 1.39 -> 1.33 and 0.78 -> 0.63
 // ms), and the camera-ray march at 2 blocks of 128 (GXY_TUNE_PMARCH_BLOCKS;
 // 1.40 -> 1.36 ms).
-template <class K>
-static unsigned resident_grid(K kernel) {
-    int sms = 152, per = 1;
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, g_device);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, kThreads, 0);
-    return (unsigned)(sms * (per < 1 ? 1 : per));
-}
 static unsigned query_grid() {
     int sms = 152, per = 1;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, g_device);
@@ -2660,9 +2665,9 @@ static int render(Scene *sc, const gxy_camera &cam, const gxy_lighting &lt, floa
         if (g_tune_minb == 3) {
             const bool pq2 = g_tune_pquery_blocks == 2;
             if (kind == K_CAMERA && A.split_prim && g_tune_cam_packet && pq2 && lines)
-                k_cam_packet<2, true><<<resident_grid(k_cam_packet<2, true>), kThreads, 0, st>>>(S, A);
+                k_cam_packet<2, true><<<one_wave(k_cam_packet<2, true>), kThreads, 0, st>>>(S, A);
             else if (kind == K_CAMERA && A.split_prim && g_tune_cam_packet && pq2)
-                k_cam_packet<2, false><<<resident_grid(k_cam_packet<2, false>), kThreads, 0, st>>>(S, A);
+                k_cam_packet<2, false><<<one_wave(k_cam_packet<2, false>), kThreads, 0, st>>>(S, A);
             else if (kind == K_CAMERA && A.split_prim && g_tune_cam_packet && lines)
                 k_cam_packet<4, true><<<query_grid(), kThreads, 0, st>>>(S, A);
             else if (kind == K_CAMERA && A.split_prim && g_tune_cam_packet)
@@ -2676,22 +2681,22 @@ static int render(Scene *sc, const gxy_camera &cam, const gxy_lighting &lt, floa
             else if (kind == K_SECONDARY && A.split && g_tune_sec_packet)
                 k_sec_packet<4, false><<<query_grid(), kThreads, 0, st>>>(S, A);
             else if (kind == K_SECONDARY && A.split && g_tune_query_blocks == 2 && lines)
-                k_sec_query<false, 2, true><<<resident_grid(k_sec_query<false, 2, true>), kThreads, 0, st>>>(S, A);
+                k_sec_query<false, 2, true><<<one_wave(k_sec_query<false, 2, true>), kThreads, 0, st>>>(S, A);
             else if (kind == K_SECONDARY && A.split && g_tune_query_blocks == 2)
-                k_sec_query<false, 2, false><<<resident_grid(k_sec_query<false, 2, false>), kThreads, 0, st>>>(S, A);
+                k_sec_query<false, 2, false><<<one_wave(k_sec_query<false, 2, false>), kThreads, 0, st>>>(S, A);
             else if (kind == K_SECONDARY && A.split && g_tune_query_blocks == 3 && lines)
-                k_sec_query<false, 3, true><<<resident_grid(k_sec_query<false, 3, true>), kThreads, 0, st>>>(S, A);
+                k_sec_query<false, 3, true><<<one_wave(k_sec_query<false, 3, true>), kThreads, 0, st>>>(S, A);
             else if (kind == K_SECONDARY && A.split && g_tune_query_blocks == 3)
-                k_sec_query<false, 3, false><<<resident_grid(k_sec_query<false, 3, false>), kThreads, 0, st>>>(S, A);
+                k_sec_query<false, 3, false><<<one_wave(k_sec_query<false, 3, false>), kThreads, 0, st>>>(S, A);
             else if (kind == K_SECONDARY && A.split && lines) k_sec_query<false, 4, true><<<query_grid(), kThreads, 0, st>>>(S, A);
             else if (kind == K_SECONDARY && A.split) k_sec_query<false, 4, false><<<query_grid(), kThreads, 0, st>>>(S, A);
             else if (kind == K_SECONDARY) k_secondary<3><<<g, kThreads, 0, st>>>(S, A);
-            else if (kind == K_PMARCH && g_tune_pmarch_blocks == 2) launch_prim_march<false, 2>(march_grid(2), st, S, A);
-            else if (kind == K_PMARCH) launch_prim_march<false, 3>(march_grid(3), st, S, A);
+            else if (kind == K_PMARCH && g_tune_pmarch_blocks == 2) launch_prim_march<false, 2>(st, S, A);
+            else if (kind == K_PMARCH) launch_prim_march<false, 3>(st, S, A);
             else if (kind == K_PQUERY && pq2 && lines)
-                k_prim_query<2, true><<<resident_grid(k_prim_query<2, true>), kThreads, 0, st>>>(S, A);
+                k_prim_query<2, true><<<one_wave(k_prim_query<2, true>), kThreads, 0, st>>>(S, A);
             else if (kind == K_PQUERY && pq2)
-                k_prim_query<2, false><<<resident_grid(k_prim_query<2, false>), kThreads, 0, st>>>(S, A);
+                k_prim_query<2, false><<<one_wave(k_prim_query<2, false>), kThreads, 0, st>>>(S, A);
             else if (kind == K_PQUERY && lines) k_prim_query<4, true><<<query_grid(), kThreads, 0, st>>>(S, A);
             else if (kind == K_PQUERY) k_prim_query<4, false><<<query_grid(), kThreads, 0, st>>>(S, A);
             else launch_sec_march<false, 4>(query_grid(), st, S, A);
@@ -2711,7 +2716,7 @@ static int render(Scene *sc, const gxy_camera &cam, const gxy_lighting &lt, floa
             else if (kind == K_SECONDARY && A.split && lines) k_sec_query<false, 2, true><<<march_grid(2), kThreads, 0, st>>>(S, A);
             else if (kind == K_SECONDARY && A.split) k_sec_query<false, 2, false><<<march_grid(2), kThreads, 0, st>>>(S, A);
             else if (kind == K_SECONDARY) k_secondary<2><<<g, kThreads, 0, st>>>(S, A);
-            else if (kind == K_PMARCH) launch_prim_march<false, 2>(march_grid(2), st, S, A);
+            else if (kind == K_PMARCH) launch_prim_march<false, 2>(st, S, A);
             else if (kind == K_PQUERY && lines) k_prim_query<2, true><<<march_grid(2), kThreads, 0, st>>>(S, A);
             else if (kind == K_PQUERY) k_prim_query<2, false><<<march_grid(2), kThreads, 0, st>>>(S, A);
             else launch_sec_march<false, 2>(march_grid(2), st, S, A);
@@ -3712,12 +3717,12 @@ static int batch_enqueue(Batch *b, const DevScene &Su, bool uniform, const Frame
                 if (mb3) {
                     if (lines) k_cam_query<true, 4, true><<<query_grid(), kThreads, 0, st>>>(Su, a);
                     else k_cam_query<true, 4, false><<<query_grid(), kThreads, 0, st>>>(Su, a);
-                    if (g_tune_pmarch_blocks == 2) launch_prim_march<true, 2>(march_grid(2), st, Su, a);
-                    else launch_prim_march<true, 3>(march_grid(3), st, Su, a);
+                    if (g_tune_pmarch_blocks == 2) launch_prim_march<true, 2>(st, Su, a);
+                    else launch_prim_march<true, 3>(st, Su, a);
                 } else {
                     if (lines) k_cam_query<true, 2, true><<<march_grid(2), kThreads, 0, st>>>(Su, a);
                     else k_cam_query<true, 2, false><<<march_grid(2), kThreads, 0, st>>>(Su, a);
-                    launch_prim_march<true, 2>(march_grid(2), st, Su, a);
+                    launch_prim_march<true, 2>(st, Su, a);
                 }
             } else {
                 CK(cudaEventRecord(b->fork[g], st));
@@ -3726,12 +3731,12 @@ static int batch_enqueue(Batch *b, const DevScene &Su, bool uniform, const Frame
                 else k_batch_gen<K_PRIMARY, true, 2><<<grid, kThreads, 0, b->side>>>(Su, a, cin);
                 CK(cudaEventRecord(b->join[g], b->side));
                 if (mb3 && g_tune_query_blocks == 2) {
-                    if (lines) k_sec_query<true, 2, true><<<resident_grid(k_sec_query<true, 2, true>), kThreads, 0, st>>>(Su, a);
-                    else k_sec_query<true, 2, false><<<resident_grid(k_sec_query<true, 2, false>), kThreads, 0, st>>>(Su, a);
+                    if (lines) k_sec_query<true, 2, true><<<one_wave(k_sec_query<true, 2, true>), kThreads, 0, st>>>(Su, a);
+                    else k_sec_query<true, 2, false><<<one_wave(k_sec_query<true, 2, false>), kThreads, 0, st>>>(Su, a);
                     launch_sec_march<true, 4>(query_grid(), st, Su, a);
                 } else if (mb3 && g_tune_query_blocks == 3) {
-                    if (lines) k_sec_query<true, 3, true><<<resident_grid(k_sec_query<true, 3, true>), kThreads, 0, st>>>(Su, a);
-                    else k_sec_query<true, 3, false><<<resident_grid(k_sec_query<true, 3, false>), kThreads, 0, st>>>(Su, a);
+                    if (lines) k_sec_query<true, 3, true><<<one_wave(k_sec_query<true, 3, true>), kThreads, 0, st>>>(Su, a);
+                    else k_sec_query<true, 3, false><<<one_wave(k_sec_query<true, 3, false>), kThreads, 0, st>>>(Su, a);
                     launch_sec_march<true, 4>(query_grid(), st, Su, a);
                 } else if (mb3) {
                     if (lines) k_sec_query<true, 4, true><<<query_grid(), kThreads, 0, st>>>(Su, a);
