@@ -836,6 +836,18 @@ __device__ __forceinline__ void load_tfs(const DevScene &S, DevTF *sh) {
     __syncthreads();
 }
 
+// The transfer function of volume 0 into shared memory: the split passes
+// run only on scenes with one volume, so they hold one 4 KB table (a block
+// that holds all kMaxVol tables takes 16 KB of the SM's L1/shared space).
+__device__ __forceinline__ void load_tf0(const DevScene &S, DevTF *sh) {
+    if (S.n_vol > 0) {
+        const float4 *src = reinterpret_cast<const float4 *>(S.tfs + S.vol[0].tf);
+        float4 *dst = reinterpret_cast<float4 *>(sh);
+        for (int i = threadIdx.x; i < (int)(sizeof(DevTF) / 16); i += blockDim.x) dst[i] = __ldg(src + i);
+    }
+    __syncthreads();
+}
+
 // Box::intersect (src/data/Box.cpp:107-150).
 __device__ __forceinline__ bool box_intersect(const float lo[3], const float hi[3], V3 org, V3 dir, float &tmin,
                                               float &tmax) {
@@ -1744,11 +1756,11 @@ __global__ void __launch_bounds__(kThreads, MINB) k_sec_packet(DevScene S, Frame
 // records in pixel order; further bricks of one pixel go after slot npix.
 template <bool BATCH, int MINB, bool LINES>
 __global__ void __launch_bounds__(kThreads, MINB) k_cam_query(DevScene S, FrameArgs A) {
-    __shared__ DevTF tfs[kMaxVol];
+    __shared__ DevTF tfs[1];   // split passes: one volume (split_eligible)
     __shared__ long long pix0[BATCH ? kMaxJobs : 1];
     if (BATCH)
         for (int j = threadIdx.x; j < A.n_jobs; j += blockDim.x) pix0[j] = A.jobs[j].pix0;
-    load_tfs(S, tfs);
+    load_tf0(S, tfs);
     RayStats st;
     LocalCounters c;
     const int lane = threadIdx.x & 31;
@@ -1870,8 +1882,8 @@ __global__ void __launch_bounds__(kThreads, MINB) k_cam_query(DevScene S, FrameA
 // classifies and routes exactly as for camera rays.
 template <int MINB, bool LINES>
 __global__ void __launch_bounds__(kThreads, MINB) k_prim_query(DevScene S, FrameArgs A) {
-    __shared__ DevTF tfs[kMaxVol];
-    load_tfs(S, tfs);
+    __shared__ DevTF tfs[1];   // split passes: one volume (split_eligible)
+    load_tf0(S, tfs);
     RayStats st;
     LocalCounters c;
     const int lane = threadIdx.x & 31;
@@ -1951,9 +1963,9 @@ __global__ void __launch_bounds__(kThreads, MINB) k_prim_query(DevScene S, Frame
 // enters no brick, further bricks after slot npix.
 template <int MINB, bool LINES>
 __global__ void __launch_bounds__(kThreads, MINB) k_cam_packet(DevScene S, FrameArgs A) {
-    __shared__ DevTF tfs[kMaxVol];
+    __shared__ DevTF tfs[1];   // split passes: one volume (split_eligible)
     __shared__ uint2 wstacks[kThreads / 32][64];
-    load_tfs(S, tfs);
+    load_tf0(S, tfs);
     RayStats st;
     LocalCounters c;
     const unsigned FULL = 0xffffffffu;
@@ -2038,8 +2050,8 @@ __global__ void __launch_bounds__(kThreads, MINB) k_cam_packet(DevScene S, Frame
 // diffuse, shadow spawn), classify, route and accumulate as primary_ray does.
 template <bool BATCH, int MINB, int SKIP>
 __global__ void __launch_bounds__(kThreads, MINB) k_prim_march(DevScene S, FrameArgs A) {
-    __shared__ DevTF tfs[kMaxVol];
-    load_tfs(S, tfs);
+    __shared__ DevTF tfs[1];   // split passes: one volume (split_eligible)
+    load_tf0(S, tfs);
     RayStats st;
     LocalCounters c;
     const int lane = threadIdx.x & 31;
@@ -2108,8 +2120,8 @@ __global__ void __launch_bounds__(kThreads, MINB) k_prim_march(DevScene S, Frame
 // flag.  USCENE / batch as for the other frame kernels (uniform scene only).
 template <bool BATCH, int MINB, int SKIP>
 __global__ void __launch_bounds__(kThreads, MINB) k_sec_march(DevScene S, FrameArgs A) {
-    __shared__ DevTF tfs[kMaxVol];
-    load_tfs(S, tfs);
+    __shared__ DevTF tfs[1];   // split passes: one volume (split_eligible)
+    load_tf0(S, tfs);
     RayStats st;
     LocalCounters c;
     const int lane = threadIdx.x & 31;
