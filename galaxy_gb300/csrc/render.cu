@@ -1337,9 +1337,15 @@ __device__ __forceinline__ void queue_pass(const DevScene &Sp, const DevTF *tfs_
 
 // Host-driven generations (one launch per kind, counts from the host); the
 // single-frame path and the per-launch profile use these.
+// The transfer functions of the scene's volumes in dynamic shared memory
+// (tf_smem bytes at launch): a geometry-only scene holds none, so its
+// traversal keeps the whole L1.
+extern __shared__ DevTF dyn_tfs[];
+static size_t tf_smem(const DevScene &S) { return sizeof(DevTF) * (size_t)S.n_vol; }
+
 template <int KIND, int MINB>
 __global__ void __launch_bounds__(kThreads, MINB) k_primary(DevScene S, FrameArgs A) {
-    __shared__ DevTF tfs[kMaxVol];
+    DevTF *tfs = dyn_tfs;
     load_tfs(S, tfs);
     RayStats st;
     LocalCounters c;
@@ -1356,7 +1362,7 @@ __global__ void __launch_bounds__(kThreads, MINB) k_primary(DevScene S, FrameArg
 
 template <int MINB>
 __global__ void __launch_bounds__(kThreads, MINB) k_secondary(DevScene S, FrameArgs A) {
-    __shared__ DevTF tfs[kMaxVol];
+    DevTF *tfs = dyn_tfs;
     load_tfs(S, tfs);
     RayStats st;
     LocalCounters c;
@@ -2686,8 +2692,8 @@ static int render(Scene *sc, const gxy_camera &cam, const gxy_lighting &lt, floa
                 k_cam_packet<4, false><<<query_grid(), kThreads, 0, st>>>(S, A);
             else if (kind == K_CAMERA && A.split_prim && lines) k_cam_query<false, 4, true><<<query_grid(), kThreads, 0, st>>>(S, A);
             else if (kind == K_CAMERA && A.split_prim) k_cam_query<false, 4, false><<<query_grid(), kThreads, 0, st>>>(S, A);
-            else if (kind == K_CAMERA) k_primary<K_CAMERA, 3><<<g, kThreads, 0, st>>>(S, A);
-            else if (kind == K_PRIMARY) k_primary<K_PRIMARY, 3><<<g, kThreads, 0, st>>>(S, A);
+            else if (kind == K_CAMERA) k_primary<K_CAMERA, 3><<<g, kThreads, tf_smem(S), st>>>(S, A);
+            else if (kind == K_PRIMARY) k_primary<K_PRIMARY, 3><<<g, kThreads, tf_smem(S), st>>>(S, A);
             else if (kind == K_SECONDARY && A.split && g_tune_sec_packet && lines)
                 k_sec_packet<4, true><<<query_grid(), kThreads, 0, st>>>(S, A);
             else if (kind == K_SECONDARY && A.split && g_tune_sec_packet)
@@ -2702,7 +2708,7 @@ static int render(Scene *sc, const gxy_camera &cam, const gxy_lighting &lt, floa
                 k_sec_query<false, 3, false><<<one_wave(k_sec_query<false, 3, false>), kThreads, 0, st>>>(S, A);
             else if (kind == K_SECONDARY && A.split && lines) k_sec_query<false, 4, true><<<query_grid(), kThreads, 0, st>>>(S, A);
             else if (kind == K_SECONDARY && A.split) k_sec_query<false, 4, false><<<query_grid(), kThreads, 0, st>>>(S, A);
-            else if (kind == K_SECONDARY) k_secondary<3><<<g, kThreads, 0, st>>>(S, A);
+            else if (kind == K_SECONDARY) k_secondary<3><<<g, kThreads, tf_smem(S), st>>>(S, A);
             else if (kind == K_PMARCH && g_tune_pmarch_blocks == 2) launch_prim_march<false, 2>(st, S, A);
             else if (kind == K_PMARCH) launch_prim_march<false, 3>(st, S, A);
             else if (kind == K_PQUERY && pq2 && lines)
@@ -2719,15 +2725,15 @@ static int render(Scene *sc, const gxy_camera &cam, const gxy_lighting &lt, floa
                 k_cam_packet<2, false><<<march_grid(2), kThreads, 0, st>>>(S, A);
             else if (kind == K_CAMERA && A.split_prim && lines) k_cam_query<false, 2, true><<<march_grid(2), kThreads, 0, st>>>(S, A);
             else if (kind == K_CAMERA && A.split_prim) k_cam_query<false, 2, false><<<march_grid(2), kThreads, 0, st>>>(S, A);
-            else if (kind == K_CAMERA) k_primary<K_CAMERA, 2><<<g, kThreads, 0, st>>>(S, A);
-            else if (kind == K_PRIMARY) k_primary<K_PRIMARY, 2><<<g, kThreads, 0, st>>>(S, A);
+            else if (kind == K_CAMERA) k_primary<K_CAMERA, 2><<<g, kThreads, tf_smem(S), st>>>(S, A);
+            else if (kind == K_PRIMARY) k_primary<K_PRIMARY, 2><<<g, kThreads, tf_smem(S), st>>>(S, A);
             else if (kind == K_SECONDARY && A.split && g_tune_sec_packet && lines)
                 k_sec_packet<2, true><<<march_grid(2), kThreads, 0, st>>>(S, A);
             else if (kind == K_SECONDARY && A.split && g_tune_sec_packet)
                 k_sec_packet<2, false><<<march_grid(2), kThreads, 0, st>>>(S, A);
             else if (kind == K_SECONDARY && A.split && lines) k_sec_query<false, 2, true><<<march_grid(2), kThreads, 0, st>>>(S, A);
             else if (kind == K_SECONDARY && A.split) k_sec_query<false, 2, false><<<march_grid(2), kThreads, 0, st>>>(S, A);
-            else if (kind == K_SECONDARY) k_secondary<2><<<g, kThreads, 0, st>>>(S, A);
+            else if (kind == K_SECONDARY) k_secondary<2><<<g, kThreads, tf_smem(S), st>>>(S, A);
             else if (kind == K_PMARCH) launch_prim_march<false, 2>(st, S, A);
             else if (kind == K_PQUERY && lines) k_prim_query<2, true><<<march_grid(2), kThreads, 0, st>>>(S, A);
             else if (kind == K_PQUERY) k_prim_query<2, false><<<march_grid(2), kThreads, 0, st>>>(S, A);
