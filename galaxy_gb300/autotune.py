@@ -64,13 +64,15 @@ def apply(setting):
             gpu.set_tuning(knob, int(setting[name]))
 
 
-def descend(measure, start, knobs=KNOBS, passes=2):
+def descend(measure, start, knobs=KNOBS, passes=2, min_gain=0.0):
     """Coordinate descent: from the setting `start` (knob name -> value),
     try every other value of one knob at a time, keep a change when
-    measure(setting) -- a time, lower is better -- improves, and repeat the
-    sweep while a pass still changes something (at most `passes` sweeps).
-    Each distinct setting is measured once.  Returns (best setting, its
-    time, [setting with ms_per_frame, ...] in measurement order)."""
+    measure(setting) -- a time, lower is better -- improves by more than the
+    fraction `min_gain` (a change within timing noise is not taken), and
+    repeat the sweep while a pass still changes something (at most `passes`
+    sweeps).  Each distinct setting is measured once.  Returns (best
+    setting, its time, [setting with ms_per_frame, ...] in measurement
+    order)."""
     measured = {}
     results = []
 
@@ -91,42 +93,60 @@ def descend(measure, start, knobs=KNOBS, passes=2):
                     continue
                 cand = dict(best, **{name: v})
                 ms = cost(cand)
-                if ms < best_ms:
+                if ms < best_ms * (1.0 - min_gain):
                     best, best_ms, changed = cand, ms, True
         if not changed:
             break
     return best, best_ms, results
 
 
-def tune(scene, camera, lighting, frames=3, passes=2, knobs=KNOBS, verbose=False):
+def tune(scene, camera, lighting, frames=3, passes=2, knobs=KNOBS, verbose=False, target_ms=30.0, min_gain=0.005):
     """descend() over real frames of the caller's scene, timed with CUDA
     events on the render stream after one warm-up frame per setting; leaves
-    the library set to the best setting."""
+    the library set to the best setting.  Each setting is timed over at
+    least `frames` frames and at least `target_ms` of rendering (short
+    frames are dominated by launch and host gaps, so a few of them time
+    noise), a change is kept only when it gains more than `min_gain`, and
+    the winner is timed once more against the starting setting over twice
+    the frames before it is kept."""
+    import math
     import torch
     stream = torch.cuda.current_stream()
     cam = camera.c() if hasattr(camera, "c") else camera
     fb = torch.zeros((cam.height, cam.width, 4), dtype=torch.float32, device="cuda")
 
-    def measure(setting):
+    def timed(setting, n):
         apply(setting)
         fb.zero_()
         scene.render(cam, lighting, fb.data_ptr(), stream.cuda_stream)
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        for _ in range(frames):
+        for _ in range(n):
             fb.zero_()
             scene.render(cam, lighting, fb.data_ptr(), stream.cuda_stream)
         e1.record(stream)
         torch.cuda.synchronize()
-        ms = e0.elapsed_time(e1) / frames
+        return e0.elapsed_time(e1) / n
+
+    start = current()
+    n_frames = max(1, frames, int(math.ceil(target_ms / max(timed(start, frames), 1e-3))))
+
+    def measure(setting):
+        ms = timed(setting, n_frames)
         if verbose:
             print("autotune", dict(setting, ms_per_frame=ms), flush=True)
         return ms
 
-    best, best_ms, results = descend(measure, current(), knobs, passes)
+    best, best_ms, results = descend(measure, start, knobs, passes, min_gain)
+    if best != start:
+        ms_best, ms_start = timed(best, 2 * n_frames), timed(start, 2 * n_frames)
+        if ms_start <= ms_best:
+            best, best_ms = start, ms_start
+        else:
+            best_ms = ms_best
     apply(best)
-    return {"best": dict(best, ms_per_frame=best_ms), "candidates": results}
+    return {"best": dict(best, ms_per_frame=best_ms), "frames_per_setting": n_frames, "candidates": results}
 
 
 def tune_bvh(vis, camera, lighting, values=(0, 64), frames=2, verbose=False):

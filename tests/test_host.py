@@ -135,6 +135,19 @@ def test_autotune_descent_keeps_start_when_nothing_is_faster():
     assert best == {"a": 2, "b": 8} and ms == 5.0 and len(results) == 3
 
 
+def test_autotune_descent_ignores_gains_within_the_noise_margin():
+    """With min_gain, a setting faster by less than that fraction does not
+    replace the current one; a larger gain still does."""
+    from galaxy_gb300 import autotune
+    knobs = (("a", 1, (1, 2)), ("b", 2, (4, 8)))
+    cost = {(1, 4): 10.0, (2, 4): 9.97, (1, 8): 9.0, (2, 8): 8.99}
+    best, ms, _ = autotune.descend(lambda s: cost[(s["a"], s["b"])], {"a": 1, "b": 4}, knobs, passes=3,
+                                   min_gain=0.005)
+    assert best == {"a": 1, "b": 8} and ms == 9.0
+    best0, ms0, _ = autotune.descend(lambda s: cost[(s["a"], s["b"])], {"a": 1, "b": 4}, knobs, passes=3)
+    assert best0 == {"a": 2, "b": 8} and ms0 == 8.99
+
+
 def test_poisson_requests_are_seeded_and_shaped():
     """Serving arrivals: Poisson at the given rate (mean gap 1/rate),
     image sides log-uniform within the range, deterministic per seed."""
