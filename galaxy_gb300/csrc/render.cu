@@ -1431,10 +1431,14 @@ __global__ void __launch_bounds__(kThreads) k_wavefront(DevScene Su, FrameArgs A
 // counts + 3*g.  KIND: K_CAMERA (all jobs' pixels), K_SECONDARY, which
 // here takes the primary, shadow and AO queues in one index space, or
 // K_PRIMARY (the primary queue alone, beside the split shadow/AO passes).
+// Shared memory: the uniform scene's transfer functions in dynamic shared
+// memory (batch_tf_smem bytes at launch; none for a geometry-only scene or
+// a batch of several scenes, whose rays read their own scene's tables), the
+// jobs' first pixels only in the camera generation.
 template <int KIND, bool USCENE, int MINB>
 __global__ void __launch_bounds__(kThreads, MINB) k_batch_gen(DevScene Su, FrameArgs A, const unsigned *cin) {
-    __shared__ DevTF tfs[kMaxVol];
-    __shared__ long long pix0[kMaxJobs];
+    DevTF *tfs = dyn_tfs;
+    __shared__ long long pix0[KIND == K_CAMERA ? kMaxJobs : 1];
     if (KIND == K_CAMERA)
         for (int j = threadIdx.x; j < A.n_jobs; j += blockDim.x) pix0[j] = A.jobs[j].pix0;
     if (USCENE) load_tfs(Su, tfs);
@@ -3665,15 +3669,17 @@ struct Batch {
 
 constexpr int kBatchGens = 10;   // generations per submission in per-generation mode
 
-static int gen_grid(bool uniform) {
+static size_t batch_tf_smem(bool uniform, const DevScene &Su) { return uniform ? tf_smem(Su) : 0; }
+
+static int gen_grid(bool uniform, size_t smem) {
     int sms = 152, per = 1;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, g_device);
     if (g_tune_minb == 3) {
-        if (uniform) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_batch_gen<K_SECONDARY, true, 3>, kThreads, 0);
-        else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_batch_gen<K_SECONDARY, false, 3>, kThreads, 0);
+        if (uniform) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_batch_gen<K_SECONDARY, true, 3>, kThreads, smem);
+        else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_batch_gen<K_SECONDARY, false, 3>, kThreads, smem);
     } else {
-        if (uniform) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_batch_gen<K_SECONDARY, true, 2>, kThreads, 0);
-        else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_batch_gen<K_SECONDARY, false, 2>, kThreads, 0);
+        if (uniform) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_batch_gen<K_SECONDARY, true, 2>, kThreads, smem);
+        else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_batch_gen<K_SECONDARY, false, 2>, kThreads, smem);
     }
     if (per < 1) per = 1;
     return sms * per;
@@ -3710,7 +3716,8 @@ static int batch_enqueue(Batch *b, const DevScene &Su, bool uniform, const Frame
         // Split passes as in a single frame: camera query + primary march,
         // then per generation the continuing primaries (side stream) beside
         // the shadow/AO query and march; counts are read on the device.
-        const int grid = gen_grid(true);
+        const size_t tsm = batch_tf_smem(true, Su);
+        const int grid = gen_grid(true, tsm);
         const bool lines = Su.n_seg > 0;
         for (int g = g_first; g < kBatchGens; g++) {
             FrameArgs a = A;
@@ -3745,8 +3752,8 @@ static int batch_enqueue(Batch *b, const DevScene &Su, bool uniform, const Frame
             } else {
                 CK(cudaEventRecord(b->fork[g], st));
                 CK(cudaStreamWaitEvent(b->side, b->fork[g], 0));
-                if (mb3) k_batch_gen<K_PRIMARY, true, 3><<<grid, kThreads, 0, b->side>>>(Su, a, cin);
-                else k_batch_gen<K_PRIMARY, true, 2><<<grid, kThreads, 0, b->side>>>(Su, a, cin);
+                if (mb3) k_batch_gen<K_PRIMARY, true, 3><<<grid, kThreads, tsm, b->side>>>(Su, a, cin);
+                else k_batch_gen<K_PRIMARY, true, 2><<<grid, kThreads, tsm, b->side>>>(Su, a, cin);
                 CK(cudaEventRecord(b->join[g], b->side));
                 if (mb3 && g_tune_query_blocks == 2) {
                     if (lines) k_sec_query<true, 2, true><<<one_wave(k_sec_query<true, 2, true>), kThreads, 0, st>>>(Su, a);
@@ -3779,7 +3786,8 @@ static int batch_enqueue(Batch *b, const DevScene &Su, bool uniform, const Frame
     if (!cooperative) {
         const bool split = uniform && split_eligible(Su);
         // generation g reads counts[g-1], writes counts[g] and queue set g&1
-        int grid = gen_grid(uniform);
+        const size_t tsm = batch_tf_smem(uniform, Su);
+        int grid = gen_grid(uniform, tsm);
         for (int g = g_first; g < kBatchGens; g++) {
             FrameArgs a = A;
             for (int k = 0; k < NQ; k++) {
@@ -3795,11 +3803,11 @@ static int batch_enqueue(Batch *b, const DevScene &Su, bool uniform, const Frame
 #define GXY_GEN_LAUNCH(MB)                                                                          \
     do {                                                                                            \
         if (g == 0) {                                                                               \
-            if (uniform) k_batch_gen<K_CAMERA, true, MB><<<grid, kThreads, 0, st>>>(Su, a, cin);    \
-            else k_batch_gen<K_CAMERA, false, MB><<<grid, kThreads, 0, st>>>(Su, a, cin);           \
+            if (uniform) k_batch_gen<K_CAMERA, true, MB><<<grid, kThreads, tsm, st>>>(Su, a, cin);  \
+            else k_batch_gen<K_CAMERA, false, MB><<<grid, kThreads, tsm, st>>>(Su, a, cin);         \
         } else {                                                                                    \
-            if (uniform) k_batch_gen<K_SECONDARY, true, MB><<<grid, kThreads, 0, st>>>(Su, a, cin); \
-            else k_batch_gen<K_SECONDARY, false, MB><<<grid, kThreads, 0, st>>>(Su, a, cin);        \
+            if (uniform) k_batch_gen<K_SECONDARY, true, MB><<<grid, kThreads, tsm, st>>>(Su, a, cin); \
+            else k_batch_gen<K_SECONDARY, false, MB><<<grid, kThreads, tsm, st>>>(Su, a, cin);        \
         }                                                                                           \
     } while (0)
             if (g_tune_minb == 3) GXY_GEN_LAUNCH(3);
