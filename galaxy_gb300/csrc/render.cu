@@ -3740,7 +3740,11 @@ static int batch_enqueue(Batch *b, const DevScene &Su, bool uniform, const Frame
             const bool mb3 = g_tune_minb == 3;
             if (g == 0) {
                 if (mb3) {
-                    if (lines) k_cam_query<true, 4, true><<<query_grid(), kThreads, 0, st>>>(Su, a);
+                    if (g_tune_pquery_blocks == 2 && lines)
+                        k_cam_query<true, 2, true><<<one_wave(k_cam_query<true, 2, true>), kThreads, 0, st>>>(Su, a);
+                    else if (g_tune_pquery_blocks == 2)
+                        k_cam_query<true, 2, false><<<one_wave(k_cam_query<true, 2, false>), kThreads, 0, st>>>(Su, a);
+                    else if (lines) k_cam_query<true, 4, true><<<query_grid(), kThreads, 0, st>>>(Su, a);
                     else k_cam_query<true, 4, false><<<query_grid(), kThreads, 0, st>>>(Su, a);
                     if (g_tune_pmarch_blocks == 2) launch_prim_march<true, 2>(st, Su, a);
                     else launch_prim_march<true, 3>(st, Su, a);

@@ -407,7 +407,8 @@ int gxy_gpu_set_profiling(gxy_scene scene, int on);
                                         128 registers per thread) or 3 (80 registers) */
 #define GXY_TUNE_PQUERY_BLOCKS  22   /* with GXY_TUNE_BLOCKS_PER_SM 3: resident blocks per SM of a
                                         frame's warp-cooperative camera query and handed-off primary
-                                        query, 2 (default: 128 registers per thread) or 4 (64) */
+                                        query and of a batch's camera query, 2 (default: 128
+                                        registers per thread) or 4 (64) */
 #define GXY_TUNE_CARRY_HITS     13   /* 1 (default): a shadow/AO ray that moves to the next
                                         partition carries the closest hit its query found
                                         over its whole extent, and the next partition's
