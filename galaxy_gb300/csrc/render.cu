@@ -1890,14 +1890,14 @@ __global__ void __launch_bounds__(kThreads, MINB) k_cam_query(DevScene S, FrameA
 // record (stop distance, surface flag, hit normal and colour beside it) for
 // k_prim_march, which composites with clear-brick skipping, shades, spawns,
 // classifies and routes exactly as for camera rays.
-template <int MINB, bool LINES>
+template <bool BATCH, int MINB, bool LINES>
 __global__ void __launch_bounds__(kThreads, MINB) k_prim_query(DevScene S, FrameArgs A) {
     __shared__ DevTF tfs[1];   // split passes: one volume (split_eligible)
     load_tf0(S, tfs);
     RayStats st;
     LocalCounters c;
     const int lane = threadIdx.x & 31;
-    const unsigned n = frame_nin(A, Q_PRIM);
+    const unsigned n = BATCH ? min(__ldg(A.nin_dev + Q_PRIM), A.qcap[Q_PRIM]) : frame_nin(A, Q_PRIM);
     unsigned *cursor = A.pmarch_count + 2;
     TravState T;
     uint2 stack_mem[64];
@@ -2716,11 +2716,11 @@ static int render(Scene *sc, const gxy_camera &cam, const gxy_lighting &lt, floa
             else if (kind == K_PMARCH && g_tune_pmarch_blocks == 2) launch_prim_march<false, 2>(st, S, A);
             else if (kind == K_PMARCH) launch_prim_march<false, 3>(st, S, A);
             else if (kind == K_PQUERY && pq2 && lines)
-                k_prim_query<2, true><<<one_wave(k_prim_query<2, true>), kThreads, 0, st>>>(S, A);
+                k_prim_query<false, 2, true><<<one_wave(k_prim_query<false, 2, true>), kThreads, 0, st>>>(S, A);
             else if (kind == K_PQUERY && pq2)
-                k_prim_query<2, false><<<one_wave(k_prim_query<2, false>), kThreads, 0, st>>>(S, A);
-            else if (kind == K_PQUERY && lines) k_prim_query<4, true><<<query_grid(), kThreads, 0, st>>>(S, A);
-            else if (kind == K_PQUERY) k_prim_query<4, false><<<query_grid(), kThreads, 0, st>>>(S, A);
+                k_prim_query<false, 2, false><<<one_wave(k_prim_query<false, 2, false>), kThreads, 0, st>>>(S, A);
+            else if (kind == K_PQUERY && lines) k_prim_query<false, 4, true><<<query_grid(), kThreads, 0, st>>>(S, A);
+            else if (kind == K_PQUERY) k_prim_query<false, 4, false><<<query_grid(), kThreads, 0, st>>>(S, A);
             else launch_sec_march<false, 4>(query_grid(), st, S, A);
         } else {
             if (kind == K_CAMERA && A.split_prim && g_tune_cam_packet && lines)
@@ -2739,8 +2739,8 @@ static int render(Scene *sc, const gxy_camera &cam, const gxy_lighting &lt, floa
             else if (kind == K_SECONDARY && A.split) k_sec_query<false, 2, false><<<march_grid(2), kThreads, 0, st>>>(S, A);
             else if (kind == K_SECONDARY) k_secondary<2><<<g, kThreads, tf_smem(S), st>>>(S, A);
             else if (kind == K_PMARCH) launch_prim_march<false, 2>(st, S, A);
-            else if (kind == K_PQUERY && lines) k_prim_query<2, true><<<march_grid(2), kThreads, 0, st>>>(S, A);
-            else if (kind == K_PQUERY) k_prim_query<2, false><<<march_grid(2), kThreads, 0, st>>>(S, A);
+            else if (kind == K_PQUERY && lines) k_prim_query<false, 2, true><<<march_grid(2), kThreads, 0, st>>>(S, A);
+            else if (kind == K_PQUERY) k_prim_query<false, 2, false><<<march_grid(2), kThreads, 0, st>>>(S, A);
             else launch_sec_march<false, 2>(march_grid(2), st, S, A);
         }
         CK(cudaGetLastError());
@@ -3614,7 +3614,8 @@ struct Batch {
     DRay *q[2][NQ] = {{nullptr, nullptr, nullptr}, {nullptr, nullptr, nullptr}};
     size_t qcap[NQ] = {0, 0, 0};
     unsigned *counts = nullptr;        // kMaxGen x NQ (cooperative mode uses the first 3 x NQ)
-    unsigned *mcounts = nullptr;       // kBatchGens x 4: march records, march cursor (split path)
+    unsigned *mcounts = nullptr;       // kBatchGens x 4: march records, march cursor (split path); then 4 for
+                                       // the camera march and kBatchGens x 4 for handed-off primaries
     DRay *qmarch = nullptr;
     size_t qmarch_cap = 0;
     DRay *pmarch = nullptr;            // split camera rays (uniform-scene batches)
@@ -3707,7 +3708,7 @@ static int batch_enqueue(Batch *b, const DevScene &Su, bool uniform, const Frame
         for (int k = 0; k < NQ; k++) std::swap(W.q[0][k], W.q[1][k]);
     if (!cont) CK(cudaMemcpyAsync(b->d_jobs, b->h_jobs, n_jobs * sizeof(DevJob), cudaMemcpyHostToDevice, st));
     CK(cudaMemsetAsync(b->counts, 0, (kBatchGens + 1) * NQ * sizeof(unsigned), st));
-    CK(cudaMemsetAsync(b->mcounts, 0, (kBatchGens + 1) * 4 * sizeof(unsigned), st));
+    CK(cudaMemsetAsync(b->mcounts, 0, (2 * kBatchGens + 1) * 4 * sizeof(unsigned), st));
     if (!cont) CK(cudaMemsetAsync(b->ctr, 0, sizeof(DevCounters), st));
     if (cont)
         CK(cudaMemcpyAsync(b->counts, b->d_status + 2, NQ * sizeof(unsigned), cudaMemcpyDeviceToDevice, st));
@@ -3756,8 +3757,28 @@ static int batch_enqueue(Batch *b, const DevScene &Su, bool uniform, const Frame
             } else {
                 CK(cudaEventRecord(b->fork[g], st));
                 CK(cudaStreamWaitEvent(b->side, b->fork[g], 0));
-                if (mb3) k_batch_gen<K_PRIMARY, true, 3><<<grid, kThreads, tsm, b->side>>>(Su, a, cin);
-                else k_batch_gen<K_PRIMARY, true, 2><<<grid, kThreads, tsm, b->side>>>(Su, a, cin);
+                if (g_tune_split_handoff) {
+                    // handed-off primaries as the frame path traces them: a
+                    // query to the partition exit into this generation's
+                    // march records, then the skipping camera-ray march
+                    FrameArgs ap = a;
+                    ap.pmarch_count = b->mcounts + 4 * (kBatchGens + g);
+                    const bool pq2 = !mb3 || g_tune_pquery_blocks == 2;
+                    if (pq2 && lines)
+                        k_prim_query<true, 2, true><<<one_wave(k_prim_query<true, 2, true>), kThreads, 0, b->side>>>(Su, ap);
+                    else if (pq2)
+                        k_prim_query<true, 2, false><<<one_wave(k_prim_query<true, 2, false>), kThreads, 0, b->side>>>(Su, ap);
+                    else if (lines)
+                        k_prim_query<true, 4, true><<<query_grid(), kThreads, 0, b->side>>>(Su, ap);
+                    else
+                        k_prim_query<true, 4, false><<<query_grid(), kThreads, 0, b->side>>>(Su, ap);
+                    if (!mb3 || g_tune_pmarch_blocks == 2) launch_prim_march<true, 2>(b->side, Su, ap);
+                    else launch_prim_march<true, 3>(b->side, Su, ap);
+                } else if (mb3) {
+                    k_batch_gen<K_PRIMARY, true, 3><<<grid, kThreads, tsm, b->side>>>(Su, a, cin);
+                } else {
+                    k_batch_gen<K_PRIMARY, true, 2><<<grid, kThreads, tsm, b->side>>>(Su, a, cin);
+                }
                 CK(cudaEventRecord(b->join[g], b->side));
                 if (mb3 && g_tune_query_blocks == 2) {
                     if (lines) k_sec_query<true, 2, true><<<one_wave(k_sec_query<true, 2, true>), kThreads, 0, st>>>(Su, a);
@@ -3878,7 +3899,7 @@ int gxy_gpu_batch_create(int64_t max_pixels, int max_jobs, int max_shadow, int m
     }
     int rc;
     if ((rc = b->dalloc((void **)&b->counts, (kBatchGens + 1) * NQ * sizeof(unsigned)))) return rc;
-    if ((rc = b->dalloc((void **)&b->mcounts, (kBatchGens + 1) * 4 * sizeof(unsigned)))) return rc;
+    if ((rc = b->dalloc((void **)&b->mcounts, (2 * kBatchGens + 1) * 4 * sizeof(unsigned)))) return rc;
     b->qmarch_cap = need[1] + need[2];
     if ((rc = b->dalloc((void **)&b->qmarch, b->qmarch_cap * sizeof(DRay)))) return rc;
     b->pmarch_cap = need[0];
