@@ -1461,6 +1461,49 @@ __global__ void __launch_bounds__(kThreads, MINB) k_batch_gen(DevScene Su, Frame
     flush_counters(A.ctr, c, st);
 }
 
+// Set-up of the shadow/AO query of a record `in` in its partition: the clip
+// to the partition (sec_clip: dir, ray_t0, ray_t), the slice planes (a
+// plane before ray_t becomes the stop, `surface`; one before tmax sets
+// `slice_ahead`), the zero-payload test and the occlusion shortcut
+// (GXY_TUNE_SKIP_MODE bit 3): when every march position of this partition,
+// tEntry .. ray_t, lies in clear superbricks, the march would leave the
+// payload as it is, so a surface anywhere before ray_t ends the ray here
+// with the payload unchanged -- the nearest surface is not needed and the
+// query may stop at the first hit before `stop_below` = ray_t (-inf: no
+// shortcut).
+__device__ __forceinline__ void sec_query_setup(const DevScene &S, const FrameArgs &A, const TraceIn &in, V3 &dir,
+                                                float &ray_t0, float &ray_t, bool &surface, bool &slice_ahead,
+                                                bool &zero, float &stop_below) {
+    float tEntry, tExitVolume;
+    sec_clip(S, in, dir, ray_t0, ray_t, tEntry, tExitVolume);
+    surface = false;
+    slice_ahead = false;
+    for (int m = 0; m < S.n_vol; m++) {
+        const DevVolume &vv = S.vol[m];
+        for (int k = 0; k < vv.n_slices; k++) {
+            float4 pl = vv.slices[k];
+            V3 pn = v3(pl.x, pl.y, pl.z);
+            float denom = dot(dir, pn);
+            if (fabsf(denom) > 0.0001f) {
+                float t = (pl.w - dot(in.org, pn)) / denom;
+                if (t >= ray_t0 && t <= in.tmax) slice_ahead = true;
+                if (t >= ray_t0 && t <= ray_t) {
+                    ray_t = t;
+                    surface = true;
+                }
+            }
+        }
+    }
+    zero = in.r == 0.0f && in.g == 0.0f && in.b == 0.0f && in.o == 0.0f;
+    stop_below = -INFINITY;
+    if ((A.skip_mode & 8) && S.vol[0].sclear && !zero) {
+        const DevVolume &vv = S.vol[0];
+        const VolPos g = vol_pos(vv, in.org + tEntry * dir);
+        if (__ldg(vv.sclear + super_of(vv, g)) && clear_run_end(vv, in.org, dir, g, tEntry, ray_t) > ray_t)
+            stop_below = ray_t;
+    }
+}
+
 // Query pass of split shadow/AO tracing with per-lane refill: each lane
 // runs the box clip and slice test of its ray, then steps the resumable
 // BVH8 traversal a few nodes at a time; a lane whose traversal is complete
@@ -1521,6 +1564,9 @@ __global__ void __launch_bounds__(kThreads, MINB) k_sec_query(DevScene S, FrameA
                 src = idx;
                 load_ray(idx < ns ? A.qin[Q_SHADOW] : A.qin[Q_AO], idx < ns ? idx : idx - ns, in, x, y, job);
                 c.seg++;
+                // sec_query_setup's steps, written out here: as a call, the
+                // kernel's register allocation spilled (72 bytes at 80
+                // registers per thread)
                 V3 dir;
                 float ray_t0, tEntry, tExitVolume;
                 sec_clip(S, in, dir, ray_t0, ray_t, tEntry, tExitVolume);
@@ -1543,12 +1589,7 @@ __global__ void __launch_bounds__(kThreads, MINB) k_sec_query(DevScene S, FrameA
                     }
                 }
                 zero = in.r == 0.0f && in.g == 0.0f && in.b == 0.0f && in.o == 0.0f;
-                // Occlusion shortcut (GXY_TUNE_SKIP_MODE bit 3): when every
-                // march position of this partition, tEntry .. ray_t, lies in
-                // clear superbricks, the march would leave the payload as it
-                // is, so a surface anywhere before ray_t ends the ray here
-                // with the payload unchanged -- the nearest surface is not
-                // needed and the query stops at the first hit before ray_t.
+                // occlusion shortcut (sec_query_setup)
                 stop_below = -INFINITY;
                 if ((A.skip_mode & 8) && S.vol[0].sclear && !zero) {
                     const DevVolume &vv = S.vol[0];
@@ -2128,7 +2169,7 @@ __global__ void __launch_bounds__(kThreads, MINB) k_prim_march(DevScene S, Frame
 // lanes keep marching, so warps stay full across rays of different march
 // lengths.  Each record carries the query pass's stop distance and surface
 // flag.  USCENE / batch as for the other frame kernels (uniform scene only).
-template <bool BATCH, int MINB, int SKIP>
+template <bool BATCH, int MINB, int SKIP, bool CONT = false>
 __global__ void __launch_bounds__(kThreads, MINB) k_sec_march(DevScene S, FrameArgs A) {
     __shared__ DevTF tfs[1];   // split passes: one volume (split_eligible)
     load_tf0(S, tfs);
@@ -2183,6 +2224,48 @@ __global__ void __launch_bounds__(kThreads, MINB) k_sec_march(DevScene S, FrameA
                 c.drop++;
             } else {
                 c.hand++;
+            }
+            if (CONT && dest >= 0 && A.qmarch_hit) {
+                // The ray moves on to brick `dest`.  It carries its query's
+                // closest hit over its whole extent (carry, 0: none), which
+                // is the next query's answer too, so the next generation's
+                // query needs no traversal: its set-up and decisions run
+                // here, and the lane marches on in the new brick.
+                TraceIn nx = in;
+                nx.t = M.tTerm;
+                nx.r = M.cr; nx.g = M.cg; nx.b = M.cb; nx.o = M.ca;
+                nx.part = dest;
+                c.seg++;
+                V3 ndir;
+                float nt0, nt, nstop;
+                bool nsurf, nahead, nzero;
+                sec_query_setup(S, A, nx, ndir, nt0, nt, nsurf, nahead, nzero, nstop);
+                const bool found = !nzero && !(nsurf && nstop > -INFINITY) && carry > 0.0f;
+                dest = GXY_DROP_ON_FLOOR;   // nothing is written to the next generation's queues
+                if (nstop > -INFINITY && (nsurf || (found && carry < nstop))) {
+                    // ends at a surface inside its clear segment (payload unchanged)
+                    const bool op = fmin_(fmin_(nx.r, nx.g), nx.b) >= 1.0f || nx.o > S.opaque_alpha;
+                    const int ncls = classify_ray(nx.type, (op ? GXY_RAY_OPAQUE : 0) | GXY_RAY_SURFACE);
+                    if (assign_destination(S, nx.part, nx.type, ncls, nx.org, nx.dir) == GXY_TERMINATED) {
+                        c.term++;
+                        add_pixel(J.fb, J.cam.width, x, y, nx.r, nx.g, nx.b, nx.o);
+                    } else {
+                        c.drop++;
+                    }
+                } else {
+                    if (found && carry < nt) {
+                        nt = carry;
+                        nsurf = true;
+                    }
+                    if (nzero || (!found && !nsurf && !nahead && !S.has_iso)) {
+                        c.drop++;
+                    } else {
+                        c.march++;
+                        in = nx;
+                        sec_march_init(S, in, nt, nsurf, M);
+                        fin = false;
+                    }
+                }
             }
         }
         if (__any_sync(0xffffffffu, fin && dest >= 0)) emit_secondary(fin, dest, q, job, in, x, y, T, A, c, carry);
@@ -2393,6 +2476,7 @@ static int g_tune_runahead = 16;     // frame generations launched per host read
 static int g_tune_query_blocks = 3;  // shadow/AO query at 2 (128 registers), 3 (80) or 4 (64) blocks per SM (blocks_per_sm 3)
 static int g_tune_pmarch_blocks = 2; // camera-ray march at 2 (128 registers) or 3 (80) blocks per SM (blocks_per_sm 3)
 static int g_tune_pquery_blocks = 2; // frame camera and handed-off primary queries at 2 (128 registers) or 4 (64)
+static int g_tune_continue = 1;      // shadow/AO rays that change brick march on in the same lane (carried hits on)
 int leaf_max() { return g_tune_leaf; }
 static int g_tune_collapse = 1;     // BVH8 collapse: surface-area cost programme (1) or largest child first (0)
 bool collapse_cost() { return g_tune_collapse != 0; }
@@ -2443,11 +2527,11 @@ static void launch_prim_march(cudaStream_t st, const DevScene &S, const FrameArg
     else
         k_prim_march<BATCH, MINB, 0><<<one_wave(k_prim_march<BATCH, MINB, 0>), kThreads, 0, st>>>(S, A);
 }
-template <bool BATCH, int MINB>
+template <bool BATCH, int MINB, bool CONT = false>
 static void launch_sec_march(unsigned grid, cudaStream_t st, const DevScene &S, const FrameArgs &A) {
-    if (S.vol[0].clear && (A.skip_mode & 4)) k_sec_march<BATCH, MINB, 2><<<grid, kThreads, 0, st>>>(S, A);
-    else if (S.vol[0].clear && (A.skip_mode & 2)) k_sec_march<BATCH, MINB, 1><<<grid, kThreads, 0, st>>>(S, A);
-    else k_sec_march<BATCH, MINB, 0><<<grid, kThreads, 0, st>>>(S, A);
+    if (S.vol[0].clear && (A.skip_mode & 4)) k_sec_march<BATCH, MINB, 2, CONT><<<grid, kThreads, 0, st>>>(S, A);
+    else if (S.vol[0].clear && (A.skip_mode & 2)) k_sec_march<BATCH, MINB, 1, CONT><<<grid, kThreads, 0, st>>>(S, A);
+    else k_sec_march<BATCH, MINB, 0, CONT><<<grid, kThreads, 0, st>>>(S, A);
 }
 
 // The shadow/AO march and the batches' camera query run at 4 resident
@@ -2721,6 +2805,7 @@ static int render(Scene *sc, const gxy_camera &cam, const gxy_lighting &lt, floa
                 k_prim_query<false, 2, false><<<one_wave(k_prim_query<false, 2, false>), kThreads, 0, st>>>(S, A);
             else if (kind == K_PQUERY && lines) k_prim_query<false, 4, true><<<query_grid(), kThreads, 0, st>>>(S, A);
             else if (kind == K_PQUERY) k_prim_query<false, 4, false><<<query_grid(), kThreads, 0, st>>>(S, A);
+            else if (g_tune_continue && A.qmarch_hit) launch_sec_march<false, 4, true>(query_grid(), st, S, A);
             else launch_sec_march<false, 4>(query_grid(), st, S, A);
         } else {
             if (kind == K_CAMERA && A.split_prim && g_tune_cam_packet && lines)
@@ -3378,6 +3463,10 @@ int gxy_gpu_set_tuning(int knob, int value) {
         g_tune_query_blocks = value;
         return GXY_OK;
     }
+    if (knob == GXY_TUNE_CONTINUE) {
+        g_tune_continue = value ? 1 : 0;
+        return GXY_OK;
+    }
     if (knob == GXY_TUNE_PQUERY_BLOCKS) {
         if (value != 2 && value != 4) return set_error(GXY_ERR_INVALID, "primary query blocks per SM must be 2 or 4");
         g_tune_pquery_blocks = value;
@@ -3425,6 +3514,7 @@ int gxy_gpu_get_tuning(int knob, int *value) {
     else if (knob == GXY_TUNE_QUERY_BLOCKS) *value = g_tune_query_blocks;
     else if (knob == GXY_TUNE_PMARCH_BLOCKS) *value = g_tune_pmarch_blocks;
     else if (knob == GXY_TUNE_PQUERY_BLOCKS) *value = g_tune_pquery_blocks;
+    else if (knob == GXY_TUNE_CONTINUE) *value = g_tune_continue;
     else return set_error(GXY_ERR_INVALID, "unknown tuning knob");
     return GXY_OK;
 }

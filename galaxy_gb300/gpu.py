@@ -130,6 +130,7 @@ TUNE_RUNAHEAD = 19
 TUNE_QUERY_BLOCKS = 20
 TUNE_PMARCH_BLOCKS = 21
 TUNE_PQUERY_BLOCKS = 22
+TUNE_CONTINUE = 23
 
 
 def set_tuning(knob, value):

@@ -409,6 +409,11 @@ int gxy_gpu_set_profiling(gxy_scene scene, int on);
                                         frame's warp-cooperative camera query and handed-off primary
                                         query and of a batch's camera query, 2 (default: 128
                                         registers per thread) or 4 (64) */
+#define GXY_TUNE_CONTINUE       23   /* 1 (default): in a frame, a shadow/AO ray that moves to the
+                                        next brick, carrying its query's closest hit
+                                        (GXY_TUNE_CARRY_HITS), is set up for that brick and marches
+                                        on in the same lane instead of waiting for the next
+                                        generation; 0: hand it on through the queues (same frames) */
 #define GXY_TUNE_CARRY_HITS     13   /* 1 (default): a shadow/AO ray that moves to the next
                                         partition carries the closest hit its query found
                                         over its whole extent, and the next partition's

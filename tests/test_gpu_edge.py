@@ -155,7 +155,11 @@ def test_carried_hits_same_frames(gpu):
     L = S.resolve_lights(vis.lighting, cam)
     sc = gpu.Scene(vis)
     before = gpu.get_tuning(gpu.TUNE_CARRY_HITS)
+    cont = gpu.get_tuning(gpu.TUNE_CONTINUE)
     try:
+        # rays carried through the queues (continuing them in the march
+        # kernel, GXY_TUNE_CONTINUE, also changes the generation counts)
+        gpu.set_tuning(gpu.TUNE_CONTINUE, 0)
         gpu.set_tuning(gpu.TUNE_CARRY_HITS, 1)
         a = sc.render_host(cam, L)
         ca = sc.counters()
@@ -164,6 +168,7 @@ def test_carried_hits_same_frames(gpu):
         cb = sc.counters()
     finally:
         gpu.set_tuning(gpu.TUNE_CARRY_HITS, before)
+        gpu.set_tuning(gpu.TUNE_CONTINUE, cont)
     assert float(np.abs(a - b).max()) <= 1e-6
     for k in ca:
         if k not in ("nodes", "prim_tests", "sph_tests", "tri_tests"):

@@ -337,6 +337,39 @@ def test_sah_top_bvh_matches_oracle(gpu, which):
     assert c["primary_rays"] == cnt["primary"] and c["shadow_rays"] == cnt["shadow"]
 
 
+@pytest.mark.parametrize("shortcut", [0, 8])
+@pytest.mark.parametrize("which", ["mixed", "pathlines"])
+def test_continued_shadow_ao_rays_same_frames(gpu, which, shortcut):
+    """Shadow/AO rays that move to the next brick march on in the same lane
+    (GXY_TUNE_CONTINUE 1) or wait for the next generation (0), with and
+    without the occlusion shortcut: the same frames and ray counts, fewer
+    generations, equal to the oracle."""
+    if which == "mixed":
+        cam, vis = scenes.mixed_scene(n=64, n_spheres=20000, width=128, height=128, partitions=(2, 2, 2), n_ao=4)
+    else:
+        cam, vis = scenes.pathlines_scene(n_lines=600, n_vertices=48, width=112, height=112, volume=True,
+                                          partitions=(2, 2, 1))
+    L = S.resolve_lights(vis.lighting, cam)
+    sc = gpu.Scene(vis)
+    mode = gpu.get_tuning(gpu.TUNE_SKIP_MODE)
+    out = {}
+    try:
+        gpu.set_tuning(gpu.TUNE_SKIP_MODE, (mode & ~8) | shortcut)
+        for v in (0, 1):
+            gpu.set_tuning(gpu.TUNE_CONTINUE, v)
+            out[v] = (sc.render_host(cam, L), sc.counters())
+    finally:
+        gpu.set_tuning(gpu.TUNE_CONTINUE, 1)
+        gpu.set_tuning(gpu.TUNE_SKIP_MODE, mode)
+    (a, ca), (b, cb) = out[1], out[0]
+    assert float(np.abs(a - b).max()) <= 1e-6
+    for k in ("primary_rays", "shadow_rays", "ao_rays", "terminated", "dropped", "handoffs", "segments", "samples"):
+        assert ca[k] == cb[k], k
+    assert cb["handoffs"] > 0 and ca["bounces"] <= cb["bounces"]
+    ref, cnt = O.OracleScene(vis).render(cam, L)
+    image_close(a, ref)
+
+
 @pytest.mark.parametrize("sah", [0, 16])
 @pytest.mark.parametrize("which", ["triangles", "mixed"])
 def test_cost_collapse_same_frames_fewer_nodes(gpu, which, sah):
