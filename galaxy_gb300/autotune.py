@@ -51,6 +51,7 @@ KNOBS = (
     ("query_blocks", gpu.TUNE_QUERY_BLOCKS, (3, 4)),
     ("pmarch_blocks", gpu.TUNE_PMARCH_BLOCKS, (2, 3)),
     ("pquery_blocks", gpu.TUNE_PQUERY_BLOCKS, (2, 4)),
+    ("continue", gpu.TUNE_CONTINUE, (0, 1)),
 )
 
 
