@@ -634,12 +634,20 @@ def main():
     tf = os.path.join(ROOT, "profiles", "traffic_%s.json" % args.workload)
     if os.path.exists(tf) and not args.image:
         t = json.load(open(tf))
-        traffic = t.get("bytes_per_launch")
+        frame_traffic = t.get("bytes_per_frame")
         binding = t.get("binding")
-        if traffic:
-            gbs = traffic / (dom_ms / 1e3) / 1e9
-            dram = {"achieved": gbs, "frac": gbs / peak, "bytes_per_launch": traffic,
-                    "traffic_over_algorithmic": traffic / dom_bytes, "measured_at": t.get("measured_at")}
+        if frame_traffic:
+            # per frame: the measured launches of a frame need not be as many
+            # as this run's (the later generations' launches are small), so
+            # DRAM bytes and kernel time are both taken per frame
+            frames = max(1, args.steps)
+            dom_frame_ms = sum(gen_ms[dom]) / frames
+            traffic = frame_traffic / max(1e-9, len(gen_ms[dom]) / frames)   # per launch, like `achieved`
+            gbs = frame_traffic / (dom_frame_ms / 1e3) / 1e9
+            dram = {"achieved": gbs, "frac": gbs / peak, "bytes_per_frame": frame_traffic,
+                    "bytes_per_launch": traffic,
+                    "traffic_over_algorithmic": frame_traffic / (sum(gen_bytes[dom]) / frames),
+                    "measured_at": t.get("measured_at")}
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "traffic": traffic, "dram": dram, "binding": binding, "peak_source": peak_kind,
             "model": "algorithmic bytes (64 B per record read and written, 128 B per node line, 16 B per sphere "
