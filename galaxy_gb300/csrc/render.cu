@@ -3707,6 +3707,7 @@ struct Batch {
     unsigned *mcounts = nullptr;       // kBatchGens x 4: march records, march cursor (split path); then 4 for
                                        // the camera march and kBatchGens x 4 for handed-off primaries
     DRay *qmarch = nullptr;
+    float *qmarch_hit = nullptr;       // per march record: the query's closest hit (carried hits)
     size_t qmarch_cap = 0;
     DRay *pmarch = nullptr;            // split camera rays (uniform-scene batches)
     float4 *pmarch_hit = nullptr;
@@ -3785,6 +3786,14 @@ static int batch_grid(bool uniform) {
     return sms * per;
 }
 
+// Shadow/AO march of a uniform split batch at 4 blocks per SM; rays that
+// move to the next brick with a carried closest hit march on in the same
+// lane (GXY_TUNE_CONTINUE), as in the frame path.
+static void launch_batch_sec_march(cudaStream_t st, const DevScene &Su, const FrameArgs &a) {
+    if (g_tune_continue && a.qmarch_hit) launch_sec_march<true, 4, true>(query_grid(), st, Su, a);
+    else launch_sec_march<true, 4>(query_grid(), st, Su, a);
+}
+
 // Enqueue one submission on the batch stream (captured into a graph or not).
 // cont: a continuation of the last submission -- no camera generation; the
 // queue counts the last generation left (copied aside into d_status[2..4])
@@ -3821,6 +3830,7 @@ static int batch_enqueue(Batch *b, const DevScene &Su, bool uniform, const Frame
             a.nin_dev = cin;
             a.split = 1;
             a.qmarch = b->qmarch;
+            a.qmarch_hit = g_tune_carry_hits ? b->qmarch_hit : nullptr;
             a.qmarch_count = b->mcounts + 4 * g;
             a.qmarch_cap = (unsigned)b->qmarch_cap;
             a.split_prim = 1;
@@ -3873,15 +3883,15 @@ static int batch_enqueue(Batch *b, const DevScene &Su, bool uniform, const Frame
                 if (mb3 && g_tune_query_blocks == 2) {
                     if (lines) k_sec_query<true, 2, true><<<one_wave(k_sec_query<true, 2, true>), kThreads, 0, st>>>(Su, a);
                     else k_sec_query<true, 2, false><<<one_wave(k_sec_query<true, 2, false>), kThreads, 0, st>>>(Su, a);
-                    launch_sec_march<true, 4>(query_grid(), st, Su, a);
+                    launch_batch_sec_march(st, Su, a);
                 } else if (mb3 && g_tune_query_blocks == 3) {
                     if (lines) k_sec_query<true, 3, true><<<one_wave(k_sec_query<true, 3, true>), kThreads, 0, st>>>(Su, a);
                     else k_sec_query<true, 3, false><<<one_wave(k_sec_query<true, 3, false>), kThreads, 0, st>>>(Su, a);
-                    launch_sec_march<true, 4>(query_grid(), st, Su, a);
+                    launch_batch_sec_march(st, Su, a);
                 } else if (mb3) {
                     if (lines) k_sec_query<true, 4, true><<<query_grid(), kThreads, 0, st>>>(Su, a);
                     else k_sec_query<true, 4, false><<<query_grid(), kThreads, 0, st>>>(Su, a);
-                    launch_sec_march<true, 4>(query_grid(), st, Su, a);
+                    launch_batch_sec_march(st, Su, a);
                 } else {
                     if (lines) k_sec_query<true, 2, true><<<march_grid(2), kThreads, 0, st>>>(Su, a);
                     else k_sec_query<true, 2, false><<<march_grid(2), kThreads, 0, st>>>(Su, a);
@@ -3976,7 +3986,7 @@ int gxy_gpu_batch_create(int64_t max_pixels, int max_jobs, int max_shadow, int m
                        (size_t)max_pixels * max_ao + slack};
     size_t bytes = 0;
     for (int k = 0; k < NQ; k++) bytes += 2 * need[k] * sizeof(DRay);
-    bytes += (need[1] + need[2]) * sizeof(DRay) + need[0] * (sizeof(DRay) + 2 * sizeof(float4));   // march queues
+    bytes += (need[1] + need[2]) * (sizeof(DRay) + sizeof(float)) + need[0] * (sizeof(DRay) + 2 * sizeof(float4));   // march queues
     if (!arena().would_fit(bytes + 16 * 1024 * 1024))
         return set_error(GXY_ERR_ADMISSION, "batch queues (" + std::to_string(bytes) + " bytes) exceed the HBM budget");
     for (int k = 0; k < NQ; k++) {
@@ -3992,6 +4002,7 @@ int gxy_gpu_batch_create(int64_t max_pixels, int max_jobs, int max_shadow, int m
     if ((rc = b->dalloc((void **)&b->mcounts, (2 * kBatchGens + 1) * 4 * sizeof(unsigned)))) return rc;
     b->qmarch_cap = need[1] + need[2];
     if ((rc = b->dalloc((void **)&b->qmarch, b->qmarch_cap * sizeof(DRay)))) return rc;
+    if ((rc = b->dalloc((void **)&b->qmarch_hit, b->qmarch_cap * sizeof(float)))) return rc;
     b->pmarch_cap = need[0];
     if ((rc = b->dalloc((void **)&b->pmarch, b->pmarch_cap * sizeof(DRay)))) return rc;
     if ((rc = b->dalloc((void **)&b->pmarch_hit, 2 * b->pmarch_cap * sizeof(float4)))) return rc;
