@@ -43,6 +43,36 @@ def test_resolve_lights_python_matches_c_abi():
         assert list(a.lights[i]) == list(b.lights[i])
 
 
+def test_register_budget_and_continue_knobs():
+    """Host side only: the per-kernel register-budget knobs take the block
+    counts their kernels are built for and refuse the rest; the knobs read
+    back what was set; GXY_TUNE_CONTINUE is an on/off switch."""
+    knobs = {gpu.TUNE_QUERY_BLOCKS: ((2, 3, 4), (1, 5)), gpu.TUNE_PMARCH_BLOCKS: ((2, 3), (1, 4)),
+             gpu.TUNE_PQUERY_BLOCKS: ((2, 4), (3, 5))}
+    for knob, (good, bad) in knobs.items():
+        before = gpu.get_tuning(knob)
+        try:
+            for v in good:
+                gpu.set_tuning(knob, v)
+                assert gpu.get_tuning(knob) == v
+            for v in bad:
+                with pytest.raises(gpu.GxyError):
+                    gpu.set_tuning(knob, v)
+                assert gpu.get_tuning(knob) == good[-1]
+        finally:
+            gpu.set_tuning(knob, before)
+    before = gpu.get_tuning(gpu.TUNE_CONTINUE)
+    try:
+        gpu.set_tuning(gpu.TUNE_CONTINUE, 0)
+        assert gpu.get_tuning(gpu.TUNE_CONTINUE) == 0
+        gpu.set_tuning(gpu.TUNE_CONTINUE, 7)
+        assert gpu.get_tuning(gpu.TUNE_CONTINUE) == 1
+    finally:
+        gpu.set_tuning(gpu.TUNE_CONTINUE, before)
+    assert (gpu.get_tuning(gpu.TUNE_QUERY_BLOCKS), gpu.get_tuning(gpu.TUNE_PMARCH_BLOCKS),
+            gpu.get_tuning(gpu.TUNE_PQUERY_BLOCKS), gpu.get_tuning(gpu.TUNE_CONTINUE)) == (3, 2, 2, 1)
+
+
 @pytest.mark.parametrize("parts", [(1, 1, 1), (2, 1, 1), (2, 2, 2), (3, 2, 1)])
 def test_partitions_product_equals_oracle(parts):
     vol = scenes.radial_volume("oneBall", 40)
