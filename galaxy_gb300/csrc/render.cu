@@ -938,6 +938,7 @@ struct DevJob {
     float *fb;
     const DevScene *scene;             // device copy of the job's scene (batches)
     long long pix0;                    // first global pixel index of the job
+    long long tile0;                   // first 8x4 pixel tile of the job among all jobs' tiles
 };
 
 struct FrameArgs {
@@ -945,6 +946,7 @@ struct FrameArgs {
     const DevJob *jobs;                // batch launches
     int n_jobs;
     long long total_pix;
+    long long total_tiles;             // batches: 8x4 pixel tiles of all jobs (warp-cooperative camera query)
     // single-frame camera passes: the band of image rows [band_y0,
     // band_y0 + band_rows) this launch generates (the whole image unless the
     // frame is split into bands to fit its queues)
@@ -2005,27 +2007,32 @@ __global__ void __launch_bounds__(kThreads, MINB) k_prim_query(DevScene S, Frame
     flush_counters(A.ctr, c, st);
 }
 
-// Query pass of split camera-ray tracing, warp-cooperative (single-frame
-// path): a warp takes the next 8x4 pixel tile from a device cursor and, for
-// each brick the lanes' camera rays enter first (Camera.cpp:431-441), clips
-// and tests slices per lane, then finds the closest hits of the 32 coherent
-// rays with one shared traversal (packet_closest).  Records as k_cam_query:
-// pixel i's first record in slot i, a hole record for a pixel whose ray
-// enters no brick, further bricks after slot npix.
-template <int MINB, bool LINES>
+// Query pass of split camera-ray tracing, warp-cooperative: a warp takes
+// the next 8x4 pixel tile from a device cursor and, for each brick the
+// lanes' camera rays enter first (Camera.cpp:431-441), clips and tests
+// slices per lane, then finds the closest hits of the 32 coherent rays with
+// one shared traversal (packet_closest).  Records as k_cam_query: pixel i's
+// first record in slot i, a hole record for a pixel whose ray enters no
+// brick, further bricks after slot npix.  Single frame: the tiles of the
+// band of rows [band_y0, band_y0 + band_rows); BATCH: the tiles of every
+// job's image, job by job (DevJob::tile0), a tile never spanning two jobs,
+// so a warp's rays share one camera.
+template <bool BATCH, int MINB, bool LINES>
 __global__ void __launch_bounds__(kThreads, MINB) k_cam_packet(DevScene S, FrameArgs A) {
     __shared__ DevTF tfs[1];   // split passes: one volume (split_eligible)
     __shared__ uint2 wstacks[kThreads / 32][64];
+    __shared__ long long tile0[BATCH ? kMaxJobs : 1];
+    if (BATCH)
+        for (int j = threadIdx.x; j < A.n_jobs; j += blockDim.x) tile0[j] = A.jobs[j].tile0;
     load_tf0(S, tfs);
     RayStats st;
     LocalCounters c;
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     uint2 *wstack = wstacks[threadIdx.x >> 5];
-    const DevCamera &cam = A.job0.cam;
-    const int w = cam.width, y0 = A.band_y0, hgt = A.band_rows;   // rows [y0, y0 + hgt) of the image
-    const unsigned npix = (unsigned)w * (unsigned)hgt;
-    const unsigned tiles_x = (unsigned)(w + 7) / 8, ntiles = tiles_x * (unsigned)((hgt + 3) / 4);
+    const unsigned npix = BATCH ? (unsigned)A.total_pix : (unsigned)A.job0.cam.width * (unsigned)A.band_rows;
+    const unsigned ntiles = BATCH ? (unsigned)A.total_tiles
+                                  : (unsigned)(A.job0.cam.width + 7) / 8 * (unsigned)((A.band_rows + 3) / 4);
     unsigned *cursor = A.pmarch_count + 2;
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(A.pmarch_count, npix);   // slots [0, npix)
     for (;;) {
@@ -2033,10 +2040,21 @@ __global__ void __launch_bounds__(kThreads, MINB) k_cam_packet(DevScene S, Frame
         if (lane == 0) tile = atomicAdd(cursor, 1u);
         tile = __shfl_sync(FULL, tile, 0);
         if (tile >= ntiles) break;
+        int job = 0;
+        if (BATCH) {
+            job = find_job(tile0, A.n_jobs, tile);
+            tile -= (unsigned)tile0[job];
+        }
+        const DevCamera &cam = BATCH ? A.jobs[job].cam : A.job0.cam;
+        const int w = cam.width;
+        const int y0 = BATCH ? 0 : A.band_y0, hgt = BATCH ? cam.height : A.band_rows;   // rows [y0, y0 + hgt)
+        const unsigned tiles_x = (unsigned)(w + 7) / 8;
         const int x = (int)(tile % tiles_x) * 8 + (lane & 7), yb = (int)(tile / tiles_x) * 4 + (lane >> 3);
         const int y = y0 + yb;
         const bool valid = x < w && yb < hgt;
-        const unsigned pix = valid ? (unsigned)yb * (unsigned)w + (unsigned)x : 0u;   // slot within the band
+        // slot: the pixel's index within the band (BATCH: among all jobs' pixels)
+        const unsigned pix = valid ? (BATCH ? (unsigned)A.jobs[job].pix0 : 0u) + (unsigned)yb * (unsigned)w + (unsigned)x
+                                   : 0u;
         V3 org = v3(0, 0, 0), dir0 = v3(1, 1, 1);
         uint64_t pending = 0;
         if (valid) {
@@ -2087,7 +2105,7 @@ __global__ void __launch_bounds__(kThreads, MINB) k_cam_packet(DevScene S, Frame
                 r->o = make_float4(org.x, org.y, org.z, 0.0f);
                 r->d = make_float4(dir0.x, dir0.y, dir0.z, FLT_MAX);
                 r->c = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-                r->m = make_int4(x, y, make_meta(GXY_RAY_PRIMARY | (surface ? 8 : 0), part, 0), __float_as_int(ray_t));
+                r->m = make_int4(x, y, make_meta(GXY_RAY_PRIMARY | (surface ? 8 : 0), part, job), __float_as_int(ray_t));
                 A.pmarch_hit[2 * (size_t)idx] = make_float4(hit_n.x, hit_n.y, hit_n.z, hit_c.x);
                 A.pmarch_hit[2 * (size_t)idx + 1] = make_float4(hit_c.y, hit_c.z, 0.0f, 0.0f);
             }
@@ -2771,13 +2789,13 @@ static int render(Scene *sc, const gxy_camera &cam, const gxy_lighting &lt, floa
         if (g_tune_minb == 3) {
             const bool pq2 = g_tune_pquery_blocks == 2;
             if (kind == K_CAMERA && A.split_prim && g_tune_cam_packet && pq2 && lines)
-                k_cam_packet<2, true><<<one_wave(k_cam_packet<2, true>), kThreads, 0, st>>>(S, A);
+                k_cam_packet<false, 2, true><<<one_wave(k_cam_packet<false, 2, true>), kThreads, 0, st>>>(S, A);
             else if (kind == K_CAMERA && A.split_prim && g_tune_cam_packet && pq2)
-                k_cam_packet<2, false><<<one_wave(k_cam_packet<2, false>), kThreads, 0, st>>>(S, A);
+                k_cam_packet<false, 2, false><<<one_wave(k_cam_packet<false, 2, false>), kThreads, 0, st>>>(S, A);
             else if (kind == K_CAMERA && A.split_prim && g_tune_cam_packet && lines)
-                k_cam_packet<4, true><<<query_grid(), kThreads, 0, st>>>(S, A);
+                k_cam_packet<false, 4, true><<<query_grid(), kThreads, 0, st>>>(S, A);
             else if (kind == K_CAMERA && A.split_prim && g_tune_cam_packet)
-                k_cam_packet<4, false><<<query_grid(), kThreads, 0, st>>>(S, A);
+                k_cam_packet<false, 4, false><<<query_grid(), kThreads, 0, st>>>(S, A);
             else if (kind == K_CAMERA && A.split_prim && lines) k_cam_query<false, 4, true><<<query_grid(), kThreads, 0, st>>>(S, A);
             else if (kind == K_CAMERA && A.split_prim) k_cam_query<false, 4, false><<<query_grid(), kThreads, 0, st>>>(S, A);
             else if (kind == K_CAMERA) k_primary<K_CAMERA, 3><<<g, kThreads, tf_smem(S), st>>>(S, A);
@@ -2809,9 +2827,9 @@ static int render(Scene *sc, const gxy_camera &cam, const gxy_lighting &lt, floa
             else launch_sec_march<false, 4>(query_grid(), st, S, A);
         } else {
             if (kind == K_CAMERA && A.split_prim && g_tune_cam_packet && lines)
-                k_cam_packet<2, true><<<march_grid(2), kThreads, 0, st>>>(S, A);
+                k_cam_packet<false, 2, true><<<march_grid(2), kThreads, 0, st>>>(S, A);
             else if (kind == K_CAMERA && A.split_prim && g_tune_cam_packet)
-                k_cam_packet<2, false><<<march_grid(2), kThreads, 0, st>>>(S, A);
+                k_cam_packet<false, 2, false><<<march_grid(2), kThreads, 0, st>>>(S, A);
             else if (kind == K_CAMERA && A.split_prim && lines) k_cam_query<false, 2, true><<<march_grid(2), kThreads, 0, st>>>(S, A);
             else if (kind == K_CAMERA && A.split_prim) k_cam_query<false, 2, false><<<march_grid(2), kThreads, 0, st>>>(S, A);
             else if (kind == K_CAMERA) k_primary<K_CAMERA, 2><<<g, kThreads, tf_smem(S), st>>>(S, A);
@@ -3840,7 +3858,17 @@ static int batch_enqueue(Batch *b, const DevScene &Su, bool uniform, const Frame
             a.pmarch_cap = (unsigned)b->pmarch_cap;
             const bool mb3 = g_tune_minb == 3;
             if (g == 0) {
-                if (mb3) {
+                if (mb3 && g_tune_cam_packet) {
+                    // warp-cooperative camera query over every job's 8x4 tiles
+                    if (g_tune_pquery_blocks == 2 && lines)
+                        k_cam_packet<true, 2, true><<<one_wave(k_cam_packet<true, 2, true>), kThreads, 0, st>>>(Su, a);
+                    else if (g_tune_pquery_blocks == 2)
+                        k_cam_packet<true, 2, false><<<one_wave(k_cam_packet<true, 2, false>), kThreads, 0, st>>>(Su, a);
+                    else if (lines) k_cam_packet<true, 4, true><<<query_grid(), kThreads, 0, st>>>(Su, a);
+                    else k_cam_packet<true, 4, false><<<query_grid(), kThreads, 0, st>>>(Su, a);
+                    if (g_tune_pmarch_blocks == 2) launch_prim_march<true, 2>(st, Su, a);
+                    else launch_prim_march<true, 3>(st, Su, a);
+                } else if (mb3) {
                     if (g_tune_pquery_blocks == 2 && lines)
                         k_cam_query<true, 2, true><<<one_wave(k_cam_query<true, 2, true>), kThreads, 0, st>>>(Su, a);
                     else if (g_tune_pquery_blocks == 2)
@@ -4049,7 +4077,7 @@ int gxy_gpu_batch_submit(gxy_batch batch, const gxy_job *jobs, int n_jobs, int f
         if (q == cudaErrorNotReady) return set_error(GXY_ERR_INVALID, "previous submission still running");
     }
     if (n_jobs > b->max_jobs) return set_error(GXY_ERR_INVALID, "too many jobs for this batch");
-    long long pix = 0;
+    long long pix = 0, tiles = 0;
     Scene *first = reinterpret_cast<Scene *>(jobs[0].scene);
     bool uniform = true;
     for (int j = 0; j < n_jobs; j++) {
@@ -4068,7 +4096,9 @@ int gxy_gpu_batch_submit(gxy_batch batch, const gxy_job *jobs, int n_jobs, int f
         D.fb = J.fb_rgba;
         D.scene = sc->d_scene;
         D.pix0 = pix;
+        D.tile0 = tiles;
         pix += (long long)J.camera.width * J.camera.height;
+        tiles += (long long)((J.camera.width + 7) / 8) * ((J.camera.height + 3) / 4);
     }
     if (pix > b->max_pixels) return set_error(GXY_ERR_ADMISSION, "batch pixel budget exceeded");
     FrameArgs A;
@@ -4080,6 +4110,7 @@ int gxy_gpu_batch_submit(gxy_batch batch, const gxy_job *jobs, int n_jobs, int f
     A.march_steps = g_tune_march_steps;
     A.skip_mode = g_tune_skip_mode;
     A.total_pix = pix;
+    A.total_tiles = tiles;
     A.job0 = b->h_jobs[0];
     for (int k = 0; k < NQ; k++) A.qcap[k] = (unsigned)b->qcap[k];
     A.ctr = b->ctr;

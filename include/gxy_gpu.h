@@ -338,9 +338,10 @@ int gxy_gpu_set_profiling(gxy_scene scene, int on);
                                         passes, 1-64 (default 8) */
 #define GXY_TUNE_MARCH_STEPS     8   /* volume samples per refill round of the march
                                         passes, 1-256 (default 16) */
-#define GXY_TUNE_CAMERA_PACKET   9   /* 1 (default): camera rays of a frame queried by
-                                        warps over 8x4 pixel tiles with one shared BVH8
-                                        traversal; 0: per-lane refill traversal */
+#define GXY_TUNE_CAMERA_PACKET   9   /* 1 (default): camera rays of a frame, and of a batch of
+                                        jobs of one volume scene, queried by warps over 8x4
+                                        pixel tiles (a batch's tiles job by job) with one shared
+                                        BVH8 traversal; 0: per-lane refill traversal */
 #define GXY_TUNE_SKIP_CLEAR     10   /* read at scene commit.  1 (default): flag the volume
                                         bricks whose samples all lie below the transfer
                                         function's zero-opacity threshold; the march
