@@ -108,6 +108,22 @@ def algorithmic_bytes(g):
             16 * g["sph_tests"] + 4 * (g["samples"] - g.get("samples_skipped", 0)) + 32 * g["terminated"])
 
 
+def dram_roofline(frame_traffic, kernel_ms, kernel_bytes, frames, peak):
+    """DRAM-measured roofline of the dominant kernel: the DRAM bytes ncu
+    measured for its launches of one frame (frame_traffic) over its CUDA-event
+    time per frame (kernel_ms: its launch times over `frames` frames).  Both
+    are taken per frame, so the figure does not depend on how many launches
+    a frame has; bytes_per_launch is the per-launch mean, beside the
+    algorithmic bytes (kernel_bytes: per launch, the same launches)."""
+    frames = max(1, frames)
+    launches = max(1e-9, len(kernel_ms) / frames)
+    frame_ms = sum(kernel_ms) / frames
+    gbs = frame_traffic / (frame_ms / 1e3) / 1e9
+    return {"achieved": gbs, "frac": gbs / peak, "bytes_per_frame": frame_traffic,
+            "bytes_per_launch": frame_traffic / launches,
+            "traffic_over_algorithmic": frame_traffic / (sum(kernel_bytes) / frames)}
+
+
 def measured_peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -637,17 +653,9 @@ def main():
         frame_traffic = t.get("bytes_per_frame")
         binding = t.get("binding")
         if frame_traffic:
-            # per frame: the measured launches of a frame need not be as many
-            # as this run's (the later generations' launches are small), so
-            # DRAM bytes and kernel time are both taken per frame
-            frames = max(1, args.steps)
-            dom_frame_ms = sum(gen_ms[dom]) / frames
-            traffic = frame_traffic / max(1e-9, len(gen_ms[dom]) / frames)   # per launch, like `achieved`
-            gbs = frame_traffic / (dom_frame_ms / 1e3) / 1e9
-            dram = {"achieved": gbs, "frac": gbs / peak, "bytes_per_frame": frame_traffic,
-                    "bytes_per_launch": traffic,
-                    "traffic_over_algorithmic": frame_traffic / (sum(gen_bytes[dom]) / frames),
-                    "measured_at": t.get("measured_at")}
+            dram = dram_roofline(frame_traffic, gen_ms[dom], gen_bytes[dom], args.steps, peak)
+            dram["measured_at"] = t.get("measured_at")
+            traffic = dram["bytes_per_launch"]   # per launch, like `achieved`
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "traffic": traffic, "dram": dram, "binding": binding, "peak_source": peak_kind,
             "model": "algorithmic bytes (64 B per record read and written, 128 B per node line, 16 B per sphere "

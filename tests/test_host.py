@@ -226,3 +226,22 @@ def test_algorithmic_bytes_of_a_generation():
     assert bench.algorithmic_bytes(g) == 64 * 13 + 128 * 7 + 48 * 2 + 16 * 5 + 4 * 40 + 32 * 4
     g.pop("samples_skipped")
     assert bench.algorithmic_bytes(g) == 64 * 13 + 128 * 7 + 48 * 2 + 16 * 5 + 4 * 100 + 32 * 4
+
+
+def test_dram_roofline_is_taken_per_frame():
+    """The DRAM-measured roofline divides a frame's measured bytes by the
+    kernel's time per frame, so the same frame split into more or fewer
+    launches gives the same figure."""
+    import importlib.util
+    import os
+    spec = importlib.util.spec_from_file_location(
+        "bench_mod", os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "bench.py"))
+    bench = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(bench)
+    # two frames of 3 launches (4 ms per frame) against two frames of 5 launches (same 4 ms)
+    a = bench.dram_roofline(2.0e9, [3.0, 0.5, 0.5] * 2, [3e9, 5e8, 5e8] * 2, 2, 1000.0)
+    b = bench.dram_roofline(2.0e9, [2.0, 1.0, 0.5, 0.25, 0.25] * 2, [2e9, 1e9, 5e8, 2.5e8, 2.5e8] * 2, 2, 1000.0)
+    assert abs(a["achieved"] - 500.0) < 1e-9 and abs(b["achieved"] - 500.0) < 1e-9
+    assert abs(a["frac"] - 0.5) < 1e-12
+    assert a["bytes_per_launch"] == 2.0e9 / 3 and b["bytes_per_launch"] == 2.0e9 / 5
+    assert abs(a["traffic_over_algorithmic"] - 0.5) < 1e-12 and abs(b["traffic_over_algorithmic"] - 0.5) < 1e-12
